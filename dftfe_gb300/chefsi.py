@@ -1,0 +1,290 @@
+"""Host-side mirror of DFT-FE's CheFSI interface over the GB300 C ABI.
+
+Names and argument meaning follow the reference:
+
+* ``KohnShamOperator`` -- ``operatorDFTDeviceClass`` (include/operatorDevice.h:43-420):
+  ``HX`` (:176-185, with ``scaleFlag`` / ``scalar``), ``XtHX`` (:230-241),
+  ``getSqrtMassVec`` / ``getInvSqrtMassVec`` (:68-72);
+* ``ChebyshevOrthogonalizedSubspaceIterationSolver`` --
+  ``chebyshevOrthogonalizedSubspaceIterationSolverDevice``
+  (include/chebyshevOrthogonalizedSubspaceIterationSolverDevice.h:37-166): ``solve``,
+  ``solveNoRR``, ``reinitSpectrumBounds``;
+* ``lanczosLowerUpperBoundEigenSpectrum``, ``chebyshevFilter``, ``fillOverlapMatrix``,
+  ``rayleighRitzGEP``, ``pseudoGramSchmidtOrthogonalization``, ``computeEigenResidualNorm``
+  -- the linearAlgebraOperationsDevice functions of the same names.
+
+Vectors are torch CUDA tensors in DFT-FE's flattened layout [n_dofs, n_vectors]
+(vector index fastest). Every call goes through libchefsi_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import PRECISIONS, check
+
+
+def _ptr(t: torch.Tensor | None) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _np_ptr(a: np.ndarray | None) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if a is None else a.ctypes.data)
+
+
+def _stream(stream=None) -> ctypes.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _prec(p) -> int:
+    return PRECISIONS[p] if isinstance(p, str) else int(p)
+
+
+class KohnShamOperator:
+    """A = M^{-1/2}(H_loc + H_nl)M^{-1/2} on one GPU (operatorDFTDeviceClass)."""
+
+    def __init__(self, cell_map, cell_mats, sqrt_mass, inv_sqrt_mass, n_dofs: int | None = None,
+                 projectors=None, constraints=None):
+        lib = _lib.load()
+        cm = np.ascontiguousarray(cell_map, dtype=np.int32)
+        self.is_complex = bool(np.iscomplexobj(cell_mats))
+        mats = np.ascontiguousarray(cell_mats, dtype=np.complex128 if self.is_complex else np.float64)
+        sm = np.ascontiguousarray(sqrt_mass, dtype=np.float64)
+        ism = np.ascontiguousarray(inv_sqrt_mass, dtype=np.float64)
+        self.n_dofs = int(n_dofs if n_dofs is not None else len(sm))
+        self.n_cells, self.nodes_per_cell = cm.shape
+        d = _lib.OperatorDesc()
+        d.n_dofs, d.n_cells, d.nodes_per_cell = self.n_dofs, self.n_cells, self.nodes_per_cell
+        d.is_complex = int(self.is_complex)
+        d.cell_dof_map, d.cell_matrices = _np_ptr(cm), _np_ptr(mats)
+        d.sqrt_mass, d.inv_sqrt_mass = _np_ptr(sm), _np_ptr(ism)
+        keep = [cm, mats, sm, ism]
+        if constraints is not None:
+            ids, ptr, mas, w = (np.ascontiguousarray(a, dt) for a, dt in
+                                zip(constraints, (np.int32, np.int32, np.int32, np.float64)))
+            keep += [ids, ptr, mas, w]
+            d.n_constrained = len(ids)
+            d.constrained_ids, d.constraint_ptr = _np_ptr(ids), _np_ptr(ptr)
+            d.master_ids, d.master_weights = _np_ptr(mas), _np_ptr(w)
+        if projectors is not None and projectors.n_atoms > 0:
+            ap = np.ascontiguousarray(projectors.ptr, np.int32)
+            ad = np.ascontiguousarray(projectors.dofs, np.int32)
+            av = np.ascontiguousarray(projectors.values, np.float64)
+            cp = np.ascontiguousarray(projectors.couplings, np.float64)
+            keep += [ap, ad, av, cp]
+            d.n_atoms, d.n_proj = projectors.n_atoms, projectors.n_proj
+            d.atom_dof_ptr, d.atom_dofs = _np_ptr(ap), _np_ptr(ad)
+            d.atom_proj, d.couplings = _np_ptr(av), _np_ptr(cp)
+        h = ctypes.c_void_p()
+        check(lib.chefsi_operator_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self._sqrt = torch.from_numpy(sm).cuda()
+        self._isqrt = torch.from_numpy(ism).cuda()
+        self.dtype = torch.complex128 if self.is_complex else torch.float64
+
+    @classmethod
+    def from_problem(cls, pr, constraints=None):
+        return cls(pr.cell_map, pr.cell_mats, pr.sqrt_mass, pr.inv_sqrt_mass, pr.n_dofs,
+                   projectors=pr.nonlocal_, constraints=constraints)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.chefsi_operator_destroy(h)
+            self._h = None
+
+    def getSqrtMassVec(self) -> torch.Tensor:
+        return self._sqrt
+
+    def getInvSqrtMassVec(self) -> torch.Tensor:
+        return self._isqrt
+
+    def HX(self, src: torch.Tensor, dst: torch.Tensor, scalar: float = 1.0,
+           scaleFlag: bool = False, precision="fp64", stream=None) -> torch.Tensor:
+        """dst = (scaleFlag ? dst : 0) + scalar * A src (operatorDFTDeviceClass::HX)."""
+        n_vec = 1 if src.dim() == 1 else src.shape[1]
+        ld_s = 1 if src.dim() == 1 else src.stride(0)
+        ld_d = 1 if dst.dim() == 1 else dst.stride(0)
+        check(_lib.load().chefsi_hx(self._h, _ptr(src), ld_s, _ptr(dst), ld_d, n_vec,
+                                    float(scalar), int(bool(scaleFlag)), _prec(precision),
+                                    _stream(stream)))
+        return dst
+
+    def apply(self, X: torch.Tensor, precision="fp64") -> torch.Tensor:
+        Y = torch.empty_like(X)
+        return self.HX(X, Y, 1.0, False, precision)
+
+    def XtHX(self, X: torch.Tensor, precision="fp64") -> torch.Tensor:
+        N = X.shape[1]
+        Hp = torch.zeros((N, N), dtype=X.dtype, device=X.device)
+        check(_lib.load().chefsi_xthx(self._h, _ptr(X), X.stride(0), N, _ptr(Hp), _prec(precision),
+                                      _stream()))
+        return Hp
+
+    def overlap(self, X: torch.Tensor, precision="fp64") -> torch.Tensor:
+        N = X.shape[1]
+        S = torch.zeros((N, N), dtype=X.dtype, device=X.device)
+        check(_lib.load().chefsi_overlap(self._h, _ptr(X), X.stride(0), N, _ptr(S), _prec(precision),
+                                         _stream()))
+        return S
+
+
+fillOverlapMatrix = KohnShamOperator.overlap
+
+
+def lanczosLowerUpperBoundEigenSpectrum(op: KohnShamOperator, k: int = 20,
+                                        reproducible: bool = False, v0: np.ndarray | None = None,
+                                        seed: int = 0):
+    lo, up = ctypes.c_double(), ctypes.c_double()
+    v = None if v0 is None else np.ascontiguousarray(v0, np.float64)
+    check(_lib.load().chefsi_lanczos_bounds(op.handle, k, int(reproducible), _np_ptr(v), seed,
+                                            ctypes.byref(lo), ctypes.byref(up), _stream()))
+    return lo.value, up.value
+
+
+def chebyshevFilter(op: KohnShamOperator, X: torch.Tensor, m: int, a: float, b: float, a0: float,
+                    precision="fp64") -> torch.Tensor:
+    check(_lib.load().chefsi_chebyshev_filter(op.handle, _ptr(X), X.stride(0), X.shape[1], m,
+                                              float(a), float(b), float(a0), _prec(precision),
+                                              _stream()))
+    return X
+
+
+def pseudoGramSchmidtOrthogonalization(op: KohnShamOperator, X: torch.Tensor, precision="fp64"):
+    check(_lib.load().chefsi_cholesky_gs(op.handle, _ptr(X), X.stride(0), X.shape[1],
+                                         _prec(precision), _stream()))
+    return X
+
+
+def rayleighRitzGEP(op: KohnShamOperator, X: torch.Tensor, precision="fp64", want_hx=False):
+    N = X.shape[1]
+    ev = np.zeros(N)
+    HX = torch.empty_like(X) if want_hx else None
+    check(_lib.load().chefsi_rayleigh_ritz(op.handle, _ptr(X), X.stride(0), N, _np_ptr(ev),
+                                           _ptr(HX), _prec(precision), _stream()))
+    return (ev, HX) if want_hx else ev
+
+
+def computeEigenResidualNorm(op: KohnShamOperator, X: torch.Tensor, eig) -> np.ndarray:
+    N = X.shape[1]
+    e = np.ascontiguousarray(eig, np.float64)
+    r = np.zeros(N)
+    check(_lib.load().chefsi_residual_norms(op.handle, _ptr(X), X.stride(0), N, _np_ptr(e),
+                                            _np_ptr(r), _stream()))
+    return r
+
+
+def syevd(A: torch.Tensor):
+    """Symmetric eigensolve on the GPU (FP64): returns (w ascending, Z with vectors in columns)."""
+    N = A.shape[0]
+    Ac = A.clone().contiguous()
+    w = torch.empty(N, dtype=torch.float64, device=A.device)
+    Z = torch.empty((N, N), dtype=torch.float64, device=A.device)
+    check(_lib.load().chefsi_syevd(N, _ptr(Ac), _ptr(w), _ptr(Z), _stream()))
+    return w, Z
+
+
+def chebyshev_order(upper_bound: float) -> int:
+    return int(_lib.load().chefsi_chebyshev_order(float(upper_bound)))
+
+
+@dataclass
+class SolverParams:
+    """The dftParameters fields the CheFSI path reads (utils/dftParameters.cc:1224-1287)."""
+    chebyshevOrder: int = 0
+    chebyWfcBlockSize: int = 400
+    wfcBlockSize: int = 400
+    mixed_precision: str = "mixed"     # precision used when solve(useMixedPrec=True)
+    lanczos_steps: int = 20
+    reproducible_output: bool = False
+    chebyshevFilterPolyDegreeFirstScfScalingFactor: float = 1.34
+    keep_hx: bool = True
+
+
+class ChebyshevOrthogonalizedSubspaceIterationSolver:
+    """chebyshevOrthogonalizedSubspaceIterationSolverDevice on the GB300 C ABI."""
+
+    def __init__(self, params: SolverParams | None = None):
+        self.params = params or SolverParams()
+        self._h = {}
+        self._lib = _lib.load()
+
+    def _handle(self, mixed: bool):
+        key = bool(mixed)
+        if key not in self._h:
+            p = _lib.Params()
+            p.chebyshev_degree = self.params.chebyshevOrder
+            p.cheby_wfc_block = self.params.chebyWfcBlockSize
+            p.wfc_block = self.params.wfcBlockSize
+            p.precision = _prec(self.params.mixed_precision) if mixed else _lib.PREC_FP64
+            p.lanczos_steps = self.params.lanczos_steps
+            p.reproducible = int(self.params.reproducible_output)
+            p.first_scf_degree_scale = self.params.chebyshevFilterPolyDegreeFirstScfScalingFactor
+            p.keep_hx = int(self.params.keep_hx)
+            h = ctypes.c_void_p()
+            check(self._lib.chefsi_solver_create(ctypes.byref(p), ctypes.byref(h)))
+            self._h[key] = h
+            if hasattr(self, "_bounds"):
+                check(self._lib.chefsi_solver_reinit_spectrum_bounds(h, *self._bounds))
+        return self._h[key]
+
+    def __del__(self):
+        for h in getattr(self, "_h", {}).values():
+            if _lib._lib is not None:
+                _lib._lib.chefsi_solver_destroy(h)
+
+    def reinitSpectrumBounds(self, lowerBoundWantedSpectrum: float,
+                             lowerBoundUnWantedSpectrum: float,
+                             upperBoundUnWantedSpectrum: float):
+        self._bounds = (float(lowerBoundWantedSpectrum), float(lowerBoundUnWantedSpectrum),
+                        float(upperBoundUnWantedSpectrum))
+        for h in self._h.values():
+            check(self._lib.chefsi_solver_reinit_spectrum_bounds(h, *self._bounds))
+
+    def solve(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, eigenValues=None,
+              residualNorms=None, computeResidual: bool = True, useMixedPrec: bool = False,
+              isFirstScf: bool = False):
+        """One CheFSI iteration on X [n_dofs, N] in place; returns (eigenValues, residualNorms)."""
+        N = X.shape[1]
+        ev = np.zeros(N) if eigenValues is None else eigenValues
+        rn = np.zeros(N) if residualNorms is None else residualNorms
+        h = self._handle(useMixedPrec)
+        check(self._lib.chefsi_solve(h, operatorMatrix.handle, _ptr(X), N, _np_ptr(ev),
+                                     _np_ptr(rn), int(computeResidual), int(isFirstScf), _stream()))
+        return ev, rn
+
+    def solveNoRR(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, numberPasses: int = 1,
+                  useMixedPrec: bool = False, isFirstScf: bool = False):
+        h = self._handle(useMixedPrec)
+        check(self._lib.chefsi_solve_no_rr(h, operatorMatrix.handle, _ptr(X), X.shape[1],
+                                           numberPasses, int(isFirstScf), _stream()))
+        return X
+
+    def timings(self, mixed: bool = False) -> dict:
+        t = (ctypes.c_double * 7)()
+        check(self._lib.chefsi_solver_timings(self._handle(mixed), t))
+        keys = ["filter", "overlap_cholesky", "xthx", "eig", "rotation", "residual", "total"]
+        return dict(zip(keys, list(t)))
+
+    def last_degree(self, mixed: bool = False) -> int:
+        d = ctypes.c_int32()
+        check(self._lib.chefsi_solver_get_bounds(self._handle(mixed), None, None, None,
+                                                 ctypes.byref(d)))
+        return d.value
+
+
+def initial_bounds(op: KohnShamOperator, n_wfc: int, k: int = 20, reproducible: bool = False,
+                   v0=None, seed: int = 0):
+    """First-call bounds of kohnShamEigenSpaceCompute (src/dft/kohnShamEigenSolve.cc:335-365)."""
+    lo, up = lanczosLowerUpperBoundEigenSpectrum(op, k, reproducible, v0, seed)
+    blow = lo + (up - lo) / op.n_dofs * n_wfc * (10.0 if reproducible else 200.0)
+    return lo, blow, up

@@ -1,0 +1,622 @@
+// C ABI of the CheFSI library and the solver driver.
+//
+// chefsi_solve follows chebyshevOrthogonalizedSubspaceIterationSolverDevice::solve
+// (src/solvers/eigenSolvers/chebyshevOrthogonalizedSubspaceIterationSolverDevice.cc:155-736)
+// with the CGS / Rayleigh-Ritz-GEP branch: block-wise Chebyshev filtering of all N vectors
+// (chebyWfcBlockSize columns at a time), then the generalised Rayleigh-Ritz step
+// (rayleighRitzGEP, src/linAlg/rayleighRitzDevice.cc:356-819) and the residual norms
+// (computeEigenResidualNorm). Every dense step runs on the device; only eigenvalues,
+// residual norms and bounds come back to the host.
+#include "internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+namespace chefsi {
+const char* last_error_cstr();
+chefsi_operator_s* create_operator(const chefsi_operator_desc* d);
+}  // namespace chefsi
+
+using namespace chefsi;
+
+struct chefsi_solver_s {
+  chefsi_params p{};
+  double a0 = 0.0, b_low = 0.0, b_up = 0.0;
+  int last_degree = 0;
+  DeviceBuffer<double> Xb64, Yb64, S, Hp, T1, Z, W, evals, HX, rot, resid, scal;
+  DeviceBuffer<float> Xb32, Yb32;
+  double times[7] = {0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t ev[8] = {};
+  chefsi_solver_s() {
+    for (auto& e : ev) cudaEventCreate(&e);
+  }
+  ~chefsi_solver_s() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+#define CHEFSI_API_BEGIN try {
+#define CHEFSI_API_END                                        \
+  return CHEFSI_OK;                                           \
+  }                                                           \
+  catch (const chefsi::Error& e) {                            \
+    chefsi::set_last_error(e.what());                         \
+    return e.code;                                            \
+  }                                                           \
+  catch (const std::exception& e) {                           \
+    chefsi::set_last_error(e.what());                         \
+    return CHEFSI_ERR_INVALID;                                \
+  }                                                           \
+  catch (...) {                                               \
+    chefsi::set_last_error("unknown error");                  \
+    return CHEFSI_ERR_INVALID;                                \
+  }
+
+namespace {
+
+const int kOrderLookup[][2] = {{500, 24},    {750, 30},     {1000, 39},    {1500, 50},
+                               {2000, 53},   {3000, 57},    {4000, 62},    {5000, 69},
+                               {9000, 77},   {14000, 104},  {20000, 119},  {30000, 162},
+                               {50000, 300}, {80000, 450},  {100000, 550}, {200000, 700},
+                               {500000, 1000}};
+
+bool is_mixed(int prec) { return prec == CHEFSI_PREC_MIXED || prec == CHEFSI_PREC_FP32; }
+
+// HX of the FP32 filter vectors: tensor cores (FP16 split) for MIXED, SIMT FP32 otherwise
+void hx_filter32(chefsi_operator_s* op, int prec, const float* src, float* dst, int B,
+                 double scalar, bool acc, cudaStream_t st) {
+  if (prec == CHEFSI_PREC_MIXED && hx_tc(op, src, B, dst, B, B, scalar, acc, st)) return;
+  hx_f32(op, src, B, dst, B, B, scalar, acc, st);
+}
+
+// Chebyshev filter (sigma form) of a contiguous block [M][B]; result returned in X.
+// linearAlgebraOperationsDevice::chebyshevFilter, src/linAlg/linearAlgebraOperationsDevice.cc:531-727:
+//   Y = (sigma1/e)(A X - c X);  for degree 2..m: X = alpha2 X - c alpha1 Y;  X += alpha1 A Y; swap.
+// The reference's combinedDeviceKernel step is the axpby; HX accumulates into its output.
+template <typename T, typename HXF>
+void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double a0, HXF hx,
+                 cudaStream_t st) {
+  const double e = (b - a) / 2.0, c = (b + a) / 2.0;
+  double sigma = e / (a0 - c);
+  const double sigma1 = sigma, gamma = 2.0 / sigma1;
+  double alpha1 = sigma1 / e, alpha2 = -c;
+  copy_block<T, T>(X, B, Y, B, M, B, alpha1 * alpha2, st);
+  hx(X, Y, alpha1, true);
+  T* x = X;
+  T* y = Y;
+  for (int degree = 2; degree < m + 1; ++degree) {
+    const double sigma2 = 1.0 / (gamma - sigma);
+    alpha1 = 2.0 * sigma2 / e;
+    alpha2 = -(sigma * sigma2);
+    axpby_block<T>(y, B, x, B, M, B, -c * alpha1, alpha2, st);
+    hx(y, x, alpha1, true);
+    std::swap(x, y);
+    sigma = sigma2;
+  }
+  if (y != X) copy_block<T, T>(y, B, X, B, M, B, 1.0, st);
+}
+
+// filter columns [j0, j0+B) of X (ld) in place
+void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int j0,
+                    int B, int m, double a, double b, double a0, int prec, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  if (!is_mixed(prec)) {
+    double* Xb = s->Xb64.ensure((size_t)M * B);
+    double* Yb = s->Yb64.ensure((size_t)M * B);
+    copy_block<double, double>(X + j0, ld, Xb, B, M, B, 1.0, st);
+    cheb_filter<double>(Xb, Yb, M, B, m, a, b, a0,
+                        [&](const double* src, double* dst, double sc, bool acc) {
+                          hx_f64(op, src, B, dst, B, B, sc, acc, st);
+                        },
+                        st);
+    copy_block<double, double>(Xb, B, X + j0, ld, M, B, 1.0, st);
+    return;
+  }
+  // FP32 block vectors scaled by a power of two so that the largest entry is ~2^8 (keeps the
+  // FP16 split of the tensor-core HX in its normal range; the recurrence is linear)
+  double* sc = s->scal.ensure(1);
+  absmax_block_f64(X + j0, ld, M, B, sc, st);
+  double amax = 0.0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  double scale = 1.0;
+  if (amax > 0.0 && std::isfinite(amax)) scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
+  float* Xb = s->Xb32.ensure((size_t)M * B);
+  float* Yb = s->Yb32.ensure((size_t)M * B);
+  copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
+  cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
+                     [&](const float* src, float* dst, double scv, bool acc) {
+                       hx_filter32(op, prec, src, dst, B, scv, acc, st);
+                     },
+                     st);
+  copy_block<float, double>(Xb, B, X + j0, ld, M, B, 1.0 / scale, st);
+}
+
+void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m, int prec,
+                cudaStream_t st) {
+  const int Bmax = std::max(1, std::min(s->p.cheby_wfc_block > 0 ? s->p.cheby_wfc_block : N, N));
+  for (int j0 = 0; j0 < N; j0 += Bmax) {
+    const int B = std::min(Bmax, N - j0);
+    if (op->is_complex) {
+      cplx* Xc = reinterpret_cast<cplx*>(X);
+      cplx* Xb = reinterpret_cast<cplx*>(s->Xb64.ensure((size_t)op->n_dofs * B * 2));
+      cplx* Yb = reinterpret_cast<cplx*>(s->Yb64.ensure((size_t)op->n_dofs * B * 2));
+      copy_block<cplx, cplx>(Xc + j0, N, Xb, B, op->n_dofs, B, 1.0, st);
+      cheb_filter<cplx>(Xb, Yb, op->n_dofs, B, m, s->b_low, s->b_up, s->a0,
+                        [&](const cplx* src, cplx* dst, double sc, bool acc) {
+                          hx_c64(op, src, B, dst, B, B, sc, acc, st);
+                        },
+                        st);
+      copy_block<cplx, cplx>(Xb, B, Xc + j0, N, op->n_dofs, B, 1.0, st);
+    } else {
+      filter_columns(s, op, reinterpret_cast<double*>(X), N, j0, B, m, s->b_low, s->b_up, s->a0,
+                     prec, st);
+    }
+  }
+}
+
+// FP64 HX of all N columns of X into HX (blocks of wfc_block columns)
+void hx_all_f64(chefsi_operator_s* op, const double* X, int64_t ld, int N, double* HX, int wfc_block,
+                cudaStream_t st) {
+  const int Bmax = std::max(1, std::min(wfc_block > 0 ? wfc_block : N, N));
+  for (int j0 = 0; j0 < N; j0 += Bmax) {
+    const int B = std::min(Bmax, N - j0);
+    hx_f64(op, X + j0, ld, HX + j0, N, B, 1.0, false, st);
+  }
+}
+
+// X[M][N] <- X W (row blocks through a temporary)
+void rotate_rows(chefsi_solver_s* s, double* X, int64_t ld, int64_t M, int N, const double* W,
+                 int prec, cudaStream_t st) {
+  const int64_t rows = std::min<int64_t>(M, std::max<int64_t>(4096, (int64_t)(256ll << 20) / (8ll * N)));
+  double* tmp = s->rot.ensure((size_t)rows * N);
+  for (int64_t r0 = 0; r0 < M; r0 += rows) {
+    const int64_t nr = std::min(rows, M - r0);
+    gemm_f64('N', 'N', nr, N, N, 1.0, X + r0 * ld, ld, W, N, 0.0, tmp, N, prec, st);
+    copy_block<double, double>(tmp, N, X + r0 * ld, ld, nr, N, 1.0, st);
+  }
+}
+
+__global__ void k_negate_diag0(double* S) { S[0] = -fabs(S[0]) - 1.0; }
+
+__global__ void k_transpose(const double* __restrict__ A, double* __restrict__ B, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    B[t] = A[(t % N) * N + t / N];
+}
+
+// Rayleigh-Ritz, generalised form (rayleighRitzGEP): returns eigenvalues (device) and
+// rotates X (and HX if requested) to the Ritz basis.
+int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int N,
+                       int prec, bool want_hx, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  double* S = s->S.ensure((size_t)N * N);
+  double* Hp = s->Hp.ensure((size_t)N * N);
+  double* T1 = s->T1.ensure((size_t)N * N);
+  double* Z = s->Z.ensure((size_t)N * N);
+  double* W = s->W.ensure((size_t)N * N);
+  double* w = s->evals.ensure(N);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  // S = X^T X (lower), then mirrored
+  CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+  gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+  symmetrize_lower(S, N, st);
+  if (fault_injected("not_spd")) {
+    k_negate_diag0<<<1, 1, 0, st>>>(S);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower(S, N, st);  // S now holds L^{-1}
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  // Hp = X^T (A X): FP64 HX in every precision mode
+  double* HX = s->HX.ensure((size_t)M * N);
+  hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
+  gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
+  symmetrize_lower(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  // C = L^{-1} Hp L^{-T}
+  gemm_f64('N', 'N', N, N, N, 1.0, S, N, Hp, N, 0.0, T1, N, CHEFSI_PREC_FP64, st);
+  gemm_f64('N', 'T', N, N, N, 1.0, T1, N, S, N, 0.0, Hp, N, CHEFSI_PREC_FP64, st);
+  symmetrize_lower(Hp, N, st);
+  rc = syevd(Hp, N, w, Z, st);
+  if (rc != CHEFSI_OK) return rc;
+  // W = L^{-T} Q
+  gemm_f64('T', 'N', N, N, N, 1.0, S, N, Z, N, 0.0, W, N, CHEFSI_PREC_FP64, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  rotate_rows(s, X, ld, M, N, W, prec, st);
+  if (want_hx) rotate_rows(s, HX, N, M, N, W, prec, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  return CHEFSI_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.f;
+  }
+  return ms;
+}
+
+chefsi_params default_params() {
+  chefsi_params p{};
+  p.chebyshev_degree = 0;
+  p.cheby_wfc_block = 400;
+  p.wfc_block = 400;
+  p.precision = CHEFSI_PREC_FP64;
+  p.lanczos_steps = 20;
+  p.reproducible = 0;
+  p.first_scf_degree_scale = 1.34;
+  p.keep_hx = 1;
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* chefsi_last_error(void) { return chefsi::last_error_cstr(); }
+const char* chefsi_version(void) { return "chefsi-gb300 0.1 (sm_103a)"; }
+
+int32_t chefsi_chebyshev_order(double upper) {
+  const unsigned ub = upper > 0 ? (unsigned)upper : 0u;
+  for (const auto& e : kOrderLookup)
+    if (ub <= (unsigned)e[0]) return e[1];
+  return 1250;
+}
+
+int chefsi_operator_create(const chefsi_operator_desc* desc, chefsi_operator* out) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(out != nullptr, "null output handle");
+  *out = nullptr;
+  *out = create_operator(desc);
+  CHEFSI_API_END
+}
+
+int chefsi_operator_destroy(chefsi_operator op) {
+  CHEFSI_API_BEGIN
+  delete op;
+  CHEFSI_API_END
+}
+
+int chefsi_operator_info(chefsi_operator op, int64_t* n_dofs, int32_t* n_cells,
+                         int32_t* nodes_per_cell, int32_t* is_complex) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op != nullptr, "null operator");
+  if (n_dofs) *n_dofs = op->n_dofs;
+  if (n_cells) *n_cells = op->n_cells;
+  if (nodes_per_cell) *nodes_per_cell = op->n_e;
+  if (is_complex) *is_complex = op->is_complex;
+  CHEFSI_API_END
+}
+
+int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, int64_t ld_dst,
+              int32_t n_vec, double scalar, int32_t accumulate, int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && src && dst, "null argument");
+  CHEFSI_REQUIRE(n_vec >= 1 && ld_src >= n_vec && ld_dst >= n_vec, "bad block shape");
+  cudaStream_t st = as_stream(stream);
+  if (op->is_complex) {
+    CHEFSI_REQUIRE(precision == CHEFSI_PREC_FP64, "complex operators run in FP64");
+    hx_c64(op, (const cplx*)src, ld_src, (cplx*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+  } else if (precision == CHEFSI_PREC_FP64) {
+    hx_f64(op, (const double*)src, ld_src, (double*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+  } else if (precision == CHEFSI_PREC_MIXED) {
+    if (!hx_tc(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st))
+      throw Error(CHEFSI_ERR_UNSUPPORTED, "tensor-core HX unavailable for this operator");
+  } else if (precision == CHEFSI_PREC_FP32) {
+    hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+  } else {
+    throw Error(CHEFSI_ERR_INVALID, "unknown precision");
+  }
+  CHEFSI_API_END
+}
+
+int chefsi_overlap(chefsi_operator op, const void* X, int64_t ld, int32_t N, double* S,
+                   int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && S && N >= 1 && ld >= N, "bad argument");
+  cudaStream_t st = as_stream(stream);
+  if (op->is_complex) {
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * 2 * N * N, st));
+    gram_c64((const cplx*)X, ld, (const cplx*)X, ld, op->n_dofs, N, N, (cplx*)S, N, true, st);
+    symmetrize_lower_c((cplx*)S, N, st);
+  } else {
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+    gram_f64((const double*)X, ld, (const double*)X, ld, op->n_dofs, N, N, S, N, precision, true, st);
+    symmetrize_lower(S, N, st);
+  }
+  CHEFSI_API_END
+}
+
+int chefsi_xthx(chefsi_operator op, const void* X, int64_t ld, int32_t N, double* Hp,
+                int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && Hp && N >= 1 && ld >= N, "bad argument");
+  cudaStream_t st = as_stream(stream);
+  const int64_t M = op->n_dofs;
+  if (op->is_complex) {
+    DeviceBuffer<double> HX((size_t)M * N * 2);
+    hx_c64(op, (const cplx*)X, ld, (cplx*)HX.ptr, N, N, 1.0, false, st);
+    CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * 2 * N * N, st));
+    gram_c64((const cplx*)X, ld, (const cplx*)HX.ptr, N, M, N, N, (cplx*)Hp, N, true, st);
+    symmetrize_lower_c((cplx*)Hp, N, st);
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+  } else {
+    DeviceBuffer<double> HX((size_t)M * N);
+    hx_all_f64(op, (const double*)X, ld, N, HX.ptr, 400, st);
+    CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
+    gram_f64((const double*)X, ld, HX.ptr, N, M, N, N, Hp, N, precision, true, st);
+    symmetrize_lower(Hp, N, st);
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+  }
+  CHEFSI_API_END
+}
+
+int chefsi_chebyshev_filter(chefsi_operator op, void* X, int64_t ld, int32_t n_vec, int32_t m,
+                            double a, double b, double a0, int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && n_vec >= 1 && ld >= n_vec && m >= 1, "bad argument");
+  CHEFSI_REQUIRE(b > a, "need b > a");
+  cudaStream_t st = as_stream(stream);
+  chefsi_solver_s tmp;
+  tmp.p = default_params();
+  tmp.p.cheby_wfc_block = n_vec;
+  tmp.a0 = a0;
+  tmp.b_low = a;
+  tmp.b_up = b;
+  if (op->is_complex) {
+    CHEFSI_REQUIRE(ld == n_vec, "complex filter needs ld == n_vec");
+    filter_all(&tmp, op, X, n_vec, m, CHEFSI_PREC_FP64, st);
+  } else {
+    filter_columns(&tmp, op, (double*)X, ld, 0, n_vec, m, a, b, a0, precision, st);
+  }
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_syevd(int32_t N, double* A, double* w, double* Z, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(A && w && Z && N >= 1, "bad argument");
+  int rc = syevd(A, N, w, Z, as_stream(stream));
+  if (rc != CHEFSI_OK) return rc;
+  CHEFSI_API_END
+}
+
+int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible, const double* v0_host,
+                          uint64_t seed, double* lower, double* upper, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && lower && upper && k >= 2, "bad argument");
+  CHEFSI_REQUIRE(!op->is_complex, "Lanczos bounds: complex operators not supported");
+  cudaStream_t st = as_stream(stream);
+  const int64_t M = op->n_dofs;
+  std::vector<double> h(M);
+  if (v0_host) {
+    std::memcpy(h.data(), v0_host, sizeof(double) * M);
+  } else {
+    std::mt19937_64 gen(seed);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    for (auto& x : h) x = U(gen);
+  }
+  DeviceBuffer<double> v(M), v0(M), f(M), sc(1);
+  CHEFSI_CUDA(cudaMemcpyAsync(v.ptr, h.data(), sizeof(double) * M, cudaMemcpyHostToDevice, st));
+  auto dot = [&](const double* x, const double* y) {
+    double r = 0.0;
+    dot_f64(x, y, M, sc.ptr, st);
+    CHEFSI_CUDA(cudaMemcpyAsync(&r, sc.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+    return r;
+  };
+  const double n0 = std::sqrt(dot(v.ptr, v.ptr));
+  CHEFSI_REQUIRE(n0 > 0.0, "Lanczos start vector is zero");
+  scale_block<double>(v.ptr, 1, M, 1, 1.0 / n0, st);
+  hx_f64(op, v.ptr, 1, f.ptr, 1, 1, 1.0, false, st);
+  double alpha = dot(f.ptr, v.ptr);
+  axpby_block<double>(v.ptr, 1, f.ptr, 1, M, 1, -alpha, 1.0, st);
+  std::vector<double> T((size_t)k * k, 0.0);
+  T[0] = alpha;
+  for (int j = 1; j < k; ++j) {
+    const double beta = std::sqrt(dot(f.ptr, f.ptr));
+    CHEFSI_CUDA(cudaMemcpyAsync(v0.ptr, v.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
+    copy_block<double, double>(f.ptr, 1, v.ptr, 1, M, 1, 1.0 / beta, st);
+    hx_f64(op, v.ptr, 1, f.ptr, 1, 1, 1.0, false, st);
+    axpby_block<double>(v0.ptr, 1, f.ptr, 1, M, 1, -beta, 1.0, st);
+    alpha = dot(f.ptr, v.ptr);
+    axpby_block<double>(v.ptr, 1, f.ptr, 1, M, 1, -alpha, 1.0, st);
+    T[(size_t)j * k + j - 1] = beta;
+    T[(size_t)(j - 1) * k + j] = beta;
+    T[(size_t)j * k + j] = alpha;
+  }
+  const double fn = std::sqrt(dot(f.ptr, f.ptr));
+  DeviceBuffer<double> dT((size_t)k * k), dw(k), dZ((size_t)k * k);
+  CHEFSI_CUDA(cudaMemcpyAsync(dT.ptr, T.data(), sizeof(double) * k * k, cudaMemcpyHostToDevice, st));
+  int rc = syevd(dT.ptr, k, dw.ptr, dZ.ptr, st);
+  if (rc != CHEFSI_OK) return rc;
+  std::vector<double> w(k);
+  CHEFSI_CUDA(cudaMemcpyAsync(w.data(), dw.ptr, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  std::sort(w.begin(), w.end());
+  *lower = std::floor(w[0]);
+  *upper = std::ceil(w[k - 1] + (reproducible ? fn : fn / 10.0));
+  CHEFSI_API_END
+}
+
+int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32_t precision,
+                       void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && N >= 1 && ld >= N, "bad argument");
+  CHEFSI_REQUIRE(!op->is_complex, "Cholesky-GS: complex operators not supported");
+  cudaStream_t st = as_stream(stream);
+  chefsi_solver_s s;
+  s.p = default_params();
+  double* S = s.S.ensure((size_t)N * N);
+  double* W = s.W.ensure((size_t)N * N);
+  CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+  gram_f64((double*)X, ld, (double*)X, ld, op->n_dofs, N, N, S, N, precision, true, st);
+  symmetrize_lower(S, N, st);
+  if (fault_injected("not_spd")) {
+    k_negate_diag0<<<1, 1, 0, st>>>(S);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower(S, N, st);
+  // X <- X L^{-T}
+  k_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);
+  CHEFSI_CHECK_LAUNCH();
+  rotate_rows(&s, (double*)X, ld, op->n_dofs, N, W, precision, st);
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
+                         double* HX_out, int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && eig_host && N >= 1 && ld >= N, "bad argument");
+  CHEFSI_REQUIRE(!op->is_complex, "Rayleigh-Ritz: complex operators not supported");
+  cudaStream_t st = as_stream(stream);
+  chefsi_solver_s s;
+  s.p = default_params();
+  int rc = rayleigh_ritz_real(&s, op, (double*)X, ld, N, precision, HX_out != nullptr, st);
+  if (rc != CHEFSI_OK) return rc;
+  if (HX_out)
+    CHEFSI_CUDA(cudaMemcpyAsync(HX_out, s.HX.ptr, sizeof(double) * op->n_dofs * N,
+                                cudaMemcpyDeviceToDevice, st));
+  CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,
+                          const double* eig_host, double* res_host, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && eig_host && res_host && N >= 1 && ld >= N, "bad argument");
+  cudaStream_t st = as_stream(stream);
+  const int64_t M = op->n_dofs;
+  DeviceBuffer<double> lam(N), out(N);
+  CHEFSI_CUDA(cudaMemcpyAsync(lam.ptr, eig_host, sizeof(double) * N, cudaMemcpyHostToDevice, st));
+  if (op->is_complex) {
+    DeviceBuffer<double> HX((size_t)M * N * 2);
+    hx_c64(op, (const cplx*)X, ld, (cplx*)HX.ptr, N, N, 1.0, false, st);
+    residual_norms_c64((const cplx*)X, ld, (const cplx*)HX.ptr, N, M, N, lam.ptr, out.ptr, st);
+  } else {
+    DeviceBuffer<double> HX((size_t)M * N);
+    hx_all_f64(op, (const double*)X, ld, N, HX.ptr, 400, st);
+    residual_norms_f64((const double*)X, ld, HX.ptr, N, M, N, lam.ptr, out.ptr, st);
+  }
+  CHEFSI_CUDA(cudaMemcpyAsync(res_host, out.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_solver_create(const chefsi_params* params, chefsi_solver* out) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(out != nullptr, "null output handle");
+  auto* s = new chefsi_solver_s();
+  s->p = params ? *params : default_params();
+  if (s->p.cheby_wfc_block <= 0) s->p.cheby_wfc_block = 400;
+  if (s->p.wfc_block <= 0) s->p.wfc_block = 400;
+  if (s->p.lanczos_steps <= 0) s->p.lanczos_steps = s->p.reproducible ? 40 : 20;
+  if (s->p.first_scf_degree_scale <= 0) s->p.first_scf_degree_scale = 1.0;
+  *out = s;
+  CHEFSI_API_END
+}
+
+int chefsi_solver_destroy(chefsi_solver s) {
+  CHEFSI_API_BEGIN
+  delete s;
+  CHEFSI_API_END
+}
+
+int chefsi_solver_reinit_spectrum_bounds(chefsi_solver s, double lower_wanted,
+                                         double lower_unwanted, double upper_unwanted) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s != nullptr, "null solver");
+  s->a0 = lower_wanted;
+  s->b_low = lower_unwanted;
+  s->b_up = upper_unwanted;
+  CHEFSI_API_END
+}
+
+int chefsi_solver_get_bounds(chefsi_solver s, double* a0, double* bl, double* bu, int32_t* deg) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s != nullptr, "null solver");
+  if (a0) *a0 = s->a0;
+  if (bl) *bl = s->b_low;
+  if (bu) *bu = s->b_up;
+  if (deg) *deg = s->last_degree;
+  CHEFSI_API_END
+}
+
+int chefsi_solver_timings(chefsi_solver s, double* ms7) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s && ms7, "bad argument");
+  for (int i = 0; i < 7; ++i) ms7[i] = s->times[i];
+  CHEFSI_API_END
+}
+
+static int degree_for(chefsi_solver_s* s, int is_first_scf) {
+  int m = s->p.chebyshev_degree > 0 ? s->p.chebyshev_degree : chefsi_chebyshev_order(s->b_up);
+  if (is_first_scf) m = (int)(m * s->p.first_scf_degree_scale);
+  return std::max(1, m);
+}
+
+int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
+                 double* res_host, int32_t compute_residual, int32_t is_first_scf, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s && op && X && eig_host && N >= 1, "bad argument");
+  CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
+  CHEFSI_REQUIRE(!op->is_complex, "chefsi_solve: complex operators not supported");
+  cudaStream_t st = as_stream(stream);
+  const int prec = s->p.precision;
+  const int m = degree_for(s, is_first_scf);
+  s->last_degree = m;
+  CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
+  filter_all(s, op, X, N, m, prec, st);
+  int rc = rayleigh_ritz_real(s, op, (double*)X, N, N, prec, true, st);
+  if (rc != CHEFSI_OK) return rc;
+  const int64_t M = op->n_dofs;
+  double* res = s->resid.ensure(N);
+  if (compute_residual) residual_norms_f64((double*)X, N, s->HX.ptr, N, M, N, s->evals.ptr, res, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[6], st));
+  CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s->evals.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  if (compute_residual && res_host)
+    CHEFSI_CUDA(cudaMemcpyAsync(res_host, res, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  s->times[0] = elapsed(s->ev[0], s->ev[1]);
+  s->times[1] = elapsed(s->ev[1], s->ev[2]);
+  s->times[2] = elapsed(s->ev[2], s->ev[3]);
+  s->times[3] = elapsed(s->ev[3], s->ev[4]);
+  s->times[4] = elapsed(s->ev[4], s->ev[5]);
+  s->times[5] = elapsed(s->ev[5], s->ev[6]);
+  s->times[6] = elapsed(s->ev[0], s->ev[6]);
+  CHEFSI_API_END
+}
+
+int chefsi_solve_no_rr(chefsi_solver s, chefsi_operator op, void* X, int32_t N, int32_t n_passes,
+                       int32_t is_first_scf, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s && op && X && N >= 1 && n_passes >= 1, "bad argument");
+  CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set");
+  cudaStream_t st = as_stream(stream);
+  const int m = degree_for(s, is_first_scf);
+  s->last_degree = m;
+  for (int p = 0; p < n_passes; ++p) filter_all(s, op, X, N, m, s->p.precision, st);
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+}  // extern "C"

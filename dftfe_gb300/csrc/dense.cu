@@ -1,0 +1,848 @@
+// Dense linear algebra of the CheFSI Rayleigh-Ritz step, all on the device:
+//   * split-K Gram products C += A^H B over the long dof dimension (overlap X^H X and
+//     projected Hamiltonian X^H (HX); fillParallelOverlapMatScalapack / XtHX in DFT-FE);
+//   * a general row-major GEMM (subspace rotation X <- X Q, small N x N products);
+//   * blocked Cholesky, triangular inverse (the ELPA/ScaLAPACK steps of rayleighRitzGEP);
+//   * a symmetric eigensolver: Householder tridiagonalisation, Sturm-count bisection,
+//     inverse iteration with re-orthogonalisation inside clusters, back-transformation;
+//   * column residual norms.
+// FP64 on GB300 runs at roughly 1/64 of the FP32 rate, so the mixed-precision variants of the
+// Gram and rotation products compute in FP32 inside K chunks of 256 and carry FP64 across
+// chunks (errors stay at FP32 rounding of each chunk, unbiased, instead of growing with K).
+#include "internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace chefsi {
+
+__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__device__ __forceinline__ cplx cconj(cplx a) { return {a.x, -a.y}; }
+
+// ======================================================================= Gram (split K)
+// C[i][j] += sum_k A[k][i] * B[k][j]. Tile 64x64, 256 threads (4x4 per thread, strided).
+// Tc: compute type inside a chunk; every kChunk rows the chunk sum is added to FP64.
+constexpr int GT = 64, GK = 16;
+
+template <typename Tc>
+__global__ void __launch_bounds__(256)
+    gram_kernel(const double* __restrict__ A, int64_t lda, const double* __restrict__ B,
+                int64_t ldb, int64_t K, int N1, int N2, double* __restrict__ C, int ldc,
+                int64_t k_per_split, int ntj, int lower_only, int chunk) {
+  __shared__ Tc As[GK][GT];
+  __shared__ Tc Bs[GK][GT];
+  const int tile = blockIdx.x;
+  const int ti = tile / ntj, tj = tile % ntj;
+  if (lower_only && tj > ti) return;
+  const int i0 = ti * GT, j0 = tj * GT;
+  const int64_t k_begin = (int64_t)blockIdx.y * k_per_split;
+  const int64_t k_end = min(K, k_begin + k_per_split);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4];
+  Tc part[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) acc[r][s] = 0.0, part[r][s] = (Tc)0;
+  int since = 0;
+  for (int64_t k0 = k_begin; k0 < k_end; k0 += GK) {
+    for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
+      const int k = idx / GT, c = idx % GT;
+      const int64_t gk = k0 + k;
+      As[k][c] = (gk < k_end && i0 + c < N1) ? (Tc)A[gk * lda + i0 + c] : (Tc)0;
+      Bs[k][c] = (gk < k_end && j0 + c < N2) ? (Tc)B[gk * ldb + j0 + c] : (Tc)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < GK; ++k) {
+      Tc a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[k][ty + 16 * r];
+#pragma unroll
+      for (int s = 0; s < 4; ++s) b[s] = Bs[k][tx + 16 * s];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) part[r][s] = fma(a[r], b[s], part[r][s]);
+    }
+    __syncthreads();
+    since += GK;
+    if (since >= chunk) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) acc[r][s] += (double)part[r][s], part[r][s] = (Tc)0;
+      since = 0;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * s;
+      if (i < N1 && j < N2) atomicAdd(&C[(int64_t)i * ldc + j], acc[r][s] + (double)part[r][s]);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    gram_kernel_c(const cplx* __restrict__ A, int64_t lda, const cplx* __restrict__ B, int64_t ldb,
+                  int64_t K, int N1, int N2, cplx* __restrict__ C, int ldc, int64_t k_per_split,
+                  int ntj, int lower_only) {
+  constexpr int T = 32;
+  __shared__ cplx As[GK][T];
+  __shared__ cplx Bs[GK][T];
+  const int tile = blockIdx.x;
+  const int ti = tile / ntj, tj = tile % ntj;
+  if (lower_only && tj > ti) return;
+  const int i0 = ti * T, j0 = tj * T;
+  const int64_t k_begin = (int64_t)blockIdx.y * k_per_split;
+  const int64_t k_end = min(K, k_begin + k_per_split);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 per thread
+  cplx acc[2][2];
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) acc[r][s] = {0.0, 0.0};
+  for (int64_t k0 = k_begin; k0 < k_end; k0 += GK) {
+    for (int idx = threadIdx.x; idx < GK * T; idx += 256) {
+      const int k = idx / T, c = idx % T;
+      const int64_t gk = k0 + k;
+      As[k][c] = (gk < k_end && i0 + c < N1) ? A[gk * lda + i0 + c] : cplx{0.0, 0.0};
+      Bs[k][c] = (gk < k_end && j0 + c < N2) ? B[gk * ldb + j0 + c] : cplx{0.0, 0.0};
+    }
+    __syncthreads();
+    for (int k = 0; k < GK; ++k)
+      for (int r = 0; r < 2; ++r)
+        for (int s = 0; s < 2; ++s)
+          acc[r][s] = cadd(acc[r][s], cmul(cconj(As[k][ty + 16 * r]), Bs[k][tx + 16 * s]));
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * s;
+      if (i < N1 && j < N2) {
+        atomicAdd(&C[(int64_t)i * ldc + j].x, acc[r][s].x);
+        atomicAdd(&C[(int64_t)i * ldc + j].y, acc[r][s].y);
+      }
+    }
+}
+
+static int64_t choose_split(int64_t K, int tiles, int64_t min_rows) {
+  int64_t want = std::max<int64_t>(1, (int64_t)kNumSMs * 4 / std::max(1, tiles));
+  int64_t per = (K + want - 1) / want;
+  per = std::max<int64_t>(per, min_rows);
+  per = (per + GK - 1) / GK * GK;
+  return per;
+}
+
+void gram_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t K, int N1,
+              int N2, double* C, int ldc, int prec, bool lower_only, cudaStream_t st) {
+  const int nti = (N1 + GT - 1) / GT, ntj = (N2 + GT - 1) / GT;
+  const int tiles = lower_only ? nti * (nti + 1) / 2 : nti * ntj;
+  const int64_t per = choose_split(K, tiles, 256);
+  const int64_t splits = (K + per - 1) / per;
+  CHEFSI_REQUIRE(splits < 65536, "gram split too large");
+  dim3 grid(nti * ntj, (unsigned)splits);
+  if (prec == CHEFSI_PREC_FP64)
+    gram_kernel<double><<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj,
+                                              lower_only, 1 << 30);
+  else
+    gram_kernel<float><<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj,
+                                             lower_only, 256);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void gram_c64(const cplx* A, int64_t lda, const cplx* B, int64_t ldb, int64_t K, int N1, int N2,
+              cplx* C, int ldc, bool lower_only, cudaStream_t st) {
+  const int nti = (N1 + 31) / 32, ntj = (N2 + 31) / 32;
+  const int tiles = lower_only ? nti * (nti + 1) / 2 : nti * ntj;
+  const int64_t per = choose_split(K, tiles, 256);
+  const int64_t splits = (K + per - 1) / per;
+  CHEFSI_REQUIRE(splits < 65536, "gram split too large");
+  dim3 grid(nti * ntj, (unsigned)splits);
+  gram_kernel_c<<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj, lower_only);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// ======================================================================= GEMM
+// C[M][N] = alpha op(A) op(B) + beta C, row-major. op(A)[m][k] = ta=='N' ? A[m][k] : A[k][m].
+template <typename Tc>
+__global__ void __launch_bounds__(256)
+    gemm_kernel(int ta, int tb, int64_t M, int N, int K, double alpha,
+                const double* __restrict__ A, int64_t lda, const double* __restrict__ B,
+                int64_t ldb, double beta, double* __restrict__ C, int64_t ldc, int chunk) {
+  __shared__ Tc As[GK][GT + 1];
+  __shared__ Tc Bs[GK][GT];
+  const int64_t m0 = (int64_t)blockIdx.x * GT;
+  const int n0 = blockIdx.y * GT;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4];
+  Tc part[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) acc[r][s] = 0.0, part[r][s] = (Tc)0;
+  int since = 0;
+  for (int k0 = 0; k0 < K; k0 += GK) {
+    for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
+      int k, mm;
+      if (ta) {  // A is [K][M]: contiguous along m
+        k = idx / GT, mm = idx % GT;
+      } else {  // A is [M][K]: contiguous along k
+        mm = idx / GK, k = idx % GK;
+      }
+      const int64_t gm = m0 + mm;
+      const int gk = k0 + k;
+      double v = 0.0;
+      if (gm < M && gk < K) v = ta ? A[(int64_t)gk * lda + gm] : A[gm * lda + gk];
+      As[k][mm] = (Tc)v;
+    }
+    for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
+      int k, nn;
+      if (tb) {  // B is [N][K]
+        nn = idx / GK, k = idx % GK;
+      } else {  // B is [K][N]
+        k = idx / GT, nn = idx % GT;
+      }
+      const int gn = n0 + nn, gk = k0 + k;
+      double v = 0.0;
+      if (gn < N && gk < K) v = tb ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn];
+      Bs[k][nn] = (Tc)v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < GK; ++k) {
+      Tc a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[k][ty + 16 * r];
+#pragma unroll
+      for (int s = 0; s < 4; ++s) b[s] = Bs[k][tx + 16 * s];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) part[r][s] = fma(a[r], b[s], part[r][s]);
+    }
+    __syncthreads();
+    since += GK;
+    if (since >= chunk) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int s = 0; s < 4; ++s) acc[r][s] += (double)part[r][s], part[r][s] = (Tc)0;
+      since = 0;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int64_t m = m0 + ty + 16 * r;
+      const int n = n0 + tx + 16 * s;
+      if (m < M && n < N) {
+        const double v = alpha * (acc[r][s] + (double)part[r][s]);
+        double* c = &C[m * ldc + n];
+        *c = (beta == 0.0) ? v : v + beta * *c;
+      }
+    }
+}
+
+void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const double* A, int64_t lda,
+              const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int prec,
+              cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid((unsigned)((M + GT - 1) / GT), (N + GT - 1) / GT);
+  CHEFSI_REQUIRE(grid.y < 65536, "gemm N too large");
+  const int ita = (ta == 'T' || ta == 't' || ta == 'C' || ta == 'c');
+  const int itb = (tb == 'T' || tb == 't' || tb == 'C' || tb == 'c');
+  if (prec == CHEFSI_PREC_FP64)
+    gemm_kernel<double><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                              ldc, 1 << 30);
+  else
+    gemm_kernel<float><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                             ldc, 256);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// complex GEMM (FP64), 32x32 tiles, 2x2 per thread
+__global__ void __launch_bounds__(256)
+    gemm_kernel_c(int ta, int tb, int64_t M, int N, int K, cplx alpha, const cplx* __restrict__ A,
+                  int64_t lda, const cplx* __restrict__ B, int64_t ldb, cplx beta,
+                  cplx* __restrict__ C, int64_t ldc) {
+  constexpr int T = 32;
+  __shared__ cplx As[GK][T + 1];
+  __shared__ cplx Bs[GK][T];
+  const int64_t m0 = (int64_t)blockIdx.x * T;
+  const int n0 = blockIdx.y * T;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  cplx acc[2][2];
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) acc[r][s] = {0.0, 0.0};
+  for (int k0 = 0; k0 < K; k0 += GK) {
+    for (int idx = threadIdx.x; idx < GK * T; idx += 256) {
+      const int k = idx / T, mm = idx % T;
+      const int64_t gm = m0 + mm;
+      const int gk = k0 + k;
+      cplx v = {0.0, 0.0};
+      if (gm < M && gk < K) v = ta ? cconj(A[(int64_t)gk * lda + gm]) : A[gm * lda + gk];
+      As[k][mm] = v;
+      const int gn = n0 + mm;
+      cplx w = {0.0, 0.0};
+      if (gn < N && gk < K) w = tb ? cconj(B[(int64_t)gn * ldb + gk]) : B[(int64_t)gk * ldb + gn];
+      Bs[k][mm] = w;
+    }
+    __syncthreads();
+    for (int k = 0; k < GK; ++k)
+      for (int r = 0; r < 2; ++r)
+        for (int s = 0; s < 2; ++s)
+          acc[r][s] = cadd(acc[r][s], cmul(As[k][ty + 16 * r], Bs[k][tx + 16 * s]));
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int64_t m = m0 + ty + 16 * r;
+      const int n = n0 + tx + 16 * s;
+      if (m < M && n < N) {
+        cplx v = cmul(alpha, acc[r][s]);
+        cplx* c = &C[m * ldc + n];
+        if (beta.x != 0.0 || beta.y != 0.0) v = cadd(v, cmul(beta, *c));
+        *c = v;
+      }
+    }
+}
+
+void gemm_c64(char ta, char tb, int64_t M, int N, int K, cplx alpha, const cplx* A, int64_t lda,
+              const cplx* B, int64_t ldb, cplx beta, cplx* C, int64_t ldc, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid((unsigned)((M + 31) / 32), (N + 31) / 32);
+  const int ita = (ta != 'N' && ta != 'n');
+  const int itb = (tb != 'N' && tb != 'n');
+  gemm_kernel_c<<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// ======================================================================= small helpers
+__global__ void k_symmetrize_lower(double* A, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (j > i) A[t] = A[(int64_t)j * N + i];
+  }
+}
+void symmetrize_lower(double* A, int N, cudaStream_t st) {
+  k_symmetrize_lower<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(A, N);
+  CHEFSI_CHECK_LAUNCH();
+}
+__global__ void k_symmetrize_lower_c(cplx* A, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (j > i) A[t] = cconj(A[(int64_t)j * N + i]);
+    if (j == i) A[t].y = 0.0;
+  }
+}
+void symmetrize_lower_c(cplx* A, int N, cudaStream_t st) {
+  k_symmetrize_lower_c<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(A, N);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// ======================================================================= Cholesky
+constexpr int CB = 32;
+
+// unblocked Cholesky of the nb x nb diagonal block at (k0, k0); flag set on a bad pivot
+__global__ void k_potf2(double* A, int N, int k0, int nb, int* info) {
+  __shared__ double L[CB][CB + 1];
+  const int t = threadIdx.x;  // CB threads
+  for (int i = 0; i < nb; ++i)
+    if (t < nb) L[i][t] = A[(int64_t)(k0 + i) * N + k0 + t];
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (t == 0) {
+      const double djj = L[j][j];
+      if (!(djj > 0.0) || !isfinite(djj)) {
+        atomicCAS(info, 0, k0 + j + 1);
+        L[j][j] = 1.0;
+      } else {
+        L[j][j] = sqrt(djj);
+      }
+    }
+    __syncthreads();
+    if (t > j && t < nb) L[t][j] /= L[j][j];
+    __syncthreads();
+    // trailing update of the lower part, column by column
+    if (t > j && t < nb)
+      for (int i = t; i < nb; ++i) L[i][t] -= L[i][j] * L[t][j];
+    __syncthreads();
+  }
+  for (int i = 0; i < nb; ++i)
+    if (t < nb) A[(int64_t)(k0 + i) * N + k0 + t] = (t <= i) ? L[i][t] : 0.0;
+}
+
+// rows r >= k0+nb: A[r][k0:k0+nb] <- A[r][k0:k0+nb] L11^{-T}
+__global__ void k_trsm_panel(double* A, int N, int k0, int nb) {
+  __shared__ double L[CB][CB + 1];
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x)
+    L[idx / nb][idx % nb] = A[(int64_t)(k0 + idx / nb) * N + k0 + idx % nb];
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  double x[CB];
+  double* row = A + (int64_t)r * N + k0;
+  for (int j = 0; j < nb; ++j) {
+    double v = row[j];
+    for (int l = 0; l < j; ++l) v -= x[l] * L[j][l];
+    x[j] = v / L[j][j];
+  }
+  for (int j = 0; j < nb; ++j) row[j] = x[j];
+}
+
+__global__ void k_zero_upper(double* A, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    if ((int)(t % N) > (int)(t / N)) A[t] = 0.0;
+}
+
+int cholesky_lower(double* A, int N, cudaStream_t st) {
+  DeviceBuffer<int> info(1);
+  CHEFSI_CUDA(cudaMemsetAsync(info.ptr, 0, sizeof(int), st));
+  for (int k0 = 0; k0 < N; k0 += CB) {
+    const int nb = std::min(CB, N - k0);
+    k_potf2<<<1, CB, 0, st>>>(A, N, k0, nb, info.ptr);
+    CHEFSI_CHECK_LAUNCH();
+    const int rest = N - k0 - nb;
+    if (rest > 0) {
+      k_trsm_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, N, k0, nb);
+      CHEFSI_CHECK_LAUNCH();
+      // A22 -= L21 L21^T (full trailing square; the upper part is zeroed at the end)
+      const int64_t off = (int64_t)(k0 + nb) * N;
+      gemm_f64('N', 'T', rest, rest, nb, -1.0, A + off + k0, N, A + off + k0, N, 1.0,
+               A + off + k0 + nb, N, CHEFSI_PREC_FP64, st);
+    }
+  }
+  k_zero_upper<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(A, N);
+  CHEFSI_CHECK_LAUNCH();
+  int h = 0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&h, info.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  return h ? CHEFSI_ERR_NOT_SPD : CHEFSI_OK;
+}
+
+// ======================================================================= triangular inverse
+// invert each CB x CB diagonal block of the lower-triangular L in place
+__global__ void k_trtri_diag(double* L, int N) {
+  __shared__ double T[CB][CB + 1];
+  __shared__ double Z[CB][CB + 1];
+  const int k0 = blockIdx.x * CB;
+  const int nb = min(CB, N - k0);
+  const int t = threadIdx.x;
+  for (int i = 0; i < nb; ++i)
+    if (t < nb) T[i][t] = L[(int64_t)(k0 + i) * N + k0 + t], Z[i][t] = 0.0;
+  __syncthreads();
+  // column t of the inverse by forward substitution
+  if (t < nb) {
+    for (int i = 0; i < nb; ++i) {
+      double v = (i == t) ? 1.0 : 0.0;
+      for (int l = t; l < i; ++l) v -= T[i][l] * Z[l][t];
+      Z[i][t] = (i >= t) ? v / T[i][i] : 0.0;
+    }
+  }
+  __syncthreads();
+  for (int i = 0; i < nb; ++i)
+    if (t < nb) L[(int64_t)(k0 + i) * N + k0 + t] = Z[i][t];
+}
+
+void trtri_lower(double* L, int N, cudaStream_t st) {
+  const int nblk = (N + CB - 1) / CB;
+  // Z = L^{-1}: first invert diagonal blocks, then block rows top-down:
+  // Z[i, 0:i] = -Z_ii * (L[i, 0:i] * Z[0:i, 0:i])
+  k_trtri_diag<<<nblk, CB, 0, st>>>(L, N);
+  CHEFSI_CHECK_LAUNCH();
+  DeviceBuffer<double> tmp((size_t)CB * N);
+  for (int bi = 1; bi < nblk; ++bi) {
+    const int r0 = bi * CB;
+    const int nb = std::min(CB, N - r0);
+    // tmp[nb][r0] = L[r0:r0+nb, 0:r0] * Z[0:r0, 0:r0]
+    gemm_f64('N', 'N', nb, r0, r0, 1.0, L + (int64_t)r0 * N, N, L, N, 0.0, tmp.ptr, r0,
+             CHEFSI_PREC_FP64, st);
+    // L[r0:r0+nb, 0:r0] = -Z_ii * tmp
+    gemm_f64('N', 'N', nb, r0, nb, -1.0, L + (int64_t)r0 * N + r0, N, tmp.ptr, r0, 0.0,
+             L + (int64_t)r0 * N, N, CHEFSI_PREC_FP64, st);
+  }
+}
+
+// ======================================================================= eigensolver
+// Householder step k on the symmetric row-major A (full storage maintained):
+// x = A[k+1:N, k]; v = x - alpha e1 with alpha = -sign(x0) |x|; tau = 2 / v^T v.
+// The reflector is kept in V[k][k+1:N] with tau[k]; d[k] = A[k][k], e[k] = alpha.
+__global__ void k_hh_vector(double* A, int N, int k, double* V, double* tau, double* d, double* e) {
+  __shared__ double red[32];
+  const int n = N - k - 1;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = A[(int64_t)(k + 1 + i) * N + k];
+    s += x * x;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) red[0] = s;
+  }
+  __syncthreads();
+  const double nrm2 = red[0];
+  const double x0 = A[(int64_t)(k + 1) * N + k];
+  const double nrm = sqrt(nrm2);
+  const double alpha = (x0 >= 0.0) ? -nrm : nrm;
+  // v^T v = nrm2 - 2 alpha x0 + alpha^2 = 2 (nrm2 - alpha x0)
+  const double vtv = 2.0 * (nrm2 - alpha * x0);
+  const bool skip = !(vtv > 0.0) || nrm == 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = A[(int64_t)(k + 1 + i) * N + k];
+    V[(int64_t)k * N + k + 1 + i] = skip ? 0.0 : (i == 0 ? x - alpha : x);
+  }
+  if (threadIdx.x == 0) {
+    tau[k] = skip ? 0.0 : 2.0 / vtv;
+    d[k] = A[(int64_t)k * N + k];
+    e[k] = skip ? x0 : alpha;
+  }
+}
+
+// p = tau * A22 v   (one warp per row of the trailing block)
+__global__ void k_hh_symv(const double* __restrict__ A, int N, int k, const double* __restrict__ V,
+                          const double* __restrict__ tau, double* __restrict__ p) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n = N - k - 1;
+  if (warp >= n) return;
+  const double* row = A + (int64_t)(k + 1 + warp) * N + k + 1;
+  const double* v = V + (int64_t)k * N + k + 1;
+  double s = 0.0;
+  for (int j = lane; j < n; j += 32) s += row[j] * v[j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) p[warp] = tau[k] * s;
+}
+
+// w = p - (tau/2)(p^T v) v   (single CTA)
+__global__ void k_hh_w(int N, int k, const double* __restrict__ V, const double* __restrict__ tau,
+                       double* p) {
+  __shared__ double red[32];
+  const int n = N - k - 1;
+  const double* v = V + (int64_t)k * N + k + 1;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i] * v[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) red[0] = s;
+  }
+  __syncthreads();
+  const double f = 0.5 * tau[k] * red[0];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] -= f * v[i];
+}
+
+// A22 -= v w^T + w v^T
+__global__ void k_hh_rank2(double* A, int N, int k, const double* __restrict__ V,
+                           const double* __restrict__ w) {
+  const int n = N - k - 1;
+  const int64_t tot = (int64_t)n * n;
+  const double* v = V + (int64_t)k * N + k + 1;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    A[(int64_t)(k + 1 + i) * N + k + 1 + j] -= v[i] * w[j] + w[i] * v[j];
+  }
+}
+
+__global__ void k_tail(const double* A, int N, double* d, double* e) {
+  if (threadIdx.x == 0) {
+    if (N >= 2) {
+      d[N - 2] = A[(int64_t)(N - 2) * N + N - 2];
+      e[N - 2] = A[(int64_t)(N - 1) * N + N - 2];
+    }
+    d[N - 1] = A[(int64_t)(N - 1) * N + N - 1];
+  }
+}
+
+// number of eigenvalues of the tridiagonal (d, e) below x (Sturm sequence)
+__device__ int sturm_count(const double* d, const double* e, int n, double x, double pivmin) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0) ++cnt;
+  for (int j = 1; j < n; ++j) {
+    q = d[j] - x - e[j - 1] * e[j - 1] / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0) ++cnt;
+  }
+  return cnt;
+}
+
+__global__ void k_bisect(const double* __restrict__ d, const double* __restrict__ e, int n,
+                         double* __restrict__ w) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  double lo = 1e300, hi = -1e300, emax = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const double r = (j > 0 ? fabs(e[j - 1]) : 0.0) + (j < n - 1 ? fabs(e[j]) : 0.0);
+    lo = fmin(lo, d[j] - r);
+    hi = fmax(hi, d[j] + r);
+    if (j < n - 1) emax = fmax(emax, e[j] * e[j]);
+  }
+  const double tnorm = fmax(fabs(lo), fabs(hi));
+  const double pivmin = fmax(2.2250738585072014e-308 * fmax(emax, 1.0), 1e-300);
+  lo -= 2.2e-16 * tnorm + pivmin;
+  hi += 2.2e-16 * tnorm + pivmin;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (hi - lo <= 4.0 * 2.2e-16 * fmax(fabs(lo), fabs(hi)) + pivmin || mid == lo || mid == hi)
+      break;
+    if (sturm_count(d, e, n, mid, pivmin) > idx)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  w[idx] = 0.5 * (lo + hi);
+}
+
+// Inverse iteration for the eigenvectors of the tridiagonal (d, e): Gaussian elimination with
+// partial pivoting of T - lam I (the scheme of LAPACK's dlagtf / dlagts; the U factor has a
+// second super-diagonal where rows were swapped), five iterations from a deterministic start
+// vector, modified Gram-Schmidt against earlier members of the same cluster (eigenvalues
+// closer than ortol). One thread owns a whole cluster. Workspace per vector: 5n doubles.
+__global__ void k_inverse_iteration(const double* __restrict__ d, const double* __restrict__ e,
+                                    int n, const double* __restrict__ w, double* __restrict__ Z,
+                                    int ldz, double* __restrict__ work, unsigned char* swaps,
+                                    double ortol) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  // only the first member of a cluster works; it handles the whole cluster sequentially
+  if (idx > 0 && w[idx] - w[idx - 1] <= ortol) return;
+  int last = idx;
+  while (last + 1 < n && w[last + 1] - w[last] <= ortol) ++last;
+  double tnorm = 0.0;
+  for (int j = 0; j < n; ++j)
+    tnorm = fmax(tnorm, fabs(d[j]) + (j > 0 ? fabs(e[j - 1]) : 0.0) + (j < n - 1 ? fabs(e[j]) : 0.0));
+  const double eps = 2.2e-16;
+  const double tiny = eps * fmax(tnorm, 1e-300);
+  double* a = work + (size_t)idx * 5 * n;
+  double* b = a + n;
+  double* c = b + n;
+  double* c2 = c + n;
+  double* x = c2 + n;
+  unsigned char* sw = swaps + (size_t)idx * n;
+  double prev_lam = -1e300;
+  for (int t = idx; t <= last; ++t) {
+    double lam = w[t];
+    if (t > idx && lam - prev_lam < 10.0 * eps * fabs(lam)) lam = prev_lam + 10.0 * eps * fabs(lam);
+    prev_lam = lam;
+    // factor T - lam I with partial pivoting; record swaps
+    for (int j = 0; j < n; ++j) a[j] = d[j] - lam;
+    for (int j = 0; j < n - 1; ++j) b[j] = e[j], c2[j] = 0.0;
+    for (int j = 0; j < n - 1; ++j) {
+      const double sub = e[j];
+      if (fabs(a[j]) >= fabs(sub)) {
+        if (a[j] == 0.0) a[j] = tiny;
+        const double m = sub / a[j];
+        c[j] = m;
+        a[j + 1] -= m * b[j];
+        sw[j] = 0;
+      } else {
+        const double m = a[j] / sub;
+        const double bj = b[j];
+        const double bj1 = (j + 1 < n - 1) ? b[j + 1] : 0.0;
+        a[j] = sub;
+        b[j] = a[j + 1];
+        c2[j] = bj1;
+        a[j + 1] = bj - m * b[j];
+        if (j + 1 < n - 1) b[j + 1] = -m * bj1;
+        c[j] = m;
+        sw[j] = 1;
+      }
+    }
+    if (a[n - 1] == 0.0) a[n - 1] = tiny;
+    // deterministic start vector
+    unsigned int s = 2654435761u * (unsigned)(t + 1);
+    for (int j = 0; j < n; ++j) {
+      s = s * 1664525u + 1013904223u;
+      x[j] = ((double)(s >> 8) / 16777216.0) - 0.5 + 1e-3;
+    }
+    for (int iter = 0; iter < 5; ++iter) {
+      // forward: apply L^{-1} with the recorded swaps
+      for (int j = 0; j < n - 1; ++j) {
+        if (sw[j]) {
+          const double tmp = x[j];
+          x[j] = x[j + 1];
+          x[j + 1] = tmp - c[j] * x[j];
+        } else {
+          x[j + 1] -= c[j] * x[j];
+        }
+      }
+      // backward: U x = y, U has diag a, super b, second super c2
+      x[n - 1] /= a[n - 1];
+      if (n >= 2) x[n - 2] = (x[n - 2] - b[n - 2] * x[n - 1]) / a[n - 2];
+      for (int j = n - 3; j >= 0; --j) x[j] = (x[j] - b[j] * x[j + 1] - c2[j] * x[j + 2]) / a[j];
+      // orthogonalise against earlier members of the cluster (MGS)
+      for (int q = idx; q < t; ++q) {
+        double dot = 0.0;
+        for (int j = 0; j < n; ++j) dot += Z[(int64_t)j * ldz + q] * x[j];
+        for (int j = 0; j < n; ++j) x[j] -= dot * Z[(int64_t)j * ldz + q];
+      }
+      double nrm = 0.0;
+      for (int j = 0; j < n; ++j) nrm += x[j] * x[j];
+      nrm = sqrt(nrm);
+      if (!(nrm > 0.0)) nrm = 1.0;
+      for (int j = 0; j < n; ++j) x[j] /= nrm;
+    }
+    for (int j = 0; j < n; ++j) Z[(int64_t)j * ldz + t] = x[j];
+  }
+}
+
+// r[j] = v^T Z[:, j] over rows k+1..N-1
+__global__ void k_bt_dot(const double* __restrict__ V, int N, int k, const double* __restrict__ Z,
+                         double* __restrict__ r) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const double* v = V + (int64_t)k * N;
+  double s = 0.0;
+  for (int i = k + 1; i < N; ++i) s += v[i] * Z[(int64_t)i * N + j];
+  r[j] = s;
+}
+__global__ void k_bt_update(const double* __restrict__ V, int N, int k,
+                            const double* __restrict__ tau, double* __restrict__ Z,
+                            const double* __restrict__ r) {
+  const int n = N - k - 1;
+  const int64_t tot = (int64_t)n * N;
+  const double* v = V + (int64_t)k * N;
+  const double t = tau[k];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = k + 1 + (int)(q / N), j = (int)(q % N);
+    Z[(int64_t)i * N + j] -= t * v[i] * r[j];
+  }
+}
+
+int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
+  CHEFSI_REQUIRE(N >= 1, "syevd: N must be positive");
+  DeviceBuffer<double> V((size_t)N * N), tau(N), d(N), e(N), p(N);
+  CHEFSI_CUDA(cudaMemsetAsync(V.ptr, 0, sizeof(double) * N * N, st));
+  CHEFSI_CUDA(cudaMemsetAsync(tau.ptr, 0, sizeof(double) * N, st));
+  CHEFSI_CUDA(cudaMemsetAsync(e.ptr, 0, sizeof(double) * N, st));
+  for (int k = 0; k + 2 < N; ++k) {
+    const int n = N - k - 1;
+    k_hh_vector<<<1, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, d.ptr, e.ptr);
+    k_hh_symv<<<(n * 32 + 255) / 256, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, p.ptr);
+    k_hh_w<<<1, 256, 0, st>>>(N, k, V.ptr, tau.ptr, p.ptr);
+    k_hh_rank2<<<grid_for((int64_t)n * n, 256), 256, 0, st>>>(A, N, k, V.ptr, p.ptr);
+  }
+  k_tail<<<1, 32, 0, st>>>(A, N, d.ptr, e.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  k_bisect<<<(N + 127) / 128, 128, 0, st>>>(d.ptr, e.ptr, N, w);
+  CHEFSI_CHECK_LAUNCH();
+  // cluster tolerance relative to the tridiagonal's scale
+  std::vector<double> hd(N), he(N);
+  CHEFSI_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaMemcpyAsync(he.data(), e.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  double tn = 0.0;
+  for (int j = 0; j < N; ++j)
+    tn = std::max(tn, std::fabs(hd[j]) + (j > 0 ? std::fabs(he[j - 1]) : 0.0) +
+                          (j < N - 1 ? std::fabs(he[j]) : 0.0));
+  const double ortol = 1e-5 * std::max(tn, 1e-300);
+  DeviceBuffer<double> work((size_t)N * 5 * N);
+  DeviceBuffer<unsigned char> swaps((size_t)N * N);
+  k_inverse_iteration<<<(N + 63) / 64, 64, 0, st>>>(d.ptr, e.ptr, N, w, Z, N, work.ptr, swaps.ptr,
+                                                    ortol);
+  CHEFSI_CHECK_LAUNCH();
+  for (int k = N - 3; k >= 0; --k) {
+    k_bt_dot<<<(N + 127) / 128, 128, 0, st>>>(V.ptr, N, k, Z, p.ptr);
+    k_bt_update<<<grid_for((int64_t)(N - k - 1) * N, 256), 256, 0, st>>>(V.ptr, N, k, tau.ptr, Z,
+                                                                         p.ptr);
+  }
+  CHEFSI_CHECK_LAUNCH();
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  return CHEFSI_OK;
+}
+
+// ======================================================================= residuals, dots
+__global__ void k_resid(const double* __restrict__ X, int64_t ldx, const double* __restrict__ HX,
+                        int64_t ldh, int64_t M, int N, const double* __restrict__ lam,
+                        double* __restrict__ out, int64_t rows_per) {
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per;
+  const int64_t r1 = min(M, r0 + rows_per);
+  const double l = lam[j];
+  double s = 0.0;
+  for (int64_t i = r0; i < r1; ++i) {
+    const double t = HX[i * ldh + j] - l * X[i * ldx + j];
+    s += t * t;
+  }
+  atomicAdd(&out[j], s);
+}
+__global__ void k_resid_c(const cplx* __restrict__ X, int64_t ldx, const cplx* __restrict__ HX,
+                          int64_t ldh, int64_t M, int N, const double* __restrict__ lam,
+                          double* __restrict__ out, int64_t rows_per) {
+  const int j = blockIdx.y * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per;
+  const int64_t r1 = min(M, r0 + rows_per);
+  const double l = lam[j];
+  double s = 0.0;
+  for (int64_t i = r0; i < r1; ++i) {
+    const cplx h = HX[i * ldh + j], x = X[i * ldx + j];
+    const double tr = h.x - l * x.x, ti = h.y - l * x.y;
+    s += tr * tr + ti * ti;
+  }
+  atomicAdd(&out[j], s);
+}
+__global__ void k_sqrt(double* x, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = sqrt(x[i]);
+}
+
+void residual_norms_f64(const double* X, int64_t ldx, const double* HX, int64_t ldh, int64_t M,
+                        int N, const double* lam, double* out, cudaStream_t st) {
+  CHEFSI_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * N, st));
+  const int64_t rows_per = std::max<int64_t>(64, (M + 1023) / 1024);
+  dim3 grid((unsigned)((M + rows_per - 1) / rows_per), (N + 127) / 128);
+  k_resid<<<grid, 128, 0, st>>>(X, ldx, HX, ldh, M, N, lam, out, rows_per);
+  CHEFSI_CHECK_LAUNCH();
+  k_sqrt<<<(N + 127) / 128, 128, 0, st>>>(out, N);
+  CHEFSI_CHECK_LAUNCH();
+}
+void residual_norms_c64(const cplx* X, int64_t ldx, const cplx* HX, int64_t ldh, int64_t M, int N,
+                        const double* lam, double* out, cudaStream_t st) {
+  CHEFSI_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * N, st));
+  const int64_t rows_per = std::max<int64_t>(64, (M + 1023) / 1024);
+  dim3 grid((unsigned)((M + rows_per - 1) / rows_per), (N + 127) / 128);
+  k_resid_c<<<grid, 128, 0, st>>>(X, ldx, HX, ldh, M, N, lam, out, rows_per);
+  CHEFSI_CHECK_LAUNCH();
+  k_sqrt<<<(N + 127) / 128, 128, 0, st>>>(out, N);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+__global__ void k_dot(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
+                      double* out) {
+  double s = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    s += x[t] * y[t];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+void dot_f64(const double* x, const double* y, int64_t n, double* out, cudaStream_t st) {
+  CHEFSI_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+  k_dot<<<grid_for(n, 256, kNumSMs * 4), 256, 0, st>>>(x, y, n, out);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+}  // namespace chefsi

@@ -1,0 +1,123 @@
+// Internal types shared by the CheFSI translation units (not part of the C ABI).
+#pragma once
+
+#include "common.cuh"
+
+#include <string>
+#include <vector>
+
+namespace chefsi {
+
+struct cplx {
+  double x, y;
+};
+
+// Tensor-core copy of the cell matrices: FP16 hi/lo split of 2^mat_shift * A_e, rows padded
+// to a multiple of 16 and columns (the K dimension) to kpad (a multiple of 64), stored
+// [n_cells][npad][kpad] so that one TMA box of [rows][64 halves] is one 128-byte-swizzled
+// operand tile.
+struct TensorCellMats {
+  DeviceBuffer<__half> hi, lo;
+  int npad = 0;
+  int kpad = 0;
+  float scale = 1.f;   // power of two applied before the split
+  bool ready = false;
+};
+
+}  // namespace chefsi
+
+struct chefsi_operator_s {
+  int64_t n_dofs = 0;
+  int n_cells = 0;
+  int n_e = 0;
+  int is_complex = 0;
+  bool folded = true;  // M^{-1/2} folded into the cell matrices / projectors
+
+  chefsi::DeviceBuffer<int> map;          // [n_cells][n_e]
+  chefsi::DeviceBuffer<double> mats64;    // [n_cells][n_e][n_e] (x2 for complex)
+  chefsi::DeviceBuffer<float> mats32;     // FP32 copy (real only)
+  chefsi::TensorCellMats tc;              // FP16 split copy for the tensor-core filter HX
+  chefsi::DeviceBuffer<double> sqrt_mass, inv_sqrt_mass;
+
+  // constraints
+  int n_con = 0;
+  chefsi::DeviceBuffer<int> con_ids, con_ptr, con_master;
+  chefsi::DeviceBuffer<double> con_w;
+
+  // nonlocal projectors
+  int n_atoms = 0, n_proj = 0;
+  int64_t nl_nnz = 0;
+  chefsi::DeviceBuffer<int> nl_ptr, nl_dofs;
+  chefsi::DeviceBuffer<double> nl_vals64, couplings;
+  chefsi::DeviceBuffer<float> nl_vals32;
+  int nl_n_chunks = 0;
+  chefsi::DeviceBuffer<int> nl_chunk_atom, nl_chunk_row0;
+
+  // workspaces (grow-only)
+  chefsi::DeviceBuffer<double> ws64a, ws64b, nlW64;
+  chefsi::DeviceBuffer<float> nlW32;
+};
+
+namespace chefsi {
+
+// ---- operator apply (operator.cu) -------------------------------------------------------
+// dst = (accumulate ? dst : 0) + scalar * A src
+void hx_f64(chefsi_operator_s* op, const double* src, int64_t lds, double* dst, int64_t ldd,
+            int B, double scalar, bool accumulate, cudaStream_t st);
+void hx_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd,
+            int B, double scalar, bool accumulate, cudaStream_t st);
+void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int64_t ldd, int B,
+            double scalar, bool accumulate, cudaStream_t st);
+// tensor-core (FP16 split) apply on FP32 vectors; returns false if unavailable for this op
+bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+           double scalar, bool accumulate, cudaStream_t st);
+void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st);
+
+// ---- elementwise helpers (operator.cu) ----------------------------------------------------
+template <typename T>
+void scale_block(T* x, int64_t ld, int64_t rows, int B, double s, cudaStream_t st);
+// y = a*x + b*y on [rows][B] blocks
+template <typename T>
+void axpby_block(const T* x, int64_t ldx, T* y, int64_t ldy, int64_t rows, int B, double a,
+                 double b, cudaStream_t st);
+// column block copy / precision conversion: dst[i][j] = s * src[i][j]
+template <typename Ts, typename Td>
+void copy_block(const Ts* src, int64_t lds, Td* dst, int64_t ldd, int64_t rows, int B, double s,
+                cudaStream_t st);
+// max |x| over a block (device scalar out, as float bits via atomicMax)
+void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
+                      cudaStream_t st);
+
+// ---- dense linear algebra (dense.cu) ------------------------------------------------------
+// C (N x N, row-major, ldc) += A^H B for A [K][N1] (lda), B [K][N2] (ldb), K split across CTAs.
+// prec FP64: FP64 throughout; MIXED/FP32: FP32 products inside K chunks, FP64 across chunks.
+// lower_only: only tiles with row-tile >= col-tile (for A == B)
+void gram_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t K, int N1,
+              int N2, double* C, int ldc, int prec, bool lower_only, cudaStream_t st);
+void gram_c64(const cplx* A, int64_t lda, const cplx* B, int64_t ldb, int64_t K, int N1, int N2,
+              cplx* C, int ldc, bool lower_only, cudaStream_t st);
+// C[M][N] = alpha * op(A) op(B) + beta * C  (row-major; op: 'N' or 'T' (conj for complex))
+void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const double* A,
+              int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+              int prec, cudaStream_t st);
+void gemm_c64(char ta, char tb, int64_t M, int N, int K, cplx alpha, const cplx* A, int64_t lda,
+              const cplx* B, int64_t ldb, cplx beta, cplx* C, int64_t ldc, cudaStream_t st);
+void symmetrize_lower(double* A, int N, cudaStream_t st);
+void symmetrize_lower_c(cplx* A, int N, cudaStream_t st);
+// in-place lower Cholesky of N x N row-major A (upper part zeroed). Returns CHEFSI_OK or
+// CHEFSI_ERR_NOT_SPD (synchronises the stream to read the flag).
+int cholesky_lower(double* A, int N, cudaStream_t st);
+// lower-triangular inverse in place
+void trtri_lower(double* L, int N, cudaStream_t st);
+// symmetric eigensolve (Householder tridiagonalisation, bisection, inverse iteration,
+// back-transformation); A overwritten; eigenvalues ascending in w; vectors in columns of Z.
+int syevd(double* A, int N, double* w, double* Z, cudaStream_t st);
+// residual norms of columns: out[j] = || HX[:,j] - lam[j] X[:,j] ||
+void residual_norms_f64(const double* X, int64_t ldx, const double* HX, int64_t ldh, int64_t M,
+                        int N, const double* lam_dev, double* out_dev, cudaStream_t st);
+void residual_norms_c64(const cplx* X, int64_t ldx, const cplx* HX, int64_t ldh, int64_t M, int N,
+                        const double* lam_dev, double* out_dev, cudaStream_t st);
+// dot / norm helpers for Lanczos (device scalar results)
+void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaStream_t st);
+
+}  // namespace chefsi

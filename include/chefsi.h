@@ -1,0 +1,206 @@
+/*
+ * chefsi.h -- C ABI of the GB300-native Chebyshev-filtered subspace iteration (CheFSI).
+ *
+ * A drop-in for DFT-FE's CheFSI hot path on one GPU. The entry points replace these
+ * reference interfaces (paths inside the DFT-FE source tree):
+ *
+ *   chefsi_operator_create / _destroy
+ *       kohnShamDFTOperatorDeviceClass::init + reinit + computeHamiltonianMatricesAllkpt
+ *       (src/dftOperator/kohnShamDFTOperatorDevice.cc:494-933,
+ *        src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:1075-1375);
+ *       the cell Hamiltonians, cell->dof map, mass vector, constraints and nonlocal
+ *       projectors are passed in instead of being built from deal.II objects.
+ *   chefsi_hx        operatorDFTDeviceClass::HX / HXCheby (include/operatorDevice.h:176-197;
+ *                    src/dftOperator/kohnShamDFTOperatorDevice.cc:3767-3860, :3876-3997)
+ *   chefsi_xthx      operatorDFTDeviceClass::XtHX (include/operatorDevice.h:230-241;
+ *                    src/dftOperator/kohnShamDFTOperatorDevice.cc:4003-4157)
+ *   chefsi_overlap   linearAlgebraOperationsDevice::fillParallelOverlapMatScalapack[MixedPrec]
+ *                    (src/linAlg/linearAlgebraOperationsDevice.cc:3079-3240, :3544-3798)
+ *   chefsi_chebyshev_filter
+ *                    linearAlgebraOperationsDevice::chebyshevFilter
+ *                    (src/linAlg/linearAlgebraOperationsDevice.cc:531-727)
+ *   chefsi_lanczos_bounds
+ *                    linearAlgebraOperationsDevice::lanczosLowerUpperBoundEigenSpectrum
+ *                    (src/linAlg/linearAlgebraOperationsDevice.cc:341-527)
+ *   chefsi_cholesky_gs
+ *                    pseudoGramSchmidtOrthogonalization (src/linAlg/pseudoGSDevice.cc:82-463)
+ *   chefsi_rayleigh_ritz
+ *                    rayleighRitzGEP (src/linAlg/rayleighRitzDevice.cc:356-819)
+ *   chefsi_residual_norms
+ *                    computeEigenResidualNorm (src/linAlg/linearAlgebraOperationsDevice.cc:4611-)
+ *   chefsi_solver_create / _reinit_spectrum_bounds / chefsi_solve / chefsi_solve_no_rr
+ *                    chebyshevOrthogonalizedSubspaceIterationSolverDevice constructor,
+ *                    reinitSpectrumBounds, solve, solveNoRR
+ *                    (include/chebyshevOrthogonalizedSubspaceIterationSolverDevice.h:37-166)
+ *   chefsi_syevd     the projected eigensolve done by ELPA/ScaLAPACK in the reference
+ *                    (src/linAlg/rayleighRitzDevice.cc:720-749), here FP64 on the GPU
+ *
+ * Conventions
+ *   - Block vectors are dof-major, wavefunction-fastest: X[i * ld + j] for dof i, vector j
+ *     (DFT-FE's flattened layout, include/MultiVector.h:126). All vector and matrix
+ *     pointers passed to compute calls are DEVICE pointers unless the name says host.
+ *   - Small N x N matrices (overlap, projected Hamiltonian, rotations) are row-major on the
+ *     device.
+ *   - The operator is A = M^{-1/2} (H_loc + H_nl) M^{-1/2} in Hartree; CheFSI works on
+ *     vectors already scaled by M^{1/2} (src/dft/kohnShamEigenSolve.cc:322-329).
+ *   - Every call returns an int status (CHEFSI_OK == 0); no C++ exception crosses the ABI.
+ *     chefsi_last_error() returns the message of the last failure on the calling thread.
+ *   - Compute calls take a cudaStream_t (passed as void*) and enqueue work on it. Calls that
+ *     return host results (eigenvalues, residuals, bounds) synchronise that stream.
+ *   - Handles are not thread-safe: one host thread per handle.
+ *   - Precision: CHEFSI_PREC_FP64 computes everything in FP64. CHEFSI_PREC_MIXED runs the
+ *     filter HX on the tensor cores with FP16-split operands (hi+lo, three products,
+ *     FP32 accumulation) on FP32 block vectors, and the Gram / rotation GEMMs in FP32 with
+ *     FP64 accumulation across K chunks; the HX feeding the projected Hamiltonian, the
+ *     Cholesky, the projected eigensolve and the residual norms stay in FP64.
+ *     CHEFSI_PREC_FP32 is the SIMT FP32 filter (no tensor cores), kept for comparison.
+ */
+#ifndef CHEFSI_GB300_H
+#define CHEFSI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CHEFSI_OK 0
+#define CHEFSI_ERR_INVALID 1     /* bad argument (null pointer, size out of range) */
+#define CHEFSI_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define CHEFSI_ERR_NOT_SPD 3     /* Cholesky met a non-positive pivot */
+#define CHEFSI_ERR_NO_CONVERGENCE 4
+#define CHEFSI_ERR_ALLOC 5       /* device allocation failed */
+#define CHEFSI_ERR_TIMEOUT 6     /* a bounded device wait ran out */
+#define CHEFSI_ERR_NAN 7         /* non-finite input detected */
+#define CHEFSI_ERR_UNSUPPORTED 8 /* valid request this build does not implement */
+
+/* precision modes */
+#define CHEFSI_PREC_FP64 0
+#define CHEFSI_PREC_MIXED 1
+#define CHEFSI_PREC_FP32 2
+
+typedef struct chefsi_operator_s* chefsi_operator;
+typedef struct chefsi_solver_s* chefsi_solver;
+
+/* Description of one Kohn-Sham operator (one k-point / spin). Host pointers. */
+typedef struct {
+  int64_t n_dofs;               /* M: locally owned dofs (length of a vector) */
+  int32_t n_cells;              /* number of cells */
+  int32_t nodes_per_cell;       /* n_e = (p+1)^3 */
+  int32_t is_complex;           /* 0: real (Gamma point), 1: complex Bloch */
+  const int32_t* cell_dof_map;  /* [n_cells][n_e] dof of each cell node */
+  const void* cell_matrices;    /* [n_cells][n_e][n_e] FP64 (or interleaved complex FP64),
+                                   row I column J, the matrix applied to the cell vector */
+  const double* sqrt_mass;      /* [n_dofs] M^{1/2} (lumped) */
+  const double* inv_sqrt_mass;  /* [n_dofs] M^{-1/2} */
+  /* constraints: slave rows in CSR form over master dofs (0 rows = none). When present the
+     operator runs DFT-FE's sequence (scale, distribute, cell products, adjoint distribute,
+     scale); otherwise the mass scaling is folded into the cell matrices. */
+  int32_t n_constrained;
+  const int32_t* constrained_ids; /* [n_constrained] */
+  const int32_t* constraint_ptr;  /* [n_constrained+1] */
+  const int32_t* master_ids;      /* [nnz] */
+  const double* master_weights;   /* [nnz] */
+  /* nonlocal projectors: H_nl = sum_a C_a diag(V_a) C_a^T, C_a dense over its dof list */
+  int32_t n_atoms;
+  int32_t n_proj;               /* projectors per atom (uniform) */
+  const int32_t* atom_dof_ptr;  /* [n_atoms+1] */
+  const int32_t* atom_dofs;     /* [nnz_dofs] */
+  const double* atom_proj;      /* [nnz_dofs][n_proj] */
+  const double* couplings;      /* [n_atoms][n_proj] */
+} chefsi_operator_desc;
+
+/* Solver parameters (subset of dftParameters that the path reads). */
+typedef struct {
+  int32_t chebyshev_degree;     /* 0: from the upper bound via DFT-FE's lookup table */
+  int32_t cheby_wfc_block;      /* chebyWfcBlockSize */
+  int32_t wfc_block;            /* wfcBlockSize (residual / XtHX blocks) */
+  int32_t precision;            /* CHEFSI_PREC_* */
+  int32_t lanczos_steps;        /* 20 (40 with reproducible output) */
+  int32_t reproducible;         /* REPRODUCIBLE OUTPUT */
+  double first_scf_degree_scale;/* chebyshevFilterPolyDegreeFirstScfScalingFactor */
+  int32_t keep_hx;              /* 1: keep H X from the RR step for the residuals */
+} chefsi_params;
+
+const char* chefsi_last_error(void);
+const char* chefsi_version(void);
+
+int chefsi_operator_create(const chefsi_operator_desc* desc, chefsi_operator* out);
+int chefsi_operator_destroy(chefsi_operator op);
+int chefsi_operator_info(chefsi_operator op, int64_t* n_dofs, int32_t* n_cells,
+                         int32_t* nodes_per_cell, int32_t* is_complex);
+
+/* dst = (accumulate ? dst : 0) + scalar * A src over n_vec vectors (DFT-FE's HX with
+   scaleFlag == accumulate). Real: src/dst FP64 (precision FP64) or FP32 (FP32 / MIXED).
+   Complex: interleaved complex FP64 only. ld_* are leading dimensions in elements. */
+int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, int64_t ld_dst,
+              int32_t n_vec, double scalar, int32_t accumulate, int32_t precision, void* stream);
+
+/* S = X^H X (lower triangle mirrored, N x N row-major FP64, device). */
+int chefsi_overlap(chefsi_operator op, const void* X, int64_t ld, int32_t N, double* S,
+                   int32_t precision, void* stream);
+
+/* Hp = X^H A X (N x N row-major FP64, device). The HX is FP64 in every mode. */
+int chefsi_xthx(chefsi_operator op, const void* X, int64_t ld, int32_t N, double* Hp,
+                int32_t precision, void* stream);
+
+/* In-place Chebyshev filter of the n_vec columns starting at X (ld): degree m on the
+   unwanted interval [a, b] with lower wanted bound a0 (sigma-scaled recurrence). */
+int chefsi_chebyshev_filter(chefsi_operator op, void* X, int64_t ld, int32_t n_vec,
+                            int32_t m, double a, double b, double a0, int32_t precision,
+                            void* stream);
+
+/* k-step Lanczos from the host start vector v0 (length n_dofs; null: seeded uniform(0,1)).
+   Returns floor(lambda_min(T)) and ceil(lambda_max(T) + |f| (reproducible) or |f|/10). */
+int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible,
+                          const double* v0_host, uint64_t seed, double* lower, double* upper,
+                          void* stream);
+
+/* Symmetric (Hermitian for complex) eigensolve of an N x N row-major device matrix:
+   eigenvalues ascending into w (device, N), eigenvectors into the columns of Z (device).
+   A is overwritten. */
+int chefsi_syevd(int32_t N, double* A, double* w, double* Z, void* stream);
+
+/* Cholesky-Gram-Schmidt: S = X^H X, S = L L^H, X <- X L^{-H}. */
+int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32_t precision,
+                       void* stream);
+
+/* Rayleigh-Ritz in the generalised form; eigenvalues to host eig_host (N), X rotated in
+   place to the Ritz vectors. If HX_out is non-null it receives A X_rot (FP64, [M][N]). */
+int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
+                         double* HX_out, int32_t precision, void* stream);
+
+/* residual norms r_i = || A x_i - lambda_i x_i || (host arrays eig, res). */
+int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,
+                          const double* eig_host, double* res_host, void* stream);
+
+int chefsi_solver_create(const chefsi_params* params, chefsi_solver* out);
+int chefsi_solver_destroy(chefsi_solver s);
+int chefsi_solver_reinit_spectrum_bounds(chefsi_solver s, double lower_wanted,
+                                         double lower_unwanted, double upper_unwanted);
+int chefsi_solver_get_bounds(chefsi_solver s, double* lower_wanted, double* lower_unwanted,
+                             double* upper_unwanted, int32_t* last_degree);
+/* Per-phase device times of the last solve in milliseconds:
+   [filter, overlap+cholesky, xthx(hx+gemm), eig, rotation, residual, total]. */
+int chefsi_solver_timings(chefsi_solver s, double* ms7);
+
+/* One CheFSI iteration on X (device, [n_dofs][N], ld = N; FP64 or complex FP64):
+   filter all vectors, Rayleigh-Ritz (GEP), residual norms. Eigenvalues and residual norms
+   are written to host arrays. The bounds are NOT updated (the caller owns a0 / bLow, as
+   kohnShamEigenSpaceCompute does); see chefsi_solver_reinit_spectrum_bounds. */
+int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
+                 double* res_host, int32_t compute_residual, int32_t is_first_scf,
+                 void* stream);
+
+/* Filter only (no Rayleigh-Ritz), solveNoRR. */
+int chefsi_solve_no_rr(chefsi_solver s, chefsi_operator op, void* X, int32_t N,
+                       int32_t n_passes, int32_t is_first_scf, void* stream);
+
+/* Chebyshev degree from DFT-FE's lookup table (solver .cc:24-56). */
+int32_t chefsi_chebyshev_order(double upper_bound_unwanted);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHEFSI_GB300_H */

@@ -1,0 +1,269 @@
+"""CPU oracle for CheFSI -- TEST INFRASTRUCTURE ONLY (the checker and the CPU baseline).
+
+FP64 restatement of DFT-FE's CPU CheFSI. The operator apply and the Chebyshev filter are in
+``chefsi_oracle.cpp`` (compiled by ``build()`` with g++/OpenMP); the dense steps are numpy
+/ LAPACK here:
+
+* ``lanczos_bounds``   -- lanczosLowerUpperBoundEigenSpectrum,
+                          src/linAlg/linearAlgebraOperationsOpt.cc:2892-3025
+* ``rayleigh_ritz_gep`` -- rayleighRitzGEP, src/linAlg/linearAlgebraOperationsOpt.cc:613-969
+                          (S = X^T X, Cholesky, L^{-1}, Hp = X^T H X lower triangle mirrored,
+                           L^{-1} Hp L^{-T}, eig, X <- X L^{-T} Q)
+* ``solve``            -- chebyshevOrthogonalizedSubspaceIterationSolver::solve (CGS branch),
+                          src/solvers/eigenSolvers/chebyshevOrthogonalizedSubspaceIterationSolver.cc:116-607
+* ``chebyshev_order``  -- the degree lookup table, same file :24-56
+* bounds update       -- kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:335-365,489-498
+
+Parity status: the reference ships no golden vectors at this boundary (its tests pin total
+energies only) and cannot be built here (deal.II, MPI, ELPA absent), so parity with the
+reference is unpinned; the oracle is pinned to analytic known answers instead (free-particle
+spectra 1/2|G+k|^2, dense eigendecompositions of small assembled operators).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libchefsi_oracle.so")
+SRC = os.path.join(HERE, "chefsi_oracle.cpp")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library with g++ (-O3 -fopenmp)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+                           SRC, "-o", tmp])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.oracle_hx.restype = None
+        _lib.oracle_chebyshev_filter.restype = None
+        _lib.oracle_residual_norms.restype = None
+        _lib.oracle_cell_hamiltonians.restype = None
+        _lib.oracle_colour_cells.restype = ctypes.c_int
+        _lib.oracle_num_threads.restype = ctypes.c_int
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(0) if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class _OpStruct(ctypes.Structure):
+    _fields_ = [("n_dofs", ctypes.c_int64), ("n_cells", ctypes.c_int32), ("n_e", ctypes.c_int32),
+                ("is_complex", ctypes.c_int32),
+                ("cell_map", ctypes.c_void_p), ("cell_mats", ctypes.c_void_p),
+                ("inv_sqrt_mass", ctypes.c_void_p),
+                ("n_slaves", ctypes.c_int32), ("slave_ids", ctypes.c_void_p),
+                ("slave_ptr", ctypes.c_void_p), ("master_ids", ctypes.c_void_p),
+                ("weights", ctypes.c_void_p),
+                ("n_atoms", ctypes.c_int32), ("n_proj", ctypes.c_int32),
+                ("atom_ptr", ctypes.c_void_p), ("atom_dofs", ctypes.c_void_p),
+                ("atom_vals", ctypes.c_void_p), ("couplings", ctypes.c_void_p),
+                ("n_colours", ctypes.c_int32), ("colour_ptr", ctypes.c_void_p),
+                ("colour_cells", ctypes.c_void_p)]
+
+
+def colour_cells(cell_map: np.ndarray, n_dofs: int):
+    cm = np.ascontiguousarray(cell_map, dtype=np.int32)
+    nc = cm.shape[0]
+    ptr = np.zeros(nc + 1, np.int32)
+    cells = np.zeros(nc, np.int32)
+    ncol = lib().oracle_colour_cells(ctypes.c_int32(nc), ctypes.c_int32(cm.shape[1]), _p(cm),
+                                     ctypes.c_int64(n_dofs), _p(ptr), _p(cells))
+    return ptr[:ncol + 1].copy(), cells
+
+
+class OracleOperator:
+    """FP64 Kohn-Sham operator A = M^{-1/2} (H_loc + H_nl) M^{-1/2} on the CPU."""
+
+    def __init__(self, cell_map, cell_mats, inv_sqrt_mass, n_dofs, projectors=None,
+                 constraints=None):
+        self.n_dofs = int(n_dofs)
+        self.cell_map = np.ascontiguousarray(cell_map, dtype=np.int32)
+        self.is_complex = np.iscomplexobj(cell_mats)
+        self.dtype = np.complex128 if self.is_complex else np.float64
+        self.cell_mats = np.ascontiguousarray(cell_mats, dtype=self.dtype)
+        self.inv_sqrt_mass = np.ascontiguousarray(inv_sqrt_mass, dtype=np.float64)
+        self.colour_ptr, self.colour_cells = colour_cells(self.cell_map, self.n_dofs)
+        s = _OpStruct()
+        s.n_dofs = self.n_dofs
+        s.n_cells, s.n_e = self.cell_map.shape
+        s.is_complex = int(self.is_complex)
+        s.cell_map, s.cell_mats, s.inv_sqrt_mass = _p(self.cell_map), _p(self.cell_mats), _p(self.inv_sqrt_mass)
+        self._keep = []
+        if constraints is not None:
+            sid, sptr, mid, w = [np.ascontiguousarray(a, dt) for a, dt in
+                                 zip(constraints, (np.int32, np.int32, np.int32, np.float64))]
+            self._keep += [sid, sptr, mid, w]
+            s.n_slaves = len(sid)
+            s.slave_ids, s.slave_ptr, s.master_ids, s.weights = _p(sid), _p(sptr), _p(mid), _p(w)
+        if projectors is not None and projectors.n_atoms > 0:
+            ap = np.ascontiguousarray(projectors.ptr, np.int32)
+            ad = np.ascontiguousarray(projectors.dofs, np.int32)
+            av = np.ascontiguousarray(projectors.values, np.float64)
+            cp = np.ascontiguousarray(projectors.couplings, np.float64)
+            self._keep += [ap, ad, av, cp]
+            s.n_atoms, s.n_proj = projectors.n_atoms, projectors.n_proj
+            s.atom_ptr, s.atom_dofs, s.atom_vals, s.couplings = _p(ap), _p(ad), _p(av), _p(cp)
+        s.n_colours = len(self.colour_ptr) - 1
+        s.colour_ptr, s.colour_cells = _p(self.colour_ptr), _p(self.colour_cells)
+        self._s = s
+
+    def HX(self, src: np.ndarray, scalar: float = 1.0, dst: np.ndarray | None = None,
+           accumulate: bool = False) -> np.ndarray:
+        """dst = (accumulate ? dst : 0) + scalar * A src; src, dst are [M][B] (B fastest)."""
+        src = np.ascontiguousarray(src, dtype=self.dtype)
+        B = 1 if src.ndim == 1 else src.shape[1]
+        if dst is None:
+            dst = np.zeros_like(src)
+        lib().oracle_hx(ctypes.byref(self._s), _p(src), _p(dst), ctypes.c_int32(B),
+                        ctypes.c_double(scalar), ctypes.c_int32(int(accumulate)))
+        return dst
+
+    def chebyshev_filter(self, X: np.ndarray, m: int, a: float, b: float, a0: float) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=self.dtype).copy()
+        lib().oracle_chebyshev_filter(ctypes.byref(self._s), _p(X), ctypes.c_int32(X.shape[1]),
+                                      ctypes.c_int32(m), ctypes.c_double(a), ctypes.c_double(b),
+                                      ctypes.c_double(a0))
+        return X
+
+    def residual_norms(self, X: np.ndarray, eig: np.ndarray, wfc_block: int = 400) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=self.dtype)
+        ev = np.ascontiguousarray(eig, dtype=np.float64)
+        out = np.zeros(X.shape[1])
+        lib().oracle_residual_norms(ctypes.byref(self._s), _p(X), ctypes.c_int32(X.shape[1]),
+                                    _p(ev), ctypes.c_int32(wfc_block), _p(out))
+        return out
+
+    def dense(self) -> np.ndarray:
+        """Assembled A (small problems only)."""
+        I = np.eye(self.n_dofs, dtype=self.dtype)
+        return self.HX(I)
+
+
+def cell_hamiltonians_direct(K: np.ndarray, N: np.ndarray, vjxw: np.ndarray) -> np.ndarray:
+    """H[c] = 1/2 K + N^T diag(vjxw[c]) N by the direct q-loop of hamMatrixKernelLDA."""
+    nc, nq = vjxw.shape
+    ne = K.shape[0]
+    H = np.zeros((nc, ne, ne))
+    K, N, v = (np.ascontiguousarray(a, np.float64) for a in (K, N, vjxw))
+    lib().oracle_cell_hamiltonians(ctypes.c_int32(nc), ctypes.c_int32(ne), ctypes.c_int32(nq),
+                                   _p(K), _p(N), _p(v), _p(H))
+    return H
+
+
+# ---------------------------------------------------------------------------- dense steps
+
+_ORDER_LOOKUP = [(500, 24), (750, 30), (1000, 39), (1500, 50), (2000, 53), (3000, 57),
+                 (4000, 62), (5000, 69), (9000, 77), (14000, 104), (20000, 119), (30000, 162),
+                 (50000, 300), (80000, 450), (100000, 550), (200000, 700), (500000, 1000)]
+
+
+def chebyshev_order(upper_bound_unwanted: float) -> int:
+    """internal::setChebyshevOrder (chebyshevOrthogonalizedSubspaceIterationSolver.cc:24-56)."""
+    ub = int(upper_bound_unwanted)
+    for lim, deg in _ORDER_LOOKUP:
+        if ub <= lim:
+            return deg
+    return 1250
+
+
+def lanczos_bounds(op: OracleOperator, v0: np.ndarray, k: int = 20, reproducible: bool = False):
+    """k-step Lanczos on start vector v0 (linearAlgebraOperationsOpt.cc:2892-3025).
+
+    Returns (floor(lambda_min(T)), ceil(lambda_max(T) + ||f|| (or ||f||/10))).
+    """
+    v = np.asarray(v0, dtype=op.dtype).reshape(-1, 1).copy()
+    v /= np.linalg.norm(v)
+    f = op.HX(v)
+    alpha = np.vdot(f[:, 0], v[:, 0]) if op.is_complex else float(f[:, 0] @ v[:, 0])
+    # reference: fVector.dot(vVector) = sum f * v (complex: conj on first argument)
+    f = f - alpha * v
+    T = np.zeros((k, k), dtype=op.dtype)
+    T[0, 0] = alpha
+    for j in range(1, k):
+        beta = np.linalg.norm(f)
+        v0_ = v
+        v = f / beta
+        f = op.HX(v)
+        f = f - beta * v0_
+        alpha = np.vdot(f[:, 0], v[:, 0]) if op.is_complex else float(f[:, 0] @ v[:, 0])
+        f = f - alpha * v
+        T[j, j - 1] = beta
+        T[j, j] = alpha
+    ev = np.sort(np.linalg.eigvalsh(T, UPLO='L'))
+    fn = np.linalg.norm(f)
+    return float(np.floor(ev[0])), float(np.ceil(ev[-1] + (fn if reproducible else fn / 10.0)))
+
+
+def rayleigh_ritz_gep(op: OracleOperator, X: np.ndarray):
+    """RR in the generalised form (rayleighRitzGEP, linearAlgebraOperationsOpt.cc:613-969).
+
+    Returns (eigenvalues, rotated X, HX of rotated X).
+    """
+    Xc = X.conj() if op.is_complex else X
+    S = Xc.T @ X
+    L = np.linalg.cholesky(S)                      # S = L L^H, lower
+    Linv = np.linalg.inv(L)
+    Linv = np.tril(Linv)
+    HX = op.HX(X)
+    Hp = Xc.T @ HX
+    # the reference fills the lower triangle and mirrors it (rayleighRitzDevice.cc:672-687)
+    Hl = np.tril(Hp)
+    Hp = Hl + np.tril(Hl, -1).conj().T
+    C = Linv @ Hp @ Linv.conj().T
+    ev, Q = np.linalg.eigh(C, UPLO='L')
+    W = Linv.conj().T @ Q
+    return ev, X @ W, HX @ W
+
+
+@dataclass
+class SolverState:
+    a0: float
+    b_low: float
+    b_up: float
+
+
+def solve(op: OracleOperator, X: np.ndarray, state: SolverState, m: int | None = None):
+    """One CheFSI iteration: filter all vectors, RR-GEP, residual norms; updates bounds.
+
+    Returns (eigenvalues, residual norms, X). Mirrors solve() + the bounds update of
+    kohnShamEigenSpaceCompute (a0 <- lambda_0, bLow <- lambda_{N-1}).
+    """
+    if m is None:
+        m = chebyshev_order(state.b_up)
+    Xf = op.chebyshev_filter(X, m, state.b_low, state.b_up, state.a0)
+    ev, Xr, HXr = rayleigh_ritz_gep(op, Xf)
+    res = np.sqrt((np.abs(HXr - Xr * ev[None, :]) ** 2).sum(0))
+    state.a0 = float(ev[0])
+    state.b_low = float(ev[-1])
+    return ev, res, Xr
+
+
+def initial_bounds(op: OracleOperator, n_wfc: int, v0: np.ndarray, k: int = 20,
+                   reproducible: bool = False) -> SolverState:
+    """First-call bounds (kohnShamEigenSolve.cc:335-365):
+    a0 = floor(lambda_min), b = Lanczos upper bound,
+    bLow = a0 + (b - a0) * N / M * (10 or 200)."""
+    lo, up = lanczos_bounds(op, v0, k, reproducible)
+    blow = lo + (up - lo) / op.n_dofs * n_wfc * (10.0 if reproducible else 200.0)
+    return SolverState(a0=lo, b_low=blow, b_up=up)

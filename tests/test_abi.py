@@ -1,0 +1,48 @@
+"""CPU tests of the drop-in boundary: the C-ABI library builds, loads without a GPU and
+exports every entry point include/chefsi.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "chefsi.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(chefsi_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from dftfe_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_the_entry_points():
+    syms = declared_symbols()
+    assert "chefsi_solve" in syms and "chefsi_hx" in syms and len(syms) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_lists_every_export():
+    from dftfe_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.EXPORTS)
+
+
+def test_host_only_entry_points(lib):
+    from dftfe_gb300 import _lib
+    l = _lib.load()
+    assert b"sm_103a" in l.chefsi_version()
+    assert l.chefsi_chebyshev_order(400.0) == 24
+    assert l.chefsi_chebyshev_order(1.0e9) == 1250
+    # null handles are rejected with a status, not a crash
+    assert l.chefsi_operator_create(None, None) == _lib.CHEFSI_ERR_INVALID
+    assert b"null" in l.chefsi_last_error()

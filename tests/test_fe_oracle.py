@@ -1,0 +1,163 @@
+"""CPU tests: finite-element inputs and the FP64 oracle against analytic known answers.
+
+The reference ships no golden vectors at the CheFSI boundary (its regression tests pin total
+energies only), so the oracle is pinned here by known answers: free-particle spectra
+1/2|G+k|^2, dense eigendecompositions of small assembled operators, and the scalar
+Chebyshev polynomial of the sigma-form recurrence.
+"""
+import numpy as np
+import pytest
+
+from dftfe_gb300 import fe
+from oracle import oracle as orc
+from tests.helpers import cheb_scalar, dense_operator, oracle_op, small_problem
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6, 7])
+def test_gll_rule_exactness(p):
+    x, w = fe.gll_nodes_weights(p)
+    assert abs(w.sum() - 1.0) < 1e-14
+    for k in range(2 * p):  # GLL with p+1 points is exact to degree 2p-1
+        assert abs((w * x ** k).sum() - 1.0 / (k + 1)) < 1e-13
+
+
+def test_lagrange_basis_interpolates():
+    x, _ = fe.gll_nodes_weights(4)
+    phi, dphi = fe.lagrange_1d(x, x)
+    assert np.allclose(phi, np.eye(5), atol=1e-13)
+    assert np.allclose(dphi.sum(1), 0.0, atol=1e-11)   # derivative of the constant 1
+
+
+def test_mass_and_map():
+    m = fe.PeriodicCubeMesh(3, 6.0, 3)
+    assert abs(m.lumped_mass().sum() - 6.0 ** 3) < 1e-10
+    cm = m.cell_dof_map()
+    assert cm.min() == 0 and cm.max() == m.n_dofs - 1
+    assert len(np.unique(cm)) == m.n_dofs
+
+
+def test_cell_matrix_sum_factorisation_matches_direct_formula():
+    pr = small_problem(n=2, L=4.0, p=3, wells=3)
+    mesh = pr.mesh
+    nq1 = mesh.p + 3
+    xq, _ = fe.gauss_nodes_weights(nq1)
+    phi, _ = mesh.shape_1d(xq)
+    q = np.arange(nq1 ** 3)
+    qx, qy, qz = q % nq1, (q // nq1) % nq1, q // (nq1 * nq1)
+    i = np.arange(mesh.nodes_per_cell)
+    p1 = mesh.p + 1
+    N = phi[qx][:, i % p1] * phi[qy][:, (i // p1) % p1] * phi[qz][:, i // (p1 * p1)]
+    Hdir = orc.cell_hamiltonians_direct(mesh.stiffness_cell(), N, pr.info["vjxw"])
+    assert np.abs(Hdir - pr.cell_mats).max() < 1e-12 * np.abs(Hdir).max()
+
+
+@pytest.mark.parametrize("n,L,p", [(2, 6.0, 4), (3, 6.0, 3)])
+def test_free_particle_spectrum_matches_plane_waves(n, L, p):
+    """K1: V = 0 gives 1/2|G|^2 to FE accuracy (degenerate multiplets intact)."""
+    mesh = fe.PeriodicCubeMesh(n, L, p)
+    K = mesh.stiffness_cell()
+    mats = np.broadcast_to(0.5 * K, (mesh.n_cells,) + K.shape).copy()
+    op = orc.OracleOperator(mesh.cell_dof_map(), mats, 1 / np.sqrt(mesh.lumped_mass()), mesh.n_dofs)
+    ev = np.linalg.eigvalsh(op.dense())
+    g = 2 * np.pi / L
+    assert abs(ev[0]) < 1e-10
+    assert np.allclose(ev[1:7], 0.5 * g * g, rtol=2e-2)
+    assert np.ptp(ev[1:4]) < 1e-9     # cubic symmetry: exact 3-fold (x, y, z) degeneracy
+
+
+def test_bloch_free_particle():
+    """Complex Bloch cell matrices: Hermitian assembly, eigenvalues 1/2|G+k|^2."""
+    mesh = fe.PeriodicCubeMesh(2, 6.0, 4)
+    k = np.array([0.1, -0.2, 0.15])
+    v = np.zeros((mesh.n_cells, (mesh.p + 3) ** 3))
+    Hc = fe.cell_hamiltonians(mesh, v, kpoint=k)
+    op = orc.OracleOperator(mesh.cell_dof_map(), Hc, 1 / np.sqrt(mesh.lumped_mass()), mesh.n_dofs)
+    A = op.dense()
+    assert np.abs(A - A.conj().T).max() < 1e-12
+    ev = np.linalg.eigvalsh(A)
+    g = 2 * np.pi / 6.0
+    pw = sorted(0.5 * np.sum((g * np.array([i, j, l]) + k) ** 2)
+                for i in range(-2, 3) for j in range(-2, 3) for l in range(-2, 3))
+    assert np.allclose(ev[:6], pw[:6], rtol=1e-3)
+
+
+def test_oracle_hx_matches_dense_assembly_with_projectors():
+    pr = small_problem(projectors=True, wells=2)
+    op = oracle_op(pr)
+    A = dense_operator(pr)
+    X = np.random.default_rng(3).standard_normal((pr.n_dofs, 5))
+    Y = op.HX(X)
+    assert np.abs(Y - A @ X).max() < 1e-12 * np.abs(A @ X).max()
+    # scaleFlag semantics: dst + scalar * A src
+    Z = np.ones_like(X)
+    op.HX(X, scalar=0.5, dst=Z, accumulate=True)
+    assert np.allclose(Z, 1.0 + 0.5 * (A @ X), atol=1e-12)
+
+
+def test_oracle_constraint_path_matches_folded_map():
+    """Periodicity as constraint rows on the unfolded lattice == folded map (masters)."""
+    pr = small_problem(n=2, L=4.0, p=2, wells=2)
+    folded = oracle_op(pr)
+    emap, n_ext, cons, mass_ext = __import__("tests.helpers", fromlist=["x"]).unfolded_setup(pr)
+    unf = orc.OracleOperator(emap, pr.cell_mats, 1 / np.sqrt(mass_ext), n_ext, constraints=cons)
+    X = np.random.default_rng(4).standard_normal((pr.n_dofs, 3))
+    e2f = pr.mesh.extended_to_folded()
+    Xe = X[e2f]
+    Ye = unf.HX(Xe)
+    Yf = folded.HX(X)
+    is_master = np.ones(n_ext, bool)
+    is_master[cons[0]] = False
+    assert np.abs(Ye[cons[0]]).max() == 0.0
+    assert np.allclose(Ye[is_master], Yf[e2f[is_master]], atol=1e-12)
+
+
+def test_oracle_filter_is_the_chebyshev_polynomial():
+    pr = small_problem(wells=2)
+    op = oracle_op(pr)
+    A = dense_operator(pr)
+    lam, Q = np.linalg.eigh(A)
+    X = Q[:, :4] + 0.1 * Q[:, 10:14]
+    a, b, a0, m = lam[8], lam[-1] + 0.1, lam[0] - 0.5, 7
+    Y = op.chebyshev_filter(X, m, a, b, a0)
+    ref = Q @ (cheb_scalar(lam, m, a, b, a0)[:, None] * (Q.T @ X))
+    assert np.abs(Y - ref).max() < 1e-10 * np.abs(ref).max()
+
+
+def test_oracle_chefsi_converges_to_dense_eigenvalues():
+    """K2: CheFSI Ritz values equal the dense eigenvalues (tiny mesh)."""
+    pr = small_problem(projectors=True, nwfc=10)
+    op = oracle_op(pr)
+    exact = np.linalg.eigvalsh(dense_operator(pr))
+    X = pr.initial_vectors()
+    st = orc.SolverState(a0=np.floor(exact[0]), b_low=exact[14], b_up=np.ceil(exact[-1] + 0.5))
+    for _ in range(25):
+        ev, res, X = orc.solve(op, X, st, m=12)
+    assert np.abs(ev[:8] - exact[:8]).max() < 1e-10
+    assert res[:8].max() < 1e-8
+
+
+def test_chebyshev_order_table():
+    assert orc.chebyshev_order(400) == 24
+    assert orc.chebyshev_order(600) == 30
+    assert orc.chebyshev_order(1e9) == 1250
+
+
+def test_lanczos_bounds_enclose_spectrum():
+    pr = small_problem(wells=2)
+    op = oracle_op(pr)
+    ev = np.linalg.eigvalsh(dense_operator(pr))
+    lo, up = orc.lanczos_bounds(op, np.random.default_rng(0).uniform(0, 1, pr.n_dofs), k=20)
+    assert lo <= ev[0] and up >= ev[-1] - 1e-8
+
+
+def test_golden_fixture_reproduces():
+    """The committed golden fixture (tests/golden/make_golden.py) still matches the oracle."""
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "small_p2.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture not generated")
+    from tests.golden.make_golden import build_case
+    g = np.load(path)
+    out = build_case()
+    for k in g.files:
+        assert np.allclose(out[k], g[k], rtol=1e-11, atol=1e-12), k
