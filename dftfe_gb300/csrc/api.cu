@@ -133,6 +133,10 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
                        hx_filter32(op, prec, src, dst, B, scv, acc, st);
                      },
                      st);
+  if (prec == CHEFSI_PREC_MIXED) {
+    const int tc = tc_check_error(op, st);
+    if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
+  }
   copy_block<float, double>(Xb, B, X + j0, ld, M, B, 1.0 / scale, st);
 }
 
@@ -314,6 +318,8 @@ int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, in
   } else if (precision == CHEFSI_PREC_MIXED) {
     if (!hx_tc(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st))
       throw Error(CHEFSI_ERR_UNSUPPORTED, "tensor-core HX unavailable for this operator");
+    const int tc = tc_check_error(op, st);
+    if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   } else if (precision == CHEFSI_PREC_FP32) {
     hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
   } else {

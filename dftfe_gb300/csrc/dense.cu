@@ -475,6 +475,9 @@ void trtri_lower(double* L, int N, cudaStream_t st) {
 }
 
 // ======================================================================= eigensolver
+// The eigensolver kernels read and write the same work arrays through derived pointers; they
+// carry no __restrict__ qualifiers (with them, nvcc produced wrong inverse-iteration vectors
+// on sm_103a while the identical host build was exact).
 // Householder step k on the symmetric row-major A (full storage maintained):
 // x = A[k+1:N, k]; v = x - alpha e1 with alpha = -sign(x0) |x|; tau = 2 / v^T v.
 // The reflector is kept in V[k][k+1:N] with tau[k]; d[k] = A[k][k], e[k] = alpha.
@@ -514,8 +517,8 @@ __global__ void k_hh_vector(double* A, int N, int k, double* V, double* tau, dou
 }
 
 // p = tau * A22 v   (one warp per row of the trailing block)
-__global__ void k_hh_symv(const double* __restrict__ A, int N, int k, const double* __restrict__ V,
-                          const double* __restrict__ tau, double* __restrict__ p) {
+__global__ void k_hh_symv(const double* A, int N, int k, const double* V,
+                          const double* tau, double* p) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int n = N - k - 1;
@@ -529,7 +532,7 @@ __global__ void k_hh_symv(const double* __restrict__ A, int N, int k, const doub
 }
 
 // w = p - (tau/2)(p^T v) v   (single CTA)
-__global__ void k_hh_w(int N, int k, const double* __restrict__ V, const double* __restrict__ tau,
+__global__ void k_hh_w(int N, int k, const double* V, const double* tau,
                        double* p) {
   __shared__ double red[32];
   const int n = N - k - 1;
@@ -550,8 +553,8 @@ __global__ void k_hh_w(int N, int k, const double* __restrict__ V, const double*
 }
 
 // A22 -= v w^T + w v^T
-__global__ void k_hh_rank2(double* A, int N, int k, const double* __restrict__ V,
-                           const double* __restrict__ w) {
+__global__ void k_hh_rank2(double* A, int N, int k, const double* V,
+                           const double* w) {
   const int n = N - k - 1;
   const int64_t tot = (int64_t)n * n;
   const double* v = V + (int64_t)k * N + k + 1;
@@ -586,8 +589,8 @@ __device__ int sturm_count(const double* d, const double* e, int n, double x, do
   return cnt;
 }
 
-__global__ void k_bisect(const double* __restrict__ d, const double* __restrict__ e, int n,
-                         double* __restrict__ w) {
+__global__ void k_bisect(const double* d, const double* e, int n,
+                         double* w) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
   double lo = 1e300, hi = -1e300, emax = 0.0;
@@ -618,9 +621,9 @@ __global__ void k_bisect(const double* __restrict__ d, const double* __restrict_
 // second super-diagonal where rows were swapped), five iterations from a deterministic start
 // vector, modified Gram-Schmidt against earlier members of the same cluster (eigenvalues
 // closer than ortol). One thread owns a whole cluster. Workspace per vector: 5n doubles.
-__global__ void k_inverse_iteration(const double* __restrict__ d, const double* __restrict__ e,
-                                    int n, const double* __restrict__ w, double* __restrict__ Z,
-                                    int ldz, double* __restrict__ work, unsigned char* swaps,
+__global__ void k_inverse_iteration(const double* d, const double* e,
+                                    int n, const double* w, double* Z,
+                                    int ldz, double* work, unsigned char* swaps,
                                     double ortol) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
@@ -707,8 +710,8 @@ __global__ void k_inverse_iteration(const double* __restrict__ d, const double* 
 }
 
 // r[j] = v^T Z[:, j] over rows k+1..N-1
-__global__ void k_bt_dot(const double* __restrict__ V, int N, int k, const double* __restrict__ Z,
-                         double* __restrict__ r) {
+__global__ void k_bt_dot(const double* V, int N, int k, const double* Z,
+                         double* r) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= N) return;
   const double* v = V + (int64_t)k * N;
@@ -716,9 +719,9 @@ __global__ void k_bt_dot(const double* __restrict__ V, int N, int k, const doubl
   for (int i = k + 1; i < N; ++i) s += v[i] * Z[(int64_t)i * N + j];
   r[j] = s;
 }
-__global__ void k_bt_update(const double* __restrict__ V, int N, int k,
-                            const double* __restrict__ tau, double* __restrict__ Z,
-                            const double* __restrict__ r) {
+__global__ void k_bt_update(const double* V, int N, int k,
+                            const double* tau, double* Z,
+                            const double* r) {
   const int n = N - k - 1;
   const int64_t tot = (int64_t)n * N;
   const double* v = V + (int64_t)k * N;

@@ -53,6 +53,8 @@ struct chefsi_operator_s {
   int nl_n_chunks = 0;
   chefsi::DeviceBuffer<int> nl_chunk_atom, nl_chunk_row0;
 
+  chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
+
   // workspaces (grow-only)
   chefsi::DeviceBuffer<double> ws64a, ws64b, nlW64;
   chefsi::DeviceBuffer<float> nlW32;
@@ -72,6 +74,11 @@ void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int6
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st);
 void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st);
+// device error flag of the tensor-core kernel (CHEFSI_OK or CHEFSI_ERR_TIMEOUT); clears it
+int tc_check_error(chefsi_operator_s* op, cudaStream_t st);
+// nonlocal term y += scalar * C V C^T x for FP32 vectors (used by the tensor-core path)
+void apply_nonlocal_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst,
+                        int64_t ldd, int B, double scalar, cudaStream_t st);
 
 // ---- elementwise helpers (operator.cu) ----------------------------------------------------
 template <typename T>

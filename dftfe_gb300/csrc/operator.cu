@@ -490,6 +490,13 @@ void hx_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
                     accumulate, st, cell_f32);
 }
 
+void apply_nonlocal_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst,
+                        int64_t ldd, int B, double scalar, cudaStream_t st) {
+  if (op->n_atoms == 0) return;
+  float* W = op->nlW32.ensure((size_t)op->n_atoms * op->n_proj * B);
+  apply_nonlocal<float>(op, op->nl_vals32.ptr, W, src, lds, dst, ldd, B, scalar, st);
+}
+
 void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int64_t ldd, int B,
             double scalar, bool accumulate, cudaStream_t st) {
   CHEFSI_REQUIRE(op->is_complex, "hx_c64 on a real operator");

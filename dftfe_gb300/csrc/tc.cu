@@ -1,10 +1,510 @@
-// Tensor-core (tcgen05) filter HX: placeholder until the kernel lands.
+// Tensor-core filter HX on GB300: tcgen05 MMAs with FP16-split operands, FP32 accumulation
+// in tensor memory, fused gather / scatter through the cell -> dof map.
+//
+// DFT-FE's local HX (src/dftOperator/matrixVectorProductImplementationsDevice.cc:27-117)
+// gathers X into n_cells x n_e x B cell blocks, calls gemmStridedBatched and scatter-adds.
+// Here one CTA owns one (cell, 128-vector chunk):
+//   * warp 0 (one lane) streams K-blocks of the cell matrix (FP16 hi and lo parts, 64-byte
+//     rows, 64B-swizzled) into shared memory with TMA;
+//   * warps 2..5 gather the chunk's X rows (FP32) straight from the global block through the
+//     cell's dof map, split each value into FP16 hi + lo and write them K-major with the same
+//     swizzle (one thread per vector, so the global loads coalesce along the vectors);
+//   * warp 1 (one lane) issues tcgen05.mma kind::f16 with M = 128 vectors, N = the cell's
+//     rows (one or two MMAs of N <= 256), K = 16:
+//       D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T           (the lo*lo term is below 2^-22)
+//     and the accumulator D[vector][row] (FP32) stays in tensor memory;
+//   * warps 2..5 then read D with tcgen05.ld (lane = vector) and scatter-add
+//     scalar * D / 2^s into the output rows with red.global.add.f32 -- for every cell row the
+//     32 lanes of a warp hit 32 consecutive floats, so each atomic instruction is one 128-byte
+//     line.
+// A 3..4-stage mbarrier pipeline overlaps TMA, the X split and the MMAs. Every mbarrier wait
+// is bounded: on expiry the CTA records CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded)
+// for its own TMA copies, frees its tensor memory and returns.
 #include "internal.h"
 
+#include <cuda.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
 namespace chefsi {
-void prepare_tensor_mats(chefsi_operator_s*, cudaStream_t) {}
-bool hx_tc(chefsi_operator_s*, const float*, int64_t, float*, int64_t, int, double, bool,
-           cudaStream_t) {
+
+namespace {
+
+constexpr int kVec = 128;          // vectors per CTA (MMA M)
+constexpr int kKB = 32;            // halves per K-block (64-byte rows)
+constexpr int kRowBytes = kKB * 2; // 64
+constexpr int kThreads = 192;      // 6 warps
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; returns false on expiry (and records the timeout)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (i > 64) __nanosleep(128);
+  }
+  atomicExch(err, CHEFSI_ERR_TIMEOUT);
+  *abort_flag = 1;
   return false;
 }
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);          // start address
+  d |= (uint64_t)(1) << 16;                        // leading byte offset (unused, K-major swizzled)
+  d |= (uint64_t)((512 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                          // descriptor version for tcgen05
+  d |= (uint64_t)4 << 61;                          // layout: SWIZZLE_64B
+  return d;
+}
+
+// instruction descriptor, kind::f16: A = B = F16, D = F32, both K-major
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcArgs {
+  const float* src;
+  int64_t lds;
+  float* dst;
+  int64_t ldd;
+  const int* map;
+  int n_e;
+  int npad;
+  int nkb;
+  int B;
+  int n_chunks;
+  int n_mma;      // 1 or 2 MMAs along N
+  int n_half;     // N per MMA
+  int tmem_cols;
+  int stages;
+  float out_scale;  // scalar / 2^s
+  int* err;
+};
+
+// shared memory carve-up (offsets from a 1024-byte aligned base)
+struct Layout {
+  int x_tile;   // 128 rows x 64 B = 8 KB
+  int a_tile;   // npad rows x 64 B
+  int stage;    // xhi, xlo, ahi, alo
+  int bars;     // barrier block offset
+  int maps;     // cell dof map
+  int total;
+};
+__host__ __device__ inline Layout make_layout(int npad, int stages, int n_e) {
+  Layout L;
+  L.x_tile = kVec * kRowBytes;
+  L.a_tile = ((npad * kRowBytes + 1023) / 1024) * 1024;
+  L.stage = 2 * L.x_tile + 2 * L.a_tile;
+  L.bars = stages * L.stage;
+  L.maps = L.bars + 8 * (3 * stages + 4);
+  L.total = L.maps + 4 * ((n_e + 3) / 4 * 4) + 16;
+  return L;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
+                      const __grid_constant__ CUtensorMap tm_lo, TcArgs args) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int S = args.stages;
+  const Layout L = make_layout(args.npad, S, args.n_e);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
+  uint64_t* tma_full = bars;            // [S] TMA bytes landed
+  uint64_t* x_full = bars + S;          // [S] 128 producer arrivals
+  uint64_t* empty = bars + 2 * S;       // [S] MMA finished reading
+  uint64_t* acc_full = bars + 3 * S;    // accumulator ready
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 3 * S + 2);
+  int* smap = reinterpret_cast<int*>(smem + L.maps);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x / args.n_chunks;
+  const int chunk = blockIdx.x % args.n_chunks;
+  const int b0 = chunk * kVec;
+
+  for (int i = threadIdx.x; i < args.n_e; i += kThreads)
+    smap[i] = args.map[(int64_t)cell * args.n_e + i];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&tma_full[s], 1);
+      mbar_init(&x_full[s], kVec);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(args.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int nkb = args.nkb;
+  if (warp == 0) {
+    // ---------------- TMA producer: cell-matrix K-blocks (hi, lo)
+    if (lane == 0) {
+      const uint32_t bytes = 2u * args.npad * kRowBytes;
+      int issued = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % S, r = kb / S;
+        if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
+        uint8_t* st = smem + s * L.stage;
+        mbar_arrive_expect_tx(&tma_full[s], bytes);
+        for (int h = 0; h < args.n_mma; ++h) {
+          tma_load_3d(st + 2 * L.x_tile + h * args.n_half * kRowBytes, &tm_hi, kb * kKB,
+                      h * args.n_half, cell, &tma_full[s]);
+          tma_load_3d(st + 2 * L.x_tile + L.a_tile + h * args.n_half * kRowBytes, &tm_lo,
+                      kb * kKB, h * args.n_half, cell, &tma_full[s]);
+        }
+        issued = kb + 1;
+      }
+      if (*abort_flag) {
+        // let our own copies land before the CTA exits (bounded)
+        for (int kb = (issued > S ? issued - S : 0); kb < issued; ++kb) {
+          const int s = kb % S, r = kb / S;
+          for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(&tma_full[s], r & 1); ++i)
+            __nanosleep(128);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = idesc_f16(kVec, args.n_half);
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % S, r = kb / S;
+        if (!mbar_wait(&tma_full[s], r & 1, args.err, abort_flag)) break;
+        if (!mbar_wait(&x_full[s], r & 1, args.err, abort_flag)) break;
+        fence_after();
+        const uint32_t st = smem_u32(smem + s * L.stage);
+        const uint32_t xhi = st, xlo = st + L.x_tile;
+        const uint32_t ahi = st + 2 * L.x_tile, alo = ahi + L.a_tile;
+#pragma unroll
+        for (int ks = 0; ks < kKB / 16; ++ks) {
+          const uint32_t koff = ks * 32;  // 16 halves = 32 bytes along K
+          for (int h = 0; h < args.n_mma; ++h) {
+            const uint32_t d = tmem + h * args.n_half;
+            const uint32_t boff = h * args.n_half * kRowBytes + koff;
+            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(ahi + boff), idesc, acc0);
+            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(alo + boff), idesc, 1u);
+            mma_f16(d, smem_desc_sw64(xlo + koff), smem_desc_sw64(ahi + boff), idesc, 1u);
+          }
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(acc_full);
+      // the MMAs must be complete before tensor memory is freed, also on the abort path
+      for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(acc_full, 0); ++i) __nanosleep(128);
+    }
+  } else {
+    // ---------------- X producers (warps 2..5), then the epilogue
+    const int q = warp & 3;                  // tensor-memory lane quarter of this warp
+    const int v = q * 32 + lane;             // vector within the chunk (= MMA row)
+    const int gb = b0 + v;
+    const bool vok = gb < args.B;
+    const float* src = args.src + gb;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % S, r = kb / S;
+      if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
+      uint8_t* st = smem + s * L.stage;
+      float x[kKB];
+#pragma unroll
+      for (int j = 0; j < kKB; ++j) {
+        const int J = kb * kKB + j;
+        x[j] = (vok && J < args.n_e) ? __ldg(src + (int64_t)smap[J] * args.lds) : 0.f;
+      }
+      uint8_t* rhi = st + v * kRowBytes;
+      uint8_t* rlo = st + L.x_tile + v * kRowBytes;
+      const int sw = (v >> 1) & 3;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        uint32_t hv[4], lv[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const float a0 = x[c * 8 + 2 * t], a1 = x[c * 8 + 2 * t + 1];
+          const __half2 h = __floats2half2_rn(a0, a1);
+          const float2 hf = __half22float2(h);
+          const __half2 l = __floats2half2_rn(a0 - hf.x, a1 - hf.y);
+          hv[t] = *reinterpret_cast<const uint32_t*>(&h);
+          lv[t] = *reinterpret_cast<const uint32_t*>(&l);
+        }
+        const int pc = (c ^ sw) * 16;
+        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&x_full[s]);
+    }
+    // epilogue (warp-uniform decision: tcgen05.ld is a .sync.aligned instruction)
+    const bool acc_ok = __all_sync(0xffffffffu, mbar_wait(acc_full, 0, args.err, abort_flag));
+    if (acc_ok) {
+      fence_after();
+      const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+      float* dstb = args.dst + gb;
+      const int ncols = args.n_mma * args.n_half;
+      for (int c0 = 0; c0 < ncols; c0 += 16) {
+        float vals[16];
+        tmem_ld16(tq + c0, vals);
+        if (vok) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int I = c0 + i;
+            if (I < args.n_e) atomicAdd(dstb + (int64_t)smap[I] * args.ldd, args.out_scale * vals[i]);
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(args.tmem_cols));
+  }
+}
+
+// ---------------------------------------------------------------- host side
+__global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n_e, int npad,
+                             double scale, __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int64_t n = (int64_t)n_cells * npad * npad;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / ((int64_t)npad * npad);
+    const int r = (int)(t % ((int64_t)npad * npad));
+    const int I = r / npad, J = r % npad;
+    double v = 0.0;
+    if (I < n_e && J < n_e) v = scale * mats[(c * n_e + I) * n_e + J];
+    const __half h = __double2half(v);
+    hi[t] = h;
+    lo[t] = __double2half(v - (double)__half2float(h));
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {(cuuint64_t)npad, (cuuint64_t)npad, (cuuint64_t)n_cells};
+  cuuint64_t strides[2] = {(cuuint64_t)npad * 2, (cuuint64_t)npad * npad * 2};
+  cuuint32_t box[3] = {(cuuint32_t)kKB, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+struct TcPlan {
+  int npad, n_mma, n_half, tmem_cols, stages, smem;
+};
+
+TcPlan plan_for(int n_e) {
+  TcPlan p{};
+  p.npad = (n_e + 31) / 32 * 32;
+  if (p.npad <= 256) {
+    p.n_mma = 1;
+    p.n_half = p.npad;
+  } else {
+    p.n_mma = 2;
+    p.n_half = p.npad / 2;  // multiple of 16
+  }
+  const int ncol = p.n_mma * p.n_half;
+  p.tmem_cols = ncol <= 32 ? 32 : ncol <= 64 ? 64 : ncol <= 128 ? 128 : ncol <= 256 ? 256 : 512;
+  const int budget = 220 * 1024;
+  p.stages = 4;
+  while (p.stages > 2 && make_layout(p.npad, p.stages, n_e).total + 1024 > budget) --p.stages;
+  p.smem = make_layout(p.npad, p.stages, n_e).total + 1024;
+  return p;
+}
+
+}  // namespace
+
+void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
+  auto& tc = op->tc;
+  if (tc.ready || op->is_complex || !op->folded) return;
+  const int n_e = op->n_e;
+  const TcPlan p = plan_for(n_e);
+  CHEFSI_REQUIRE(p.n_half <= 256 && p.n_half % 16 == 0, "cell too large for the tensor path");
+  // power-of-two scale: largest |A_e| -> [2^14, 2^15)
+  DeviceBuffer<double> amax(1);
+  absmax_block_f64(op->mats64.ptr, n_e, (int64_t)op->n_cells * n_e, n_e, amax.ptr, st);
+  double h = 0.0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&h, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  const int e = (h > 0 && std::isfinite(h)) ? 14 - (int)std::floor(std::log2(h)) : 0;
+  tc.scale = (float)std::ldexp(1.0, e);
+  tc.npad = p.npad;
+  tc.kpad = p.npad;
+  const size_t n = (size_t)op->n_cells * p.npad * p.npad;
+  tc.hi.reset(n);
+  tc.lo.reset(n);
+  k_split_mats<<<grid_for((int64_t)n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, n_e, p.npad,
+                                                          std::ldexp(1.0, e), tc.hi.ptr, tc.lo.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  tc.ready = true;
+}
+
+bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+           double scalar, bool accumulate, cudaStream_t st) {
+  if (op->is_complex || !op->folded || op->n_e > 512) return false;
+  if (!get_encode()) return false;
+  int dev = 0, major = 0, minor = 0;
+  CHEFSI_CUDA(cudaGetDevice(&dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (major != 10) return false;  // sm_100 family (GB300 = 10.3)
+  prepare_tensor_mats(op, st);
+  const TcPlan p = plan_for(op->n_e);
+  if (!op->tc_err.ptr) {
+    op->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  }
+  CUtensorMap mhi, mlo;
+  make_map(&mhi, op->tc.hi.ptr, op->n_cells, p.npad, p.n_half);
+  make_map(&mlo, op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
+  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  TcArgs a{};
+  a.src = src;
+  a.lds = lds;
+  a.dst = dst;
+  a.ldd = ldd;
+  a.map = op->map.ptr;
+  a.n_e = op->n_e;
+  a.npad = p.npad;
+  a.nkb = p.npad / kKB;
+  a.B = B;
+  a.n_chunks = (B + kVec - 1) / kVec;
+  a.n_mma = p.n_mma;
+  a.n_half = p.n_half;
+  a.tmem_cols = p.tmem_cols;
+  a.stages = p.stages;
+  a.out_scale = (float)(scalar / op->tc.scale);
+  a.err = op->tc_err.ptr;
+  static bool attr_set = false;
+  if (!attr_set) {
+    CHEFSI_CUDA(cudaFuncSetAttribute(cell_hx_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     227 * 1024));
+    attr_set = true;
+  }
+  const int64_t blocks = (int64_t)op->n_cells * a.n_chunks;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "tensor HX grid too large");
+  cell_hx_tc_kernel<<<(unsigned)blocks, kThreads, p.smem, st>>>(mhi, mlo, a);
+  CHEFSI_CHECK_LAUNCH();
+  apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
+  return true;
+}
+
+int tc_check_error(chefsi_operator_s* op, cudaStream_t st) {
+  if (!op->tc_err.ptr) return CHEFSI_OK;
+  int h = 0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&h, op->tc_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  if (h) CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  return h;
+}
+
 }  // namespace chefsi

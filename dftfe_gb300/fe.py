@@ -204,18 +204,29 @@ def min_image(d: np.ndarray, L: float) -> np.ndarray:
 
 
 def gaussian_wells_potential(points: np.ndarray, centres: np.ndarray, depths: np.ndarray,
-                             width: float, L: float, chunk: int = 1 << 18) -> np.ndarray:
-    """V(r) = -sum_w d_w exp(-|r - R_w|^2 / (2 s^2)) under the minimum-image convention."""
-    pts = points.reshape(-1, 3)
-    out = np.zeros(len(pts))
-    for s in range(0, len(pts), chunk):
-        blk = pts[s:s + chunk]
-        acc = np.zeros(len(blk))
-        for R, dep in zip(centres, depths):
-            d = min_image(blk - R[None, :], L)
-            acc -= dep * np.exp(-(d * d).sum(1) / (2.0 * width * width))
-        out[s:s + chunk] = acc
-    return out.reshape(points.shape[:-1])
+                             width: float, L: float, cutoff_sigmas: float = 8.0) -> np.ndarray:
+    """V(r) = -sum_w d_w exp(-|r - R_w|^2 / (2 s^2)) under the minimum-image convention.
+
+    ``points`` is [n_cells, nq, 3]; each well is evaluated on the cells whose bounding box
+    lies within ``cutoff_sigmas`` widths of its centre (exp(-32) ~ 1e-14 beyond 8 widths).
+    """
+    pts = np.asarray(points)
+    nc = pts.shape[0]
+    out = np.zeros(pts.shape[:-1])
+    lo_c = pts.min(axis=1)
+    hi_c = pts.max(axis=1)
+    rc = cutoff_sigmas * width
+    for R, dep in zip(centres, depths):
+        lo = min_image(lo_c - R[None, :], L)
+        span = hi_c - lo_c
+        gap = np.where((lo <= 0.0) & (lo + span >= 0.0), 0.0,
+                       np.minimum(np.abs(lo), np.abs(lo + span)))
+        sel = np.nonzero((gap * gap).sum(1) < rc * rc)[0] if nc > 1 else np.arange(nc)
+        if len(sel) == 0:
+            continue
+        d = min_image(pts[sel] - R[None, None, :], L)
+        out[sel] -= dep * np.exp(-(d * d).sum(-1) / (2.0 * width * width))
+    return out
 
 
 def cell_mass_like_matrices(mesh: PeriodicCubeMesh, weights: np.ndarray, nq1: int,
