@@ -1,0 +1,358 @@
+"""Benchmark: one CheFSI iteration (filter + Rayleigh-Ritz + residuals) on one GB300.
+
+Workload (default, the mixed-precision configuration): periodic cube L = 30 bohr, 20^3 cells,
+FE degree 6 (1,728,000 dofs), 64 seeded Gaussian wells with 8 Gaussian projectors each,
+1024 wavefunctions, Chebyshev degree 30, filter HX on the tensor cores with FP16-split
+operands, FP64 Cholesky and projected eigensolve. Synthetic seeded inputs (the reference
+publishes no input decks for this path). A "step" is one CheFSI iteration (chefsi_solve).
+
+Prints one JSON line. With --impl reference it times the CPU oracle (the FP64 restatement
+of the reference's CPU CheFSI) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+METRIC = "CheFSI iter time & HX GFLOP/s on 1 GB300: mixed vs FP64 at <=1e-6 Ha Ritz error"
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i, v in enumerate(r[5:9])
+                          if v.strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def hx_algorithmic(pr, B, s_h=4, s_x=4):
+    """Bytes and flops of one filter HX over B vectors (reference formulation):
+    flops = 2 n_c n_e^2 B + 4 n_nlc-rows P B; bytes = s_H n_c n_e^2 + 2 s_X M B + 4 n_c n_e."""
+    nc, ne = pr.mesh.n_cells, pr.mesh.nodes_per_cell
+    nl_rows = 0 if pr.nonlocal_ is None else int(pr.nonlocal_.ptr[-1])
+    P = 0 if pr.nonlocal_ is None else pr.nonlocal_.n_proj
+    flops = 2.0 * nc * ne * ne * B + 4.0 * nl_rows * P * B
+    bytes_ = s_h * nc * ne * ne + 2.0 * s_x * pr.n_dofs * B + 4.0 * nc * ne
+    return flops, bytes_
+
+
+def build_workload(name, seed):
+    from dftfe_gb300 import problems
+    return problems.workload(name, seed=seed)
+
+
+def cpu_sample(pr, m, N, max_seconds=25.0):
+    """Time the CPU oracle's HX on a bounded block of vectors and extrapolate one CheFSI
+    iteration: (m + 2) HX over all N vectors + the dense RR products (numpy BLAS, timed on
+    an (M x n_s) sample and scaled by (N/n_s)^2)."""
+    from oracle import oracle as orc
+    op = orc.OracleOperator(pr.cell_map, pr.cell_mats, pr.inv_sqrt_mass, pr.n_dofs,
+                            projectors=pr.nonlocal_)
+    threads = orc.lib().oracle_num_threads()
+    rng = np.random.default_rng(0)
+    B = 8
+    X = rng.uniform(-1, 1, (pr.n_dofs, B))
+    op.HX(X)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        op.HX(X)
+        reps += 1
+        if time.perf_counter() - t0 > max_seconds * 0.6 or reps >= 3:
+            break
+    t_hx = (time.perf_counter() - t0) / reps
+    ns = min(N, 128)
+    Xs = rng.standard_normal((pr.n_dofs, ns))
+    t0 = time.perf_counter()
+    S = Xs.T @ Xs
+    _ = Xs @ S
+    t_gemm = (time.perf_counter() - t0) / 2.0   # one (M x ns x ns) product
+    t_iter = (m + 2) * t_hx * (N / B) + 4 * t_gemm * (N / ns) ** 2
+    return {"value": t_iter, "unit": "s/iter", "cores": threads, "kind": "port",
+            "sample": f"oracle HX on {B} of {N} vectors x{reps} ({t_hx:.2f} s each) and a "
+                      f"{pr.n_dofs}x{ns}x{ns} numpy GEMM; iteration = (m+2) HX x N/{B} + "
+                      f"4 GEMM x (N/{ns})^2"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    pr = build_workload(args.workload, args.seed)
+    m = pr.cheb_degree
+    N = pr.n_wfc
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        base = cpu_sample(pr, m, N, max_seconds=20.0 if i < args.warmup else 25.0)
+        if i >= args.warmup:
+            vals.append(base["value"])
+    v = float(np.median(vals))
+    line = {"metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "n_dofs": pr.n_dofs, "n_wfc": N,
+                       "cheb_degree": m},
+            "cpu_baseline": dict(base, value=v),
+            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from dftfe_gb300 import build, chefsi
+    build.build()
+    pr = build_workload(args.workload, args.seed + rank)   # independent replica per rank
+    N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    lo, blow, up = chefsi.initial_bounds(op, N)
+    params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=N,
+                                 mixed_precision="mixed", rr_precision=args.rr_precision)
+    solver = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params)
+    solver.reinitSpectrumBounds(lo, blow, up)
+    solver.set_profiling(True, mixed=True)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 1)
+    X = (torch.rand((M, N), generator=g, device=dev, dtype=torch.float64) * 2 - 1)
+
+    def step(Xd):
+        ev, res = solver.solve(op, Xd, useMixedPrec=True)
+        solver.reinitSpectrumBounds(ev[0], ev[-1], up)
+        return ev, res
+
+    for _ in range(args.warmup):
+        step(X)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    hx_n, hx_ms = 0, 0.0
+    lib = __import__("dftfe_gb300._lib", fromlist=["load"]).load()
+    launches0 = lib.chefsi_launch_count()
+    with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed")
+        start.record()
+        for _ in range(args.steps):
+            ev, res = step(X)
+            n_, t_ = solver.hx_stats(True)
+            hx_n += n_
+            hx_ms += t_
+        end.record()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+    launches = lib.chefsi_launch_count() - launches0
+    if world > 1:
+        dist.barrier()
+    t_ms = start.elapsed_time(end) / args.steps
+    tm = torch.tensor([t_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+    t_ms = float(tm.item())
+    phases = solver.timings(True)
+
+    # end to end through the public API with host buffers: H2D of X, solve, D2H of X and
+    # of the eigenvalues / residual norms
+    host = torch.empty((M, N), dtype=torch.float64, pin_memory=True)
+    host.copy_(X)
+    Xd = torch.empty_like(X)
+    e2e_steps = max(1, min(args.steps, 2))
+    torch.cuda.synchronize()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record()
+    for _ in range(e2e_steps):
+        Xd.copy_(host, non_blocking=True)
+        ev, res = step(Xd)
+        host.copy_(Xd, non_blocking=True)
+    e2.record()
+    torch.cuda.synchronize()
+    e2e_ms = s2.elapsed_time(e2) / e2e_steps
+
+    hx_flops, hx_bytes = hx_algorithmic(pr, N)
+    hbm, bf16, src = peaks()
+    avg_hx_ms = hx_ms / max(hx_n, 1)
+    achieved = hx_bytes / (avg_hx_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": t_ms / 1e3, "unit": "s/iter", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f16split/f64",
+        "data": "synthetic (seeded wells/projectors, X0 ~ U(-1,1)); inputs larger than L2",
+        "config": {"workload": args.workload, "n_dofs": M, "n_cells": pr.mesh.n_cells,
+                   "fe_degree": pr.mesh.p, "n_wfc": N, "cheb_degree": m, "wells": 64,
+                   "projectors_per_well": 8, "precision": "mixed",
+                   "rr_hx_precision": args.rr_precision, "l2": "inputs > L2 (X is 14 GB)",
+                   "parallelism": f"replicas{world}"},
+        "hx_gflops": hx_flops / (avg_hx_ms * 1e-3) / 1e9,
+        "hx_ms": avg_hx_ms, "hx_launches_timed": hx_n,
+        "phases_ms": phases,
+        "ritz_sample": [float(ev[0]), float(ev[N // 2]), float(ev[-1])],
+        "gpu_launches": None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "kernel": "cell_hx_tc_kernel (+ nonlocal, filter HX)",
+                     "algorithmic_bytes_per_launch": hx_bytes},
+        "e2e": {"value": e2e_ms / 1e3, "unit": "s/iter", "h2d_bytes_per_step": M * N * 8,
+                "d2h_bytes_per_step": M * N * 8 + 2 * N * 8},
+        "clocks": clk.summary(),
+    }
+    line["gpu_launches"] = int(launches)
+    if args.fp64_compare:
+        line["fp64"] = fp64_compare(pr, op, lo, blow, up, m, N, dev)
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_sample(pr, m, N)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_hx_only(args):
+    """K launches of the mixed filter HX (tensor-core cell kernel + nonlocal) on FP32 blocks."""
+    import torch
+    from dftfe_gb300 import build, chefsi
+    build.build()
+    dev = torch.device("cuda", 0)
+    pr = build_workload(args.workload, args.seed)
+    N, M = pr.n_wfc, pr.n_dofs
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 1)
+    X = torch.rand((M, N), generator=g, device=dev, dtype=torch.float32) * 2 - 1
+    Y = torch.empty_like(X)
+    for _ in range(args.warmup):
+        op.HX(X, Y, precision="mixed")
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
+    s.record()
+    for _ in range(args.steps):
+        op.HX(X, Y, precision="mixed")
+    e.record()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.steps
+    fl, by = hx_algorithmic(pr, N)
+    hbm, bf16, src = peaks()
+    print(json.dumps({"metric": "filter HX (mixed) time", "value": ms, "unit": "ms",
+                      "workload": args.workload, "n_dofs": M, "n_wfc": N,
+                      "hx_gflops": fl / (ms * 1e-3) / 1e9,
+                      "achieved_gbs": by / (ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm,
+                      "algorithmic_bytes": by, "algorithmic_flops": fl}))
+    return 0
+
+
+def fp64_compare(pr, op, lo, blow, up, m, N, dev):
+    """One FP64 HX over all N vectors, timed, and the FP64 iteration estimate."""
+    import torch
+    from dftfe_gb300 import chefsi
+    X = torch.rand((pr.n_dofs, N), device=dev, dtype=torch.float64)
+    Y = torch.empty_like(X)
+    op.HX(X[:, :64].contiguous(), Y[:, :64].contiguous())
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    op.HX(X, Y)
+    e.record()
+    torch.cuda.synchronize()
+    hx64 = s.elapsed_time(e)
+    return {"hx_fp64_ms": hx64, "iter_fp64_ms_est": (m + 2) * hx64,
+            "note": "FP64 iteration estimated as (m+2) FP64 HX; dense FP64 steps excluded"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixed", choices=["mixed", "small", "large", "mixed_small"])
+    ap.add_argument("--hx-only", action="store_true",
+                    help="time only the tensor-core filter HX (K launches after W warm-up)")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--rr-precision", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--fp64-compare", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.hx_only:
+        return run_hx_only(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

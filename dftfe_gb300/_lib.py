@@ -28,12 +28,13 @@ _ERRNAMES = {1: "INVALID", 2: "CUDA", 3: "NOT_SPD", 4: "NO_CONVERGENCE", 5: "ALL
 
 # every symbol include/chefsi.h declares
 EXPORTS = [
-    "chefsi_last_error", "chefsi_version", "chefsi_operator_create", "chefsi_operator_destroy",
+    "chefsi_last_error", "chefsi_version", "chefsi_launch_count", "chefsi_operator_create", "chefsi_operator_destroy",
     "chefsi_operator_info", "chefsi_hx", "chefsi_overlap", "chefsi_xthx",
     "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_cholesky_gs",
     "chefsi_rayleigh_ritz", "chefsi_residual_norms", "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
-    "chefsi_solver_timings", "chefsi_solve", "chefsi_solve_no_rr", "chefsi_chebyshev_order",
+    "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
+    "chefsi_solve", "chefsi_solve_no_rr", "chefsi_chebyshev_order",
 ]
 
 
@@ -64,6 +65,7 @@ class Params(ctypes.Structure):
         ("wfc_block", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("lanczos_steps", ctypes.c_int32), ("reproducible", ctypes.c_int32),
         ("first_scf_degree_scale", ctypes.c_double), ("keep_hx", ctypes.c_int32),
+        ("rr_precision", ctypes.c_int32),
     ]
 
 
@@ -85,6 +87,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
     sig = {
         "chefsi_last_error": ([], ctypes.c_char_p),
         "chefsi_version": ([], ctypes.c_char_p),
+        "chefsi_launch_count": ([], ctypes.c_uint64),
         "chefsi_operator_create": ([ctypes.POINTER(OperatorDesc), ctypes.POINTER(vp)], ctypes.c_int),
         "chefsi_operator_destroy": ([vp], ctypes.c_int),
         "chefsi_operator_info": ([vp, vp, vp, vp, vp], ctypes.c_int),
@@ -102,6 +105,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solver_reinit_spectrum_bounds": ([vp, f64, f64, f64], ctypes.c_int),
         "chefsi_solver_get_bounds": ([vp, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_solver_timings": ([vp, vp], ctypes.c_int),
+        "chefsi_solver_set_profiling": ([vp, i32], ctypes.c_int),
+        "chefsi_solver_hx_stats": ([vp, vp, vp], ctypes.c_int),
         "chefsi_solve": ([vp, vp, vp, i32, vp, vp, i32, i32, vp], ctypes.c_int),
         "chefsi_solve_no_rr": ([vp, vp, vp, i32, i32, i32, vp], ctypes.c_int),
         "chefsi_chebyshev_order": ([f64], i32),

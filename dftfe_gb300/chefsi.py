@@ -208,6 +208,7 @@ class SolverParams:
     reproducible_output: bool = False
     chebyshevFilterPolyDegreeFirstScfScalingFactor: float = 1.34
     keep_hx: bool = True
+    rr_precision: str = "fp64"         # HX precision feeding X^T H X in mixed mode
 
 
 class ChebyshevOrthogonalizedSubspaceIterationSolver:
@@ -230,6 +231,7 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
             p.reproducible = int(self.params.reproducible_output)
             p.first_scf_degree_scale = self.params.chebyshevFilterPolyDegreeFirstScfScalingFactor
             p.keep_hx = int(self.params.keep_hx)
+            p.rr_precision = _prec(self.params.rr_precision)
             h = ctypes.c_void_p()
             check(self._lib.chefsi_solver_create(ctypes.byref(p), ctypes.byref(h)))
             self._h[key] = h
@@ -274,6 +276,14 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
         check(self._lib.chefsi_solver_timings(self._handle(mixed), t))
         keys = ["filter", "overlap_cholesky", "xthx", "eig", "rotation", "residual", "total"]
         return dict(zip(keys, list(t)))
+
+    def set_profiling(self, enable: bool = True, mixed: bool = True):
+        check(self._lib.chefsi_solver_set_profiling(self._handle(mixed), int(enable)))
+
+    def hx_stats(self, mixed: bool = True):
+        n, t = ctypes.c_int32(), ctypes.c_double()
+        check(self._lib.chefsi_solver_hx_stats(self._handle(mixed), ctypes.byref(n), ctypes.byref(t)))
+        return n.value, t.value
 
     def last_degree(self, mixed: bool = False) -> int:
         d = ctypes.c_int32()

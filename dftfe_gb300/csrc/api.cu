@@ -17,6 +17,7 @@
 
 namespace chefsi {
 const char* last_error_cstr();
+unsigned long long launch_count();
 chefsi_operator_s* create_operator(const chefsi_operator_desc* d);
 }  // namespace chefsi
 
@@ -30,12 +31,41 @@ struct chefsi_solver_s {
   DeviceBuffer<float> Xb32, Yb32;
   double times[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
+  bool profile = false;
+  std::vector<cudaEvent_t> hx_ev;   // pairs around filter HX launches
+  int hx_used = 0;
+  int hx_launches = 0;
+  double hx_ms = 0.0;
+  void hx_mark(cudaStream_t st) {
+    if (!profile) return;
+    if (hx_used >= (int)hx_ev.size()) {
+      cudaEvent_t e;
+      CHEFSI_CUDA(cudaEventCreate(&e));
+      hx_ev.push_back(e);
+    }
+    CHEFSI_CUDA(cudaEventRecord(hx_ev[hx_used++], st));
+  }
+  void hx_collect() {
+    hx_launches = 0;
+    hx_ms = 0.0;
+    for (int i = 0; i + 1 < hx_used; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, hx_ev[i], hx_ev[i + 1]) == cudaSuccess) {
+        hx_ms += ms;
+        ++hx_launches;
+      } else {
+        cudaGetLastError();
+      }
+    }
+    hx_used = 0;
+  }
   chefsi_solver_s() {
     for (auto& e : ev) cudaEventCreate(&e);
   }
   ~chefsi_solver_s() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    for (auto& e : hx_ev) cudaEventDestroy(e);
   }
 };
 
@@ -110,7 +140,9 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
     copy_block<double, double>(X + j0, ld, Xb, B, M, B, 1.0, st);
     cheb_filter<double>(Xb, Yb, M, B, m, a, b, a0,
                         [&](const double* src, double* dst, double sc, bool acc) {
+                          s->hx_mark(st);
                           hx_f64(op, src, B, dst, B, B, sc, acc, st);
+                          s->hx_mark(st);
                         },
                         st);
     copy_block<double, double>(Xb, B, X + j0, ld, M, B, 1.0, st);
@@ -130,7 +162,9 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
   copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
   cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
                      [&](const float* src, float* dst, double scv, bool acc) {
+                       s->hx_mark(st);
                        hx_filter32(op, prec, src, dst, B, scv, acc, st);
+                       s->hx_mark(st);
                      },
                      st);
   if (prec == CHEFSI_PREC_MIXED) {
@@ -221,9 +255,19 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   }
   trtri_lower(S, N, st);  // S now holds L^{-1}
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
-  // Hp = X^T (A X): FP64 HX in every precision mode
+  // Hp = X^T (A X). The HX is FP64 unless the mixed mode asks for the FP32 SIMT apply; then
+  // X is rounded to FP32 once and the same rounded basis enters S (the mixed Gram converts on
+  // load), HX and Hp, so the generalised problem stays consistent.
   double* HX = s->HX.ensure((size_t)M * N);
-  hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
+  if (is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32) {
+    float* x32 = s->Xb32.ensure((size_t)M * N);
+    float* y32 = s->Yb32.ensure((size_t)M * N);
+    copy_block<double, float>(X, ld, x32, N, M, N, 1.0, st);
+    hx_f32(op, x32, N, y32, N, N, 1.0, false, st);
+    copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
+  } else {
+    hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
+  }
   CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
   gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
   symmetrize_lower(Hp, N, st);
@@ -262,6 +306,7 @@ chefsi_params default_params() {
   p.reproducible = 0;
   p.first_scf_degree_scale = 1.34;
   p.keep_hx = 1;
+  p.rr_precision = CHEFSI_PREC_FP64;
   return p;
 }
 
@@ -271,6 +316,8 @@ extern "C" {
 
 const char* chefsi_last_error(void) { return chefsi::last_error_cstr(); }
 const char* chefsi_version(void) { return "chefsi-gb300 0.1 (sm_103a)"; }
+
+uint64_t chefsi_launch_count(void) { return (uint64_t)chefsi::launch_count(); }
 
 int32_t chefsi_chebyshev_order(double upper) {
   const unsigned ub = upper > 0 ? (unsigned)upper : 0u;
@@ -574,6 +621,21 @@ int chefsi_solver_timings(chefsi_solver s, double* ms7) {
   CHEFSI_API_END
 }
 
+int chefsi_solver_set_profiling(chefsi_solver s, int32_t enable) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s != nullptr, "null solver");
+  s->profile = enable != 0;
+  CHEFSI_API_END
+}
+
+int chefsi_solver_hx_stats(chefsi_solver s, int32_t* launches, double* total_ms) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s != nullptr, "null solver");
+  if (launches) *launches = s->hx_launches;
+  if (total_ms) *total_ms = s->hx_ms;
+  CHEFSI_API_END
+}
+
 static int degree_for(chefsi_solver_s* s, int is_first_scf) {
   int m = s->p.chebyshev_degree > 0 ? s->p.chebyshev_degree : chefsi_chebyshev_order(s->b_up);
   if (is_first_scf) m = (int)(m * s->p.first_scf_degree_scale);
@@ -609,6 +671,7 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
   s->times[4] = elapsed(s->ev[4], s->ev[5]);
   s->times[5] = elapsed(s->ev[5], s->ev[6]);
   s->times[6] = elapsed(s->ev[0], s->ev[6]);
+  s->hx_collect();
   CHEFSI_API_END
 }
 

@@ -31,7 +31,13 @@ void set_last_error(const std::string& msg);
                                                  __FILE__ + ":" + std::to_string(__LINE__)); \
   } while (0)
 
-#define CHEFSI_CHECK_LAUNCH() CHEFSI_CUDA(cudaGetLastError())
+// every kernel launch of the library is followed by CHEFSI_CHECK_LAUNCH, which also counts it
+void count_launch();
+#define CHEFSI_CHECK_LAUNCH()      \
+  do {                             \
+    ::chefsi::count_launch();      \
+    CHEFSI_CUDA(cudaGetLastError()); \
+  } while (0)
 
 #define CHEFSI_REQUIRE(cond, msg)                                   \
   do {                                                              \

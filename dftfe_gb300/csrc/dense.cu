@@ -742,9 +742,13 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   for (int k = 0; k + 2 < N; ++k) {
     const int n = N - k - 1;
     k_hh_vector<<<1, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, d.ptr, e.ptr);
+    CHEFSI_CHECK_LAUNCH();
     k_hh_symv<<<(n * 32 + 255) / 256, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, p.ptr);
+    CHEFSI_CHECK_LAUNCH();
     k_hh_w<<<1, 256, 0, st>>>(N, k, V.ptr, tau.ptr, p.ptr);
+    CHEFSI_CHECK_LAUNCH();
     k_hh_rank2<<<grid_for((int64_t)n * n, 256), 256, 0, st>>>(A, N, k, V.ptr, p.ptr);
+    CHEFSI_CHECK_LAUNCH();
   }
   k_tail<<<1, 32, 0, st>>>(A, N, d.ptr, e.ptr);
   CHEFSI_CHECK_LAUNCH();
@@ -767,8 +771,10 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   CHEFSI_CHECK_LAUNCH();
   for (int k = N - 3; k >= 0; --k) {
     k_bt_dot<<<(N + 127) / 128, 128, 0, st>>>(V.ptr, N, k, Z, p.ptr);
+    CHEFSI_CHECK_LAUNCH();
     k_bt_update<<<grid_for((int64_t)(N - k - 1) * N, 256), 256, 0, st>>>(V.ptr, N, k, tau.ptr, Z,
                                                                          p.ptr);
+    CHEFSI_CHECK_LAUNCH();
   }
   CHEFSI_CHECK_LAUNCH();
   CHEFSI_CUDA(cudaStreamSynchronize(st));

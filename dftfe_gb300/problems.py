@@ -93,6 +93,9 @@ WORKLOADS = {
     "mixed": dict(n=20, L=30.0, p=6, n_wells=64, n_wfc=1024, cheb_degree=30, projectors=True),
     "adjoint": dict(n=10, L=15.0, p=4, n_wells=8, n_wfc=256, cheb_degree=24, n_occupied=128),
     "large": dict(n=32, L=48.0, p=5, n_wells=256, n_wfc=4096, cheb_degree=40, projectors=True),
+    # the mixed workload's cell type (degree 6, 1.5 bohr cells) on an 8^3 mesh: the size used
+    # for detailed kernel profiles (inputs still larger than L2, a few GB on the device)
+    "mixed_small": dict(n=8, L=12.0, p=6, n_wells=8, n_wfc=1024, cheb_degree=30, projectors=True),
 }
 
 

@@ -121,10 +121,14 @@ typedef struct {
   int32_t reproducible;         /* REPRODUCIBLE OUTPUT */
   double first_scf_degree_scale;/* chebyshevFilterPolyDegreeFirstScfScalingFactor */
   int32_t keep_hx;              /* 1: keep H X from the RR step for the residuals */
+  int32_t rr_precision;         /* precision of the H X feeding X^T H X in mixed mode:
+                                   CHEFSI_PREC_FP64 (default) or CHEFSI_PREC_FP32 */
 } chefsi_params;
 
 const char* chefsi_last_error(void);
 const char* chefsi_version(void);
+/* number of kernels this library has launched in the process (all streams) */
+uint64_t chefsi_launch_count(void);
 
 int chefsi_operator_create(const chefsi_operator_desc* desc, chefsi_operator* out);
 int chefsi_operator_destroy(chefsi_operator op);
@@ -184,6 +188,10 @@ int chefsi_solver_get_bounds(chefsi_solver s, double* lower_wanted, double* lowe
 /* Per-phase device times of the last solve in milliseconds:
    [filter, overlap+cholesky, xthx(hx+gemm), eig, rotation, residual, total]. */
 int chefsi_solver_timings(chefsi_solver s, double* ms7);
+/* Filter HX launches of the last solve: their count and summed device time (CUDA events
+   recorded on the solve's stream around every filter HX when profiling is enabled). */
+int chefsi_solver_set_profiling(chefsi_solver s, int32_t enable);
+int chefsi_solver_hx_stats(chefsi_solver s, int32_t* launches, double* total_ms);
 
 /* One CheFSI iteration on X (device, [n_dofs][N], ld = N; FP64 or complex FP64):
    filter all vectors, Rayleigh-Ritz (GEP), residual norms. Eigenvalues and residual norms
