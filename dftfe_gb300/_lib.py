@@ -30,7 +30,8 @@ _ERRNAMES = {1: "INVALID", 2: "CUDA", 3: "NOT_SPD", 4: "NO_CONVERGENCE", 5: "ALL
 EXPORTS = [
     "chefsi_last_error", "chefsi_version", "chefsi_launch_count", "chefsi_operator_create", "chefsi_operator_destroy",
     "chefsi_operator_info", "chefsi_hx", "chefsi_overlap", "chefsi_xthx",
-    "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_cholesky_gs",
+    "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_syevd_noalloc",
+    "chefsi_cholesky_gs",
     "chefsi_rayleigh_ritz", "chefsi_residual_norms", "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
@@ -97,6 +98,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_chebyshev_filter": ([vp, vp, i64, i32, i32, f64, f64, f64, i32, vp], ctypes.c_int),
         "chefsi_lanczos_bounds": ([vp, i32, i32, vp, ctypes.c_uint64, vp, vp, vp], ctypes.c_int),
         "chefsi_syevd": ([i32, vp, vp, vp, vp], ctypes.c_int),
+        "chefsi_syevd_noalloc": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_cholesky_gs": ([vp, vp, i64, i32, i32, vp], ctypes.c_int),
         "chefsi_rayleigh_ritz": ([vp, vp, i64, i32, vp, vp, i32, vp], ctypes.c_int),
         "chefsi_residual_norms": ([vp, vp, i64, i32, vp, vp, vp], ctypes.c_int),

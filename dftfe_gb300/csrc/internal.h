@@ -127,4 +127,19 @@ void residual_norms_c64(const cplx* X, int64_t ldx, const cplx* HX, int64_t ldh,
 // dot / norm helpers for Lanczos (device scalar results)
 void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaStream_t st);
 
+// eigensolver kernels (dense.cu), launched by the eigensolver drivers
+__global__ void k_hh_vector(double* A, int N, int k, double* V, double* tau, double* d, double* e);
+__global__ void k_hh_symv(const double* A, int N, int k, const double* V, const double* tau,
+                          double* p);
+__global__ void k_hh_w(int N, int k, const double* V, const double* tau, double* p);
+__global__ void k_hh_rank2(double* A, int N, int k, const double* V, const double* w);
+__global__ void k_tail(const double* A, int N, double* d, double* e);
+__global__ void k_bisect(const double* d, const double* e, int n, double* w);
+__global__ void k_inverse_iteration(const double* d, const double* e, int n, const double* w,
+                                    double* Z, int ldz, double* work, unsigned char* swaps,
+                                    double ortol);
+__global__ void k_bt_dot(const double* V, int N, int k, const double* Z, double* r);
+__global__ void k_bt_update(const double* V, int N, int k, const double* tau, double* Z,
+                            const double* r);
+
 }  // namespace chefsi

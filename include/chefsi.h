@@ -166,6 +166,17 @@ int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible,
    A is overwritten. */
 int chefsi_syevd(int32_t N, double* A, double* w, double* Z, void* stream);
 
+/* Allocation-free variant of chefsi_syevd (no counterpart in the reference).
+   For callers that cannot allocate device memory during a solve -- an application whose
+   pool allocator owns the GPU's memory, or one that cannot take the device-wide
+   synchronisation of cudaFree. The workspace is a file-scope device array sized for
+   N <= 256 (about 3.3 MB, held by every device that loads the library until the process
+   exits); larger N returns CHEFSI_ERR_INVALID. The first call on each device looks up the
+   array's device address (cudaGetSymbolAddress): make that first call before any stream
+   capture. All calls share the array, so calls that overlap on the GPU race; serialise them.
+   Same arguments and results as chefsi_syevd. */
+int chefsi_syevd_noalloc(int32_t N, double* A, double* w, double* Z, void* stream);
+
 /* Cholesky-Gram-Schmidt: S = X^H X, S = L L^H, X <- X L^{-H}. */
 int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32_t precision,
                        void* stream);
