@@ -363,8 +363,10 @@ int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, in
   } else if (precision == CHEFSI_PREC_FP64) {
     hx_f64(op, (const double*)src, ld_src, (double*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
   } else if (precision == CHEFSI_PREC_MIXED) {
+    // tensor cores need a real, unconstrained operator and 16-byte aligned rows; otherwise the
+    // SIMT FP32 apply serves the call
     if (!hx_tc(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st))
-      throw Error(CHEFSI_ERR_UNSUPPORTED, "tensor-core HX unavailable for this operator");
+      hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
     const int tc = tc_check_error(op, st);
     if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   } else if (precision == CHEFSI_PREC_FP32) {

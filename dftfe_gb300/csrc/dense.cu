@@ -137,6 +137,16 @@ static int64_t choose_split(int64_t K, int tiles, int64_t min_rows) {
   return per;
 }
 
+static void gemm32(bool ta, bool tb, int64_t M, int N, int64_t K, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, bool split,
+                   bool lower_only, cudaStream_t st);
+
+// C (N1 x N2) += A^T B with FP32 products, FP64 across chunks (split K, atomics)
+static void gram32(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t K, int N1,
+                   int N2, double* C, int ldc, bool lower_only, cudaStream_t st) {
+  gemm32(true, false, N1, N2, K, 1.0, A, lda, B, ldb, C, ldc, true, lower_only && N1 == N2, st);
+}
+
 void gram_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t K, int N1,
               int N2, double* C, int ldc, int prec, bool lower_only, cudaStream_t st) {
   const int nti = (N1 + GT - 1) / GT, ntj = (N2 + GT - 1) / GT;
@@ -145,13 +155,13 @@ void gram_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_
   const int64_t splits = (K + per - 1) / per;
   CHEFSI_REQUIRE(splits < 65536, "gram split too large");
   dim3 grid(nti * ntj, (unsigned)splits);
-  if (prec == CHEFSI_PREC_FP64)
+  if (prec == CHEFSI_PREC_FP64) {
     gram_kernel<double><<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj,
                                               lower_only, 1 << 30);
-  else
-    gram_kernel<float><<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj,
-                                             lower_only, 256);
-  CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CHECK_LAUNCH();
+  } else {
+    gram32(A, lda, B, ldb, K, N1, N2, C, ldc, lower_only, st);
+  }
 }
 
 void gram_c64(const cplx* A, int64_t lda, const cplx* B, int64_t ldb, int64_t K, int N1, int N2,
@@ -256,13 +266,17 @@ void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const dou
   CHEFSI_REQUIRE(grid.y < 65536, "gemm N too large");
   const int ita = (ta == 'T' || ta == 't' || ta == 'C' || ta == 'c');
   const int itb = (tb == 'T' || tb == 't' || tb == 'C' || tb == 'c');
-  if (prec == CHEFSI_PREC_FP64)
+  if (prec == CHEFSI_PREC_FP64) {
     gemm_kernel<double><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                               ldc, 1 << 30);
-  else
+    CHEFSI_CHECK_LAUNCH();
+  } else if (beta == 0.0) {
+    gemm32(ita != 0, itb != 0, M, N, K, alpha, A, lda, B, ldb, C, ldc, false, false, st);
+  } else {
     gemm_kernel<float><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                              ldc, 256);
-  CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CHECK_LAUNCH();
+  }
 }
 
 // complex GEMM (FP64), 32x32 tiles, 2x2 per thread
@@ -319,6 +333,189 @@ void gemm_c64(char ta, char tb, int64_t M, int N, int K, cplx alpha, const cplx*
   const int ita = (ta != 'N' && ta != 'n');
   const int itb = (tb != 'N' && tb != 'n');
   gemm_kernel_c<<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// ======================================================================= FP32 GEMM (mixed)
+// C[M][N] (+)= alpha op(A) op(B) over the K range of this CTA, FP64 operands converted to FP32
+// on load. 128x128 CTA tile, K-tile 8, 256 threads with an 8x8 register tile (two 4x4 quads
+// 64 rows / columns apart, so the shared-memory reads are float4 and conflict-free), register
+// double buffering of the next K-tile, FP32 products inside chunks of kChunk32 K-steps and FP64
+// accumulation across chunks. split != 0: atomicAdd into C (split-K Gram products).
+constexpr int kBM = 128, kBN = 128, kBK = 8, kChunk32 = 512;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256, 1)
+    gemm32_kernel(int64_t M, int N, int64_t K, double alpha, const double* __restrict__ A,
+                  int64_t lda, const double* __restrict__ B, int64_t ldb, double* __restrict__ C,
+                  int64_t ldc, int64_t k_per_split, int atomic_out, int ntn, int lower_only) {
+  __shared__ __align__(16) float As[2][kBK][kBM + 4];
+  __shared__ __align__(16) float Bs[2][kBK][kBN + 4];
+  const int64_t tile = blockIdx.x;
+  const int tn = (int)(tile % ntn);
+  const int64_t tm = tile / ntn;
+  if (lower_only && tn > tm) return;
+  const int64_t m0 = tm * kBM;
+  const int n0 = tn * kBN;
+  const int64_t k_begin = (int64_t)blockIdx.y * k_per_split;
+  const int64_t k_end = min(K, k_begin + k_per_split);
+  const int t = threadIdx.x;
+  const int tx = t % 16, ty = t / 16;
+
+  // global -> register loads of one K-tile (4 A values, 4 B values per thread)
+  double ra[4], rb[4];
+  auto load = [&](int64_t k0) {
+    if (TA) {  // A is [K][M]: 8 rows of 128 contiguous
+      const int kk = t / 32, mm = (t % 32) * 4;
+      const int64_t gk = k0 + kk;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        ra[i] = (gk < k_end && m0 + mm + i < M) ? A[gk * lda + m0 + mm + i] : 0.0;
+    } else {   // A is [M][K]: 128 rows of 8 contiguous
+      const int mm = t / 2, kk = (t % 2) * 4;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        ra[i] = (m0 + mm < M && k0 + kk + i < k_end) ? A[(m0 + mm) * lda + k0 + kk + i] : 0.0;
+    }
+    if (!TB) {  // B is [K][N]
+      const int kk = t / 32, nn = (t % 32) * 4;
+      const int64_t gk = k0 + kk;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        rb[i] = (gk < k_end && n0 + nn + i < N) ? B[gk * ldb + n0 + nn + i] : 0.0;
+    } else {    // B is [N][K]
+      const int nn = t / 2, kk = (t % 2) * 4;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        rb[i] = (n0 + nn < N && k0 + kk + i < k_end) ? B[(int64_t)(n0 + nn) * ldb + k0 + kk + i] : 0.0;
+    }
+  };
+  auto store = [&](int buf) {
+    if (TA) {
+      const int kk = t / 32, mm = (t % 32) * 4;
+      *reinterpret_cast<float4*>(&As[buf][kk][mm]) =
+          make_float4((float)ra[0], (float)ra[1], (float)ra[2], (float)ra[3]);
+    } else {
+      const int mm = t / 2, kk = (t % 2) * 4;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) As[buf][kk + i][mm] = (float)ra[i];
+    }
+    if (!TB) {
+      const int kk = t / 32, nn = (t % 32) * 4;
+      *reinterpret_cast<float4*>(&Bs[buf][kk][nn]) =
+          make_float4((float)rb[0], (float)rb[1], (float)rb[2], (float)rb[3]);
+    } else {
+      const int nn = t / 2, kk = (t % 2) * 4;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Bs[buf][kk + i][nn] = (float)rb[i];
+    }
+  };
+
+  // FP64 chunk sums live in shared memory ([64][256], thread-fastest: conflict-free)
+  extern __shared__ double acc64s[];
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f, acc64s[(i * 8 + j) * 256 + t] = 0.0;
+
+  int buf = 0;
+  if (k_begin < k_end) {
+    load(k_begin);
+    store(0);
+  }
+  __syncthreads();
+  int since = 0;
+  for (int64_t k0 = k_begin; k0 < k_end; k0 += kBK) {
+    const bool more = k0 + kBK < k_end;
+    if (more) load(k0 + kBK);
+#pragma unroll
+    for (int kk = 0; kk < kBK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][64 + tx * 4]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    if (more) store(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+    since += kBK;
+    if (since >= kChunk32) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc64s[(i * 8 + j) * 256 + t] += (double)acc[i][j], acc[i][j] = 0.f;
+      since = 0;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int64_t m = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
+      if (n >= N) continue;
+      const double v = alpha * (acc64s[(i * 8 + j) * 256 + t] + (double)acc[i][j]);
+      if (atomic_out)
+        atomicAdd(&C[m * ldc + n], v);
+      else
+        C[m * ldc + n] = v;
+    }
+  }
+}
+
+// mixed-precision GEMM entry: C = alpha op(A) op(B) (atomic == false, beta = 0) or split-K
+// accumulation C += alpha A^T B (gram, atomic == true)
+static void gemm32(bool ta, bool tb, int64_t M, int N, int64_t K, double alpha, const double* A,
+                   int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, bool split,
+                   bool lower_only, cudaStream_t st) {
+  const int ntn = (N + kBN - 1) / kBN;
+  const int64_t ntm = (M + kBM - 1) / kBM;
+  const int64_t tiles = ntm * ntn;
+  int64_t per = K, splits = 1;
+  if (split) {
+    const int64_t live = lower_only ? ntm * (ntm + 1) / 2 : tiles;
+    int64_t want = std::max<int64_t>(1, (int64_t)kNumSMs * 2 / std::max<int64_t>(1, live));
+    per = std::max<int64_t>(kChunk32, (K + want - 1) / want);
+    per = (per + kBK - 1) / kBK * kBK;
+    splits = (K + per - 1) / per;
+  }
+  CHEFSI_REQUIRE(tiles < (1ll << 31) && splits < 65536, "gemm32 grid too large");
+  dim3 grid((unsigned)tiles, (unsigned)splits);
+  const int atomic = split ? 1 : 0;
+  const int lo = lower_only ? 1 : 0;
+  const size_t dyn = 64 * 256 * sizeof(double);
+  static bool attr = false;
+  if (!attr) {
+    CHEFSI_CUDA(cudaFuncSetAttribute(gemm32_kernel<true, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    CHEFSI_CUDA(cudaFuncSetAttribute(gemm32_kernel<false, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    CHEFSI_CUDA(cudaFuncSetAttribute(gemm32_kernel<false, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    CHEFSI_CUDA(cudaFuncSetAttribute(gemm32_kernel<true, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    attr = true;
+  }
+  if (ta && !tb)
+    gemm32_kernel<true, false><<<grid, 256, dyn, st>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, per,
+                                                       atomic, ntn, lo);
+  else if (!ta && !tb)
+    gemm32_kernel<false, false><<<grid, 256, dyn, st>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, per,
+                                                        atomic, ntn, lo);
+  else if (!ta && tb)
+    gemm32_kernel<false, true><<<grid, 256, dyn, st>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, per,
+                                                       atomic, ntn, lo);
+  else
+    gemm32_kernel<true, true><<<grid, 256, dyn, st>>>(M, N, K, alpha, A, lda, B, ldb, C, ldc, per,
+                                                      atomic, ntn, lo);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -53,6 +53,7 @@ struct chefsi_operator_s {
   int nl_n_chunks = 0;
   chefsi::DeviceBuffer<int> nl_chunk_atom, nl_chunk_row0;
 
+
   chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
 
   // workspaces (grow-only)
@@ -73,6 +74,10 @@ void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int6
 // tensor-core (FP16 split) apply on FP32 vectors; returns false if unavailable for this op
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st);
+bool tc_usable(chefsi_operator_s* op);
+// W[a][j][b] = sum_r C[r][j] x[dof_r][b] for FP32 vectors (W zeroed here)
+void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
+                    cudaStream_t st);
 void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st);
 // device error flag of the tensor-core kernel (CHEFSI_OK or CHEFSI_ERR_TIMEOUT); clears it
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st);

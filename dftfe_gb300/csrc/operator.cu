@@ -495,11 +495,151 @@ void hx_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
                     accumulate, st, cell_f32);
 }
 
+// W[a][j][b0..b0+128) = sum over all rows of atom a of C[r][j] x[dof_r][b]: one CTA per
+// (atom, 128-vector tile), 8 warps take interleaved rows (float4 loads, 4 vectors per lane),
+// partial sums reduced in shared memory -- no atomics.
+__global__ void __launch_bounds__(256)
+    nl_project_atom(const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
+                    const float* __restrict__ C, int P, const float* __restrict__ src, int64_t lds,
+                    float* __restrict__ W, int B) {
+  __shared__ float4 red[8][kMaxProj][32];
+  const int a = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.y * 128 + lane * 4;
+  const int r0 = atom_ptr[a], r1 = atom_ptr[a + 1];
+  float4 acc[kMaxProj];
+#pragma unroll
+  for (int j = 0; j < kMaxProj; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (b < B) {
+    int r = r0 + warp;
+    for (; r + 24 < r1; r += 32) {
+      float4 x[4];
+      int rr[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        rr[u] = r + 8 * u;
+        x[u] = __ldg(reinterpret_cast<const float4*>(src + (int64_t)__ldg(dofs + rr[u]) * lds + b));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < kMaxProj; ++j) {
+          if (j >= P) break;
+          const float cv = __ldg(C + (size_t)rr[u] * P + j);
+          acc[j].x = fmaf(cv, x[u].x, acc[j].x);
+          acc[j].y = fmaf(cv, x[u].y, acc[j].y);
+          acc[j].z = fmaf(cv, x[u].z, acc[j].z);
+          acc[j].w = fmaf(cv, x[u].w, acc[j].w);
+        }
+    }
+    for (; r < r1; r += 8) {
+      const float4 x = __ldg(reinterpret_cast<const float4*>(src + (int64_t)__ldg(dofs + r) * lds + b));
+#pragma unroll
+      for (int j = 0; j < kMaxProj; ++j) {
+        if (j >= P) break;
+        const float cv = __ldg(C + (size_t)r * P + j);
+        acc[j].x = fmaf(cv, x.x, acc[j].x);
+        acc[j].y = fmaf(cv, x.y, acc[j].y);
+        acc[j].z = fmaf(cv, x.z, acc[j].z);
+        acc[j].w = fmaf(cv, x.w, acc[j].w);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kMaxProj; ++j)
+    if (j < P) red[warp][j][lane] = acc[j];
+  __syncthreads();
+  // 256 threads reduce P x 32 float4 across the 8 warps
+  for (int idx = threadIdx.x; idx < P * 32; idx += 256) {
+    const int j = idx / 32, l = idx % 32;
+    float4 sum = red[0][j][l];
+    for (int w2 = 1; w2 < 8; ++w2) {
+      const float4 v = red[w2][j][l];
+      sum.x += v.x, sum.y += v.y, sum.z += v.z, sum.w += v.w;
+    }
+    const int bb = blockIdx.y * 128 + l * 4;
+    if (bb < B) *reinterpret_cast<float4*>(&W[((size_t)a * P + j) * B + bb]) = sum;
+  }
+}
+
+void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
+                    cudaStream_t st) {
+  if (op->n_atoms == 0) return;
+  const bool vec = (B % 4 == 0) && (ldx % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+  if (vec) {
+    dim3 grid(op->n_atoms, (B + 127) / 128);
+    nl_project_atom<<<grid, 256, 0, st>>>(op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
+                                          op->n_proj, x, ldx, W, B);
+  } else {
+    CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * (size_t)op->n_atoms * op->n_proj * B, st));
+    const int threads = 128;
+    dim3 grid(op->nl_n_chunks, (B + threads - 1) / threads);
+    nl_project<float><<<grid, threads, 0, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
+                                                op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
+                                                op->n_proj, x, ldx, W, B);
+  }
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// y[dof_r][b..b+3] += scalar * sum_j C[r][j] V[a][j] W[a][j][b..b+3] (float4 atomics)
+__global__ void nl_apply_v4(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
+                            const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
+                            const float* __restrict__ C, int P, const double* __restrict__ V,
+                            const float* __restrict__ W, float* __restrict__ dst, int64_t ldd,
+                            int B, double scalar) {
+  __shared__ float Cs[kNlChunk * kMaxProj];
+  __shared__ int Ds[kNlChunk];
+  const int ch = blockIdx.x;
+  const int a = chunk_atom[ch];
+  const int r0 = chunk_row0[ch];
+  const int r1 = min(r0 + kNlChunk, atom_ptr[a + 1]);
+  const int nr = r1 - r0;
+  for (int i = threadIdx.x; i < nr * P; i += blockDim.x) Cs[i] = C[(size_t)r0 * P + i];
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) Ds[i] = dofs[r0 + i];
+  __syncthreads();
+  const int b = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
+  if (b >= B) return;
+  float4 w[kMaxProj];
+#pragma unroll
+  for (int j = 0; j < kMaxProj; ++j) {
+    if (j >= P) break;
+    const float f = (float)(scalar * V[(size_t)a * P + j]);
+    const float4 x = *reinterpret_cast<const float4*>(&W[((size_t)a * P + j) * B + b]);
+    w[j] = make_float4(f * x.x, f * x.y, f * x.z, f * x.w);
+  }
+  for (int r = 0; r < nr; ++r) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < kMaxProj; ++j) {
+      if (j >= P) break;
+      const float cv = Cs[r * P + j];
+      acc.x = fmaf(cv, w[j].x, acc.x);
+      acc.y = fmaf(cv, w[j].y, acc.y);
+      acc.z = fmaf(cv, w[j].z, acc.z);
+      acc.w = fmaf(cv, w[j].w, acc.w);
+    }
+    atomicAdd(reinterpret_cast<float4*>(dst + (int64_t)Ds[r] * ldd + b), acc);
+  }
+}
+
 void apply_nonlocal_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst,
                         int64_t ldd, int B, double scalar, cudaStream_t st) {
   if (op->n_atoms == 0) return;
   float* W = op->nlW32.ensure((size_t)op->n_atoms * op->n_proj * B);
-  apply_nonlocal<float>(op, op->nl_vals32.ptr, W, src, lds, dst, ldd, B, scalar, st);
+  const bool vec = (B % 4 == 0) && (lds % 4 == 0) && (ldd % 4 == 0) &&
+                   ((reinterpret_cast<uintptr_t>(src) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
+  if (!vec) {
+    apply_nonlocal<float>(op, op->nl_vals32.ptr, W, src, lds, dst, ldd, B, scalar, st);
+    return;
+  }
+  nl_project_f32(op, src, lds, W, B, st);
+  const int threads = 128;
+  dim3 grid(op->nl_n_chunks, (B / 4 + threads - 1) / threads);
+  nl_apply_v4<<<grid, threads, 0, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
+                                        op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
+                                        op->n_proj, op->couplings.ptr, W, dst, ldd, B, scalar);
+  CHEFSI_CHECK_LAUNCH();
 }
 
 void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int64_t ldd, int B,

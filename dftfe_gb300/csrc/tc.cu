@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <vector>
 
 namespace chefsi {
 
@@ -35,7 +36,6 @@ namespace {
 constexpr int kVec = 128;          // vectors per CTA (MMA M)
 constexpr int kKB = 32;            // halves per K-block (64-byte rows)
 constexpr int kRowBytes = kKB * 2; // 64
-constexpr int kThreads = 192;      // 6 warps
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -142,69 +142,125 @@ struct TcArgs {
   int64_t ldd;
   const int* map;
   int n_e;
-  int npad;
-  int nkb;
+  int nkb;         // K-blocks of 32 columns
   int B;
-  int n_chunks;
-  int n_mma;      // 1 or 2 MMAs along N
-  int n_half;     // N per MMA
+  int n_chunks;    // 128-vector chunks
+  int n_half;      // cell rows per work unit (= MMA N)
+  int n_halves;    // row halves per cell (1 or 2)
+  int buf_stride;  // tensor-memory column offset of accumulator 1
   int tmem_cols;
   int stages;
-  float out_scale;  // scalar / 2^s
+  int64_t n_units; // n_cells * n_chunks * n_halves
+  float out_scale; // scalar / 2^s
   int* err;
 };
 
 // shared memory carve-up (offsets from a 1024-byte aligned base)
+constexpr int kXStages = 4;                    // cp.async staging depth for the X gather
+constexpr int kXStageBytes = kKB * kVec * 4;    // [32 rows][128 vectors] FP32 = 16 KB
+
 struct Layout {
   int x_tile;   // 128 rows x 64 B = 8 KB
-  int a_tile;   // npad rows x 64 B
+  int a_tile;   // n_half rows x 64 B, rounded to 1 KB
   int stage;    // xhi, xlo, ahi, alo
-  int bars;     // barrier block offset
-  int maps;     // cell dof map
+  int xstage;   // FP32 staging ring of the gathered rows
+  int bars;     // barrier block
   int total;
 };
-__host__ __device__ inline Layout make_layout(int npad, int stages, int n_e) {
+__host__ __device__ inline Layout make_layout(int n_half, int stages) {
   Layout L;
   L.x_tile = kVec * kRowBytes;
-  L.a_tile = ((npad * kRowBytes + 1023) / 1024) * 1024;
+  L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
   L.stage = 2 * L.x_tile + 2 * L.a_tile;
-  L.bars = stages * L.stage;
-  L.maps = L.bars + 8 * (3 * stages + 4);
-  L.total = L.maps + 4 * ((n_e + 3) / 4 * 4) + 16;
+  L.xstage = stages * L.stage;
+  L.bars = L.xstage + kXStages * kXStageBytes;
+  L.total = L.bars + 8 * (3 * stages + 8);
   return L;
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// named barrier among the 128 X-producer threads (barrier 0 is __syncthreads)
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// the same barrier with an OR-reduction, so the producers take stop decisions together
+__device__ __forceinline__ bool producers_sync_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, 1, 128, pi;\n"
+      " selp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
+struct Unit {
+  int cell, chunk, half;
+};
+__device__ __forceinline__ Unit unit_of(int64_t u, const TcArgs& a) {
+  Unit w;
+  w.half = (int)(u % a.n_halves);
+  const int64_t cc = u / a.n_halves;
+  w.chunk = (int)(cc % a.n_chunks);
+  w.cell = (int)(cc / a.n_chunks);
+  return w;
+}
+
+// Persistent warp-specialised kernel, one CTA per SM. Work unit = (cell, 128-vector chunk,
+// row half); units are dealt round-robin so the CTAs of the GPU sweep the cells in order and
+// a cell's matrix halves and X rows are re-read from L2, not HBM.
+//   warp 0        TMA of the cell-matrix K-blocks (hi, lo) into the stage ring
+//   warp 1        tcgen05.mma issue (one lane), two tensor-memory accumulators
+//   warps 2..5    X gather (one thread per vector, next K-block prefetched in registers),
+//                 FP16 hi/lo split, 64B-swizzled K-major stores
+//   warps 6..9    epilogue: tcgen05.ld of a finished accumulator, red.global.add.f32 scatter,
+//                 overlapped with the MMAs of the next unit
+constexpr int kThreads2 = 320;
+
+__global__ void __launch_bounds__(kThreads2, 1)
     cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                       const __grid_constant__ CUtensorMap tm_lo, TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int S = args.stages;
-  const Layout L = make_layout(args.npad, S, args.n_e);
+  const Layout L = make_layout(args.n_half, S);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] TMA bytes landed
   uint64_t* x_full = bars + S;          // [S] 128 producer arrivals
-  uint64_t* empty = bars + 2 * S;       // [S] MMA finished reading
-  uint64_t* acc_full = bars + 3 * S;    // accumulator ready
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 3 * S + 2);
-  int* smap = reinterpret_cast<int*>(smem + L.maps);
+  uint64_t* empty = bars + 2 * S;       // [S] MMA finished reading the stage
+  uint64_t* acc_full = bars + 3 * S;    // [2] accumulator ready for the epilogue
+  uint64_t* acc_empty = bars + 3 * S + 2;  // [2] accumulator drained (128 arrivals)
+  uint64_t* mma_done = bars + 3 * S + 4;   // final MMA completion
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 3 * S + 6);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cell = blockIdx.x / args.n_chunks;
-  const int chunk = blockIdx.x % args.n_chunks;
-  const int b0 = chunk * kVec;
+  const int64_t first = blockIdx.x;
+  const int64_t step = gridDim.x;
+  const int64_t my_units = first < args.n_units ? (args.n_units - first + step - 1) / step : 0;
+  const int nkb = args.nkb;
+  const int64_t my_blocks = my_units * nkb;
 
-  for (int i = threadIdx.x; i < args.n_e; i += kThreads)
-    smap[i] = args.map[(int64_t)cell * args.n_e + i];
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&tma_full[s], 1);
       mbar_init(&x_full[s], kVec);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(acc_full, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kVec);
+    }
+    mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -219,29 +275,28 @@ __global__ void __launch_bounds__(kThreads, 1)
   fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const int nkb = args.nkb;
   if (warp == 0) {
-    // ---------------- TMA producer: cell-matrix K-blocks (hi, lo)
+    // ---------------- TMA producer
     if (lane == 0) {
-      const uint32_t bytes = 2u * args.npad * kRowBytes;
-      int issued = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % S, r = kb / S;
+      const uint32_t bytes = 2u * args.n_half * kRowBytes;
+      int64_t issued = 0;
+      for (int64_t g = 0; g < my_blocks; ++g) {
+        const Unit w = unit_of(first + (g / nkb) * step, args);
+        const int kb = (int)(g % nkb);
+        const int s = (int)(g % S);
+        const uint32_t r = (uint32_t)(g / S);
         if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
         uint8_t* st = smem + s * L.stage;
         mbar_arrive_expect_tx(&tma_full[s], bytes);
-        for (int h = 0; h < args.n_mma; ++h) {
-          tma_load_3d(st + 2 * L.x_tile + h * args.n_half * kRowBytes, &tm_hi, kb * kKB,
-                      h * args.n_half, cell, &tma_full[s]);
-          tma_load_3d(st + 2 * L.x_tile + L.a_tile + h * args.n_half * kRowBytes, &tm_lo,
-                      kb * kKB, h * args.n_half, cell, &tma_full[s]);
-        }
-        issued = kb + 1;
+        tma_load_3d(st + 2 * L.x_tile, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
+        tma_load_3d(st + 2 * L.x_tile + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell,
+                    &tma_full[s]);
+        issued = g + 1;
       }
       if (*abort_flag) {
-        // let our own copies land before the CTA exits (bounded)
-        for (int kb = (issued > S ? issued - S : 0); kb < issued; ++kb) {
-          const int s = kb % S, r = kb / S;
+        for (int64_t g = (issued > S ? issued - S : 0); g < issued; ++g) {
+          const int s = (int)(g % S);
+          const uint32_t r = (uint32_t)(g / S);
           for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(&tma_full[s], r & 1); ++i)
             __nanosleep(128);
         }
@@ -251,49 +306,87 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = idesc_f16(kVec, args.n_half);
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % S, r = kb / S;
-        if (!mbar_wait(&tma_full[s], r & 1, args.err, abort_flag)) break;
-        if (!mbar_wait(&x_full[s], r & 1, args.err, abort_flag)) break;
+      bool ok = true;
+      for (int64_t it = 0; it < my_units && ok; ++it) {
+        const int buf = (int)(it & 1);
+        const uint32_t ph = (uint32_t)((it >> 1) & 1);
+        if (!mbar_wait(&acc_empty[buf], ph ^ 1, args.err, abort_flag)) break;
         fence_after();
-        const uint32_t st = smem_u32(smem + s * L.stage);
-        const uint32_t xhi = st, xlo = st + L.x_tile;
-        const uint32_t ahi = st + 2 * L.x_tile, alo = ahi + L.a_tile;
-#pragma unroll
-        for (int ks = 0; ks < kKB / 16; ++ks) {
-          const uint32_t koff = ks * 32;  // 16 halves = 32 bytes along K
-          for (int h = 0; h < args.n_mma; ++h) {
-            const uint32_t d = tmem + h * args.n_half;
-            const uint32_t boff = h * args.n_half * kRowBytes + koff;
-            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(ahi + boff), idesc, acc0);
-            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(alo + boff), idesc, 1u);
-            mma_f16(d, smem_desc_sw64(xlo + koff), smem_desc_sw64(ahi + boff), idesc, 1u);
+        const uint32_t d = tmem + buf * args.buf_stride;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int64_t g = it * nkb + kb;
+          const int s = (int)(g % S);
+          const uint32_t r = (uint32_t)(g / S);
+          if (!mbar_wait(&tma_full[s], r & 1, args.err, abort_flag) ||
+              !mbar_wait(&x_full[s], r & 1, args.err, abort_flag)) {
+            ok = false;
+            break;
           }
-        }
-        mma_commit(&empty[s]);
-      }
-      mma_commit(acc_full);
-      // the MMAs must be complete before tensor memory is freed, also on the abort path
-      for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(acc_full, 0); ++i) __nanosleep(128);
-    }
-  } else {
-    // ---------------- X producers (warps 2..5), then the epilogue
-    const int q = warp & 3;                  // tensor-memory lane quarter of this warp
-    const int v = q * 32 + lane;             // vector within the chunk (= MMA row)
-    const int gb = b0 + v;
-    const bool vok = gb < args.B;
-    const float* src = args.src + gb;
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int s = kb % S, r = kb / S;
-      if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
-      uint8_t* st = smem + s * L.stage;
-      float x[kKB];
+          fence_after();
+          const uint32_t st = smem_u32(smem + s * L.stage);
+          const uint32_t xhi = st, xlo = st + L.x_tile;
+          const uint32_t ahi = st + 2 * L.x_tile, alo = ahi + L.a_tile;
 #pragma unroll
-      for (int j = 0; j < kKB; ++j) {
-        const int J = kb * kKB + j;
-        x[j] = (vok && J < args.n_e) ? __ldg(src + (int64_t)smap[J] * args.lds) : 0.f;
+          for (int ks = 0; ks < kKB / 16; ++ks) {
+            const uint32_t koff = ks * 32;  // 16 halves = 32 bytes along K
+            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
+            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(ahi + koff), idesc, acc0);
+            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(alo + koff), idesc, 1u);
+            mma_f16(d, smem_desc_sw64(xlo + koff), smem_desc_sw64(ahi + koff), idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+        }
+        if (ok) mma_commit(&acc_full[buf]);
       }
+      // every MMA must be complete before tensor memory is freed, also on the abort path
+      mma_commit(mma_done);
+      for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(mma_done, 0); ++i) __nanosleep(128);
+    }
+  } else if (warp < 6) {
+    // ---------------- X producers: cp.async gather into an FP32 staging ring (kXStages deep,
+    // so ~64 KB of rows are in flight per SM), then FP16 hi/lo split into the stage ring
+    const int t = threadIdx.x - 64;          // 0..127
+    const int v = (warp & 3) * 32 + lane;    // vector row this thread converts
+    uint8_t* xst = smem + L.xstage;
+    auto issue = [&](int64_t g) {
+      uint8_t* slot = xst + (int)(g % kXStages) * kXStageBytes;
+      if (g < my_blocks) {
+        const Unit w = unit_of(first + (g / nkb) * step, args);
+        const int kb = (int)(g % nkb);
+        const int* mrow = args.map + (int64_t)w.cell * args.n_e;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int q = i * 128 + t;             // 16-byte chunk of the [32][128] slot
+          const int j = q >> 5, c4 = (q & 31) * 4;
+          const int J = kb * kKB + j;
+          const int gb = w.chunk * kVec + c4;
+          const bool ok = (J < args.n_e) && (gb < args.B);
+          const float* src = ok ? args.src + (int64_t)__ldg(mrow + J) * args.lds + gb : args.src;
+          cp_async16(slot + j * (kVec * 4) + c4 * 4, src, ok);
+        }
+      }
+      cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < kXStages - 1; ++i) issue(i);
+    bool stop = false;
+    for (int64_t g = 0; g < my_blocks; ++g) {
+      issue(g + kXStages - 1);
+      cp_async_wait<kXStages - 1>();
+      // block g's rows landed for all producer threads; a stop seen by any thread ends all
+      if (producers_sync_or(stop)) break;
+      const float* slot = reinterpret_cast<const float*>(xst + (int)(g % kXStages) * kXStageBytes);
+      float cur[kKB];
+#pragma unroll
+      for (int j = 0; j < kKB; ++j) cur[j] = slot[j * kVec + v];
+      producers_sync();                       // slot may be refilled by the next issue
+      const int s = (int)(g % S);
+      const uint32_t r = (uint32_t)(g / S);
+      if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) {
+        stop = true;
+        continue;
+      }
+      uint8_t* st = smem + s * L.stage;
       uint8_t* rhi = st + v * kRowBytes;
       uint8_t* rlo = st + L.x_tile + v * kRowBytes;
       const int sw = (v >> 1) & 3;
@@ -301,13 +394,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int c = 0; c < 4; ++c) {
         uint32_t hv[4], lv[4];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const float a0 = x[c * 8 + 2 * t], a1 = x[c * 8 + 2 * t + 1];
+        for (int u = 0; u < 4; ++u) {
+          const float a0 = cur[c * 8 + 2 * u], a1 = cur[c * 8 + 2 * u + 1];
           const __half2 h = __floats2half2_rn(a0, a1);
           const float2 hf = __half22float2(h);
           const __half2 l = __floats2half2_rn(a0 - hf.x, a1 - hf.y);
-          hv[t] = *reinterpret_cast<const uint32_t*>(&h);
-          lv[t] = *reinterpret_cast<const uint32_t*>(&l);
+          hv[u] = *reinterpret_cast<const uint32_t*>(&h);
+          lv[u] = *reinterpret_cast<const uint32_t*>(&l);
         }
         const int pc = (c ^ sw) * 16;
         *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
@@ -316,24 +409,38 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&x_full[s]);
     }
-    // epilogue (warp-uniform decision: tcgen05.ld is a .sync.aligned instruction)
-    const bool acc_ok = __all_sync(0xffffffffu, mbar_wait(acc_full, 0, args.err, abort_flag));
-    if (acc_ok) {
+    cp_async_wait<0>();
+  } else {
+    // ---------------- epilogue warps 6..9
+    const int q = warp & 3;                  // tensor-memory lane quarter of this warp
+    const int v = q * 32 + lane;
+    for (int64_t it = 0; it < my_units; ++it) {
+      const int buf = (int)(it & 1);
+      const uint32_t ph = (uint32_t)((it >> 1) & 1);
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
+      if (!ok) break;
       fence_after();
-      const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+      const Unit w = unit_of(first + it * step, args);
+      const int gb = w.chunk * kVec + v;
+      const bool vok = gb < args.B;
+      const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
+      const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
       float* dstb = args.dst + gb;
-      const int ncols = args.n_mma * args.n_half;
-      for (int c0 = 0; c0 < ncols; c0 += 16) {
+      const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
+      for (int c0 = 0; c0 < args.n_half; c0 += 16) {
         float vals[16];
         tmem_ld16(tq + c0, vals);
         if (vok) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int I = c0 + i;
-            if (I < args.n_e) atomicAdd(dstb + (int64_t)smap[I] * args.ldd, args.out_scale * vals[i]);
+            if (I < nrows)
+              atomicAdd(dstb + (int64_t)__ldg(mrow + I) * args.ldd, args.out_scale * vals[i]);
           }
         }
       }
+      fence_before();
+      mbar_arrive(&acc_empty[buf]);
     }
   }
   fence_before();
@@ -399,25 +506,25 @@ void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows)
 }
 
 struct TcPlan {
-  int npad, n_mma, n_half, tmem_cols, stages, smem;
+  int npad, n_half, n_halves, buf_stride, tmem_cols, stages, smem;
 };
 
 TcPlan plan_for(int n_e) {
   TcPlan p{};
   p.npad = (n_e + 31) / 32 * 32;
   if (p.npad <= 256) {
-    p.n_mma = 1;
+    p.n_halves = 1;
     p.n_half = p.npad;
   } else {
-    p.n_mma = 2;
+    p.n_halves = 2;
     p.n_half = p.npad / 2;  // multiple of 16
   }
-  const int ncol = p.n_mma * p.n_half;
-  p.tmem_cols = ncol <= 32 ? 32 : ncol <= 64 ? 64 : ncol <= 128 ? 128 : ncol <= 256 ? 256 : 512;
+  p.buf_stride = p.n_half <= 128 ? 128 : 256;
+  p.tmem_cols = 2 * p.buf_stride;
   const int budget = 220 * 1024;
-  p.stages = 4;
-  while (p.stages > 2 && make_layout(p.npad, p.stages, n_e).total + 1024 > budget) --p.stages;
-  p.smem = make_layout(p.npad, p.stages, n_e).total + 1024;
+  p.stages = 8;
+  while (p.stages > 2 && make_layout(p.n_half, p.stages).total + 1024 > budget) --p.stages;
+  p.smem = make_layout(p.n_half, p.stages).total + 1024;
   return p;
 }
 
@@ -448,15 +555,18 @@ void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
   tc.ready = true;
 }
 
-bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
-           double scalar, bool accumulate, cudaStream_t st) {
+bool tc_usable(chefsi_operator_s* op) {
   if (op->is_complex || !op->folded || op->n_e > 512) return false;
   if (!get_encode()) return false;
-  int dev = 0, major = 0, minor = 0;
+  int dev = 0, major = 0;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
-  CHEFSI_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
-  if (major != 10) return false;  // sm_100 family (GB300 = 10.3)
+  return major == 10;  // sm_100 family (GB300 = 10.3)
+}
+
+// launch the persistent tensor-core kernel (a.out_scale set by the caller)
+static void launch_tc(chefsi_operator_s* op, TcArgs& a, const float* src, int64_t lds, float* dst,
+                      int64_t ldd, int B, cudaStream_t st) {
   prepare_tensor_mats(op, st);
   const TcPlan p = plan_for(op->n_e);
   if (!op->tc_err.ptr) {
@@ -466,23 +576,21 @@ bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int
   CUtensorMap mhi, mlo;
   make_map(&mhi, op->tc.hi.ptr, op->n_cells, p.npad, p.n_half);
   make_map(&mlo, op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
-  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
-  TcArgs a{};
   a.src = src;
   a.lds = lds;
   a.dst = dst;
   a.ldd = ldd;
   a.map = op->map.ptr;
   a.n_e = op->n_e;
-  a.npad = p.npad;
   a.nkb = p.npad / kKB;
   a.B = B;
   a.n_chunks = (B + kVec - 1) / kVec;
-  a.n_mma = p.n_mma;
   a.n_half = p.n_half;
+  a.n_halves = p.n_halves;
+  a.buf_stride = p.buf_stride;
   a.tmem_cols = p.tmem_cols;
   a.stages = p.stages;
-  a.out_scale = (float)(scalar / op->tc.scale);
+  a.n_units = (int64_t)op->n_cells * a.n_chunks * p.n_halves;
   a.err = op->tc_err.ptr;
   static bool attr_set = false;
   if (!attr_set) {
@@ -490,10 +598,27 @@ bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int
                                      227 * 1024));
     attr_set = true;
   }
-  const int64_t blocks = (int64_t)op->n_cells * a.n_chunks;
-  CHEFSI_REQUIRE(blocks < (1ll << 31), "tensor HX grid too large");
-  cell_hx_tc_kernel<<<(unsigned)blocks, kThreads, p.smem, st>>>(mhi, mlo, a);
+  int dev = 0, sms = kNumSMs;
+  CHEFSI_CUDA(cudaGetDevice(&dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t grid = std::min<int64_t>(sms, a.n_units);
+  cell_hx_tc_kernel<<<(unsigned)grid, kThreads2, p.smem, st>>>(mhi, mlo, a);
   CHEFSI_CHECK_LAUNCH();
+}
+
+// the X gather copies 16-byte pieces: rows must start 16-byte aligned
+static bool gather_aligned(const float* src, int64_t lds, int B) {
+  return (B % 4 == 0) && (lds % 4 == 0) && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
+}
+
+bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+           double scalar, bool accumulate, cudaStream_t st) {
+  if (!tc_usable(op) || !gather_aligned(src, lds, B)) return false;
+  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  prepare_tensor_mats(op, st);
+  TcArgs a{};
+  a.out_scale = (float)(scalar / op->tc.scale);
+  launch_tc(op, a, src, lds, dst, ldd, B, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
 }
