@@ -348,25 +348,42 @@ __global__ void __launch_bounds__(kThreads2, 1)
     const int t = threadIdx.x - 64;          // 0..127
     const int v = (warp & 3) * 32 + lane;    // vector row this thread converts
     uint8_t* xst = smem + L.xstage;
-    auto issue = [&](int64_t g) {
-      uint8_t* slot = xst + (int)(g % kXStages) * kXStageBytes;
+    // the dof-map entries of a K-block are loaded one issue ahead, so the cp.async of a block
+    // never waits on a dependent map load
+    int mnext[8];
+    auto load_map = [&](int64_t g, int* mv) {
       if (g < my_blocks) {
         const Unit w = unit_of(first + (g / nkb) * step, args);
         const int kb = (int)(g % nkb);
         const int* mrow = args.map + (int64_t)w.cell * args.n_e;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
+          const int J = kb * kKB + ((i * 128 + t) >> 5);
+          mv[i] = J < args.n_e ? __ldg(mrow + J) : -1;
+        }
+      }
+    };
+    auto issue = [&](int64_t g) {
+      uint8_t* slot = xst + (int)(g % kXStages) * kXStageBytes;
+      int mv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) mv[i] = mnext[i];
+      load_map(g + 1, mnext);
+      if (g < my_blocks) {
+        const Unit w = unit_of(first + (g / nkb) * step, args);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
           const int q = i * 128 + t;             // 16-byte chunk of the [32][128] slot
           const int j = q >> 5, c4 = (q & 31) * 4;
-          const int J = kb * kKB + j;
           const int gb = w.chunk * kVec + c4;
-          const bool ok = (J < args.n_e) && (gb < args.B);
-          const float* src = ok ? args.src + (int64_t)__ldg(mrow + J) * args.lds + gb : args.src;
+          const bool ok = (mv[i] >= 0) && (gb < args.B);
+          const float* src = ok ? args.src + (int64_t)mv[i] * args.lds + gb : args.src;
           cp_async16(slot + j * (kVec * 4) + c4 * 4, src, ok);
         }
       }
       cp_async_commit();
     };
+    load_map(0, mnext);
 #pragma unroll
     for (int i = 0; i < kXStages - 1; ++i) issue(i);
     bool stop = false;
