@@ -35,7 +35,9 @@ EXPORTS = [
     "chefsi_rayleigh_ritz", "chefsi_residual_norms", "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
-    "chefsi_solve", "chefsi_solve_no_rr", "chefsi_chebyshev_order",
+    "chefsi_solve", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
+    "chefsi_axpby", "chefsi_assemble_cell_hamiltonians", "chefsi_operator_update_cell_matrices",
+    "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract",
 ]
 
 
@@ -100,7 +102,14 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_syevd": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_syevd_noalloc": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_cholesky_gs": ([vp, vp, i64, i32, i32, vp], ctypes.c_int),
-        "chefsi_rayleigh_ritz": ([vp, vp, i64, i32, vp, vp, i32, vp], ctypes.c_int),
+        "chefsi_rayleigh_ritz": ([vp, vp, i64, i32, vp, vp, vp, i32, vp], ctypes.c_int),
+        "chefsi_gemm": ([ctypes.c_char, ctypes.c_char, i64, i32, i32, f64, vp, i64, vp, i64, f64,
+                         vp, i64, i32, vp], ctypes.c_int),
+        "chefsi_axpby": ([i64, i32, f64, vp, i64, f64, vp, i64, vp], ctypes.c_int),
+        "chefsi_assemble_cell_hamiltonians": ([i32, i32, i32, vp, vp, vp, vp, vp], ctypes.c_int),
+        "chefsi_operator_update_cell_matrices": ([vp, vp, vp], ctypes.c_int),
+        "chefsi_cell_outer_accumulate": ([vp, vp, vp, i64, i32, f64, vp, vp], ctypes.c_int),
+        "chefsi_cell_quadrature_contract": ([i32, i32, i32, vp, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_residual_norms": ([vp, vp, i64, i32, vp, vp, vp], ctypes.c_int),
         "chefsi_solver_create": ([ctypes.POINTER(Params), ctypes.POINTER(vp)], ctypes.c_int),
         "chefsi_solver_destroy": ([vp], ctypes.c_int),

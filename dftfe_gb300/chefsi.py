@@ -130,6 +130,18 @@ class KohnShamOperator:
                                       _stream()))
         return Hp
 
+    def update_cell_matrices(self, mats: torch.Tensor):
+        """Replace the cell Hamiltonians (device FP64 [n_cells][n_e][n_e], unscaled)."""
+        check(_lib.load().chefsi_operator_update_cell_matrices(self._h, _ptr(mats), _stream()))
+
+    def cell_outer_accumulate(self, U: torch.Tensor, V: torch.Tensor, alpha: float,
+                              G: torch.Tensor):
+        """G_c += alpha * (D U)_c (D V)_c^T over the vectors (adjoint building block)."""
+        check(_lib.load().chefsi_cell_outer_accumulate(self._h, _ptr(U), _ptr(V), U.stride(0),
+                                                       U.shape[1], float(alpha), _ptr(G),
+                                                       _stream()))
+        return G
+
     def overlap(self, X: torch.Tensor, precision="fp64") -> torch.Tensor:
         N = X.shape[1]
         S = torch.zeros((N, N), dtype=X.dtype, device=X.device)
@@ -139,6 +151,15 @@ class KohnShamOperator:
 
 
 fillOverlapMatrix = KohnShamOperator.overlap
+
+
+def cell_quadrature_contract(shape: torch.Tensor, G: torch.Tensor, jxw: torch.Tensor | None):
+    nc, ne, _ = G.shape
+    nq = shape.shape[0]
+    out = torch.empty((nc, nq), dtype=torch.float64, device=G.device)
+    check(_lib.load().chefsi_cell_quadrature_contract(nc, ne, nq, _ptr(shape), _ptr(G), _ptr(jxw),
+                                                      _ptr(out), _stream()))
+    return out
 
 
 def lanczosLowerUpperBoundEigenSpectrum(op: KohnShamOperator, k: int = 20,
@@ -165,13 +186,56 @@ def pseudoGramSchmidtOrthogonalization(op: KohnShamOperator, X: torch.Tensor, pr
     return X
 
 
-def rayleighRitzGEP(op: KohnShamOperator, X: torch.Tensor, precision="fp64", want_hx=False):
+def rayleighRitzGEP(op: KohnShamOperator, X: torch.Tensor, precision="fp64", want_hx=False,
+                    want_w=False):
+    """Generalised Rayleigh-Ritz in place on X; returns eigenvalues (and HX_rot, W if asked)."""
     N = X.shape[1]
     ev = np.zeros(N)
     HX = torch.empty_like(X) if want_hx else None
+    W = torch.empty((N, N), dtype=torch.float64, device=X.device) if want_w else None
     check(_lib.load().chefsi_rayleigh_ritz(op.handle, _ptr(X), X.stride(0), N, _np_ptr(ev),
-                                           _ptr(HX), _prec(precision), _stream()))
-    return (ev, HX) if want_hx else ev
+                                           _ptr(HX), _ptr(W), _prec(precision), _stream()))
+    out = [ev]
+    if want_hx:
+        out.append(HX)
+    if want_w:
+        out.append(W)
+    return out[0] if len(out) == 1 else tuple(out)
+
+
+def gemm(A: torch.Tensor, B: torch.Tensor, ta: str = "N", tb: str = "N", alpha: float = 1.0,
+         beta: float = 0.0, C: torch.Tensor | None = None, precision="fp64") -> torch.Tensor:
+    """C = alpha op(A) op(B) + beta C on the GPU (row-major FP64)."""
+    M = A.shape[1] if ta == "T" else A.shape[0]
+    K = A.shape[0] if ta == "T" else A.shape[1]
+    N = B.shape[0] if tb == "T" else B.shape[1]
+    if C is None:
+        C = torch.zeros((M, N), dtype=torch.float64, device=A.device)
+    check(_lib.load().chefsi_gemm(ta.encode(), tb.encode(), M, N, K, float(alpha), _ptr(A),
+                                  A.stride(0), _ptr(B), B.stride(0), float(beta), _ptr(C),
+                                  C.stride(0), _prec(precision), _stream()))
+    return C
+
+
+def axpby(a: float, x: torch.Tensor, b: float, y: torch.Tensor) -> torch.Tensor:
+    """y = a x + b y (FP64 device blocks) through the library."""
+    n = 1 if y.dim() == 1 else y.shape[1]
+    ldx = 1 if x.dim() == 1 else x.stride(0)
+    ldy = 1 if y.dim() == 1 else y.stride(0)
+    check(_lib.load().chefsi_axpby(y.shape[0], n, float(a), _ptr(x), ldx, float(b), _ptr(y), ldy,
+                                   _stream()))
+    return y
+
+
+def assemble_cell_hamiltonians(shape: torch.Tensor, stiffness: torch.Tensor,
+                               v_jxw: torch.Tensor) -> torch.Tensor:
+    """H_c = 1/2 K + N^T diag(v_jxw_c) N for every cell, on the GPU."""
+    nc, nq = v_jxw.shape
+    ne = stiffness.shape[0]
+    out = torch.empty((nc, ne, ne), dtype=torch.float64, device=v_jxw.device)
+    check(_lib.load().chefsi_assemble_cell_hamiltonians(nc, ne, nq, _ptr(shape), _ptr(stiffness),
+                                                        _ptr(v_jxw), _ptr(out), _stream()))
+    return out
 
 
 def computeEigenResidualNorm(op: KohnShamOperator, X: torch.Tensor, eig) -> np.ndarray:

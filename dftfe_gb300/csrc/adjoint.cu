@@ -1,0 +1,148 @@
+// Building blocks of the local-potential adjoint and of the on-device cell Hamiltonian
+// assembly (FP64 SIMT):
+//   * k_assemble_cells: H_c = 1/2 K + N^T diag(v_c) N, the formula of hamMatrixKernelLDA
+//     (src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:61-115), written as a
+//     per-cell product over quadrature points;
+//   * k_cell_outer: G_c[I][J] += alpha sum_b (D u)[map I][b] (D v)[map J][b] -- the
+//     contraction of an adjoint pair (u = adjoint block, v = state block) with dA/dH_c, where
+//     A = D H D and D = M^{-1/2};
+//   * k_quad_contract: g_c(q) = jxw_c(q) sum_IJ N_qI G_c[I][J] N_qJ -- dL/dV(q) from G,
+//     because dH_c[I][J]/dV_c(q) = JxW_c(q) N_qI N_qJ.
+#include "internal.h"
+
+namespace chefsi {
+
+namespace {
+
+constexpr int T = 32;  // output tile (I x J)
+
+// out[c][I][J] = 0.5 K[I][J] + sum_q N[q][I] v[c][q] N[q][J]
+__global__ void __launch_bounds__(256)
+    k_assemble_cells(int n_cells, int n_e, int n_q, const double* __restrict__ N,
+                     const double* __restrict__ K, const double* __restrict__ v,
+                     double* __restrict__ out, int nt) {
+  __shared__ double Ai[16][T + 1];
+  __shared__ double Bj[16][T + 1];
+  const int64_t blk = blockIdx.x;
+  const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
+  const int c = (int)(blk / ((int64_t)nt * nt));
+  const int i0 = ti * T, j0 = tj * T;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 per thread
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  const double* vc = v + (int64_t)c * n_q;
+  for (int q0 = 0; q0 < n_q; q0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * T; idx += 256) {
+      const int qq = idx / T, k = idx % T;
+      const int q = q0 + qq;
+      const bool okq = q < n_q;
+      Ai[qq][k] = (okq && i0 + k < n_e) ? N[(int64_t)q * n_e + i0 + k] * vc[q] : 0.0;
+      Bj[qq][k] = (okq && j0 + k < n_e) ? N[(int64_t)q * n_e + j0 + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int qq = 0; qq < 16; ++qq)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) acc[r][s] = fma(Ai[qq][ty + 16 * r], Bj[qq][tx + 16 * s], acc[r][s]);
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int I = i0 + ty + 16 * r, J = j0 + tx + 16 * s;
+      if (I < n_e && J < n_e)
+        out[((int64_t)c * n_e + I) * n_e + J] = 0.5 * K[(int64_t)I * n_e + J] + acc[r][s];
+    }
+}
+
+// G[c][I][J] += alpha * sum_b d[gI] u[gI][b] d[gJ] w[gJ][b], g = map[c][.]
+__global__ void __launch_bounds__(256)
+    k_cell_outer(const int* __restrict__ map, int n_e, const double* __restrict__ d,
+                 const double* __restrict__ u, const double* __restrict__ w, int64_t ld, int B,
+                 double alpha, double* __restrict__ G, int nt) {
+  __shared__ double Ui[16][T + 1];
+  __shared__ double Wj[16][T + 1];
+  __shared__ int gi[T], gj[T];
+  const int64_t blk = blockIdx.x;
+  const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
+  const int c = (int)(blk / ((int64_t)nt * nt));
+  const int i0 = ti * T, j0 = tj * T;
+  if (threadIdx.x < T) {
+    gi[threadIdx.x] = i0 + threadIdx.x < n_e ? map[(int64_t)c * n_e + i0 + threadIdx.x] : -1;
+    gj[threadIdx.x] = j0 + threadIdx.x < n_e ? map[(int64_t)c * n_e + j0 + threadIdx.x] : -1;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (int b0 = 0; b0 < B; b0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * T; idx += 256) {
+      const int bb = idx % 16, k = idx / 16;
+      const int b = b0 + bb;
+      Ui[bb][k] = (b < B && gi[k] >= 0) ? u[(int64_t)gi[k] * ld + b] : 0.0;
+      Wj[bb][k] = (b < B && gj[k] >= 0) ? w[(int64_t)gj[k] * ld + b] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int bb = 0; bb < 16; ++bb)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) acc[r][s] = fma(Ui[bb][ty + 16 * r], Wj[bb][tx + 16 * s], acc[r][s]);
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int I = ty + 16 * r, J = tx + 16 * s;
+      if (i0 + I < n_e && j0 + J < n_e)
+        G[((int64_t)c * n_e + i0 + I) * n_e + j0 + J] += alpha * d[gi[I]] * d[gj[J]] * acc[r][s];
+    }
+}
+
+// out[c][q] = jxw[c][q] * sum_I N[q][I] sum_J G[c][I][J] N[q][J]
+__global__ void k_quad_contract(int n_cells, int n_e, int n_q, const double* __restrict__ N,
+                                const double* __restrict__ G, const double* __restrict__ jxw,
+                                double* __restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n_cells * n_q) return;
+  const int c = (int)(t / n_q), q = (int)(t % n_q);
+  const double* Nq = N + (int64_t)q * n_e;
+  const double* Gc = G + (int64_t)c * n_e * n_e;
+  double acc = 0.0;
+  for (int I = 0; I < n_e; ++I) {
+    double s = 0.0;
+    const double* gr = Gc + (int64_t)I * n_e;
+    for (int J = 0; J < n_e; ++J) s = fma(gr[J], Nq[J], s);
+    acc = fma(Nq[I], s, acc);
+  }
+  out[t] = (jxw ? jxw[t] : 1.0) * acc;
+}
+
+}  // namespace
+
+void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
+                    const double* v, double* out, cudaStream_t st) {
+  const int nt = (n_e + T - 1) / T;
+  const int64_t blocks = (int64_t)n_cells * nt * nt;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
+  k_assemble_cells<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, K, v, out, nt);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
+                double alpha, double* G, cudaStream_t st) {
+  const int nt = (op->n_e + T - 1) / T;
+  const int64_t blocks = (int64_t)op->n_cells * nt * nt;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "cell outer grid too large");
+  k_cell_outer<<<(unsigned)blocks, 256, 0, st>>>(op->map.ptr, op->n_e, op->inv_sqrt_mass.ptr, u,
+                                                 w, ld, B, alpha, G, nt);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void quad_contract(int n_cells, int n_e, int n_q, const double* N, const double* G,
+                   const double* jxw, double* out, cudaStream_t st) {
+  const int64_t n = (int64_t)n_cells * n_q;
+  k_quad_contract<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n_cells, n_e, n_q, N, G, jxw, out);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+}  // namespace chefsi

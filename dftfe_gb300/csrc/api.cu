@@ -538,7 +538,7 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
 }
 
 int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
-                         double* HX_out, int32_t precision, void* stream) {
+                         double* HX_out, double* W_out, int32_t precision, void* stream) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op && X && eig_host && N >= 1 && ld >= N, "bad argument");
   CHEFSI_REQUIRE(!op->is_complex, "Rayleigh-Ritz: complex operators not supported");
@@ -550,8 +550,64 @@ int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, dou
   if (HX_out)
     CHEFSI_CUDA(cudaMemcpyAsync(HX_out, s.HX.ptr, sizeof(double) * op->n_dofs * N,
                                 cudaMemcpyDeviceToDevice, st));
+  if (W_out)
+    CHEFSI_CUDA(cudaMemcpyAsync(W_out, s.W.ptr, sizeof(double) * (size_t)N * N,
+                                cudaMemcpyDeviceToDevice, st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,
+                 double* y, int64_t ldy, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(x && y && rows >= 0 && n_vec >= 1 && ldx >= n_vec && ldy >= n_vec, "bad argument");
+  axpby_block<double>(x, ldx, y, ldy, rows, n_vec, a, b, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_gemm(char ta, char tb, int64_t M, int32_t N, int32_t K, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                int32_t precision, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(A && B && C && M >= 0 && N >= 0 && K >= 0, "bad argument");
+  gemm_f64(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, precision, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                      const double* shape, const double* stiffness,
+                                      const double* v_jxw, double* out, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(shape && stiffness && v_jxw && out && n_cells > 0 && nodes_per_cell > 0 && n_q > 0,
+                 "bad argument");
+  assemble_cells(n_cells, nodes_per_cell, n_q, shape, stiffness, v_jxw, out, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_operator_update_cell_matrices(chefsi_operator op, const double* cell_matrices,
+                                         void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && cell_matrices, "bad argument");
+  update_cell_matrices(op, cell_matrices, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_cell_outer_accumulate(chefsi_operator op, const double* U, const double* V, int64_t ld,
+                                 int32_t n_vec, double alpha, double* G, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && U && V && G && n_vec >= 1 && ld >= n_vec, "bad argument");
+  CHEFSI_REQUIRE(!op->is_complex, "cell outer product: real operators only");
+  cell_outer(op, U, V, ld, n_vec, alpha, G, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                    const double* shape, const double* G, const double* jxw,
+                                    double* out, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(shape && G && out && n_cells > 0 && nodes_per_cell > 0 && n_q > 0, "bad argument");
+  quad_contract(n_cells, nodes_per_cell, n_q, shape, G, jxw, out, as_stream(stream));
   CHEFSI_API_END
 }
 

@@ -132,6 +132,16 @@ void residual_norms_c64(const cplx* X, int64_t ldx, const cplx* HX, int64_t ldh,
 // dot / norm helpers for Lanczos (device scalar results)
 void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaStream_t st);
 
+// adjoint / assembly building blocks (adjoint.cu)
+void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
+                    const double* v, double* out, cudaStream_t st);
+void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
+                double alpha, double* G, cudaStream_t st);
+void quad_contract(int n_cells, int n_e, int n_q, const double* N, const double* G,
+                   const double* jxw, double* out, cudaStream_t st);
+// replace the operator's cell matrices (device, unscaled) and refresh the derived copies
+void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStream_t st);
+
 // eigensolver kernels (dense.cu), launched by the eigensolver drivers
 __global__ void k_hh_vector(double* A, int N, int k, double* V, double* tau, double* d, double* e);
 __global__ void k_hh_symv(const double* A, int N, int k, const double* V, const double* tau,

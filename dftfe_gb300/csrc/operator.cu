@@ -679,6 +679,22 @@ __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, in
     b[t] = (float)a[t];
 }
 
+void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStream_t st) {
+  CHEFSI_REQUIRE(!op->is_complex, "update_cell_matrices: real operators only");
+  const int64_t nc = op->n_cells, ne = op->n_e;
+  const size_t nm = (size_t)nc * ne * ne;
+  CHEFSI_CUDA(cudaMemcpyAsync(op->mats64.ptr, mats_dev, nm * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st));
+  if (op->folded) {
+    k_fold_mats<double><<<grid_for((int64_t)nm, 256), 256, 0, st>>>(op->mats64.ptr, op->map.ptr,
+                                                                    op->inv_sqrt_mass.ptr, nc, ne);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  k_to_f32<<<grid_for((int64_t)nm, 256), 256, 0, st>>>(op->mats64.ptr, op->mats32.ptr, nm);
+  CHEFSI_CHECK_LAUNCH();
+  op->tc.ready = false;  // the FP16 split is rebuilt on the next tensor-core apply
+}
+
 template <typename T>
 static void upload(DeviceBuffer<T>& buf, const T* host, size_t n) {
   buf.reset(n);

@@ -182,9 +182,44 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
                        void* stream);
 
 /* Rayleigh-Ritz in the generalised form; eigenvalues to host eig_host (N), X rotated in
-   place to the Ritz vectors. If HX_out is non-null it receives A X_rot (FP64, [M][N]). */
+   place to the Ritz vectors. If HX_out is non-null it receives A X_rot (FP64, [M][N]); if
+   W_out is non-null it receives the N x N coefficient matrix W = L^{-T} Q (X_rot = X W). */
 int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
-                         double* HX_out, int32_t precision, void* stream);
+                         double* HX_out, double* W_out, int32_t precision, void* stream);
+
+/* y = a x + b y on [rows][n_vec] FP64 device blocks (leading dimensions ldx, ldy). */
+int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,
+                 double* y, int64_t ldy, void* stream);
+
+/* C = alpha op(A) op(B) + beta C, row-major device matrices, op = 'N' or 'T'. FP64, or FP32
+   products with FP64 accumulation across K chunks (CHEFSI_PREC_MIXED / FP32). */
+int chefsi_gemm(char ta, char tb, int64_t M, int32_t N, int32_t K, double alpha, const double* A,
+                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                int32_t precision, void* stream);
+
+/* Cell Hamiltonians on the device (the real-case formula of hamMatrixKernelLDA,
+   src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:61-115):
+   out[c][I][J] = 0.5 stiffness[I][J] + sum_q shape[q][I] v_jxw[c][q] shape[q][J].
+   shape [n_q][n_e], stiffness [n_e][n_e], v_jxw [n_cells][n_q], out [n_cells][n_e][n_e]. */
+int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                      const double* shape, const double* stiffness,
+                                      const double* v_jxw, double* out, void* stream);
+
+/* Replace the operator's cell matrices with new unscaled ones (device pointer), as
+   computeHamiltonianMatricesAllkpt does each SCF step; derived copies are refreshed. */
+int chefsi_operator_update_cell_matrices(chefsi_operator op, const double* cell_matrices,
+                                         void* stream);
+
+/* Adjoint building block: G[c][I][J] += alpha * sum_b (D U)[map I][b] (D V)[map J][b], D = M^{-1/2},
+   U, V device [n_dofs][ld] FP64, G device [n_cells][n_e][n_e] (dL/dH_c for L = U^T A V terms). */
+int chefsi_cell_outer_accumulate(chefsi_operator op, const double* U, const double* V, int64_t ld,
+                                 int32_t n_vec, double alpha, double* G, void* stream);
+
+/* out[c][q] = jxw[c][q] * sum_IJ shape[q][I] G[c][I][J] shape[q][J]  (jxw may be null):
+   dL/dV at the quadrature points from dL/dH_c. */
+int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                    const double* shape, const double* G, const double* jxw,
+                                    double* out, void* stream);
 
 /* residual norms r_i = || A x_i - lambda_i x_i || (host arrays eig, res). */
 int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,
