@@ -313,6 +313,103 @@ def run_hx_only(args):
     return 0
 
 
+def run_ritz_check(args):
+    """Mixed vs FP64 on the same subspace: after three mixed iterations from X0, one CheFSI
+    iteration in FP64 and one in mixed precision start from the same block and bounds; the
+    Ritz values are compared (the FP64 ones are the reference) and both iterations timed."""
+    import torch
+    from dftfe_gb300 import build, chefsi
+    build.build()
+    pr = build_workload(args.workload, args.seed)
+    N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    lo, blow, up = chefsi.initial_bounds(op, N)
+    mk = lambda: chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
+        chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=min(N, 512), mixed_precision="mixed",
+        rr_precision=args.rr_precision))
+    s = mk()
+    s.reinitSpectrumBounds(lo, blow, up)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 1)
+    X = torch.rand((M, N), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    for _ in range(3):
+        ev, _ = s.solve(op, X, useMixedPrec=True)
+        s.reinitSpectrumBounds(ev[0], ev[-1], up)
+    bounds = (ev[0], ev[-1], up)
+    out = {}
+    for mode in ("fp64", "mixed"):
+        sv = mk()
+        sv.reinitSpectrumBounds(*bounds)
+        Xc = X.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e, r = sv.solve(op, Xc, useMixedPrec=(mode == "mixed"))
+        torch.cuda.synchronize()
+        out[mode] = (e.copy(), r.copy(), time.perf_counter() - t0, sv.timings(mode == "mixed"))
+        del Xc
+    e64, e32 = out["fp64"][0], out["mixed"][0]
+    nocc = pr.n_occupied
+    d = np.abs(e32 - e64)
+    print(json.dumps({
+        "metric": "mixed vs FP64 Ritz error (one iteration from the same block)",
+        "workload": args.workload, "n_dofs": M, "n_wfc": N, "occupied": nocc,
+        "max_abs_err_occupied_Ha": float(d[:nocc].max()), "max_abs_err_all_Ha": float(d.max()),
+        "fp64_iter_s": out["fp64"][2], "mixed_iter_s": out["mixed"][2],
+        "speedup_mixed_vs_fp64": out["fp64"][2] / out["mixed"][2],
+        "fp64_phases_ms": out["fp64"][3], "mixed_phases_ms": out["mixed"][3],
+        "res_occ_max_fp64": float(out["fp64"][1][:nocc].max()),
+        "res_occ_max_mixed": float(out["mixed"][1][:nocc].max())}))
+    return 0
+
+
+def run_adjoint_check(args):
+    """Adjoint workload: 10^3 cells, degree 4, 256 wavefunctions, loss = sum of the lowest 128
+    Ritz values after 5 CheFSI iterations (degree 24, checkpoints every 6); the gradient w.r.t.
+    V at every quadrature point against central differences (h = 1e-5, frozen bounds) at 64
+    seeded random points and against the density of the 128 states."""
+    import torch
+    from dftfe_gb300 import adjoint, build
+    build.build()
+    pr = build_workload("adjoint", args.seed)
+    s = adjoint.AdjointSetup.from_problem(pr, n_iter=5, n_sum=128, degree=24, checkpoint=6)
+    w3 = pr.mesh.quadrature()[1]
+    v0 = torch.from_numpy(pr.info["vjxw"] / w3[None, :]).cuda().contiguous()
+    v = v0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L = adjoint.ritz_sum(v, s)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    L.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    g = v.grad.detach()
+    _, ev, X, tape = adjoint.run_forward(s, v0)
+    rho = adjoint.density_term(s, X)
+    s.bounds_per_iter = [t[2] for t in tape]
+    rng = np.random.default_rng(args.seed + 7)
+    h = 1e-5
+    errs, vals = [], []
+    gh = g.cpu().numpy()
+    for _ in range(64):
+        c, q = int(rng.integers(v0.shape[0])), int(rng.integers(v0.shape[1]))
+        vp, vm = v0.clone(), v0.clone()
+        vp[c, q] += h
+        vm[c, q] -= h
+        fd = (adjoint.run_forward(s, vp)[0] - adjoint.run_forward(s, vm)[0]) / (2 * h)
+        errs.append(abs(fd - gh[c, q]))
+        vals.append(abs(fd))
+    scale = max(vals)
+    out = {"metric": "adjoint check", "workload": "adjoint", "n_dofs": pr.n_dofs, "n_wfc": pr.n_wfc,
+           "n_sum": 128, "iterations": 5, "degree": 24, "checkpoint": 6, "loss": float(L),
+           "forward_s": t1 - t0, "backward_s": t2 - t1,
+           "fd_points": 64, "fd_h": h, "fd_max_abs_err": float(max(errs)),
+           "fd_max_rel_err": float(max(errs) / scale), "grad_max_abs": float(scale),
+           "grad_vs_density_rel": float(((g - rho).abs().max() / rho.abs().max()).item())}
+    print(json.dumps(out))
+    return 0
+
+
 def fp64_compare(pr, op, lo, blow, up, m, N, dev):
     """One FP64 HX over all N vectors, timed, and the FP64 iteration estimate."""
     import torch
@@ -338,6 +435,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed", choices=["mixed", "small", "large", "mixed_small"])
+    ap.add_argument("--ritz-check", action="store_true",
+                    help="one FP64 and one mixed iteration from the same block: Ritz error, times")
+    ap.add_argument("--adjoint-check", action="store_true",
+                    help="adjoint workload: gradient vs central differences at 64 points")
     ap.add_argument("--hx-only", action="store_true",
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
@@ -351,6 +452,10 @@ def main():
         return run_reference(args)
     if args.hx_only:
         return run_hx_only(args)
+    if args.adjoint_check:
+        return run_adjoint_check(args)
+    if args.ritz_check:
+        return run_ritz_check(args)
     return run_ours(args)
 
 
