@@ -21,8 +21,8 @@ the boundary (in DFT-FE these come from deal.II's ``FE_Q`` / ``MatrixFree`` and 
 * Gaussian local wells and Gaussian x real-solid-harmonic nonlocal projectors.
 
 Conventions: Hartree atomic units; local node I = a + (p+1)*(b + (p+1)*c) (x fastest);
-global node g = ix + np*(iy + np*iz) on the periodic lattice np = n*p; cell
-c = cx + n*(cy + n*cz).
+global node g = ix + np*(iy + np*iz) on the periodic lattice np = n*p; cells numbered in
+Morton order of (cx, cy, cz) (``PeriodicCubeMesh.cell_xyz``).
 """
 from __future__ import annotations
 
@@ -111,19 +111,27 @@ class PeriodicCubeMesh:
         self.n_dofs = self.npts ** 3
         self.nodes_per_cell = (self.p + 1) ** 3
         self.gll_x, self.gll_w = gll_nodes_weights(self.p)
+        # cells are numbered in Morton (Z) order of their integer coordinates, the order
+        # p4est hands DFT-FE its cells in; neighbouring cells stay close in the numbering
+        lex = np.arange(self.n_cells)
+        lx, ly, lz = lex % self.n, (lex // self.n) % self.n, lex // (self.n * self.n)
+        code = np.zeros(self.n_cells, dtype=np.int64)
+        for bit in range(max(1, int(self.n - 1).bit_length())):
+            code |= ((lx >> bit) & 1) << (3 * bit)
+            code |= ((ly >> bit) & 1) << (3 * bit + 1)
+            code |= ((lz >> bit) & 1) << (3 * bit + 2)
+        order = np.argsort(code, kind="stable")
+        self.cell_xyz = np.stack([lx[order], ly[order], lz[order]], axis=1)
 
     # -- maps ---------------------------------------------------------------------------
     def cell_origin(self):
         """[n_cells, 3] lower corners of the cells."""
-        c = np.arange(self.n_cells)
-        cx, cy, cz = c % self.n, (c // self.n) % self.n, c // (self.n * self.n)
-        return np.stack([cx, cy, cz], axis=1).astype(np.float64) * self.h
+        return self.cell_xyz.astype(np.float64) * self.h
 
     def cell_dof_map(self) -> np.ndarray:
         """[n_cells, n_e] int32 global dof of each cell node, periodic images folded."""
         n, p, npts = self.n, self.p, self.npts
-        c = np.arange(self.n_cells)
-        cx, cy, cz = c % n, (c // n) % n, c // (n * n)
+        cx, cy, cz = self.cell_xyz[:, 0], self.cell_xyz[:, 1], self.cell_xyz[:, 2]
         a = np.arange(p + 1)
         ix = (cx[:, None] * p + a[None, :]) % npts          # [nc, p+1]
         iy = (cy[:, None] * p + a[None, :]) % npts
@@ -141,8 +149,7 @@ class PeriodicCubeMesh:
         """
         n, p, npts = self.n, self.p, self.npts
         m = npts + 1
-        c = np.arange(self.n_cells)
-        cx, cy, cz = c % n, (c // n) % n, c // (n * n)
+        cx, cy, cz = self.cell_xyz[:, 0], self.cell_xyz[:, 1], self.cell_xyz[:, 2]
         a = np.arange(p + 1)
         ix = cx[:, None] * p + a[None, :]
         iy = cy[:, None] * p + a[None, :]
