@@ -85,6 +85,11 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one cell_hx_tc_kernel launch (ncu capture of
+# `bench.py --workload mixed --hx-only`, summarised in profiles/cell_hx_tc_mixed_traffic.md)
+TC_TRAFFIC_BYTES = {"mixed": 37.27e9 + 10.09e9}
+
+
 def hx_algorithmic(pr, B, s_h=4, s_x=4):
     """Bytes and flops of one filter HX over B vectors (reference formulation):
     flops = 2 n_c n_e^2 B + 4 n_nlc-rows P B; bytes = s_H n_c n_e^2 + 2 s_X M B + 4 n_c n_e."""
@@ -259,7 +264,10 @@ def run_ours(args):
         "ritz_sample": [float(ev[0]), float(ev[N // 2]), float(ev[-1])],
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "frac": achieved / hbm,
+                     "traffic": TC_TRAFFIC_BYTES.get(args.workload), "peak_source": src,
+                     "traffic_scope": "cell_hx_tc_kernel launch alone, dram read + write, ncu "
+                                      "(profiles/cell_hx_tc_mixed_traffic.md)",
                      "kernel": "cell_hx_tc_kernel (+ nonlocal, filter HX)",
                      "algorithmic_bytes_per_launch": hx_bytes},
         "e2e": {"value": e2e_ms / 1e3, "unit": "s/iter", "h2d_bytes_per_step": M * N * 8,
