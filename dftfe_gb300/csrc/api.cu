@@ -29,6 +29,8 @@ struct chefsi_solver_s {
   int last_degree = 0;
   DeviceBuffer<double> Xb64, Yb64, S, Hp, T1, Z, W, evals, HX, rot, resid, scal;
   DeviceBuffer<float> Xb32, Yb32;
+  TcOperand tx, th;      // FP16 splits of X and HX for the tensor-core RR products
+  TcDenseWork tcw;
   double times[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
   bool profile = false;
@@ -210,6 +212,14 @@ void hx_all_f64(chefsi_operator_s* op, const double* X, int64_t ld, int N, doubl
 // X[M][N] <- X W (row blocks through a temporary)
 void rotate_rows(chefsi_solver_s* s, double* X, int64_t ld, int64_t M, int N, const double* W,
                  int prec, cudaStream_t st) {
+  if (prec == CHEFSI_PREC_MIXED && dense_tc_available()) {
+    tc_exponents<double>(X, ld, M, N, s->tx, st);
+    tc_split_rows<double>(X, ld, M, N, s->tx, st);
+    tc_rotate(s->tx, W, N, N, X, ld, s->tcw, st);
+    const int rc = tc_dense_check_error(s->tcw, st);
+    if (rc != CHEFSI_OK) throw Error(rc, "tensor-core rotation: a bounded device wait expired");
+    return;
+  }
   const int64_t rows = std::min<int64_t>(M, std::max<int64_t>(4096, (int64_t)(256ll << 20) / (8ll * N)));
   double* tmp = s->rot.ensure((size_t)rows * N);
   for (int64_t r0 = 0; r0 < M; r0 += rows) {
@@ -233,6 +243,8 @@ __global__ void k_transpose(const double* __restrict__ A, double* __restrict__ B
 int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int N,
                        int prec, bool want_hx, cudaStream_t st) {
   const int64_t M = op->n_dofs;
+  // mixed mode on tensor cores: FP16-split Gram products and rotations (dense_tc.cu)
+  const bool tcd = prec == CHEFSI_PREC_MIXED && dense_tc_available();
   double* S = s->S.ensure((size_t)N * N);
   double* Hp = s->Hp.ensure((size_t)N * N);
   double* T1 = s->T1.ensure((size_t)N * N);
@@ -242,7 +254,13 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
   // S = X^T X (lower), then mirrored
   CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
-  gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+  if (tcd) {
+    tc_exponents<double>(X, ld, M, N, s->tx, st);
+    tc_split_transposed<double>(X, ld, M, N, s->tx, st);
+    tc_gram(s->tx, nullptr, S, N, true, s->tcw, st);
+  } else {
+    gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+  }
   symmetrize_lower(S, N, st);
   if (fault_injected("not_spd")) {
     k_negate_diag0<<<1, 1, 0, st>>>(S);
@@ -259,17 +277,31 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   // X is rounded to FP32 once and the same rounded basis enters S (the mixed Gram converts on
   // load), HX and Hp, so the generalised problem stays consistent.
   double* HX = s->HX.ensure((size_t)M * N);
-  if (is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32) {
+  const bool hx32 = is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32;
+  float* y32 = nullptr;
+  if (hx32) {
     float* x32 = s->Xb32.ensure((size_t)M * N);
-    float* y32 = s->Yb32.ensure((size_t)M * N);
+    y32 = s->Yb32.ensure((size_t)M * N);
     copy_block<double, float>(X, ld, x32, N, M, N, 1.0, st);
     hx_f32(op, x32, N, y32, N, N, 1.0, false, st);
-    copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
+    // the tensor-core path reads the FP32 HX directly; its rotation writes the FP64 HX
+    if (!tcd) copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
   } else {
     hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
   }
   CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
-  gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
+  if (tcd) {
+    if (hx32) {
+      tc_exponents<float>(y32, N, M, N, s->th, st);
+      tc_split_transposed<float>(y32, N, M, N, s->th, st);
+    } else {
+      tc_exponents<double>(HX, N, M, N, s->th, st);
+      tc_split_transposed<double>(HX, N, M, N, s->th, st);
+    }
+    tc_gram(s->tx, &s->th, Hp, N, true, s->tcw, st);
+  } else {
+    gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
+  }
   symmetrize_lower(Hp, N, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
   // C = L^{-1} Hp L^{-T}
@@ -281,8 +313,26 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   // W = L^{-T} Q
   gemm_f64('T', 'N', N, N, N, 1.0, S, N, Z, N, 0.0, W, N, CHEFSI_PREC_FP64, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
-  rotate_rows(s, X, ld, M, N, W, prec, st);
-  if (want_hx) rotate_rows(s, HX, N, M, N, W, prec, st);
+  if (tcd) {
+    // X <- X W in place from its FP16 row split (the column exponents of X are reused)
+    tc_split_rows<double>(X, ld, M, N, s->tx, st);
+    tc_rotate(s->tx, W, N, N, X, ld, s->tcw, st);
+    if (want_hx) {
+      if (hx32)
+        tc_split_rows<float>(y32, N, M, N, s->th, st);
+      else
+        tc_split_rows<double>(HX, N, M, N, s->th, st);
+      tc_rotate(s->th, W, N, N, HX, N, s->tcw, st);
+    }
+    rc = tc_dense_check_error(s->tcw, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("tensor-core Rayleigh-Ritz products: a bounded device wait expired");
+      return rc;
+    }
+  } else {
+    rotate_rows(s, X, ld, M, N, W, prec, st);
+    if (want_hx) rotate_rows(s, HX, N, M, N, W, prec, st);
+  }
   CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
   return CHEFSI_OK;
 }

@@ -159,6 +159,8 @@ void gram_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_
     gram_kernel<double><<<grid, 256, 0, st>>>(A, lda, B, ldb, K, N1, N2, C, ldc, per, ntj,
                                               lower_only, 1 << 30);
     CHEFSI_CHECK_LAUNCH();
+  } else if (prec == CHEFSI_PREC_MIXED && dense_tc_available()) {
+    gram_tc_f64(A, lda, B, ldb, K, N1, N2, C, ldc, lower_only, st);
   } else {
     gram32(A, lda, B, ldb, K, N1, N2, C, ldc, lower_only, st);
   }
@@ -270,6 +272,16 @@ void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const dou
     gemm_kernel<double><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                               ldc, 1 << 30);
     CHEFSI_CHECK_LAUNCH();
+  } else if (prec == CHEFSI_PREC_MIXED && alpha == 1.0 && beta == 0.0 && !itb && K >= 1 &&
+             dense_tc_available()) {
+    // the two shapes of the Rayleigh-Ritz step on tensor cores: A^T B over a long K (Gram)
+    // and A B with a long M (rotation)
+    if (ita) {
+      CHEFSI_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc, 0, sizeof(double) * N, M, st));
+      gram_tc_f64(A, lda, B, ldb, K, (int)M, N, C, (int)ldc, false, st);
+    } else {
+      rotate_tc_f64(A, lda, M, K, B, ldb, N, C, ldc, st);
+    }
   } else if (beta == 0.0) {
     gemm32(ita != 0, itb != 0, M, N, K, alpha, A, lda, B, ldb, C, ldc, false, false, st);
   } else {
@@ -930,6 +942,61 @@ __global__ void k_bt_update(const double* V, int N, int k,
   }
 }
 
+// Compact WY form of a block of reflectors (LAPACK dlarft, forward / columnwise):
+// H_k0 H_k0+1 ... H_k0+nb-1 = I - V T V^T with T upper triangular,
+//   T[j][j] = tau_j,  T[0:j][j] = -tau_j T[0:j][0:j] (V^T v_j)[0:j],
+// from the Gram matrix G = V^T V of the block (nb x nb). One thread per row of T.
+__global__ void k_build_t(const double* G, const double* tau, int nb, double* T) {
+  const int i = threadIdx.x;
+  for (int j = 0; j < nb; ++j) {
+    if (i < nb) {
+      double v = 0.0;
+      if (i < j) {
+        double s = 0.0;
+        for (int l = i; l < j; ++l) s += T[i * nb + l] * G[l * nb + j];
+        v = -tau[j] * s;
+      } else if (i == j) {
+        v = tau[j];
+      }
+      T[i * nb + j] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_transpose_sq(const double* A, double* B, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    B[t] = A[(t % N) * N + t / N];
+}
+
+// Z <- H_0 H_1 ... H_{N-3} Z with the reflectors in rows of V (V[k][k+1:N], tau[k]), applied
+// as compact-WY blocks of kWY reflectors, last block first: Z -= Vb (T (Vb^T Z)).
+constexpr int kWY = 64;
+static void back_transform_wy(const double* V, const double* tau, int N, double* Z, cudaStream_t st) {
+  const int nrefl = N - 2;
+  if (nrefl <= 0) return;
+  DeviceBuffer<double> Vc((size_t)N * N), G((size_t)kWY * kWY), T((size_t)kWY * kWY),
+      W1((size_t)kWY * N), W2((size_t)kWY * N);
+  // Vc[i][k] = V[k][i]: block k0.. of reflectors is the row-major N x nb slice Vc + k0
+  k_transpose_sq<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(V, Vc.ptr, N);
+  CHEFSI_CHECK_LAUNCH();
+  for (int end = nrefl; end > 0; end -= kWY) {
+    const int k0 = std::max(0, end - kWY), nb = end - k0;
+    const double* Vb = Vc.ptr + k0;
+    CHEFSI_CUDA(cudaMemsetAsync(G.ptr, 0, sizeof(double) * nb * nb, st));
+    gram_f64(Vb, N, Vb, N, N, nb, nb, G.ptr, nb, CHEFSI_PREC_FP64, false, st);
+    k_build_t<<<1, kWY, 0, st>>>(G.ptr, tau + k0, nb, T.ptr);
+    CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CUDA(cudaMemsetAsync(W1.ptr, 0, sizeof(double) * nb * N, st));
+    gram_f64(Vb, N, Z, N, N, nb, N, W1.ptr, N, CHEFSI_PREC_FP64, false, st);        // Vb^T Z
+    gemm_f64('N', 'N', nb, N, nb, 1.0, T.ptr, nb, W1.ptr, N, 0.0, W2.ptr, N,
+             CHEFSI_PREC_FP64, st);                                                   // T (Vb^T Z)
+    gemm_f64('N', 'N', N, N, nb, -1.0, Vb, N, W2.ptr, N, 1.0, Z, N, CHEFSI_PREC_FP64, st);
+  }
+}
+
 int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   CHEFSI_REQUIRE(N >= 1, "syevd: N must be positive");
   DeviceBuffer<double> V((size_t)N * N), tau(N), d(N), e(N), p(N);
@@ -949,7 +1016,9 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   }
   k_tail<<<1, 32, 0, st>>>(A, N, d.ptr, e.ptr);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect<<<(N + 127) / 128, 128, 0, st>>>(d.ptr, e.ptr, N, w);
+  // one warp per block: the Sturm sequences are FP64-division chains, so spread them over
+  // as many SMs as there are warps
+  k_bisect<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, e.ptr, N, w);
   CHEFSI_CHECK_LAUNCH();
   // cluster tolerance relative to the tridiagonal's scale
   std::vector<double> hd(N), he(N);
@@ -963,17 +1032,10 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   const double ortol = 1e-5 * std::max(tn, 1e-300);
   DeviceBuffer<double> work((size_t)N * 5 * N);
   DeviceBuffer<unsigned char> swaps((size_t)N * N);
-  k_inverse_iteration<<<(N + 63) / 64, 64, 0, st>>>(d.ptr, e.ptr, N, w, Z, N, work.ptr, swaps.ptr,
+  k_inverse_iteration<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, e.ptr, N, w, Z, N, work.ptr, swaps.ptr,
                                                     ortol);
   CHEFSI_CHECK_LAUNCH();
-  for (int k = N - 3; k >= 0; --k) {
-    k_bt_dot<<<(N + 127) / 128, 128, 0, st>>>(V.ptr, N, k, Z, p.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    k_bt_update<<<grid_for((int64_t)(N - k - 1) * N, 256), 256, 0, st>>>(V.ptr, N, k, tau.ptr, Z,
-                                                                         p.ptr);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  CHEFSI_CHECK_LAUNCH();
+  back_transform_wy(V.ptr, tau.ptr, N, Z, st);
   CHEFSI_CUDA(cudaStreamSynchronize(st));
   return CHEFSI_OK;
 }

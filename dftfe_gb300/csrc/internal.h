@@ -12,10 +12,10 @@ struct cplx {
   double x, y;
 };
 
-// Tensor-core copy of the cell matrices: FP16 hi/lo split of 2^mat_shift * A_e, rows padded
-// to a multiple of 16 and columns (the K dimension) to kpad (a multiple of 64), stored
-// [n_cells][npad][kpad] so that one TMA box of [rows][64 halves] is one 128-byte-swizzled
-// operand tile.
+// Tensor-core copy of the cell matrices: FP16 hi/lo split of 2^s * A_e (s a power-of-two
+// exponent putting max |A_e| in [2^14, 2^15)), rows and columns zero-padded to npad (a
+// multiple of 32), stored [n_cells][npad][npad] so that one TMA box of [rows][32 halves] is
+// one 64-byte-swizzled operand tile.
 struct TensorCellMats {
   DeviceBuffer<__half> hi, lo;
   int npad = 0;
@@ -55,6 +55,7 @@ struct chefsi_operator_s {
 
 
   chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
+  chefsi::DeviceBuffer<unsigned long long> tc_sched;  // its work counter
 
   // workspaces (grow-only)
   chefsi::DeviceBuffer<double> ws64a, ws64b, nlW64;
@@ -99,6 +100,45 @@ void copy_block(const Ts* src, int64_t lds, Td* dst, int64_t ldd, int64_t rows, 
 // max |x| over a block (device scalar out, as float bits via atomicMax)
 void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
                       cudaStream_t st);
+
+// ---- tensor-core dense products (dense_tc.cu) ---------------------------------------------
+// FP16 hi/lo split of a block of vectors, each column scaled by 2^e[j] (max |entry| in
+// [2^14, 2^15)). Transposed layout [padded columns][ld = padded rows] feeds the Gram
+// products; row layout [rows][ld = padded columns] feeds the rotation.
+struct TcOperand {
+  DeviceBuffer<__half> hi, lo;
+  DeviceBuffer<int> e;
+  DeviceBuffer<unsigned long long> bits;
+  int64_t rows = 0;  // logical rows (dofs)
+  int cols = 0;      // logical columns (vectors)
+  int64_t ld = 0;    // leading dimension of the FP16 layout
+  int padded = 0;    // padded column count
+  bool transposed = false;
+};
+struct TcDenseWork {
+  DeviceBuffer<double> part;      // Gram k-slice partials
+  DeviceBuffer<__half> whi, wlo;  // rotation matrix operand
+  DeviceBuffer<int> et;           // rotation output column exponents
+  DeviceBuffer<int> err;          // bounded-wait expiry flag
+};
+bool dense_tc_available();
+template <typename T>
+void tc_exponents(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cudaStream_t st);
+template <typename T>
+void tc_split_transposed(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cudaStream_t st);
+template <typename T>
+void tc_split_rows(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cudaStream_t st);
+// C += A^T B (B == nullptr: A^T A); lower: only 128x128 tiles on or below the diagonal
+void tc_gram(const TcOperand& A, const TcOperand* B, double* C, int64_t ldc, bool lower,
+             TcDenseWork& w, cudaStream_t st);
+// Y[M][n_out] = X W, W [X.cols][n_out] (X given by its row split; Y may be X itself)
+void tc_rotate(const TcOperand& Xr, const double* W, int64_t ldw, int n_out, double* Y,
+               int64_t ldy, TcDenseWork& w, cudaStream_t st);
+int tc_dense_check_error(TcDenseWork& w, cudaStream_t st);
+void gram_tc_f64(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t K, int N1,
+                 int N2, double* C, int ldc, bool lower_only, cudaStream_t st);
+void rotate_tc_f64(const double* X, int64_t ld, int64_t M, int K, const double* W, int64_t ldw,
+                   int n_out, double* Y, int64_t ldy, cudaStream_t st);
 
 // ---- dense linear algebra (dense.cu) ------------------------------------------------------
 // C (N x N, row-major, ldc) += A^H B for A [K][N1] (lda), B [K][N2] (ldb), K split across CTAs.
