@@ -21,6 +21,7 @@
 // is bounded: on expiry the CTA records CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded)
 // for its own TMA copies, frees its tensor memory and returns.
 #include "internal.h"
+#include "tc_common.cuh"
 
 #include <cuda.h>
 
@@ -31,110 +32,13 @@
 
 namespace chefsi {
 
+using namespace tcx;
+
 namespace {
 
 constexpr int kVec = 128;          // vectors per CTA (MMA M)
 constexpr int kKB = 32;            // halves per K-block (64-byte rows)
 constexpr int kRowBytes = kKB * 2; // 64
-constexpr uint32_t kWaitLimit = 1u << 24;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait; returns false on expiry (and records the timeout)
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
-                                          volatile int* abort_flag) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (*abort_flag) return false;
-    if (i > 64) __nanosleep(128);
-  }
-  atomicExch(err, CHEFSI_ERR_TIMEOUT);
-  *abort_flag = 1;
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart
-__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);          // start address
-  d |= (uint64_t)(1) << 16;                        // leading byte offset (unused, K-major swizzled)
-  d |= (uint64_t)((512 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 64 B
-  d |= (uint64_t)1 << 46;                          // descriptor version for tcgen05
-  d |= (uint64_t)4 << 61;                          // layout: SWIZZLE_64B
-  return d;
-}
-
-// instruction descriptor, kind::f16: A = B = F16, D = F32, both K-major
-__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
-  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                        uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 struct TcArgs {
   const float* src;
   int64_t lds;
@@ -486,28 +390,6 @@ __global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn get_encode() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-    else
-      cudaGetLastError();
-  });
-  return fn;
-}
-
 void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows) {
   EncodeTiledFn enc = get_encode();
   if (!enc) throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -547,6 +429,51 @@ TcPlan plan_for(int n_e) {
 
 }  // namespace
 
+namespace tcx {
+EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+void make_map_2d(CUtensorMap* m, const __half* base, int64_t inner, int64_t rows, int64_t ld,
+                 int box_inner, int box_rows) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(base) & 15) == 0 && (ld * 2) % 16 == 0 &&
+                     (box_inner * 2) % 16 == 0 && box_rows <= 256 && box_inner <= 256,
+                 "tensor map: unaligned base, row stride or box");
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half*>(base), dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+bool tcgen05_device() {
+  if (!get_encode()) return false;
+  int dev = 0, major = 0;
+  CHEFSI_CUDA(cudaGetDevice(&dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  return major == 10;  // sm_100 family (GB300 = 10.3)
+}
+}  // namespace tcx
+
 void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
   auto& tc = op->tc;
   if (tc.ready || op->is_complex || !op->folded) return;
@@ -574,11 +501,7 @@ void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
 
 bool tc_usable(chefsi_operator_s* op) {
   if (op->is_complex || !op->folded || op->n_e > 512) return false;
-  if (!get_encode()) return false;
-  int dev = 0, major = 0;
-  CHEFSI_CUDA(cudaGetDevice(&dev));
-  CHEFSI_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
-  return major == 10;  // sm_100 family (GB300 = 10.3)
+  return tcgen05_device();
 }
 
 // launch the persistent tensor-core kernel (a.out_scale set by the caller)
