@@ -30,12 +30,12 @@ _ERRNAMES = {1: "INVALID", 2: "CUDA", 3: "NOT_SPD", 4: "NO_CONVERGENCE", 5: "ALL
 EXPORTS = [
     "chefsi_last_error", "chefsi_version", "chefsi_launch_count", "chefsi_operator_create", "chefsi_operator_destroy",
     "chefsi_operator_info", "chefsi_hx", "chefsi_overlap", "chefsi_xthx",
-    "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_syevd_noalloc",
+    "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_heevd", "chefsi_syevd_noalloc",
     "chefsi_cholesky_gs",
     "chefsi_rayleigh_ritz", "chefsi_residual_norms", "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
-    "chefsi_solve", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
+    "chefsi_solve", "chefsi_solve_batched", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
     "chefsi_axpby", "chefsi_assemble_cell_hamiltonians", "chefsi_operator_update_cell_matrices",
     "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract",
 ]
@@ -100,6 +100,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_chebyshev_filter": ([vp, vp, i64, i32, i32, f64, f64, f64, i32, vp], ctypes.c_int),
         "chefsi_lanczos_bounds": ([vp, i32, i32, vp, ctypes.c_uint64, vp, vp, vp], ctypes.c_int),
         "chefsi_syevd": ([i32, vp, vp, vp, vp], ctypes.c_int),
+        "chefsi_heevd": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_syevd_noalloc": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_cholesky_gs": ([vp, vp, i64, i32, i32, vp], ctypes.c_int),
         "chefsi_rayleigh_ritz": ([vp, vp, i64, i32, vp, vp, vp, i32, vp], ctypes.c_int),
@@ -119,6 +120,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solver_set_profiling": ([vp, i32], ctypes.c_int),
         "chefsi_solver_hx_stats": ([vp, vp, vp], ctypes.c_int),
         "chefsi_solve": ([vp, vp, vp, i32, vp, vp, i32, i32, vp], ctypes.c_int),
+        "chefsi_solve_batched": ([i32, vp, vp, vp, vp, vp, vp, i32, i32, i32], ctypes.c_int),
         "chefsi_solve_no_rr": ([vp, vp, vp, i32, i32, i32, vp], ctypes.c_int),
         "chefsi_chebyshev_order": ([f64], i32),
     }

@@ -192,7 +192,7 @@ def rayleighRitzGEP(op: KohnShamOperator, X: torch.Tensor, precision="fp64", wan
     N = X.shape[1]
     ev = np.zeros(N)
     HX = torch.empty_like(X) if want_hx else None
-    W = torch.empty((N, N), dtype=torch.float64, device=X.device) if want_w else None
+    W = torch.empty((N, N), dtype=X.dtype, device=X.device) if want_w else None
     check(_lib.load().chefsi_rayleigh_ritz(op.handle, _ptr(X), X.stride(0), N, _np_ptr(ev),
                                            _ptr(HX), _ptr(W), _prec(precision), _stream()))
     out = [ev]
@@ -248,12 +248,14 @@ def computeEigenResidualNorm(op: KohnShamOperator, X: torch.Tensor, eig) -> np.n
 
 
 def syevd(A: torch.Tensor):
-    """Symmetric eigensolve on the GPU (FP64): returns (w ascending, Z with vectors in columns)."""
+    """Symmetric (real) or Hermitian (complex) eigensolve on the GPU in FP64: returns
+    (w ascending, Z with the eigenvectors in its columns)."""
     N = A.shape[0]
     Ac = A.clone().contiguous()
     w = torch.empty(N, dtype=torch.float64, device=A.device)
-    Z = torch.empty((N, N), dtype=torch.float64, device=A.device)
-    check(_lib.load().chefsi_syevd(N, _ptr(Ac), _ptr(w), _ptr(Z), _stream()))
+    Z = torch.empty((N, N), dtype=A.dtype, device=A.device)
+    fn = _lib.load().chefsi_heevd if A.is_complex() else _lib.load().chefsi_syevd
+    check(fn(N, _ptr(Ac), _ptr(w), _ptr(Z), _stream()))
     return w, Z
 
 
@@ -362,3 +364,26 @@ def initial_bounds(op: KohnShamOperator, n_wfc: int, k: int = 20, reproducible: 
     lo, up = lanczosLowerUpperBoundEigenSpectrum(op, k, reproducible, v0, seed)
     blow = lo + (up - lo) / op.n_dofs * n_wfc * (10.0 if reproducible else 200.0)
     return lo, blow, up
+
+
+def solve_batched(solvers, operators, Xs, useMixedPrec: bool = False,
+                  computeResidual: bool = True, isFirstScf: bool = False, n_streams: int = 0):
+    """One CheFSI iteration on each independent problem (k-points, spins, Bloch Hamiltonians)
+    through chefsi_solve_batched; returns (list of eigenvalues, list of residual norms)."""
+    count = len(Xs)
+    if not (len(solvers) == len(operators) == count):
+        raise ValueError("solvers, operators and Xs must have the same length")
+    lib = _lib.load()
+    vp = ctypes.c_void_p
+    hs = (vp * count)(*[s._handle(useMixedPrec).value for s in solvers])
+    ops = (vp * count)(*[o.handle.value for o in operators])
+    xs = (vp * count)(*[X.data_ptr() for X in Xs])
+    ns = (ctypes.c_int32 * count)(*[X.shape[1] for X in Xs])
+    evs = [np.zeros(X.shape[1]) for X in Xs]
+    rns = [np.zeros(X.shape[1]) for X in Xs]
+    ev_p = (vp * count)(*[e.ctypes.data for e in evs])
+    rn_p = (vp * count)(*[r.ctypes.data for r in rns])
+    torch.cuda.synchronize()  # the worker streams do not order after the caller's stream
+    check(lib.chefsi_solve_batched(count, hs, ops, xs, ns, ev_p, rn_p, int(computeResidual),
+                                   int(isFirstScf), int(n_streams)))
+    return evs, rns

@@ -10,9 +10,13 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <numeric>
 #include <random>
+#include <thread>
 #include <vector>
 
 namespace chefsi {
@@ -28,6 +32,7 @@ struct chefsi_solver_s {
   double a0 = 0.0, b_low = 0.0, b_up = 0.0;
   int last_degree = 0;
   DeviceBuffer<double> Xb64, Yb64, S, Hp, T1, Z, W, evals, HX, rot, resid, scal;
+  DeviceBuffer<double> G2, W2;  // 2N x 2N real views for the complex tensor-core products
   DeviceBuffer<float> Xb32, Yb32;
   TcOperand tx, th;      // FP16 splits of X and HX for the tensor-core RR products
   TcDenseWork tcw;
@@ -181,7 +186,36 @@ void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m
   const int Bmax = std::max(1, std::min(s->p.cheby_wfc_block > 0 ? s->p.cheby_wfc_block : N, N));
   for (int j0 = 0; j0 < N; j0 += Bmax) {
     const int B = std::min(Bmax, N - j0);
-    if (op->is_complex) {
+    if (op->is_complex && is_mixed(prec) && op->folded) {
+      // mixed Bloch filter: the real form of the operator (2 n_dofs unknowns) on FP32 rows,
+      // so the tensor-core (FP16 split) or FP32 HX applies
+      chefsi_operator_s* rv = realified(op, st);
+      cplx* Xc = reinterpret_cast<cplx*>(X);
+      const int64_t M = op->n_dofs;
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(reinterpret_cast<double*>(Xc + j0), 2 * (int64_t)N, M, 2 * B, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      double scale = 1.0;
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
+      float* xr = s->Xb32.ensure((size_t)2 * M * B);
+      float* yr = s->Yb32.ensure((size_t)2 * M * B);
+      complex_to_real_rows(Xc + j0, N, M, B, scale, xr, st);
+      cheb_filter<float>(xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0,
+                         [&](const float* src, float* dst, double scv, bool acc) {
+                           s->hx_mark(st);
+                           hx_filter32(rv, prec, src, dst, B, scv, acc, st);
+                           s->hx_mark(st);
+                         },
+                         st);
+      if (prec == CHEFSI_PREC_MIXED) {
+        const int tc = tc_check_error(rv, st);
+        if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
+      }
+      real_rows_to_complex(xr, M, B, 1.0 / scale, Xc + j0, N, st);
+    } else if (op->is_complex) {
       cplx* Xc = reinterpret_cast<cplx*>(X);
       cplx* Xb = reinterpret_cast<cplx*>(s->Xb64.ensure((size_t)op->n_dofs * B * 2));
       cplx* Yb = reinterpret_cast<cplx*>(s->Yb64.ensure((size_t)op->n_dofs * B * 2));
@@ -230,6 +264,13 @@ void rotate_rows(chefsi_solver_s* s, double* X, int64_t ld, int64_t M, int N, co
 }
 
 __global__ void k_negate_diag0(double* S) { S[0] = -fabs(S[0]) - 1.0; }
+
+__global__ void k_conj_transpose(const cplx* __restrict__ A, cplx* __restrict__ B, int N) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    B[t] = cconj(A[(t % N) * N + t / N]);
+}
 
 __global__ void k_transpose(const double* __restrict__ A, double* __restrict__ B, int N) {
   const int64_t n = (int64_t)N * N;
@@ -332,6 +373,145 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   } else {
     rotate_rows(s, X, ld, M, N, W, prec, st);
     if (want_hx) rotate_rows(s, HX, N, M, N, W, prec, st);
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  return CHEFSI_OK;
+}
+
+// X[M][N] <- X W for complex blocks (row blocks through a temporary)
+void rotate_rows_c(chefsi_solver_s* s, cplx* X, int64_t ld, int64_t M, int N, const cplx* W,
+                   cudaStream_t st) {
+  const int64_t rows = std::min<int64_t>(M, std::max<int64_t>(2048, (int64_t)(256ll << 20) / (16ll * N)));
+  cplx* tmp = reinterpret_cast<cplx*>(s->rot.ensure((size_t)rows * N * 2));
+  const cplx one = {1.0, 0.0}, zero = {0.0, 0.0};
+  for (int64_t r0 = 0; r0 < M; r0 += rows) {
+    const int64_t nr = std::min(rows, M - r0);
+    gemm_c64('N', 'N', nr, N, N, one, X + r0 * ld, ld, W, N, zero, tmp, N, st);
+    copy_block<cplx, cplx>(tmp, N, X + r0 * ld, ld, nr, N, 1.0, st);
+  }
+}
+
+// The complex products of the mixed step run on the real tensor-core kernels through the
+// real view of an interleaved complex block, Y = [Re x_0, Im x_0, Re x_1, ...] ([M][2N]):
+// G = Y_a^T Y_b gives C = A^H B as C_ij = (G[2i][2j] + G[2i+1][2j+1]) + i (G[2i][2j+1] -
+// G[2i+1][2j]), and X W is Y W_r with the 2N x 2N real matrix
+// W_r = [[Re W, Im W], [-Im W, Re W]] interleaved the same way.
+__global__ void k_gram_to_complex(const double* G, int N, cplx* C, int lower) {
+  const int64_t n = (int64_t)N * N;
+  const int64_t ld = 2 * (int64_t)N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (lower && j > i) continue;
+    const double* r0 = G + (2 * i) * ld;
+    const double* r1 = r0 + ld;
+    C[t] = {r0[2 * j] + r1[2 * j + 1], r0[2 * j + 1] - r1[2 * j]};
+  }
+}
+__global__ void k_realify_w(const cplx* W, int N, double* Wr) {
+  const int64_t n = (int64_t)N * N;
+  const int64_t ld = 2 * (int64_t)N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / N), m = (int)(t % N);
+    const cplx w = W[t];
+    Wr[(2 * k) * ld + 2 * m] = w.x;
+    Wr[(2 * k) * ld + 2 * m + 1] = w.y;
+    Wr[(2 * k + 1) * ld + 2 * m] = -w.y;
+    Wr[(2 * k + 1) * ld + 2 * m + 1] = w.x;
+  }
+}
+
+// Rayleigh-Ritz for a complex (Bloch) operator: the generalised form with Hermitian S and Hp.
+int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, int64_t ld, int N,
+                          int prec, bool want_hx, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const bool tcd = prec == CHEFSI_PREC_MIXED && dense_tc_available();
+  cplx* S = reinterpret_cast<cplx*>(s->S.ensure((size_t)N * N * 2));
+  cplx* Hp = reinterpret_cast<cplx*>(s->Hp.ensure((size_t)N * N * 2));
+  cplx* T1 = reinterpret_cast<cplx*>(s->T1.ensure((size_t)N * N * 2));
+  cplx* Z = reinterpret_cast<cplx*>(s->Z.ensure((size_t)N * N * 2));
+  cplx* W = reinterpret_cast<cplx*>(s->W.ensure((size_t)N * N * 2));
+  double* w = s->evals.ensure(N);
+  double* Xv = reinterpret_cast<double*>(X);
+  const int N2 = 2 * N;
+  double* G = tcd ? s->G2.ensure((size_t)N2 * N2) : nullptr;
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  if (tcd) {
+    tc_exponents<double>(Xv, 2 * ld, M, N2, s->tx, st);
+    tc_split_transposed<double>(Xv, 2 * ld, M, N2, s->tx, st);
+    CHEFSI_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * N2 * N2, st));
+    tc_gram(s->tx, nullptr, G, N2, true, s->tcw, st);
+    symmetrize_lower(G, N2, st);
+    k_gram_to_complex<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(G, N, S, 1);
+    CHEFSI_CHECK_LAUNCH();
+  } else {
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(cplx) * N * N, st));
+    gram_c64(X, ld, X, ld, M, N, N, S, N, true, st);
+  }
+  symmetrize_lower_c(S, N, st);
+  if (fault_injected("not_spd")) {
+    k_negate_diag0<<<1, 1, 0, st>>>(reinterpret_cast<double*>(S));
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower_c(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower_c(S, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  // HX in FP64 (complex)
+  cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
+  {
+    const int Bmax = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
+    for (int j0 = 0; j0 < N; j0 += Bmax) {
+      const int B = std::min(Bmax, N - j0);
+      hx_c64(op, X + j0, ld, HX + j0, N, B, 1.0, false, st);
+    }
+  }
+  double* HXv = reinterpret_cast<double*>(HX);
+  if (tcd) {
+    tc_exponents<double>(HXv, N2, M, N2, s->th, st);
+    tc_split_transposed<double>(HXv, N2, M, N2, s->th, st);
+    CHEFSI_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * N2 * N2, st));
+    tc_gram(s->tx, &s->th, G, N2, true, s->tcw, st);
+    k_gram_to_complex<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(G, N, Hp, 1);
+    CHEFSI_CHECK_LAUNCH();
+  } else {
+    CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(cplx) * N * N, st));
+    gram_c64(X, ld, HX, N, M, N, N, Hp, N, true, st);
+  }
+  symmetrize_lower_c(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  const cplx one = {1.0, 0.0}, zero = {0.0, 0.0};
+  // C = L^{-1} Hp L^{-H}
+  gemm_c64('N', 'N', N, N, N, one, S, N, Hp, N, zero, T1, N, st);
+  gemm_c64('N', 'C', N, N, N, one, T1, N, S, N, zero, Hp, N, st);
+  symmetrize_lower_c(Hp, N, st);
+  rc = heevd(Hp, N, w, Z, st);
+  if (rc != CHEFSI_OK) return rc;
+  // W = L^{-H} Q
+  gemm_c64('C', 'N', N, N, N, one, S, N, Z, N, zero, W, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  if (tcd) {
+    double* Wr = s->W2.ensure((size_t)N2 * N2);
+    k_realify_w<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(W, N, Wr);
+    CHEFSI_CHECK_LAUNCH();
+    tc_split_rows<double>(Xv, 2 * ld, M, N2, s->tx, st);
+    tc_rotate(s->tx, Wr, N2, N2, Xv, 2 * ld, s->tcw, st);
+    if (want_hx) {
+      tc_split_rows<double>(HXv, N2, M, N2, s->th, st);
+      tc_rotate(s->th, Wr, N2, N2, HXv, N2, s->tcw, st);
+    }
+    rc = tc_dense_check_error(s->tcw, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("tensor-core Rayleigh-Ritz products: a bounded device wait expired");
+      return rc;
+    }
+  } else {
+    rotate_rows_c(s, X, ld, M, N, W, st);
+    if (want_hx) rotate_rows_c(s, HX, N, M, N, W, st);
   }
   CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
   return CHEFSI_OK;
@@ -498,13 +678,24 @@ int chefsi_syevd(int32_t N, double* A, double* w, double* Z, void* stream) {
   CHEFSI_API_END
 }
 
+int chefsi_heevd(int32_t N, double* A, double* w, double* Z, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(A && w && Z && N >= 1, "bad argument");
+  int rc = heevd(reinterpret_cast<cplx*>(A), N, w, reinterpret_cast<cplx*>(Z), as_stream(stream));
+  if (rc != CHEFSI_OK) return rc;
+  CHEFSI_API_END
+}
+
 int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible, const double* v0_host,
                           uint64_t seed, double* lower, double* upper, void* stream) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op && lower && upper && k >= 2, "bad argument");
-  CHEFSI_REQUIRE(!op->is_complex, "Lanczos bounds: complex operators not supported");
   cudaStream_t st = as_stream(stream);
   const int64_t M = op->n_dofs;
+  // complex operators: the vectors are interleaved complex, handled as real vectors of
+  // length 2M for the inner products (Re x^H y = real-view dot), which is the reference's
+  // alpha = f^H v up to rounding for a Hermitian operator
+  const int64_t L = op->is_complex ? 2 * M : M;
   std::vector<double> h(M);
   if (v0_host) {
     std::memcpy(h.data(), v0_host, sizeof(double) * M);
@@ -513,31 +704,40 @@ int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible, c
     std::uniform_real_distribution<double> U(0.0, 1.0);
     for (auto& x : h) x = U(gen);
   }
-  DeviceBuffer<double> v(M), v0(M), f(M), sc(1);
-  CHEFSI_CUDA(cudaMemcpyAsync(v.ptr, h.data(), sizeof(double) * M, cudaMemcpyHostToDevice, st));
+  std::vector<double> hv(L, 0.0);
+  for (int64_t i = 0; i < M; ++i) hv[op->is_complex ? 2 * i : i] = h[i];
+  DeviceBuffer<double> v(L), v0(L), f(L), sc(1);
+  CHEFSI_CUDA(cudaMemcpyAsync(v.ptr, hv.data(), sizeof(double) * L, cudaMemcpyHostToDevice, st));
   auto dot = [&](const double* x, const double* y) {
     double r = 0.0;
-    dot_f64(x, y, M, sc.ptr, st);
+    dot_f64(x, y, L, sc.ptr, st);
     CHEFSI_CUDA(cudaMemcpyAsync(&r, sc.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
     CHEFSI_CUDA(cudaStreamSynchronize(st));
     return r;
   };
+  auto apply = [&](const double* x, double* y) {
+    if (op->is_complex)
+      hx_c64(op, reinterpret_cast<const cplx*>(x), 1, reinterpret_cast<cplx*>(y), 1, 1, 1.0,
+             false, st);
+    else
+      hx_f64(op, x, 1, y, 1, 1, 1.0, false, st);
+  };
   const double n0 = std::sqrt(dot(v.ptr, v.ptr));
   CHEFSI_REQUIRE(n0 > 0.0, "Lanczos start vector is zero");
-  scale_block<double>(v.ptr, 1, M, 1, 1.0 / n0, st);
-  hx_f64(op, v.ptr, 1, f.ptr, 1, 1, 1.0, false, st);
+  scale_block<double>(v.ptr, 1, L, 1, 1.0 / n0, st);
+  apply(v.ptr, f.ptr);
   double alpha = dot(f.ptr, v.ptr);
-  axpby_block<double>(v.ptr, 1, f.ptr, 1, M, 1, -alpha, 1.0, st);
+  axpby_block<double>(v.ptr, 1, f.ptr, 1, L, 1, -alpha, 1.0, st);
   std::vector<double> T((size_t)k * k, 0.0);
   T[0] = alpha;
   for (int j = 1; j < k; ++j) {
     const double beta = std::sqrt(dot(f.ptr, f.ptr));
-    CHEFSI_CUDA(cudaMemcpyAsync(v0.ptr, v.ptr, sizeof(double) * M, cudaMemcpyDeviceToDevice, st));
-    copy_block<double, double>(f.ptr, 1, v.ptr, 1, M, 1, 1.0 / beta, st);
-    hx_f64(op, v.ptr, 1, f.ptr, 1, 1, 1.0, false, st);
-    axpby_block<double>(v0.ptr, 1, f.ptr, 1, M, 1, -beta, 1.0, st);
+    CHEFSI_CUDA(cudaMemcpyAsync(v0.ptr, v.ptr, sizeof(double) * L, cudaMemcpyDeviceToDevice, st));
+    copy_block<double, double>(f.ptr, 1, v.ptr, 1, L, 1, 1.0 / beta, st);
+    apply(v.ptr, f.ptr);
+    axpby_block<double>(v0.ptr, 1, f.ptr, 1, L, 1, -beta, 1.0, st);
     alpha = dot(f.ptr, v.ptr);
-    axpby_block<double>(v.ptr, 1, f.ptr, 1, M, 1, -alpha, 1.0, st);
+    axpby_block<double>(v.ptr, 1, f.ptr, 1, L, 1, -alpha, 1.0, st);
     T[(size_t)j * k + j - 1] = beta;
     T[(size_t)(j - 1) * k + j] = beta;
     T[(size_t)j * k + j] = alpha;
@@ -560,10 +760,28 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
                        void* stream) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op && X && N >= 1 && ld >= N, "bad argument");
-  CHEFSI_REQUIRE(!op->is_complex, "Cholesky-GS: complex operators not supported");
   cudaStream_t st = as_stream(stream);
   chefsi_solver_s s;
   s.p = default_params();
+  if (op->is_complex) {
+    cplx* S = reinterpret_cast<cplx*>(s.S.ensure((size_t)N * N * 2));
+    cplx* W = reinterpret_cast<cplx*>(s.W.ensure((size_t)N * N * 2));
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(cplx) * N * N, st));
+    gram_c64((const cplx*)X, ld, (const cplx*)X, ld, op->n_dofs, N, N, S, N, true, st);
+    symmetrize_lower_c(S, N, st);
+    int rc = cholesky_lower_c(S, N, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+      return rc;
+    }
+    trtri_lower_c(S, N, st);
+    // X <- X L^{-H}
+    k_conj_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);
+    CHEFSI_CHECK_LAUNCH();
+    rotate_rows_c(&s, (cplx*)X, ld, op->n_dofs, N, W, st);
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+    return CHEFSI_OK;
+  }
   double* S = s.S.ensure((size_t)N * N);
   double* W = s.W.ensure((size_t)N * N);
   CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
@@ -591,17 +809,19 @@ int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, dou
                          double* HX_out, double* W_out, int32_t precision, void* stream) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op && X && eig_host && N >= 1 && ld >= N, "bad argument");
-  CHEFSI_REQUIRE(!op->is_complex, "Rayleigh-Ritz: complex operators not supported");
   cudaStream_t st = as_stream(stream);
   chefsi_solver_s s;
   s.p = default_params();
-  int rc = rayleigh_ritz_real(&s, op, (double*)X, ld, N, precision, HX_out != nullptr, st);
+  const int cw = op->is_complex ? 2 : 1;
+  int rc = op->is_complex
+               ? rayleigh_ritz_complex(&s, op, (cplx*)X, ld, N, precision, HX_out != nullptr, st)
+               : rayleigh_ritz_real(&s, op, (double*)X, ld, N, precision, HX_out != nullptr, st);
   if (rc != CHEFSI_OK) return rc;
   if (HX_out)
-    CHEFSI_CUDA(cudaMemcpyAsync(HX_out, s.HX.ptr, sizeof(double) * op->n_dofs * N,
+    CHEFSI_CUDA(cudaMemcpyAsync(HX_out, s.HX.ptr, sizeof(double) * op->n_dofs * N * cw,
                                 cudaMemcpyDeviceToDevice, st));
   if (W_out)
-    CHEFSI_CUDA(cudaMemcpyAsync(W_out, s.W.ptr, sizeof(double) * (size_t)N * N,
+    CHEFSI_CUDA(cudaMemcpyAsync(W_out, s.W.ptr, sizeof(double) * (size_t)N * N * cw,
                                 cudaMemcpyDeviceToDevice, st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
@@ -755,18 +975,24 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(s && op && X && eig_host && N >= 1, "bad argument");
   CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
-  CHEFSI_REQUIRE(!op->is_complex, "chefsi_solve: complex operators not supported");
   cudaStream_t st = as_stream(stream);
   const int prec = s->p.precision;
   const int m = degree_for(s, is_first_scf);
   s->last_degree = m;
   CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
   filter_all(s, op, X, N, m, prec, st);
-  int rc = rayleigh_ritz_real(s, op, (double*)X, N, N, prec, true, st);
-  if (rc != CHEFSI_OK) return rc;
   const int64_t M = op->n_dofs;
   double* res = s->resid.ensure(N);
-  if (compute_residual) residual_norms_f64((double*)X, N, s->HX.ptr, N, M, N, s->evals.ptr, res, st);
+  if (op->is_complex) {
+    int rc = rayleigh_ritz_complex(s, op, (cplx*)X, N, N, prec, true, st);
+    if (rc != CHEFSI_OK) return rc;
+    if (compute_residual)
+      residual_norms_c64((const cplx*)X, N, (const cplx*)s->HX.ptr, N, M, N, s->evals.ptr, res, st);
+  } else {
+    int rc = rayleigh_ritz_real(s, op, (double*)X, N, N, prec, true, st);
+    if (rc != CHEFSI_OK) return rc;
+    if (compute_residual) residual_norms_f64((double*)X, N, s->HX.ptr, N, M, N, s->evals.ptr, res, st);
+  }
   CHEFSI_CUDA(cudaEventRecord(s->ev[6], st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s->evals.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   if (compute_residual && res_host)
@@ -780,6 +1006,74 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
   s->times[5] = elapsed(s->ev[5], s->ev[6]);
   s->times[6] = elapsed(s->ev[0], s->ev[6]);
   s->hx_collect();
+  CHEFSI_API_END
+}
+
+int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator* ops, void** X,
+                         const int32_t* N, double** eig_host, double** res_host,
+                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(count >= 0 && (count == 0 || (solvers && ops && X && N && eig_host)),
+                 "bad argument");
+  if (count == 0) return CHEFSI_OK;
+  for (int i = 0; i < count; ++i)
+    CHEFSI_REQUIRE(solvers[i] && ops[i] && X[i] && eig_host[i] && N[i] >= 1,
+                   "bad argument in batch entry " + std::to_string(i));
+  for (int i = 0; i < count; ++i)
+    for (int j = 0; j < i; ++j)
+      CHEFSI_REQUIRE(solvers[i] != solvers[j], "batch entries must use distinct solvers");
+  // largest first: work ~ n_dofs * N * (degree + 2) (filter) + n_dofs * N^2 (dense steps)
+  std::vector<double> cost(count);
+  for (int i = 0; i < count; ++i) {
+    const double M = (double)ops[i]->n_dofs * (ops[i]->is_complex ? 4.0 : 1.0);
+    const double deg = degree_for(solvers[i], is_first_scf) + 2.0;
+    cost[i] = M * N[i] * (deg * ops[i]->n_e + N[i]);
+  }
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  int workers = n_streams > 0 ? n_streams : std::min(count, 8);
+  workers = std::max(1, std::min(workers, count));
+  int dev = 0;
+  CHEFSI_CUDA(cudaGetDevice(&dev));
+  std::atomic<int> next{0};
+  std::mutex mu;
+  int first_rc = CHEFSI_OK;
+  std::string first_msg;
+  auto work = [&]() {
+    cudaStream_t st = nullptr;
+    if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      std::lock_guard<std::mutex> g(mu);
+      if (first_rc == CHEFSI_OK) first_rc = CHEFSI_ERR_CUDA, first_msg = "batched solve: stream creation failed";
+      return;
+    }
+    for (;;) {
+      const int k = next.fetch_add(1);
+      if (k >= count) break;
+      {
+        std::lock_guard<std::mutex> g(mu);
+        if (first_rc != CHEFSI_OK) break;
+      }
+      const int i = order[k];
+      const int rc = chefsi_solve(solvers[i], ops[i], X[i], N[i], eig_host[i],
+                                  res_host ? res_host[i] : nullptr, compute_residual,
+                                  is_first_scf, st);
+      if (rc != CHEFSI_OK) {
+        std::lock_guard<std::mutex> g(mu);
+        if (first_rc == CHEFSI_OK)
+          first_rc = rc, first_msg = "batch entry " + std::to_string(i) + ": " + chefsi_last_error();
+      }
+    }
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  };
+  std::vector<std::thread> pool;
+  for (int w = 0; w < workers; ++w) pool.emplace_back(work);
+  for (auto& t : pool) t.join();
+  if (first_rc != CHEFSI_OK) {
+    set_last_error(first_msg);
+    return first_rc;
+  }
   CHEFSI_API_END
 }
 

@@ -56,57 +56,67 @@ __global__ void k_col_absmax(const T* __restrict__ X, int64_t ld, int64_t M, int
   atomicMax(&out[j], (unsigned long long)__double_as_longlong(m));
 }
 
+// e[j]: m 2^e in [2^14, 2^15) for the column maximum m (clamped to keep 2^e a normal double);
+// sc[j] = 2^e[j]
 __global__ void k_col_exponent(const unsigned long long* __restrict__ bits, int N,
-                               int* __restrict__ e) {
+                               int* __restrict__ e, double* __restrict__ sc) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= N) return;
   const double m = __longlong_as_double((long long)bits[j]);
-  int ex = 0;
+  int ex = 0, ej = 0;
   if (m > 0.0 && isfinite(m)) {
     frexp(m, &ex);  // m = f 2^ex, f in [0.5, 1)
-    e[j] = 15 - ex; // m 2^e in [2^14, 2^15)
-  } else {
-    e[j] = 0;
+    ej = min(max(15 - ex, -1000), 1000);
   }
+  e[j] = ej;
+  sc[j] = ldexp(1.0, ej);
 }
 
 __device__ __forceinline__ void split_half(double v, __half& h, __half& l) {
   h = __double2half(v);
   l = __double2half(v - (double)__half2float(h));
 }
+// the same split from an FP32 value (the FP32 rounding keeps 24 bits, the split 22): one
+// FP64 multiply and one FP64 -> FP32 conversion per element, the rest on the FP32 pipe
+__device__ __forceinline__ float scaled_f32(double x, double sc) { return (float)(x * sc); }
+__device__ __forceinline__ float scaled_f32(float x, double sc) { return (float)((double)x * sc); }
+__device__ __forceinline__ void split_half_f32(float v, __half& h, __half& l) {
+  h = __float2half_rn(v);
+  l = __float2half_rn(v - __half2float(h));
+}
 
-// [M][N] (ld) -> hi/lo [Np][Kp] (dof index fastest), column j scaled by 2^e[j]; zero padding
+// [M][N] (ld) -> hi/lo [Np][Kp] (dof index fastest), column j scaled by sc[j]; zero padding
 template <typename T>
 __global__ void __launch_bounds__(256)
-    k_split_t(const T* __restrict__ X, int64_t ld, int64_t M, int N, const int* __restrict__ e,
+    k_split_t(const T* __restrict__ X, int64_t ld, int64_t M, int N, const double* __restrict__ sc,
               int64_t Kp, __half* __restrict__ hi, __half* __restrict__ lo) {
-  __shared__ double tile[64][65];  // [column][dof]
+  __shared__ float tile[64][65];  // [column][dof]
   const int64_t k0 = (int64_t)blockIdx.x * 64;
   const int j0 = blockIdx.y * 64;
   for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
     const int r = idx >> 6, c = idx & 63;
     const int64_t k = k0 + r;
     const int j = j0 + c;
-    double v = 0.0;
-    if (k < M && j < N) v = ldexp((double)X[k * ld + j], e[j]);
+    float v = 0.f;
+    if (k < M && j < N) v = scaled_f32(X[k * ld + j], sc[j]);
     tile[c][r] = v;
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < 64 * 32; idx += 256) {
     const int c = idx >> 5, p = idx & 31;
     __half h0, l0, h1, l1;
-    split_half(tile[c][2 * p], h0, l0);
-    split_half(tile[c][2 * p + 1], h1, l1);
+    split_half_f32(tile[c][2 * p], h0, l0);
+    split_half_f32(tile[c][2 * p + 1], h1, l1);
     const int64_t o = (int64_t)(j0 + c) * Kp + k0 + 2 * p;
     *reinterpret_cast<__half2*>(hi + o) = __halves2half2(h0, h1);
     *reinterpret_cast<__half2*>(lo + o) = __halves2half2(l0, l1);
   }
 }
 
-// [M][N] (ld) -> hi/lo [M][Kr] (row-major, columns zero-padded to Kr), column j scaled by 2^e[j]
+// [M][N] (ld) -> hi/lo [M][Kr] (row-major, columns zero-padded to Kr), column j scaled by sc[j]
 template <typename T>
 __global__ void k_split_r(const T* __restrict__ X, int64_t ld, int64_t M, int N,
-                          const int* __restrict__ e, int Kr, __half* __restrict__ hi,
+                          const double* __restrict__ sc, int Kr, __half* __restrict__ hi,
                           __half* __restrict__ lo) {
   const int64_t pairs = (int64_t)(Kr / 2);
   const int64_t total = M * pairs;
@@ -114,11 +124,11 @@ __global__ void k_split_r(const T* __restrict__ X, int64_t ld, int64_t M, int N,
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / pairs;
     const int j = (int)(t % pairs) * 2;
-    const double v0 = j < N ? ldexp((double)X[r * ld + j], e[j]) : 0.0;
-    const double v1 = j + 1 < N ? ldexp((double)X[r * ld + j + 1], e[j + 1]) : 0.0;
+    const float v0 = j < N ? scaled_f32(X[r * ld + j], sc[j]) : 0.f;
+    const float v1 = j + 1 < N ? scaled_f32(X[r * ld + j + 1], sc[j + 1]) : 0.f;
     __half h0, l0, h1, l1;
-    split_half(v0, h0, l0);
-    split_half(v1, h1, l1);
+    split_half_f32(v0, h0, l0);
+    split_half_f32(v1, h1, l1);
     *reinterpret_cast<__half2*>(hi + r * Kr + j) = __halves2half2(h0, h1);
     *reinterpret_cast<__half2*>(lo + r * Kr + j) = __halves2half2(l0, l1);
   }
@@ -580,12 +590,13 @@ template <typename T>
 void tc_exponents(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cudaStream_t st) {
   op.bits.ensure(N);
   op.e.ensure(N);
+  op.sc.ensure(N);
   CHEFSI_CUDA(cudaMemsetAsync(op.bits.ptr, 0, sizeof(unsigned long long) * N, st));
   const int64_t ysplit = std::max<int64_t>(1, std::min<int64_t>(M, 2048));
   dim3 grid((N + 255) / 256, (unsigned)ysplit);
   k_col_absmax<T><<<grid, 256, 0, st>>>(X, ld, M, N, op.bits.ptr);
   CHEFSI_CHECK_LAUNCH();
-  k_col_exponent<<<(N + 255) / 256, 256, 0, st>>>(op.bits.ptr, N, op.e.ptr);
+  k_col_exponent<<<(N + 255) / 256, 256, 0, st>>>(op.bits.ptr, N, op.e.ptr, op.sc.ptr);
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -601,7 +612,7 @@ void tc_split_transposed(const T* X, int64_t ld, int64_t M, int N, TcOperand& op
   op.lo.ensure(n);
   CHEFSI_REQUIRE(op.ld / 64 < (1ll << 31), "tensor-core split: too many rows");
   dim3 grid((unsigned)(op.ld / 64), (unsigned)(op.padded / 64));
-  k_split_t<T><<<grid, 256, 0, st>>>(X, ld, M, N, op.e.ptr, op.ld, op.hi.ptr, op.lo.ptr);
+  k_split_t<T><<<grid, 256, 0, st>>>(X, ld, M, N, op.sc.ptr, op.ld, op.hi.ptr, op.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -615,7 +626,7 @@ void tc_split_rows(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cuda
   const size_t n = (size_t)M * op.ld;
   op.hi.ensure(n);
   op.lo.ensure(n);
-  k_split_r<T><<<grid_for(M * (op.ld / 2), 256), 256, 0, st>>>(X, ld, M, N, op.e.ptr, (int)op.ld,
+  k_split_r<T><<<grid_for(M * (op.ld / 2), 256), 256, 0, st>>>(X, ld, M, N, op.sc.ptr, (int)op.ld,
                                                                 op.hi.ptr, op.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
 }

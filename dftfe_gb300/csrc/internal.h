@@ -3,6 +3,7 @@
 
 #include "common.cuh"
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -11,6 +12,13 @@ namespace chefsi {
 struct cplx {
   double x, y;
 };
+__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cplx csub(cplx a, cplx b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+__device__ __forceinline__ cplx cconj(cplx a) { return {a.x, -a.y}; }
+__device__ __forceinline__ cplx cscale(cplx a, double s) { return {a.x * s, a.y * s}; }
 
 // Tensor-core copy of the cell matrices: FP16 hi/lo split of 2^s * A_e (s a power-of-two
 // exponent putting max |A_e| in [2^14, 2^15)), rows and columns zero-padded to npad (a
@@ -56,6 +64,10 @@ struct chefsi_operator_s {
 
   chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
   chefsi::DeviceBuffer<unsigned long long> tc_sched;  // its work counter
+
+  // real form of a complex operator (2 n_dofs real unknowns, 2 n_e x 2 n_e real cell
+  // matrices) for the FP32 / tensor-core filter; built on first use
+  std::unique_ptr<chefsi_operator_s> rv;
 
   // workspaces (grow-only)
   chefsi::DeviceBuffer<double> ws64a, ws64b, nlW64;
@@ -107,8 +119,9 @@ void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* 
 // products; row layout [rows][ld = padded columns] feeds the rotation.
 struct TcOperand {
   DeviceBuffer<__half> hi, lo;
-  DeviceBuffer<int> e;
-  DeviceBuffer<unsigned long long> bits;
+  DeviceBuffer<int> e;                     // column exponents
+  DeviceBuffer<double> sc;                 // 2^e per column
+  DeviceBuffer<unsigned long long> bits;   // column maxima (bit patterns)
   int64_t rows = 0;  // logical rows (dofs)
   int cols = 0;      // logical columns (vectors)
   int64_t ld = 0;    // leading dimension of the FP16 layout
@@ -164,6 +177,10 @@ void trtri_lower(double* L, int N, cudaStream_t st);
 // symmetric eigensolve (Householder tridiagonalisation, bisection, inverse iteration,
 // back-transformation); A overwritten; eigenvalues ascending in w; vectors in columns of Z.
 int syevd(double* A, int N, double* w, double* Z, cudaStream_t st);
+// complex Hermitian counterparts (dense_c.cu)
+int cholesky_lower_c(cplx* A, int N, cudaStream_t st);
+void trtri_lower_c(cplx* L, int N, cudaStream_t st);
+int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st);
 // residual norms of columns: out[j] = || HX[:,j] - lam[j] X[:,j] ||
 void residual_norms_f64(const double* X, int64_t ldx, const double* HX, int64_t ldh, int64_t M,
                         int N, const double* lam_dev, double* out_dev, cudaStream_t st);
@@ -181,6 +198,13 @@ void quad_contract(int n_cells, int n_e, int n_q, const double* N, const double*
                    const double* jxw, double* out, cudaStream_t st);
 // replace the operator's cell matrices (device, unscaled) and refresh the derived copies
 void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStream_t st);
+// the real form of a folded complex operator (cached in op->rv)
+chefsi_operator_s* realified(chefsi_operator_s* op, cudaStream_t st);
+// complex [M][B] block (ld) <-> FP32 real rows [2M][B] (row 2g = Re, 2g+1 = Im), scaled by s
+void complex_to_real_rows(const cplx* X, int64_t ld, int64_t M, int B, double s, float* out,
+                          cudaStream_t st);
+void real_rows_to_complex(const float* in, int64_t M, int B, double s, cplx* X, int64_t ld,
+                          cudaStream_t st);
 
 // eigensolver kernels (dense.cu), launched by the eigensolver drivers
 __global__ void k_hh_vector(double* A, int N, int k, double* V, double* tau, double* d, double* e);
@@ -189,7 +213,7 @@ __global__ void k_hh_symv(const double* A, int N, int k, const double* V, const 
 __global__ void k_hh_w(int N, int k, const double* V, const double* tau, double* p);
 __global__ void k_hh_rank2(double* A, int N, int k, const double* V, const double* w);
 __global__ void k_tail(const double* A, int N, double* d, double* e);
-__global__ void k_bisect(const double* d, const double* e, int n, double* w);
+__global__ void k_bisect_warp(const double* d, const double* e, int n, double* w);
 __global__ void k_inverse_iteration(const double* d, const double* e, int n, const double* w,
                                     double* Z, int ldz, double* work, unsigned char* swaps,
                                     double ortol);

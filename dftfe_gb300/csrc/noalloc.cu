@@ -100,7 +100,7 @@ int syevd_noalloc(double* A, int N, double* w, double* Z, cudaStream_t st) {
   }
   k_tail<<<1, 32, 0, st>>>(A, N, d, e);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect<<<(N + 127) / 128, 128, 0, st>>>(d, e, N, w);
+  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d, e, N, w);
   CHEFSI_CHECK_LAUNCH();
   k_cluster_tol<<<1, 32, 0, st>>>(d, e, N, tol);
   CHEFSI_CHECK_LAUNCH();

@@ -695,6 +695,87 @@ void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStr
   op->tc.ready = false;  // the FP16 split is rebuilt on the next tensor-core apply
 }
 
+// real form of the complex cell matrices: row (I, p), column (J, q), p/q = 0 real part,
+// 1 imaginary part: [[Re A, -Im A], [Im A, Re A]] interleaved node by node
+__global__ void k_realify_cells(const cplx* __restrict__ mats, int64_t nc, int ne,
+                                double* __restrict__ out) {
+  const int ne2 = 2 * ne;
+  const int64_t n = nc * ne2 * ne2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / ((int64_t)ne2 * ne2);
+    const int r = (int)(t % ((int64_t)ne2 * ne2));
+    const int R = r / ne2, Q = r % ne2;
+    const int p = R & 1, q = Q & 1;
+    const cplx a = mats[(c * ne + (R >> 1)) * ne + (Q >> 1)];
+    out[t] = (p == q) ? a.x : (p == 0 ? -a.y : a.y);
+  }
+}
+__global__ void k_realify_map(const int* __restrict__ map, int64_t n, int* __restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = 2 * map[t >> 1] + (int)(t & 1);
+}
+
+chefsi_operator_s* realified(chefsi_operator_s* op, cudaStream_t st) {
+  if (op->rv) return op->rv.get();
+  CHEFSI_REQUIRE(op->is_complex && op->folded,
+                 "real form: folded complex operators only (no constraint rows)");
+  auto rv = std::make_unique<chefsi_operator_s>();
+  rv->n_dofs = 2 * op->n_dofs;
+  rv->n_cells = op->n_cells;
+  rv->n_e = 2 * op->n_e;
+  rv->is_complex = 0;
+  rv->folded = true;
+  const int64_t nc = op->n_cells;
+  const size_t nm = (size_t)nc * rv->n_e * rv->n_e;
+  rv->map.reset((size_t)nc * rv->n_e);
+  k_realify_map<<<grid_for(nc * op->n_e * 2, 256), 256, 0, st>>>(op->map.ptr, nc * op->n_e,
+                                                                  rv->map.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  rv->mats64.reset(nm);
+  k_realify_cells<<<grid_for((int64_t)nm, 256), 256, 0, st>>>(
+      reinterpret_cast<const cplx*>(op->mats64.ptr), nc, op->n_e, rv->mats64.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  rv->mats32.reset(nm);
+  k_to_f32<<<grid_for((int64_t)nm, 256), 256, 0, st>>>(rv->mats64.ptr, rv->mats32.ptr, nm);
+  CHEFSI_CHECK_LAUNCH();
+  op->rv = std::move(rv);
+  return op->rv.get();
+}
+
+__global__ void k_complex_to_rows(const cplx* __restrict__ X, int64_t ld, int64_t M, int B,
+                                  double s, float* __restrict__ out) {
+  const int64_t n = 2 * M * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t / B;
+    const int j = (int)(t % B);
+    const cplx v = X[(row >> 1) * ld + j];
+    out[t] = (float)(s * ((row & 1) ? v.y : v.x));
+  }
+}
+__global__ void k_rows_to_complex(const float* __restrict__ in, int64_t M, int B, double s,
+                                  cplx* __restrict__ X, int64_t ld) {
+  const int64_t n = M * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t g = t / B;
+    const int j = (int)(t % B);
+    X[g * ld + j] = {s * (double)in[(2 * g) * B + j], s * (double)in[(2 * g + 1) * B + j]};
+  }
+}
+void complex_to_real_rows(const cplx* X, int64_t ld, int64_t M, int B, double s, float* out,
+                          cudaStream_t st) {
+  k_complex_to_rows<<<grid_for(2 * M * B, 256), 256, 0, st>>>(X, ld, M, B, s, out);
+  CHEFSI_CHECK_LAUNCH();
+}
+void real_rows_to_complex(const float* in, int64_t M, int B, double s, cplx* X, int64_t ld,
+                          cudaStream_t st) {
+  k_rows_to_complex<<<grid_for(M * B, 256), 256, 0, st>>>(in, M, B, s, X, ld);
+  CHEFSI_CHECK_LAUNCH();
+}
+
 template <typename T>
 static void upload(DeviceBuffer<T>& buf, const T* host, size_t n) {
   buf.reset(n);

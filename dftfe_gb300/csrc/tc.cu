@@ -109,18 +109,23 @@ __device__ __forceinline__ bool producers_sync_or(bool v) {
 struct Unit {
   int cell, chunk, half;
 };
-__device__ __forceinline__ Unit unit_of(int64_t u, const TcArgs& a) {
+// The CTA's it-th unit: (cell, chunk) pairs are dealt round-robin over the CTAs and a CTA
+// runs both row halves of its pair back to back, so the second gather of the chunk's X rows
+// comes from L2.
+__device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
+                                        const TcArgs& a) {
   Unit w;
-  w.half = (int)(u % a.n_halves);
-  const int64_t cc = u / a.n_halves;
+  w.half = (int)(it % a.n_halves);
+  const int64_t cc = first + (it / a.n_halves) * step;
   w.chunk = (int)(cc % a.n_chunks);
   w.cell = (int)(cc / a.n_chunks);
   return w;
 }
 
 // Persistent warp-specialised kernel, one CTA per SM. Work unit = (cell, 128-vector chunk,
-// row half); units are dealt round-robin so the CTAs of the GPU sweep the cells in order and
-// a cell's matrix halves and X rows are re-read from L2, not HBM.
+// row half); (cell, chunk) pairs are dealt round-robin so the CTAs of the GPU sweep the cells
+// in order (a cell's matrix halves are re-read from L2, not HBM), and each CTA runs the two
+// halves of its pair back to back (the second gather of the pair's X rows hits L2).
 //   warp 0        TMA of the cell-matrix K-blocks (hi, lo) into the stage ring
 //   warp 1        tcgen05.mma issue (one lane), two tensor-memory accumulators
 //   warps 2..5    X gather (one thread per vector, next K-block prefetched in registers),
@@ -150,7 +155,9 @@ __global__ void __launch_bounds__(kThreads2, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t first = blockIdx.x;
   const int64_t step = gridDim.x;
-  const int64_t my_units = first < args.n_units ? (args.n_units - first + step - 1) / step : 0;
+  const int64_t n_pairs = args.n_units / args.n_halves;   // (cell, chunk) pairs
+  const int64_t my_units =
+      first < n_pairs ? ((n_pairs - first + step - 1) / step) * args.n_halves : 0;
   const int nkb = args.nkb;
   const int64_t my_blocks = my_units * nkb;
 
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
       const uint32_t bytes = 2u * args.n_half * kRowBytes;
       int64_t issued = 0;
       for (int64_t g = 0; g < my_blocks; ++g) {
-        const Unit w = unit_of(first + (g / nkb) * step, args);
+        const Unit w = unit_at(g / nkb, first, step, args);
         const int kb = (int)(g % nkb);
         const int s = (int)(g % S);
         const uint32_t r = (uint32_t)(g / S);
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
     int mnext[8];
     auto load_map = [&](int64_t g, int* mv) {
       if (g < my_blocks) {
-        const Unit w = unit_of(first + (g / nkb) * step, args);
+        const Unit w = unit_at(g / nkb, first, step, args);
         const int kb = (int)(g % nkb);
         const int* mrow = args.map + (int64_t)w.cell * args.n_e;
 #pragma unroll
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
       for (int i = 0; i < 8; ++i) mv[i] = mnext[i];
       load_map(g + 1, mnext);
       if (g < my_blocks) {
-        const Unit w = unit_of(first + (g / nkb) * step, args);
+        const Unit w = unit_at(g / nkb, first, step, args);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           const int q = i * 128 + t;             // 16-byte chunk of the [32][128] slot
@@ -341,7 +348,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
       const bool ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
       if (!ok) break;
       fence_after();
-      const Unit w = unit_of(first + it * step, args);
+      const Unit w = unit_at(it, first, step, args);
       const int gb = w.chunk * kVec + v;
       const bool vok = gb < args.B;
       const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
@@ -532,16 +539,12 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const float* src, int64_
   a.stages = p.stages;
   a.n_units = (int64_t)op->n_cells * a.n_chunks * p.n_halves;
   a.err = op->tc_err.ptr;
-  static bool attr_set = false;
-  if (!attr_set) {
-    CHEFSI_CUDA(cudaFuncSetAttribute(cell_hx_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     227 * 1024));
-    attr_set = true;
-  }
+  CHEFSI_CUDA(cudaFuncSetAttribute(cell_hx_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   227 * 1024));
   int dev = 0, sms = kNumSMs;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t grid = std::min<int64_t>(sms, a.n_units);
+  const int64_t grid = std::min<int64_t>(sms, a.n_units / p.n_halves);
   cell_hx_tc_kernel<<<(unsigned)grid, kThreads2, p.smem, st>>>(mhi, mlo, a);
   CHEFSI_CHECK_LAUNCH();
 }

@@ -166,6 +166,12 @@ int chefsi_lanczos_bounds(chefsi_operator op, int32_t k, int32_t reproducible,
    A is overwritten. */
 int chefsi_syevd(int32_t N, double* A, double* w, double* Z, void* stream);
 
+/* Hermitian eigensolve of an N x N row-major interleaved-complex device matrix A (ELPA /
+   zheevd in rayleighRitzGEP, src/linAlg/rayleighRitzDevice.cc:720-749): eigenvalues
+   ascending into w (device, N doubles), eigenvectors into the columns of Z (device, N x N
+   interleaved complex). A is overwritten. */
+int chefsi_heevd(int32_t N, double* A, double* w, double* Z, void* stream);
+
 /* Allocation-free variant of chefsi_syevd (no counterpart in the reference).
    For callers that cannot allocate device memory during a solve -- an application whose
    pool allocator owns the GPU's memory, or one that cannot take the device-wide
@@ -246,6 +252,17 @@ int chefsi_solver_hx_stats(chefsi_solver s, int32_t* launches, double* total_ms)
 int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
                  double* res_host, int32_t compute_residual, int32_t is_first_scf,
                  void* stream);
+
+/* One CheFSI iteration on each of count independent problems (the k-point / spin loop of
+   dftClass::kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:507-655, which calls
+   solve() once per (k, spin)): problem i is (solvers[i], ops[i], X[i], N[i]) with its
+   eigenvalues (and residual norms) written to eig_host[i] (res_host[i]); res_host may be
+   null. Every entry needs its own solver (bounds and workspaces). The problems run
+   concurrently on n_streams CUDA streams (n_streams <= 0: min(count, 8)), each driven by a
+   host worker thread, largest problems first. Returns the first failing entry's status. */
+int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator* ops, void** X,
+                         const int32_t* N, double** eig_host, double** res_host,
+                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams);
 
 /* Filter only (no Rayleigh-Ritz), solveNoRR. */
 int chefsi_solve_no_rr(chefsi_solver s, chefsi_operator op, void* X, int32_t N,
