@@ -87,7 +87,7 @@ class ClockSampler:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one cell_hx_tc_kernel launch (ncu capture of
 # `bench.py --workload mixed --hx-only`, summarised in profiles/cell_hx_tc_mixed_traffic.md)
-TC_TRAFFIC_BYTES = {"mixed": 37.27e9 + 10.09e9}
+TC_TRAFFIC_BYTES = {"mixed": 20.99e9 + 8.29e9}
 
 
 def hx_algorithmic(pr, B, s_h=4, s_x=4):
@@ -451,13 +451,18 @@ def run_bloch(args):
     prs = problems.bloch_set(args.batch, seed=args.seed)
     ops = [chefsi.KohnShamOperator.from_problem(p) for p in prs]
     X0 = [torch.from_numpy(p.initial_vectors()).to(dev) for p in prs]
-    bounds = [chefsi.initial_bounds(op, p.n_wfc) for op, p in zip(ops, prs)]
+    # first-call bounds of the reference; its bLow = a0 + (b - a0) N/M 200 passes b when
+    # N/M > 1/200 (the small meshes with 512 wavefunctions), so it is capped at the midpoint
+    bounds = []
+    for op, p in zip(ops, prs):
+        lo, blow, up = chefsi.initial_bounds(op, p.n_wfc)
+        bounds.append((lo, min(blow, lo + 0.5 * (up - lo)), up))
 
     def fresh():
         solvers = []
         for b in bounds:
             sv = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(
-                chefsi.SolverParams(rr_precision="fp64"))
+                chefsi.SolverParams(rr_precision=args.rr_precision))
             sv.reinitSpectrumBounds(*b)
             solvers.append(sv)
         return solvers, [x.clone() for x in X0]

@@ -35,6 +35,7 @@ struct chefsi_solver_s {
   DeviceBuffer<double> G2, W2;  // 2N x 2N real views for the complex tensor-core products
   DeviceBuffer<float> Xb32, Yb32;
   TcOperand tx, th;      // FP16 splits of X and HX for the tensor-core RR products
+  DeviceBuffer<__half> xs_hi, xs_lo;  // FP16 split of the filter's HX input
   TcDenseWork tcw;
   double times[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
@@ -137,6 +138,41 @@ void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double
   if (y != X) copy_block<T, T>(y, B, X, B, M, B, 1.0, st);
 }
 
+// Mixed Chebyshev filter on the tensor cores (same recurrence as cheb_filter). The HX input
+// is also kept as FP16 hi + lo rows: the step y_{k-1} <- -c alpha1 y_k + alpha2 y_{k-1}
+// reads y_k, the next HX's input, and writes its split in the same pass; the first input is
+// split once.
+void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
+                    int B, int m, double a, double b, double a0, cudaStream_t st) {
+  __half* hi = s->xs_hi.ensure((size_t)M * B);
+  __half* lo = s->xs_lo.ensure((size_t)M * B);
+  const double e = (b - a) / 2.0, c = (b + a) / 2.0;
+  double sigma = e / (a0 - c);
+  const double sigma1 = sigma, gamma = 2.0 / sigma1;
+  double alpha1 = sigma1 / e, alpha2 = -c;
+  auto hx = [&](const float* src, float* dst, double sc) {
+    s->hx_mark(st);
+    if (!hx_tc_split(op, hi, lo, src, B, dst, B, B, sc, true, st))
+      throw Error(CHEFSI_ERR_INVALID, "tensor-core filter HX not applicable to this block");
+    s->hx_mark(st);
+  };
+  split_rows_f32(X, B, M, B, hi, lo, st);
+  copy_block<float, float>(X, B, Y, B, M, B, alpha1 * alpha2, st);
+  hx(X, Y, alpha1);
+  float* x = X;
+  float* y = Y;
+  for (int degree = 2; degree < m + 1; ++degree) {
+    const double sigma2 = 1.0 / (gamma - sigma);
+    alpha1 = 2.0 * sigma2 / e;
+    alpha2 = -(sigma * sigma2);
+    axpby_split_f32(y, x, M, B, -c * alpha1, alpha2, hi, lo, st);
+    hx(y, x, alpha1);
+    std::swap(x, y);
+    sigma = sigma2;
+  }
+  if (y != X) copy_block<float, float>(y, B, X, B, M, B, 1.0, st);
+}
+
 // filter columns [j0, j0+B) of X (ld) in place
 void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int j0,
                     int B, int m, double a, double b, double a0, int prec, cudaStream_t st) {
@@ -167,13 +203,17 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
   float* Xb = s->Xb32.ensure((size_t)M * B);
   float* Yb = s->Yb32.ensure((size_t)M * B);
   copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
-  cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
-                     [&](const float* src, float* dst, double scv, bool acc) {
-                       s->hx_mark(st);
-                       hx_filter32(op, prec, src, dst, B, scv, acc, st);
-                       s->hx_mark(st);
-                     },
-                     st);
+  if (prec == CHEFSI_PREC_MIXED && tc_split_usable(op, B)) {
+    cheb_filter_tc(s, op, Xb, Yb, M, B, m, a, b, a0, st);
+  } else {
+    cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
+                       [&](const float* src, float* dst, double scv, bool acc) {
+                         s->hx_mark(st);
+                         hx_filter32(op, prec, src, dst, B, scv, acc, st);
+                         s->hx_mark(st);
+                       },
+                       st);
+  }
   if (prec == CHEFSI_PREC_MIXED) {
     const int tc = tc_check_error(op, st);
     if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
@@ -203,13 +243,17 @@ void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m
       float* xr = s->Xb32.ensure((size_t)2 * M * B);
       float* yr = s->Yb32.ensure((size_t)2 * M * B);
       complex_to_real_rows(Xc + j0, N, M, B, scale, xr, st);
-      cheb_filter<float>(xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0,
-                         [&](const float* src, float* dst, double scv, bool acc) {
-                           s->hx_mark(st);
-                           hx_filter32(rv, prec, src, dst, B, scv, acc, st);
-                           s->hx_mark(st);
-                         },
-                         st);
+      if (prec == CHEFSI_PREC_MIXED && tc_split_usable(rv, B)) {
+        cheb_filter_tc(s, rv, xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0, st);
+      } else {
+        cheb_filter<float>(xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0,
+                           [&](const float* src, float* dst, double scv, bool acc) {
+                             s->hx_mark(st);
+                             hx_filter32(rv, prec, src, dst, B, scv, acc, st);
+                             s->hx_mark(st);
+                           },
+                           st);
+      }
       if (prec == CHEFSI_PREC_MIXED) {
         const int tc = tc_check_error(rv, st);
         if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
@@ -461,9 +505,17 @@ int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, in
   }
   trtri_lower_c(S, N, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
-  // HX in FP64 (complex)
+  // HX: FP64 complex, or (mixed with rr_precision FP32 on a folded operator) the FP32 apply
+  // of the real form on X rounded to FP32
   cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
-  {
+  if (is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32 && op->folded) {
+    chefsi_operator_s* rv = realified(op, st);
+    float* xr = s->Xb32.ensure((size_t)2 * M * N);
+    float* yr = s->Yb32.ensure((size_t)2 * M * N);
+    complex_to_real_rows(X, ld, M, N, 1.0, xr, st);
+    hx_f32(rv, xr, N, yr, N, N, 1.0, false, st);
+    real_rows_to_complex(yr, M, N, 1.0, HX, N, st);
+  } else {
     const int Bmax = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
     for (int j0 = 0; j0 < N; j0 += Bmax) {
       const int B = std::min(Bmax, N - j0);

@@ -63,7 +63,7 @@ struct chefsi_operator_s {
 
 
   chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
-  chefsi::DeviceBuffer<unsigned long long> tc_sched;  // its work counter
+  chefsi::DeviceBuffer<__half> xs_hi, xs_lo;  // FP16 split of the HX input (chefsi_hx path)
 
   // real form of a complex operator (2 n_dofs real unknowns, 2 n_e x 2 n_e real cell
   // matrices) for the FP32 / tensor-core filter; built on first use
@@ -88,6 +88,17 @@ void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int6
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st);
 bool tc_usable(chefsi_operator_s* op);
+// the tensor-core apply reads the input as FP16 hi + lo rows [n_dofs][B] (B % 8 == 0);
+// src (FP32) feeds the nonlocal term
+bool tc_split_usable(chefsi_operator_s* op, int B);
+bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, const float* src,
+                 int64_t lds, float* dst, int64_t ldd, int B, double scalar, bool accumulate,
+                 cudaStream_t st);
+void split_rows_f32(const float* x, int64_t ldx, int64_t M, int B, __half* hi, __half* lo,
+                    cudaStream_t st);
+// y = a x + b y on contiguous [M][B] blocks and (hi, lo) = split(x)
+void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, double b, __half* hi,
+                     __half* lo, cudaStream_t st);
 // W[a][j][b] = sum_r C[r][j] x[dof_r][b] for FP32 vectors (W zeroed here)
 void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
                     cudaStream_t st);

@@ -3,23 +3,21 @@
 //
 // DFT-FE's local HX (src/dftOperator/matrixVectorProductImplementationsDevice.cc:27-117)
 // gathers X into n_cells x n_e x B cell blocks, calls gemmStridedBatched and scatter-adds.
-// Here one CTA owns one (cell, 128-vector chunk):
-//   * warp 0 (one lane) streams K-blocks of the cell matrix (FP16 hi and lo parts, 64-byte
-//     rows, 64B-swizzled) into shared memory with TMA;
-//   * warps 2..5 gather the chunk's X rows (FP32) straight from the global block through the
-//     cell's dof map, split each value into FP16 hi + lo and write them K-major with the same
-//     swizzle (one thread per vector, so the global loads coalesce along the vectors);
-//   * warp 1 (one lane) issues tcgen05.mma kind::f16 with M = 128 vectors, N = the cell's
-//     rows (one or two MMAs of N <= 256), K = 16:
-//       D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T           (the lo*lo term is below 2^-22)
-//     and the accumulator D[vector][row] (FP32) stays in tensor memory;
-//   * warps 2..5 then read D with tcgen05.ld (lane = vector) and scatter-add
+// Here no cell block is materialised. The filter keeps its FP32 vectors also as FP16 hi + lo
+// rows (written by the recurrence step that reads them anyway), and one CTA owns one
+// (cell, 128-vector chunk, half of the cell's rows) at a time:
+//   * producer warps copy the chunk's X rows through the cell's dof map (cp.async, 16-byte
+//     pieces) into a 128B-swizzled, MN-major tile, and TMA loads the cell-matrix K-block
+//     (FP16 hi and lo of 2^s A_e, K-major, 64B-swizzled);
+//   * one lane issues tcgen05.mma kind::f16 with M = 128 vectors, N = the half's rows
+//     (<= 256), K = 16:  D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T  (lo*lo is below 2^-22);
+//   * the epilogue warps read D with tcgen05.ld (lane = vector) and scatter-add
 //     scalar * D / 2^s into the output rows with red.global.add.f32 -- for every cell row the
-//     32 lanes of a warp hit 32 consecutive floats, so each atomic instruction is one 128-byte
-//     line.
-// A 3..4-stage mbarrier pipeline overlaps TMA, the X split and the MMAs. Every mbarrier wait
-// is bounded: on expiry the CTA records CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded)
-// for its own TMA copies, frees its tensor memory and returns.
+//     32 lanes of a warp hit 32 consecutive floats, one 128-byte line per instruction.
+// An mbarrier pipeline of up to 8 stages overlaps the TMA, the MMAs and the scatter of the
+// previous unit. Every mbarrier wait is bounded: on expiry the CTA records
+// CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own TMA copies, frees its
+// tensor memory and returns.
 #include "internal.h"
 #include "tc_common.cuh"
 
@@ -36,17 +34,37 @@ using namespace tcx;
 
 namespace {
 
-constexpr int kVec = 128;          // vectors per CTA (MMA M)
-constexpr int kKB = 32;            // halves per K-block (64-byte rows)
-constexpr int kRowBytes = kKB * 2; // 64
+constexpr int kVec = 128;          // vectors per work unit (MMA M)
+constexpr int kKB = 32;            // cell nodes per K-block
+constexpr int kRowBytes = kKB * 2; // 64: one K-major row of the cell-matrix tile
+
+// shared-memory descriptor of an MN-major, 128-byte-swizzled operand: atoms of 64 elements
+// (128 B) along M x 8 rows along K (1 KB); lbo = byte step between atoms along M, sbo =
+// byte step between 8-row groups along K
+__device__ __forceinline__ uint64_t smem_desc_mn_sw128(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+  return d;
+}
+
+// X tile of one K-block: 2 atoms along the 128 vectors x 4 groups of 8 nodes
+constexpr uint32_t kXAtomM = 1024;   // byte step between the two 64-vector atoms
+constexpr uint32_t kXGroupK = 2048;  // byte step between 8-node groups
+constexpr int kXTile = 8192;         // 32 nodes x 128 vectors x 2 B
+
 struct TcArgs {
-  const float* src;
-  int64_t lds;
+  const __half* xhi;
+  const __half* xlo;
+  int64_t ldx;     // halves
   float* dst;
   int64_t ldd;
   const int* map;
   int n_e;
-  int nkb;         // K-blocks of 32 columns
+  int nkb;         // K-blocks of 32 nodes
   int B;
   int n_chunks;    // 128-vector chunks
   int n_half;      // cell rows per work unit (= MMA N)
@@ -54,56 +72,44 @@ struct TcArgs {
   int buf_stride;  // tensor-memory column offset of accumulator 1
   int tmem_cols;
   int stages;
+  int lookahead;   // K-blocks of X copies in flight per producer thread
   int64_t n_units; // n_cells * n_chunks * n_halves
   float out_scale; // scalar / 2^s
   int* err;
 };
 
-// shared memory carve-up (offsets from a 1024-byte aligned base)
-constexpr int kXStages = 4;                    // cp.async staging depth for the X gather
-constexpr int kXStageBytes = kKB * kVec * 4;    // [32 rows][128 vectors] FP32 = 16 KB
-
 struct Layout {
-  int x_tile;   // 128 rows x 64 B = 8 KB
   int a_tile;   // n_half rows x 64 B, rounded to 1 KB
   int stage;    // xhi, xlo, ahi, alo
-  int xstage;   // FP32 staging ring of the gathered rows
   int bars;     // barrier block
   int total;
 };
 __host__ __device__ inline Layout make_layout(int n_half, int stages) {
   Layout L;
-  L.x_tile = kVec * kRowBytes;
   L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
-  L.stage = 2 * L.x_tile + 2 * L.a_tile;
-  L.xstage = stages * L.stage;
-  L.bars = L.xstage + kXStages * kXStageBytes;
+  L.stage = 2 * kXTile + 2 * L.a_tile;
+  L.bars = stages * L.stage;
   L.total = L.bars + 8 * (3 * stages + 8);
   return L;
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
                "r"(valid ? 16 : 0)
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-// named barrier among the 128 X-producer threads (barrier 0 is __syncthreads)
-__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-// the same barrier with an OR-reduction, so the producers take stop decisions together
-__device__ __forceinline__ bool producers_sync_or(bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, 1, 128, pi;\n"
-      " selp.u32 %0, 1, 0, po;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)v)
-      : "memory");
-  return r != 0;
+__device__ __forceinline__ void cp_async_wait_n(int n) {
+  // wait until at most n of this thread's groups are pending (n is small and warp-uniform)
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+    case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
+    case 5: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 6;" ::: "memory"); break;
+  }
 }
 
 struct Unit {
@@ -123,18 +129,21 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 }
 
 // Persistent warp-specialised kernel, one CTA per SM. Work unit = (cell, 128-vector chunk,
-// row half); (cell, chunk) pairs are dealt round-robin so the CTAs of the GPU sweep the cells
-// in order (a cell's matrix halves are re-read from L2, not HBM), and each CTA runs the two
-// halves of its pair back to back (the second gather of the pair's X rows hits L2).
-//   warp 0        TMA of the cell-matrix K-blocks (hi, lo) into the stage ring
-//   warp 1        tcgen05.mma issue (one lane), two tensor-memory accumulators
-//   warps 2..5    X gather (one thread per vector, next K-block prefetched in registers),
-//                 FP16 hi/lo split, 64B-swizzled K-major stores
-//   warps 6..9    epilogue: tcgen05.ld of a finished accumulator, red.global.add.f32 scatter,
-//                 overlapped with the MMAs of the next unit
-constexpr int kThreads2 = 320;
+// row half of the cell matrix). The filter keeps its vectors also as FP16 hi + lo rows
+// [dof][vectors], which are exactly the rows of an MN-major A operand (M = vectors):
+//   warp 0        TMA of the cell-matrix K-blocks (hi, lo; K-major, 64B-swizzled)
+//   warp 1        tcgen05.mma issue (one lane): D[vector][row] += Xhi Ahi + Xhi Alo + Xlo Ahi,
+//                 M = 128 vectors, N = the half's rows, K = 16; two accumulators in tensor
+//                 memory
+//   warps 2..5    X rows: cp.async of 16-byte pieces of the hi and lo rows of the K-block's
+//                 32 dofs (dof-map entries loaded one K-block ahead) straight into the
+//                 128B-swizzled MN-major tile, `lookahead` K-blocks in flight; no conversion
+//   warps 6..9    epilogue: tcgen05.ld of a finished accumulator (lane = vector) and
+//                 red.global.add.f32 into the output rows (one 128-byte line per warp
+//                 instruction), overlapped with the MMAs of the next unit
+constexpr int kThreads3 = 320;
 
-__global__ void __launch_bounds__(kThreads2, 1)
+__global__ void __launch_bounds__(kThreads3, 1)
     cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
                       const __grid_constant__ CUtensorMap tm_lo, TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
@@ -143,8 +152,8 @@ __global__ void __launch_bounds__(kThreads2, 1)
   const int S = args.stages;
   const Layout L = make_layout(args.n_half, S);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
-  uint64_t* tma_full = bars;            // [S] TMA bytes landed
-  uint64_t* x_full = bars + S;          // [S] 128 producer arrivals
+  uint64_t* tma_full = bars;            // [S] cell-matrix TMA bytes landed
+  uint64_t* x_full = bars + S;          // [S] 128 producer arrivals (their copies landed)
   uint64_t* empty = bars + 2 * S;       // [S] MMA finished reading the stage
   uint64_t* acc_full = bars + 3 * S;    // [2] accumulator ready for the epilogue
   uint64_t* acc_empty = bars + 3 * S + 2;  // [2] accumulator drained (128 arrivals)
@@ -175,19 +184,14 @@ __global__ void __launch_bounds__(kThreads2, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(tmem_slot)),
-                 "r"(args.tmem_cols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
+  if (warp == 1) tmem_alloc(tmem_slot, args.tmem_cols);
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    // ---------------- TMA producer
+    // ---------------- TMA producer of the cell-matrix K-blocks
     if (lane == 0) {
       const uint32_t bytes = 2u * args.n_half * kRowBytes;
       int64_t issued = 0;
@@ -199,15 +203,15 @@ __global__ void __launch_bounds__(kThreads2, 1)
         if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
         uint8_t* st = smem + s * L.stage;
         mbar_arrive_expect_tx(&tma_full[s], bytes);
-        tma_load_3d(st + 2 * L.x_tile, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
-        tma_load_3d(st + 2 * L.x_tile + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell,
+        tma_load_3d(st + 2 * kXTile, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
+        tma_load_3d(st + 2 * kXTile + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell,
                     &tma_full[s]);
         issued = g + 1;
       }
       if (*abort_flag) {
-        for (int64_t g = (issued > S ? issued - S : 0); g < issued; ++g) {
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
+        for (int64_t h = (issued > S ? issued - S : 0); h < issued; ++h) {
+          const int s = (int)(h % S);
+          const uint32_t r = (uint32_t)(h / S);
           for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(&tma_full[s], r & 1); ++i)
             __nanosleep(128);
         }
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_f16(kVec, args.n_half);
+      const uint32_t idesc = idesc_f16(kVec, args.n_half) | (1u << 15);  // A MN-major
       bool ok = true;
       for (int64_t it = 0; it < my_units && ok; ++it) {
         const int buf = (int)(it & 1);
@@ -235,15 +239,19 @@ __global__ void __launch_bounds__(kThreads2, 1)
           }
           fence_after();
           const uint32_t st = smem_u32(smem + s * L.stage);
-          const uint32_t xhi = st, xlo = st + L.x_tile;
-          const uint32_t ahi = st + 2 * L.x_tile, alo = ahi + L.a_tile;
+          const uint32_t xhi = st, xlo = st + kXTile;
+          const uint32_t ahi = st + 2 * kXTile, alo = ahi + L.a_tile;
 #pragma unroll
           for (int ks = 0; ks < kKB / 16; ++ks) {
-            const uint32_t koff = ks * 32;  // 16 halves = 32 bytes along K
+            const uint32_t xoff = ks * 2 * kXGroupK;  // 16 nodes = two 8-node groups
+            const uint32_t koff = ks * 32;            // 16 halves of a K-major row
             const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(ahi + koff), idesc, acc0);
-            mma_f16(d, smem_desc_sw64(xhi + koff), smem_desc_sw64(alo + koff), idesc, 1u);
-            mma_f16(d, smem_desc_sw64(xlo + koff), smem_desc_sw64(ahi + koff), idesc, 1u);
+            mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                    smem_desc_sw64(ahi + koff), idesc, acc0);
+            mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                    smem_desc_sw64(alo + koff), idesc, 1u);
+            mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
+                    smem_desc_sw64(ahi + koff), idesc, 1u);
           }
           mma_commit(&empty[s]);
         }
@@ -254,90 +262,64 @@ __global__ void __launch_bounds__(kThreads2, 1)
       for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(mma_done, 0); ++i) __nanosleep(128);
     }
   } else if (warp < 6) {
-    // ---------------- X producers: cp.async gather into an FP32 staging ring (kXStages deep,
-    // so ~64 KB of rows are in flight per SM), then FP16 hi/lo split into the stage ring
-    const int t = threadIdx.x - 64;          // 0..127
-    const int v = (warp & 3) * 32 + lane;    // vector row this thread converts
-    uint8_t* xst = smem + L.xstage;
-    // the dof-map entries of a K-block are loaded one issue ahead, so the cp.async of a block
-    // never waits on a dependent map load
-    int mnext[8];
-    auto load_map = [&](int64_t g, int* mv) {
+    // ---------------- X producers. Thread t copies 16-byte piece cc = t % 16 (8 vectors) of
+    // the hi and lo rows of the K-block's nodes 8 j + t / 16 (j = 0..3). Element (vector m,
+    // node k) of the tile sits in atom (m / 64, k / 8), row k % 8, 16-byte chunk
+    // (m % 64) / 8 XOR k % 8.
+    const int t = threadIdx.x - 64;
+    const int cc = t & 15, rsub = t >> 4;
+    const int mi = cc >> 3, c = cc & 7;
+    const uint32_t dst_base = mi * kXAtomM + rsub * 128 + ((uint32_t)(c ^ rsub) << 4);
+    const int D = args.lookahead;
+    int rows_next[4];
+    auto load_rows = [&](int64_t g, int* rows) {
       if (g < my_blocks) {
         const Unit w = unit_at(g / nkb, first, step, args);
         const int kb = (int)(g % nkb);
         const int* mrow = args.map + (int64_t)w.cell * args.n_e;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int J = kb * kKB + ((i * 128 + t) >> 5);
-          mv[i] = J < args.n_e ? __ldg(mrow + J) : -1;
+        for (int j = 0; j < 4; ++j) {
+          const int J = kb * kKB + j * 8 + rsub;
+          rows[j] = J < args.n_e ? __ldg(mrow + J) : -1;
         }
       }
     };
-    auto issue = [&](int64_t g) {
-      uint8_t* slot = xst + (int)(g % kXStages) * kXStageBytes;
-      int mv[8];
+    // issue the copies of block g into its stage (waits for the stage to be free)
+    auto issue = [&](int64_t g) -> bool {
+      int rows[4];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) mv[i] = mnext[i];
-      load_map(g + 1, mnext);
+      for (int j = 0; j < 4; ++j) rows[j] = rows_next[j];
+      load_rows(g + 1, rows_next);
       if (g < my_blocks) {
+        const int s = (int)(g % S);
+        const uint32_t r = (uint32_t)(g / S);
+        if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) return false;
         const Unit w = unit_at(g / nkb, first, step, args);
+        const int vb = w.chunk * kVec + cc * 8;
+        const bool vok = vb < args.B;
+        const uint32_t st = smem_u32(smem + s * L.stage);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int q = i * 128 + t;             // 16-byte chunk of the [32][128] slot
-          const int j = q >> 5, c4 = (q & 31) * 4;
-          const int gb = w.chunk * kVec + c4;
-          const bool ok = (mv[i] >= 0) && (gb < args.B);
-          const float* src = ok ? args.src + (int64_t)mv[i] * args.lds + gb : args.src;
-          cp_async16(slot + j * (kVec * 4) + c4 * 4, src, ok);
+        for (int j = 0; j < 4; ++j) {
+          const bool ok = vok && rows[j] >= 0;
+          const int64_t off = ok ? (int64_t)rows[j] * args.ldx + vb : 0;
+          const uint32_t d = st + dst_base + j * kXGroupK;
+          cp_async16(d, args.xhi + off, ok);
+          cp_async16(d + kXTile, args.xlo + off, ok);
         }
       }
       cp_async_commit();
+      return true;
     };
-    load_map(0, mnext);
-#pragma unroll
-    for (int i = 0; i < kXStages - 1; ++i) issue(i);
-    bool stop = false;
-    for (int64_t g = 0; g < my_blocks; ++g) {
-      issue(g + kXStages - 1);
-      cp_async_wait<kXStages - 1>();
-      // block g's rows landed for all producer threads; a stop seen by any thread ends all
-      if (producers_sync_or(stop)) break;
-      const float* slot = reinterpret_cast<const float*>(xst + (int)(g % kXStages) * kXStageBytes);
-      float cur[kKB];
-#pragma unroll
-      for (int j = 0; j < kKB; ++j) cur[j] = slot[j * kVec + v];
-      producers_sync();                       // slot may be refilled by the next issue
-      const int s = (int)(g % S);
-      const uint32_t r = (uint32_t)(g / S);
-      if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) {
-        stop = true;
-        continue;
-      }
-      uint8_t* st = smem + s * L.stage;
-      uint8_t* rhi = st + v * kRowBytes;
-      uint8_t* rlo = st + L.x_tile + v * kRowBytes;
-      const int sw = (v >> 1) & 3;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        uint32_t hv[4], lv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const float a0 = cur[c * 8 + 2 * u], a1 = cur[c * 8 + 2 * u + 1];
-          const __half2 h = __floats2half2_rn(a0, a1);
-          const float2 hf = __half22float2(h);
-          const __half2 l = __floats2half2_rn(a0 - hf.x, a1 - hf.y);
-          hv[u] = *reinterpret_cast<const uint32_t*>(&h);
-          lv[u] = *reinterpret_cast<const uint32_t*>(&l);
-        }
-        const int pc = (c ^ sw) * 16;
-        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
-      }
+    load_rows(0, rows_next);
+    bool ok = true;
+    for (int64_t g = 0; g < D && ok; ++g) ok = issue(g);
+    for (int64_t g = 0; g < my_blocks && ok; ++g) {
+      ok = issue(g + D);
+      cp_async_wait_n(D);                      // this thread's copies of block g landed
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&x_full[s]);
+      mbar_arrive(&x_full[(int)(g % S)]);
     }
-    cp_async_wait<0>();
+    asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
     // ---------------- epilogue warps 6..9
     const int q = warp & 3;                  // tensor-memory lane quarter of this warp
@@ -375,8 +357,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
   __syncthreads();
   if (warp == 1) {
     fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(args.tmem_cols));
+    tmem_dealloc(tmem, args.tmem_cols);
   }
 }
 
@@ -409,6 +390,54 @@ void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows)
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+// FP32 -> FP16 hi + lo (22 significant bits; the vectors are pre-scaled into FP16's range)
+__device__ __forceinline__ void split_f32(float a, __half& h, __half& l) {
+  h = __float2half_rn(a);
+  l = __float2half_rn(a - __half2float(h));
+}
+
+// (hi, lo)[r][j] = split(x[r][j]) for a [M][B] block (x leading dimension ldx, splits ld B)
+__global__ void k_split_rows(const float* __restrict__ x, int64_t ldx, int64_t M, int B,
+                             __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int64_t n = M * (int64_t)(B / 2);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / (B / 2);
+    const int j = (int)(t % (B / 2)) * 2;
+    const float2 v = *reinterpret_cast<const float2*>(x + r * ldx + j);
+    __half h0, l0, h1, l1;
+    split_f32(v.x, h0, l0);
+    split_f32(v.y, h1, l1);
+    *reinterpret_cast<__half2*>(hi + r * B + j) = __halves2half2(h0, h1);
+    *reinterpret_cast<__half2*>(lo + r * B + j) = __halves2half2(l0, l1);
+  }
+}
+
+// y = a x + b y on a contiguous [M][B] block, and (hi, lo) = split(x) (the step of the
+// Chebyshev recurrence that reads the vector the next HX multiplies)
+__global__ void k_axpby_split(const float* __restrict__ x, float* __restrict__ y, int64_t n,
+                              float a, float b, __half* __restrict__ hi, __half* __restrict__ lo) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float4 xv = reinterpret_cast<const float4*>(x)[t];
+    float4 yv = reinterpret_cast<float4*>(y)[t];
+    yv.x = a * xv.x + b * yv.x;
+    yv.y = a * xv.y + b * yv.y;
+    yv.z = a * xv.z + b * yv.z;
+    yv.w = a * xv.w + b * yv.w;
+    reinterpret_cast<float4*>(y)[t] = yv;
+    __half h[4], l[4];
+    split_f32(xv.x, h[0], l[0]);
+    split_f32(xv.y, h[1], l[1]);
+    split_f32(xv.z, h[2], l[2]);
+    split_f32(xv.w, h[3], l[3]);
+    reinterpret_cast<__half2*>(hi)[2 * t] = __halves2half2(h[0], h[1]);
+    reinterpret_cast<__half2*>(hi)[2 * t + 1] = __halves2half2(h[2], h[3]);
+    reinterpret_cast<__half2*>(lo)[2 * t] = __halves2half2(l[0], l[1]);
+    reinterpret_cast<__half2*>(lo)[2 * t + 1] = __halves2half2(l[2], l[3]);
+  }
 }
 
 struct TcPlan {
@@ -511,9 +540,9 @@ bool tc_usable(chefsi_operator_s* op) {
   return tcgen05_device();
 }
 
-// launch the persistent tensor-core kernel (a.out_scale set by the caller)
-static void launch_tc(chefsi_operator_s* op, TcArgs& a, const float* src, int64_t lds, float* dst,
-                      int64_t ldd, int B, cudaStream_t st) {
+// launch the persistent tensor-core kernel on the split rows (xhi, xlo: [rows][ldx] FP16)
+static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const __half* xlo,
+                      int64_t ldx, float* dst, int64_t ldd, int B, cudaStream_t st) {
   prepare_tensor_mats(op, st);
   const TcPlan p = plan_for(op->n_e);
   if (!op->tc_err.ptr) {
@@ -523,8 +552,10 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const float* src, int64_
   CUtensorMap mhi, mlo;
   make_map(&mhi, op->tc.hi.ptr, op->n_cells, p.npad, p.n_half);
   make_map(&mlo, op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
-  a.src = src;
-  a.lds = lds;
+  a.xhi = xhi;
+  a.xlo = xlo;
+  a.ldx = ldx;
+  a.lookahead = std::max(1, std::min(p.stages - 2, 6));
   a.dst = dst;
   a.ldd = ldd;
   a.map = op->map.ptr;
@@ -539,31 +570,59 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const float* src, int64_
   a.stages = p.stages;
   a.n_units = (int64_t)op->n_cells * a.n_chunks * p.n_halves;
   a.err = op->tc_err.ptr;
+  CHEFSI_REQUIRE(op->n_dofs < (1ll << 31), "tensor-core HX: too many dofs for 32-bit map entries");
+  CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(xhi) & 15) == 0 && (reinterpret_cast<uintptr_t>(xlo) & 15) == 0 &&
+                     ldx % 8 == 0 && B % 8 == 0,
+                 "tensor-core HX: split rows must be 16-byte aligned");
   CHEFSI_CUDA(cudaFuncSetAttribute(cell_hx_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    227 * 1024));
   int dev = 0, sms = kNumSMs;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t grid = std::min<int64_t>(sms, a.n_units / p.n_halves);
-  cell_hx_tc_kernel<<<(unsigned)grid, kThreads2, p.smem, st>>>(mhi, mlo, a);
+  cell_hx_tc_kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(mhi, mlo, a);
   CHEFSI_CHECK_LAUNCH();
 }
 
-// the X gather copies 16-byte pieces: rows must start 16-byte aligned
-static bool gather_aligned(const float* src, int64_t lds, int B) {
-  return (B % 4 == 0) && (lds % 4 == 0) && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
+bool tc_split_usable(chefsi_operator_s* op, int B) { return tc_usable(op) && B % 8 == 0; }
+
+void split_rows_f32(const float* x, int64_t ldx, int64_t M, int B, __half* hi, __half* lo,
+                    cudaStream_t st) {
+  CHEFSI_REQUIRE(B % 2 == 0 && ldx % 2 == 0, "split rows: even widths only");
+  k_split_rows<<<grid_for(M * (B / 2), 256), 256, 0, st>>>(x, ldx, M, B, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
 }
 
-bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
-           double scalar, bool accumulate, cudaStream_t st) {
-  if (!tc_usable(op) || !gather_aligned(src, lds, B)) return false;
+void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, double b, __half* hi,
+                     __half* lo, cudaStream_t st) {
+  const int64_t n = M * B;
+  CHEFSI_REQUIRE(n % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(y) & 15) == 0,
+                 "axpby split: 16-byte aligned blocks with a multiple of 4 entries");
+  k_axpby_split<<<grid_for(n / 4, 256), 256, 0, st>>>(x, y, n, (float)a, (float)b, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, const float* src,
+                 int64_t lds, float* dst, int64_t ldd, int B, double scalar, bool accumulate,
+                 cudaStream_t st) {
+  if (!tc_split_usable(op, B)) return false;
   if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
   prepare_tensor_mats(op, st);
   TcArgs a{};
   a.out_scale = (float)(scalar / op->tc.scale);
-  launch_tc(op, a, src, lds, dst, ldd, B, st);
+  launch_tc(op, a, xhi, xlo, B, dst, ldd, B, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
+}
+
+bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+           double scalar, bool accumulate, cudaStream_t st) {
+  if (!tc_split_usable(op, B) || lds % 2 != 0) return false;
+  __half* hi = op->xs_hi.ensure((size_t)op->n_dofs * B);
+  __half* lo = op->xs_lo.ensure((size_t)op->n_dofs * B);
+  split_rows_f32(src, lds, op->n_dofs, B, hi, lo, st);
+  return hx_tc_split(op, hi, lo, src, lds, dst, ldd, B, scalar, accumulate, st);
 }
 
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st) {

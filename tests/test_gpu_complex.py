@@ -72,8 +72,9 @@ def test_rayleigh_ritz_complex_matches_oracle(C, prec, tol):
     assert np.abs(r_g - r_o).max() < (1e-8 if prec == "fp64" else 1e-4) * max(1.0, r_o.max())
 
 
-@pytest.mark.parametrize("mixed,tol", [(False, 1e-10), (True, 1e-6)])
-def test_solve_complex_matches_oracle(C, mixed, tol):
+@pytest.mark.parametrize("mixed,tol,rr", [(False, 1e-10, "fp64"), (True, 1e-6, "fp64"),
+                                          (True, 1e-6, "fp32")])
+def test_solve_complex_matches_oracle(C, mixed, tol, rr):
     pr = small_problem(n=3, L=6.0, p=2, wells=3, nwfc=12, seed=7, kpoint=K)
     op, ora = C.KohnShamOperator.from_problem(pr), oracle_op(pr)
     rng = np.random.default_rng(8)
@@ -82,7 +83,8 @@ def test_solve_complex_matches_oracle(C, mixed, tol):
     Xo = X0.copy()
     for _ in range(5):
         ev_o, res_o, Xo = orc.solve(ora, Xo, st, m=10)
-    s = C.ChebyshevOrthogonalizedSubspaceIterationSolver(C.SolverParams(chebyshevOrder=10))
+    s = C.ChebyshevOrthogonalizedSubspaceIterationSolver(
+        C.SolverParams(chebyshevOrder=10, rr_precision=rr))
     s.reinitSpectrumBounds(-3.0, 3.0, 12.0)
     X = torch.from_numpy(X0.copy()).cuda()
     for _ in range(5):

@@ -51,11 +51,15 @@ def test_hx_scaleflag_semantics(chefsi):
     assert rel(d.cpu().numpy(), ref) < 1e-12
 
 
-@pytest.mark.parametrize("prec", ["fp32", "mixed"])
-def test_hx_reduced_precision(chefsi, prec):
-    pr = small_problem(n=2, L=4.0, p=4, wells=2, projectors=True)
+@pytest.mark.parametrize("prec,p,n,B", [("fp32", 4, 2, 96), ("mixed", 4, 2, 96),
+                                         ("mixed", 6, 2, 136), ("mixed", 2, 3, 8),
+                                         ("mixed", 5, 2, 256)])
+def test_hx_reduced_precision(chefsi, prec, p, n, B):
+    """FP32 SIMT and tensor-core (FP16-split) HX: cell sizes with one K-block (p = 2), one
+    row half (p = 4, 5) and two row halves (p = 6); partial and several 128-vector chunks."""
+    pr = small_problem(n=n, L=2.0 * n, p=p, wells=2, projectors=True)
     op, ora = gpu_op(chefsi, pr), oracle_op(pr)
-    X = np.random.default_rng(5).uniform(-1, 1, (pr.n_dofs, 96))
+    X = np.random.default_rng(5).uniform(-1, 1, (pr.n_dofs, B))
     Xt = torch.from_numpy(X).float().cuda()
     Y = torch.zeros_like(Xt)
     try:
