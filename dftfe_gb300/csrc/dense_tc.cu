@@ -348,13 +348,14 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       fence_after();
       const uint32_t tv = tmem + buf * 128 + hcol * 64 + lane_off;
 #pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 8) {
-        uint32_t rv[8], rl[8];
-        tmem_ld8_async(tv + c0, rv);
-        tmem_ld8_async(tl + c0, rl);
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        // 16 columns per tensor-memory round trip (the load latency is the epilogue's cost)
+        uint32_t rv[16], rl[16];
+        tmem_ld16_async(tv + c0, rv);
+        tmem_ld16_async(tl + c0, rl);
         tmem_wait_ld();
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < 16; ++u) {
           const float v = __uint_as_float(rv[u]);
           const float h = sh[c0 + u];
           const float s = __fadd_rn(h, v);
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
           sh[c0 + u] = s;
           rl[u] = __float_as_uint(__fadd_rn(__uint_as_float(rl[u]), err));
         }
-        tmem_st8(tl + c0, rl);
+        tmem_st16(tl + c0, rl);
       }
       tmem_wait_st();
       fence_before();

@@ -562,14 +562,93 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// W[a][j][b] += sum over one kNlChunk-row chunk of atom a of C[r][j] x[dof_r][b]: one CTA per
+// (row chunk, 128-vector tile). The chunk's C rows and dofs are staged in shared memory, the 8
+// warps take interleaved rows with 8 gathered float4 loads in flight per lane, the warps'
+// partial sums are reduced in shared memory and added to W with one float4 atomic per
+// (projector, lane). Many more CTAs than atoms x tiles, so the gather has enough loads in
+// flight to approach the memory bandwidth.
+__global__ void __launch_bounds__(256)
+    nl_project_chunk4(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
+                      const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
+                      const float* __restrict__ C, int P, const float* __restrict__ src,
+                      int64_t lds, float* __restrict__ W, int B) {
+  extern __shared__ float4 red_dyn[];                 // [8][P][32]
+  __shared__ float Cs[kNlChunk * kMaxProj];
+  __shared__ int Ds[kNlChunk];
+  const int ch = blockIdx.x;
+  const int a = chunk_atom[ch];
+  const int r0 = chunk_row0[ch];
+  const int nr = min(r0 + kNlChunk, atom_ptr[a + 1]) - r0;
+  for (int i = threadIdx.x; i < nr * P; i += blockDim.x) Cs[i] = C[(size_t)r0 * P + i];
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) Ds[i] = dofs[r0 + i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.y * 128 + lane * 4;
+  float4 acc[kMaxProj];
+#pragma unroll
+  for (int j = 0; j < kMaxProj; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (b < B) {
+    int r = warp;
+    for (; r + 56 < nr; r += 64) {
+      float4 xv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        xv[u] = __ldg(reinterpret_cast<const float4*>(src + (int64_t)Ds[r + 8 * u] * lds + b));
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int j = 0; j < kMaxProj; ++j) {
+          if (j >= P) break;
+          const float cv = Cs[(r + 8 * u) * P + j];
+          acc[j].x = fmaf(cv, xv[u].x, acc[j].x);
+          acc[j].y = fmaf(cv, xv[u].y, acc[j].y);
+          acc[j].z = fmaf(cv, xv[u].z, acc[j].z);
+          acc[j].w = fmaf(cv, xv[u].w, acc[j].w);
+        }
+    }
+    for (; r < nr; r += 8) {
+      const float4 xv = __ldg(reinterpret_cast<const float4*>(src + (int64_t)Ds[r] * lds + b));
+#pragma unroll
+      for (int j = 0; j < kMaxProj; ++j) {
+        if (j >= P) break;
+        const float cv = Cs[r * P + j];
+        acc[j].x = fmaf(cv, xv.x, acc[j].x);
+        acc[j].y = fmaf(cv, xv.y, acc[j].y);
+        acc[j].z = fmaf(cv, xv.z, acc[j].z);
+        acc[j].w = fmaf(cv, xv.w, acc[j].w);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kMaxProj; ++j)
+    if (j < P) red_dyn[(warp * P + j) * 32 + lane] = acc[j];
+  __syncthreads();
+  for (int t = threadIdx.x; t < P * 32; t += blockDim.x) {
+    const int j = t >> 5, l = t & 31;
+    float4 sum = red_dyn[j * 32 + l];
+    for (int w2 = 1; w2 < 8; ++w2) {
+      const float4 v = red_dyn[(w2 * P + j) * 32 + l];
+      sum.x += v.x, sum.y += v.y, sum.z += v.z, sum.w += v.w;
+    }
+    const int bb = blockIdx.y * 128 + l * 4;
+    if (bb < B) atomicAdd(reinterpret_cast<float4*>(&W[((size_t)a * P + j) * B + bb]), sum);
+  }
+}
+
 void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
                     cudaStream_t st) {
   if (op->n_atoms == 0) return;
   const bool vec = (B % 4 == 0) && (ldx % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
   if (vec) {
-    dim3 grid(op->n_atoms, (B + 127) / 128);
-    nl_project_atom<<<grid, 256, 0, st>>>(op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
-                                          op->n_proj, x, ldx, W, B);
+    CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * (size_t)op->n_atoms * op->n_proj * B, st));
+    dim3 grid(op->nl_n_chunks, (B + 127) / 128);
+    const size_t red = sizeof(float4) * 8 * op->n_proj * 32;
+    CHEFSI_CUDA(cudaFuncSetAttribute(nl_project_chunk4, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(float4) * 8 * kMaxProj * 32)));
+    nl_project_chunk4<<<grid, 256, red, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
+                                              op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
+                                              op->n_proj, x, ldx, W, B);
   } else {
     CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * (size_t)op->n_atoms * op->n_proj * B, st));
     const int threads = 128;

@@ -71,25 +71,33 @@ struct TcArgs {
   int n_halves;    // row halves per cell (1 or 2)
   int buf_stride;  // tensor-memory column offset of accumulator 1
   int tmem_cols;
-  int stages;
+  int stages;      // cell-matrix ring depth
+  int xstages;     // X ring depth
   int lookahead;   // K-blocks of X copies in flight per producer thread
   int64_t n_units; // n_cells * n_chunks * n_halves
   float out_scale; // scalar / 2^s
   int* err;
 };
 
+// Two rings: the X tiles (xhi, xlo: 16 KB a stage) and the cell-matrix tiles (ahi, alo). The X
+// ring is the deeper one, since its rows come through the gather from HBM / L2 while a cell's
+// matrix halves are shared by the eight chunks processed at about the same time (L2).
 struct Layout {
   int a_tile;   // n_half rows x 64 B, rounded to 1 KB
-  int stage;    // xhi, xlo, ahi, alo
+  int xstage;   // xhi, xlo
+  int astage;   // ahi, alo
+  int aoff;     // start of the matrix ring
   int bars;     // barrier block
   int total;
 };
-__host__ __device__ inline Layout make_layout(int n_half, int stages) {
+__host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages) {
   Layout L;
   L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
-  L.stage = 2 * kXTile + 2 * L.a_tile;
-  L.bars = stages * L.stage;
-  L.total = L.bars + 8 * (3 * stages + 8);
+  L.xstage = 2 * kXTile;
+  L.astage = 2 * L.a_tile;
+  L.aoff = xstages * L.xstage;
+  L.bars = L.aoff + stages * L.astage;
+  L.total = L.bars + 8 * (2 * stages + 2 * xstages + 8);
   return L;
 }
 
@@ -149,17 +157,18 @@ __global__ void __launch_bounds__(kThreads3, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int S = args.stages;
-  const Layout L = make_layout(args.n_half, S);
+  const int S = args.stages, SX = args.xstages;
+  const Layout L = make_layout(args.n_half, S, SX);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] cell-matrix TMA bytes landed
-  uint64_t* x_full = bars + S;          // [S] 128 producer arrivals (their copies landed)
-  uint64_t* empty = bars + 2 * S;       // [S] MMA finished reading the stage
-  uint64_t* acc_full = bars + 3 * S;    // [2] accumulator ready for the epilogue
-  uint64_t* acc_empty = bars + 3 * S + 2;  // [2] accumulator drained (128 arrivals)
-  uint64_t* mma_done = bars + 3 * S + 4;   // final MMA completion
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3 * S + 5);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 3 * S + 6);
+  uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
+  uint64_t* x_full = bars + 2 * S;      // [SX] 128 producer arrivals (their copies landed)
+  uint64_t* x_empty = bars + 2 * S + SX;   // [SX] MMA finished reading the X stage
+  uint64_t* acc_full = bars + 2 * S + 2 * SX;       // [2] accumulator ready for the epilogue
+  uint64_t* acc_empty = acc_full + 2;               // [2] accumulator drained (128 arrivals)
+  uint64_t* mma_done = acc_full + 4;                // final MMA completion
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(acc_full + 6);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t first = blockIdx.x;
@@ -173,8 +182,11 @@ __global__ void __launch_bounds__(kThreads3, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&tma_full[s], 1);
+      mbar_init(&a_empty[s], 1);
+    }
+    for (int s = 0; s < SX; ++s) {
       mbar_init(&x_full[s], kVec);
-      mbar_init(&empty[s], 1);
+      mbar_init(&x_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -195,24 +207,29 @@ __global__ void __launch_bounds__(kThreads3, 1)
     if (lane == 0) {
       const uint32_t bytes = 2u * args.n_half * kRowBytes;
       int64_t issued = 0;
-      for (int64_t g = 0; g < my_blocks; ++g) {
-        const Unit w = unit_at(g / nkb, first, step, args);
-        const int kb = (int)(g % nkb);
-        const int s = (int)(g % S);
-        const uint32_t r = (uint32_t)(g / S);
-        if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) break;
-        uint8_t* st = smem + s * L.stage;
-        mbar_arrive_expect_tx(&tma_full[s], bytes);
-        tma_load_3d(st + 2 * kXTile, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
-        tma_load_3d(st + 2 * kXTile + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell,
-                    &tma_full[s]);
-        issued = g + 1;
+      int s = 0;
+      uint32_t r = 0;
+      bool ok = true;
+      for (int64_t it = 0; it < my_units && ok; ++it) {
+        const Unit w = unit_at(it, first, step, args);
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&a_empty[s], (r & 1) ^ 1, args.err, abort_flag)) {
+            ok = false;
+            break;
+          }
+          uint8_t* st = smem + L.aoff + s * L.astage;
+          mbar_arrive_expect_tx(&tma_full[s], bytes);
+          tma_load_3d(st, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
+          tma_load_3d(st + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
+          ++issued;
+          if (++s == S) s = 0, ++r;
+        }
       }
       if (*abort_flag) {
         for (int64_t h = (issued > S ? issued - S : 0); h < issued; ++h) {
-          const int s = (int)(h % S);
-          const uint32_t r = (uint32_t)(h / S);
-          for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(&tma_full[s], r & 1); ++i)
+          const int sh = (int)(h % S);
+          const uint32_t rh = (uint32_t)(h / S);
+          for (uint32_t i = 0; i < kWaitLimit && !mbar_try_wait(&tma_full[sh], rh & 1); ++i)
             __nanosleep(128);
         }
       }
@@ -222,6 +239,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
     if (lane == 0) {
       const uint32_t idesc = idesc_f16(kVec, args.n_half) | (1u << 15);  // A MN-major
       bool ok = true;
+      int s = 0, sx = 0;            // ring positions of the next K-block
+      uint32_t r = 0, rx = 0;       // and their phases
       for (int64_t it = 0; it < my_units && ok; ++it) {
         const int buf = (int)(it & 1);
         const uint32_t ph = (uint32_t)((it >> 1) & 1);
@@ -229,18 +248,14 @@ __global__ void __launch_bounds__(kThreads3, 1)
         fence_after();
         const uint32_t d = tmem + buf * args.buf_stride;
         for (int kb = 0; kb < nkb; ++kb) {
-          const int64_t g = it * nkb + kb;
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
           if (!mbar_wait(&tma_full[s], r & 1, args.err, abort_flag) ||
-              !mbar_wait(&x_full[s], r & 1, args.err, abort_flag)) {
+              !mbar_wait(&x_full[sx], rx & 1, args.err, abort_flag)) {
             ok = false;
             break;
           }
           fence_after();
-          const uint32_t st = smem_u32(smem + s * L.stage);
-          const uint32_t xhi = st, xlo = st + kXTile;
-          const uint32_t ahi = st + 2 * kXTile, alo = ahi + L.a_tile;
+          const uint32_t xhi = smem_u32(smem + sx * L.xstage), xlo = xhi + kXTile;
+          const uint32_t ahi = smem_u32(smem + L.aoff + s * L.astage), alo = ahi + L.a_tile;
 #pragma unroll
           for (int ks = 0; ks < kKB / 16; ++ks) {
             const uint32_t xoff = ks * 2 * kXGroupK;  // 16 nodes = two 8-node groups
@@ -253,7 +268,10 @@ __global__ void __launch_bounds__(kThreads3, 1)
             mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
                     smem_desc_sw64(ahi + koff), idesc, 1u);
           }
-          mma_commit(&empty[s]);
+          mma_commit(&a_empty[s]);
+          mma_commit(&x_empty[sx]);
+          if (++s == S) s = 0, ++r;
+          if (++sx == SX) sx = 0, ++rx;
         }
         if (ok) mma_commit(&acc_full[buf]);
       }
@@ -271,53 +289,65 @@ __global__ void __launch_bounds__(kThreads3, 1)
     const int mi = cc >> 3, c = cc & 7;
     const uint32_t dst_base = mi * kXAtomM + rsub * 128 + ((uint32_t)(c ^ rsub) << 4);
     const int D = args.lookahead;
-    int rows_next[4];
-    auto load_rows = [&](int64_t g, int* rows) {
-      if (g < my_blocks) {
-        const Unit w = unit_at(g / nkb, first, step, args);
-        const int kb = (int)(g % nkb);
-        const int* mrow = args.map + (int64_t)w.cell * args.n_e;
+    // cursor over this CTA's K-blocks (no per-block divisions): unit it, K-block kb
+    int64_t c_it = 0;
+    int c_kb = 0;
+    Unit c_w = my_units > 0 ? unit_at(0, first, step, args) : Unit{0, 0, 0};
+    struct Pending {
+      int rows[4];
+      int vb;
+      bool valid;
+    } nxt;
+    // dof-map entries of the cursor's K-block (one K-block ahead of the copies)
+    auto load_next = [&]() {
+      nxt.valid = c_it < my_units;
+      if (nxt.valid) {
+        const int* mrow = args.map + (int64_t)c_w.cell * args.n_e;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const int J = kb * kKB + j * 8 + rsub;
-          rows[j] = J < args.n_e ? __ldg(mrow + J) : -1;
+          const int J = c_kb * kKB + j * 8 + rsub;
+          nxt.rows[j] = J < args.n_e ? __ldg(mrow + J) : -1;
+        }
+        nxt.vb = c_w.chunk * kVec + cc * 8;
+        if (++c_kb == nkb) {
+          c_kb = 0;
+          if (++c_it < my_units) c_w = unit_at(c_it, first, step, args);
         }
       }
     };
-    // issue the copies of block g into its stage (waits for the stage to be free)
-    auto issue = [&](int64_t g) -> bool {
-      int rows[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) rows[j] = rows_next[j];
-      load_rows(g + 1, rows_next);
-      if (g < my_blocks) {
-        const int s = (int)(g % S);
-        const uint32_t r = (uint32_t)(g / S);
-        if (!mbar_wait(&empty[s], (r & 1) ^ 1, args.err, abort_flag)) return false;
-        const Unit w = unit_at(g / nkb, first, step, args);
-        const int vb = w.chunk * kVec + cc * 8;
-        const bool vok = vb < args.B;
-        const uint32_t st = smem_u32(smem + s * L.stage);
+    int s_iss = 0;
+    uint32_t r_iss = 0;
+    // issue the copies of the next K-block into its X stage (waits for the stage to be free)
+    auto issue = [&]() -> bool {
+      const Pending cur = nxt;
+      load_next();
+      if (cur.valid) {
+        if (!mbar_wait(&x_empty[s_iss], (r_iss & 1) ^ 1, args.err, abort_flag)) return false;
+        const bool vok = cur.vb < args.B;
+        const uint32_t st = smem_u32(smem + s_iss * L.xstage);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const bool ok = vok && rows[j] >= 0;
-          const int64_t off = ok ? (int64_t)rows[j] * args.ldx + vb : 0;
+          const bool ok = vok && cur.rows[j] >= 0;
+          const int64_t off = ok ? (int64_t)cur.rows[j] * args.ldx + cur.vb : 0;
           const uint32_t d = st + dst_base + j * kXGroupK;
           cp_async16(d, args.xhi + off, ok);
           cp_async16(d + kXTile, args.xlo + off, ok);
         }
       }
       cp_async_commit();
+      if (++s_iss == SX) s_iss = 0, ++r_iss;
       return true;
     };
-    load_rows(0, rows_next);
+    load_next();
     bool ok = true;
-    for (int64_t g = 0; g < D && ok; ++g) ok = issue(g);
+    for (int i = 0; i < D && ok; ++i) ok = issue();
+    int s_arr = 0;
     for (int64_t g = 0; g < my_blocks && ok; ++g) {
-      ok = issue(g + D);
+      ok = issue();
       cp_async_wait_n(D);                      // this thread's copies of block g landed
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&x_full[(int)(g % S)]);
+      mbar_arrive(&x_full[s_arr]);
+      if (++s_arr == SX) s_arr = 0;
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
@@ -441,7 +471,7 @@ __global__ void k_axpby_split(const float* __restrict__ x, float* __restrict__ y
 }
 
 struct TcPlan {
-  int npad, n_half, n_halves, buf_stride, tmem_cols, stages, smem;
+  int npad, n_half, n_halves, buf_stride, tmem_cols, stages, xstages, smem;
 };
 
 TcPlan plan_for(int n_e) {
@@ -456,10 +486,13 @@ TcPlan plan_for(int n_e) {
   }
   p.buf_stride = p.n_half <= 128 ? 128 : 256;
   p.tmem_cols = 2 * p.buf_stride;
+  // three matrix stages, then as many X stages as fit (at most 8)
   const int budget = 220 * 1024;
-  p.stages = 8;
-  while (p.stages > 2 && make_layout(p.n_half, p.stages).total + 1024 > budget) --p.stages;
-  p.smem = make_layout(p.n_half, p.stages).total + 1024;
+  p.stages = 3;
+  p.xstages = 8;
+  while (p.xstages > 3 && make_layout(p.n_half, p.stages, p.xstages).total + 1024 > budget)
+    --p.xstages;
+  p.smem = make_layout(p.n_half, p.stages, p.xstages).total + 1024;
   return p;
 }
 
@@ -555,7 +588,7 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const
   a.xhi = xhi;
   a.xlo = xlo;
   a.ldx = ldx;
-  a.lookahead = std::max(1, std::min(p.stages - 2, 6));
+  a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
   a.dst = dst;
   a.ldd = ldd;
   a.map = op->map.ptr;
@@ -568,6 +601,7 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const
   a.buf_stride = p.buf_stride;
   a.tmem_cols = p.tmem_cols;
   a.stages = p.stages;
+  a.xstages = p.xstages;
   a.n_units = (int64_t)op->n_cells * a.n_chunks * p.n_halves;
   a.err = op->tc_err.ptr;
   CHEFSI_REQUIRE(op->n_dofs < (1ll << 31), "tensor-core HX: too many dofs for 32-bit map entries");
