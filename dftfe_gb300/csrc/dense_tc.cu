@@ -251,12 +251,12 @@ __global__ void __launch_bounds__(kGramThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       int64_t g = 0;
+      int s = 0;
+      uint32_t r = 0;
       bool ok = true;
       for (int c = slice; c < n_chunks && ok; c += a.kslices) {
         const int kb1 = min(a.nkb, (c + 1) * a.kc);
         for (int kb = c * a.kc; kb < kb1; ++kb) {
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, a.err, abort_flag)) {
             ok = false;
             break;
@@ -270,6 +270,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             tma_load_2d(st + 3 * kRows8K, &mb_lo, kb * kKB, tj * 128, &full[s]);
           }
           ++g;
+          if (++s == S) s = 0, ++r;
         }
       }
       if (*abort_flag) {
@@ -284,7 +285,8 @@ __global__ void __launch_bounds__(kGramThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = idesc_f16(128, 128);
-      int64_t g = 0;
+      int s = 0;
+      uint32_t r = 0;
       int it = 0;
       bool ok = true;
       for (int c = slice; c < n_chunks && ok; c += a.kslices, ++it) {
@@ -295,8 +297,6 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         const uint32_t d = tmem + buf * 128;
         const int kb0 = c * a.kc, kb1 = min(a.nkb, kb0 + a.kc);
         for (int kb = kb0; kb < kb1; ++kb) {
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
           if (!mbar_wait(&full[s], r & 1, a.err, abort_flag)) {
             ok = false;
             break;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             mma_f16(d, smem_desc_sw64(alo + koff), smem_desc_sw64(bhi + koff), idesc, 1u);
           }
           mma_commit(&empty[s]);
-          ++g;
+          if (++s == S) s = 0, ++r;
         }
         if (ok) mma_commit(&acc_full[buf]);
       }
@@ -466,13 +466,13 @@ __global__ void __launch_bounds__(kRotThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       int64_t g = 0;
+      int s = 0;
+      uint32_t r = 0;
       bool ok = true;
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         const int64_t t = first + it * step;
         const int nt = (int)(t / a.m_tiles), mt = (int)(t % a.m_tiles);
         for (int kb = 0; kb < a.nkb; ++kb) {
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
           if (!mbar_wait(&empty[s], (r & 1) ^ 1, a.err, abort_flag)) {
             ok = false;
             break;
@@ -484,6 +484,7 @@ __global__ void __launch_bounds__(kRotThreads, 1)
           tma_load_2d(st + 2 * kRows8K, &mx_hi, kb * kKB, nt * 256, &full[s]);
           tma_load_2d(st + 4 * kRows8K, &mx_lo, kb * kKB, nt * 256, &full[s]);
           ++g;
+          if (++s == S) s = 0, ++r;
         }
       }
       if (*abort_flag) {
@@ -498,7 +499,8 @@ __global__ void __launch_bounds__(kRotThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = idesc_f16(128, 256);
-      int64_t g = 0;
+      int s = 0;
+      uint32_t r = 0;
       bool ok = true;
       for (int64_t it = 0; it < my_tiles && ok; ++it) {
         const int buf = (int)(it & 1);
@@ -507,8 +509,6 @@ __global__ void __launch_bounds__(kRotThreads, 1)
         fence_after();
         const uint32_t d = tmem + buf * 256;
         for (int kb = 0; kb < a.nkb; ++kb) {
-          const int s = (int)(g % S);
-          const uint32_t r = (uint32_t)(g / S);
           if (!mbar_wait(&full[s], r & 1, a.err, abort_flag)) {
             ok = false;
             break;
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(kRotThreads, 1)
             mma_f16(d, smem_desc_sw64(wlo + koff), smem_desc_sw64(xhi + koff), idesc, 1u);
           }
           mma_commit(&empty[s]);
-          ++g;
+          if (++s == S) s = 0, ++r;
         }
         if (ok) mma_commit(&acc_full[buf]);
       }
