@@ -948,6 +948,156 @@ __global__ void k_bt_update(const double* V, int N, int k,
   }
 }
 
+// ---------------------------------------------------------------- fused tridiagonalisation
+// The whole Householder reduction in one cooperative launch (all CTAs co-resident) instead
+// of four launches per column: per column, CTA 0 forms the reflector, all CTAs compute
+// p = tau A22 v over their rows, then each CTA forms w = p - (tau/2)(v^T p) v itself and
+// applies the rank-2 update to its rows; three grid barriers per column. The barrier is a
+// counter plus a generation word with a bounded wait: on expiry the CTA records
+// CHEFSI_ERR_TIMEOUT and every CTA leaves (the host reads the flag).
+struct GridSync {
+  unsigned int* count;
+  unsigned int* gen;
+  int* err;
+};
+
+__device__ __forceinline__ bool grid_barrier(const GridSync& gs, unsigned int nblocks) {
+  __shared__ int fail;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fail = 0;
+    const unsigned int g = atomicAdd(gs.gen, 0u);
+    __threadfence();
+    if (atomicAdd(gs.count, 1u) == nblocks - 1) {
+      atomicExch(gs.count, 0u);
+      __threadfence();
+      atomicAdd(gs.gen, 1u);
+    } else {
+      uint32_t i = 0;
+      for (; i < (1u << 26); ++i) {
+        if (*reinterpret_cast<volatile unsigned int*>(gs.gen) != g) break;
+        if (*reinterpret_cast<volatile int*>(gs.err) != 0) break;
+        if (i > 32) __nanosleep(32);
+      }
+      if (i == (1u << 26)) atomicExch(gs.err, CHEFSI_ERR_TIMEOUT);
+    }
+    __threadfence();
+    fail = *reinterpret_cast<volatile int*>(gs.err) != 0;
+  }
+  __syncthreads();
+  return fail == 0;
+}
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(256)
+    k_tridiag_fused(double* A, int N, double* V, double* tau, double* d, double* e, double* p,
+                    GridSync gs) {
+  __shared__ double red[32];
+  const unsigned int nb = gridDim.x;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k + 2 < N; ++k) {
+    const int n = N - k - 1;
+    double* v = V + (int64_t)k * N + k + 1;
+    if (blockIdx.x == 0) {
+      double s = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double x = A[(int64_t)(k + 1 + i) * N + k];
+        s += x * x;
+      }
+      const double nrm2 = block_sum(s, red);
+      const double x0 = A[(int64_t)(k + 1) * N + k];
+      const double nrm = sqrt(nrm2);
+      const double alpha = (x0 >= 0.0) ? -nrm : nrm;
+      const double vtv = 2.0 * (nrm2 - alpha * x0);
+      const bool skip = !(vtv > 0.0) || nrm == 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double x = A[(int64_t)(k + 1 + i) * N + k];
+        v[i] = skip ? 0.0 : (i == 0 ? x - alpha : x);
+      }
+      if (threadIdx.x == 0) {
+        tau[k] = skip ? 0.0 : 2.0 / vtv;
+        d[k] = A[(int64_t)k * N + k];
+        e[k] = skip ? x0 : alpha;
+      }
+    }
+    if (!grid_barrier(gs, nb)) return;
+    const double tk = tau[k];
+    // p = tau A22 v, one warp per row
+    for (int i = gwarp; i < n; i += nwarps) {
+      const double* row = A + (int64_t)(k + 1 + i) * N + k + 1;
+      double s = 0.0;
+      for (int j = lane; j < n; j += 32) s += row[j] * v[j];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) p[i] = tk * s;
+    }
+    if (!grid_barrier(gs, nb)) return;
+    // f = (tau/2) v^T p in every CTA; A22 -= v w^T + w v^T with w = p - f v
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i] * v[i];
+    const double f = 0.5 * tk * block_sum(s, red);
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+      const double vi = v[i], wi = p[i] - f * vi;
+      double* row = A + (int64_t)(k + 1 + i) * N + k + 1;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double vj = v[j], wj = p[j] - f * vj;
+        row[j] -= vi * wj + wi * vj;
+      }
+    }
+    if (!grid_barrier(gs, nb)) return;
+  }
+}
+
+// Householder tridiagonalisation of the N x N row-major symmetric A: one cooperative launch
+// when the device supports it, else the four-launch-per-column sequence.
+static void tridiagonalise(double* A, int N, double* V, double* tau, double* d, double* e,
+                           double* p, cudaStream_t st) {
+  int dev = 0, coop = 0, sms = kNumSMs, per_sm = 0;
+  CHEFSI_CUDA(cudaGetDevice(&dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CHEFSI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_fused, 256, 0));
+  if (coop && per_sm > 0 && N > 2) {
+    DeviceBuffer<unsigned int> sync(2);
+    DeviceBuffer<int> err(1);
+    CHEFSI_CUDA(cudaMemsetAsync(sync.ptr, 0, 2 * sizeof(unsigned int), st));
+    CHEFSI_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), st));
+    GridSync gs{sync.ptr, sync.ptr + 1, err.ptr};
+    int blocks = std::min(sms, std::max(1, (N * 32 + 255) / 256));  // enough warps for the rows
+    blocks = std::min(blocks, sms * per_sm);
+    void* args[] = {&A, &N, &V, &tau, &d, &e, &p, &gs};
+    CHEFSI_CUDA(cudaLaunchCooperativeKernel((const void*)k_tridiag_fused, dim3(blocks), dim3(256),
+                                            args, 0, st));
+    CHEFSI_CHECK_LAUNCH();
+    int h = 0;
+    CHEFSI_CUDA(cudaMemcpyAsync(&h, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+    if (h) throw Error(h, "tridiagonalisation: a bounded grid barrier expired");
+    return;
+  }
+  for (int k = 0; k + 2 < N; ++k) {
+    const int n = N - k - 1;
+    k_hh_vector<<<1, 256, 0, st>>>(A, N, k, V, tau, d, e);
+    CHEFSI_CHECK_LAUNCH();
+    k_hh_symv<<<(n * 32 + 255) / 256, 256, 0, st>>>(A, N, k, V, tau, p);
+    CHEFSI_CHECK_LAUNCH();
+    k_hh_w<<<1, 256, 0, st>>>(N, k, V, tau, p);
+    CHEFSI_CHECK_LAUNCH();
+    k_hh_rank2<<<grid_for((int64_t)n * n, 256), 256, 0, st>>>(A, N, k, V, p);
+    CHEFSI_CHECK_LAUNCH();
+  }
+}
+
 // Compact WY form of a block of reflectors (LAPACK dlarft, forward / columnwise):
 // H_k0 H_k0+1 ... H_k0+nb-1 = I - V T V^T with T upper triangular,
 //   T[j][j] = tau_j,  T[0:j][j] = -tau_j T[0:j][0:j] (V^T v_j)[0:j],
@@ -1009,17 +1159,7 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   CHEFSI_CUDA(cudaMemsetAsync(V.ptr, 0, sizeof(double) * N * N, st));
   CHEFSI_CUDA(cudaMemsetAsync(tau.ptr, 0, sizeof(double) * N, st));
   CHEFSI_CUDA(cudaMemsetAsync(e.ptr, 0, sizeof(double) * N, st));
-  for (int k = 0; k + 2 < N; ++k) {
-    const int n = N - k - 1;
-    k_hh_vector<<<1, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, d.ptr, e.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    k_hh_symv<<<(n * 32 + 255) / 256, 256, 0, st>>>(A, N, k, V.ptr, tau.ptr, p.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    k_hh_w<<<1, 256, 0, st>>>(N, k, V.ptr, tau.ptr, p.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    k_hh_rank2<<<grid_for((int64_t)n * n, 256), 256, 0, st>>>(A, N, k, V.ptr, p.ptr);
-    CHEFSI_CHECK_LAUNCH();
-  }
+  tridiagonalise(A, N, V.ptr, tau.ptr, d.ptr, e.ptr, p.ptr, st);
   k_tail<<<1, 32, 0, st>>>(A, N, d.ptr, e.ptr);
   CHEFSI_CHECK_LAUNCH();
   k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d.ptr, e.ptr, N, w);

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
   uint64_t* full = bars;                 // [S] TMA bytes landed
   uint64_t* empty = bars + S;            // [S] MMAs done reading the stage
   uint64_t* acc_full = bars + 2 * S;     // [kGramAcc]
-  uint64_t* acc_empty = bars + 2 * S + 4;  // [kGramAcc] 256 epilogue arrivals
+  uint64_t* acc_empty = bars + 2 * S + 4;  // [kGramAcc] 8 epilogue-warp arrivals
   uint64_t* mma_done = bars + 2 * S + 8;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 9);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * S + 10);
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     }
     for (int b = 0; b < kGramAcc; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 256);
+      mbar_init(&acc_empty[b], 8);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       }
       tmem_wait_st();
       fence_before();
-      mbar_arrive(&acc_empty[buf]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
     // the partial in scaled units over the whole (padded) tile; the reduction reads the
     // valid part and undoes the column scalings
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(kRotThreads, 1)
   uint64_t* full = bars;
   uint64_t* empty = bars + S;
   uint64_t* acc_full = bars + 2 * S;
-  uint64_t* acc_empty = bars + 2 * S + 2;  // 128 epilogue arrivals
+  uint64_t* acc_empty = bars + 2 * S + 2;  // 4 epilogue-warp arrivals
   uint64_t* mma_done = bars + 2 * S + 4;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * S + 6);
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(kRotThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 128);
+      mbar_init(&acc_empty[b], 4);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -561,7 +562,8 @@ __global__ void __launch_bounds__(kRotThreads, 1)
         }
       }
       fence_before();
-      mbar_arrive(&acc_empty[buf]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
   }
   fence_before();

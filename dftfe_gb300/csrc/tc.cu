@@ -162,10 +162,10 @@ __global__ void __launch_bounds__(kThreads3, 1)
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] cell-matrix TMA bytes landed
   uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
-  uint64_t* x_full = bars + 2 * S;      // [SX] 128 producer arrivals (their copies landed)
+  uint64_t* x_full = bars + 2 * S;      // [SX] 4 producer-warp arrivals (their copies landed)
   uint64_t* x_empty = bars + 2 * S + SX;   // [SX] MMA finished reading the X stage
   uint64_t* acc_full = bars + 2 * S + 2 * SX;       // [2] accumulator ready for the epilogue
-  uint64_t* acc_empty = acc_full + 2;               // [2] accumulator drained (128 arrivals)
+  uint64_t* acc_empty = acc_full + 2;               // [2] accumulator drained (4 warp arrivals)
   uint64_t* mma_done = acc_full + 4;                // final MMA completion
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(acc_full + 6);
@@ -185,12 +185,12 @@ __global__ void __launch_bounds__(kThreads3, 1)
       mbar_init(&a_empty[s], 1);
     }
     for (int s = 0; s < SX; ++s) {
-      mbar_init(&x_full[s], kVec);
+      mbar_init(&x_full[s], 4);      // one arrival per producer warp
       mbar_init(&x_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kVec);
+      mbar_init(&acc_empty[b], 4);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -322,7 +322,9 @@ __global__ void __launch_bounds__(kThreads3, 1)
       const Pending cur = nxt;
       load_next();
       if (cur.valid) {
-        if (!mbar_wait(&x_empty[s_iss], (r_iss & 1) ^ 1, args.err, abort_flag)) return false;
+        // warp-uniform decision: the warp arrives on x_full as one
+        if (!__all_sync(0xffffffffu, mbar_wait(&x_empty[s_iss], (r_iss & 1) ^ 1, args.err, abort_flag)))
+          return false;
         const bool vok = cur.vb < args.B;
         const uint32_t st = smem_u32(smem + s_iss * L.xstage);
 #pragma unroll
@@ -346,7 +348,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
       ok = issue();
       cp_async_wait_n(D);                      // this thread's copies of block g landed
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&x_full[s_arr]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&x_full[s_arr]);
       if (++s_arr == SX) s_arr = 0;
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
@@ -380,7 +383,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
         }
       }
       fence_before();
-      mbar_arrive(&acc_empty[buf]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
   }
   fence_before();
