@@ -13,7 +13,9 @@
 //     (<= 256), K = 16:  D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T  (lo*lo is below 2^-22);
 //   * the epilogue warps read D with tcgen05.ld (lane = vector) and scatter-add
 //     scalar * D / 2^s into the output rows with red.global.add.f32 -- for every cell row the
-//     32 lanes of a warp hit 32 consecutive floats, one 128-byte line per instruction.
+//     32 lanes of a warp hit 32 consecutive floats, one 128-byte line per instruction. The
+//     scatter is the kernel's critical path: per-role cycle counters show the epilogue busy
+//     ~95% of the time (float4 reductions after a lane-quad transpose were 1.6x slower).
 // An mbarrier pipeline of up to 8 stages overlaps the TMA, the MMAs and the scatter of the
 // previous unit. Every mbarrier wait is bounded: on expiry the CTA records
 // CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own TMA copies, frees its
@@ -88,6 +90,7 @@ struct Layout {
   int astage;   // ahi, alo
   int aoff;     // start of the matrix ring
   int bars;     // barrier block
+  int offs;     // epilogue row offsets: 2 x 256 int64 (one table per accumulator)
   int total;
 };
 __host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages) {
@@ -97,7 +100,8 @@ __host__ __device__ inline Layout make_layout(int n_half, int stages, int xstage
   L.astage = 2 * L.a_tile;
   L.aoff = xstages * L.xstage;
   L.bars = L.aoff + stages * L.astage;
-  L.total = L.bars + 8 * (2 * stages + 2 * xstages + 8);
+  L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 8);
+  L.total = L.offs + 2 * 256 * 8;
   return L;
 }
 
@@ -118,6 +122,18 @@ __device__ __forceinline__ void cp_async_wait_n(int n) {
     case 5: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
     default: asm volatile("cp.async.wait_group 6;" ::: "memory"); break;
   }
+}
+
+// named barrier 2 among the 128 epilogue threads with an AND-reduction of v
+__device__ __forceinline__ bool epilogue_sync_and(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 2, 128, pi;\n"
+      " selp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
 }
 
 struct Unit {
@@ -148,7 +164,8 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 //                 128B-swizzled MN-major tile, `lookahead` K-blocks in flight; no conversion
 //   warps 6..9    epilogue: tcgen05.ld of a finished accumulator (lane = vector) and
 //                 red.global.add.f32 into the output rows (one 128-byte line per warp
-//                 instruction), overlapped with the MMAs of the next unit
+//                 instruction; row offsets staged in shared memory once per unit),
+//                 overlapped with the MMAs of the next unit
 constexpr int kThreads3 = 320;
 
 __global__ void __launch_bounds__(kThreads3, 1)
@@ -356,19 +373,26 @@ __global__ void __launch_bounds__(kThreads3, 1)
   } else {
     // ---------------- epilogue warps 6..9
     const int q = warp & 3;                  // tensor-memory lane quarter of this warp
-    const int v = q * 32 + lane;
     for (int64_t it = 0; it < my_units; ++it) {
       const int buf = (int)(it & 1);
       const uint32_t ph = (uint32_t)((it >> 1) & 1);
-      const bool ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
-      if (!ok) break;
+      const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
       fence_after();
       const Unit w = unit_at(it, first, step, args);
-      const int gb = w.chunk * kVec + v;
-      const bool vok = gb < args.B;
       const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
       const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
+      // the unit's output-row offsets (dof * ldd), staged once by the four warps; rows past
+      // nrows get an offset no lane uses (they are skipped)
+      int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + buf * 256;
+      if (okw)
+        for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += 128)
+          offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
+      // the four warps continue or stop together (a named barrier with an AND-reduction)
+      if (!epilogue_sync_and(okw)) break;
+      const int gb = w.chunk * kVec + q * 32 + lane;
+      const bool vok = gb < args.B;
       float* dstb = args.dst + gb;
+      const float osc = args.out_scale;
       const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
       for (int c0 = 0; c0 < args.n_half; c0 += 16) {
         float vals[16];
@@ -376,9 +400,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
         if (vok) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            const int I = c0 + i;
-            if (I < nrows)
-              atomicAdd(dstb + (int64_t)__ldg(mrow + I) * args.ldd, args.out_scale * vals[i]);
+            const int64_t o = offs[c0 + i];
+            if (o >= 0) atomicAdd(dstb + o, osc * vals[i]);
           }
         }
       }
@@ -644,7 +667,9 @@ void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, doubl
 bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, const float* src,
                  int64_t lds, float* dst, int64_t ldd, int B, double scalar, bool accumulate,
                  cudaStream_t st) {
-  if (!tc_split_usable(op, B)) return false;
+  // the scatter adds float4 pieces: output rows 16-byte aligned
+  if (!tc_split_usable(op, B) || ldd % 4 != 0 || (reinterpret_cast<uintptr_t>(dst) & 15) != 0)
+    return false;
   if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
   prepare_tensor_mats(op, st);
   TcArgs a{};
@@ -656,7 +681,9 @@ bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, co
 
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st) {
-  if (!tc_split_usable(op, B) || lds % 2 != 0) return false;
+  if (!tc_split_usable(op, B) || lds % 2 != 0 || ldd % 4 != 0 ||
+      (reinterpret_cast<uintptr_t>(dst) & 15) != 0)
+    return false;
   __half* hi = op->xs_hi.ensure((size_t)op->n_dofs * B);
   __half* lo = op->xs_lo.ensure((size_t)op->n_dofs * B);
   split_rows_f32(src, lds, op->n_dofs, B, hi, lo, st);
