@@ -362,13 +362,27 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   // X is rounded to FP32 once and the same rounded basis enters S (the mixed Gram converts on
   // load), HX and Hp, so the generalised problem stays consistent.
   double* HX = s->HX.ensure((size_t)M * N);
-  const bool hx32 = is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32;
+  // rr_precision MIXED: the tensor-core (FP16-split) apply on X rounded to FP32 and scaled by
+  // a power of two into the split's range; FP32: the FP32 SIMT apply
+  const bool hxtc = is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_MIXED &&
+                    tc_split_usable(op, N);
+  const bool hx32 = is_mixed(prec) && (s->p.rr_precision == CHEFSI_PREC_FP32 || hxtc);
   float* y32 = nullptr;
   if (hx32) {
     float* x32 = s->Xb32.ensure((size_t)M * N);
     y32 = s->Yb32.ensure((size_t)M * N);
-    copy_block<double, float>(X, ld, x32, N, M, N, 1.0, st);
-    hx_f32(op, x32, N, y32, N, N, 1.0, false, st);
+    double scale = 1.0;
+    if (hxtc) {
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(X, ld, M, N, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (amax > 0.0 && std::isfinite(amax)) scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
+    }
+    copy_block<double, float>(X, ld, x32, N, M, N, scale, st);
+    if (!(hxtc && hx_tc(op, x32, N, y32, N, N, 1.0 / scale, false, st)))
+      hx_f32(op, x32, N, y32, N, N, 1.0 / scale, false, st);
     // the tensor-core path reads the FP32 HX directly; its rotation writes the FP64 HX
     if (!tcd) copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
   } else {

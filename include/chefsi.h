@@ -122,7 +122,8 @@ typedef struct {
   double first_scf_degree_scale;/* chebyshevFilterPolyDegreeFirstScfScalingFactor */
   int32_t keep_hx;              /* 1: keep H X from the RR step for the residuals */
   int32_t rr_precision;         /* precision of the H X feeding X^T H X in mixed mode:
-                                   CHEFSI_PREC_FP64 (default) or CHEFSI_PREC_FP32 */
+                                   CHEFSI_PREC_FP64 (default), CHEFSI_PREC_FP32 (FP32 SIMT
+                                   apply) or CHEFSI_PREC_MIXED (tensor-core FP16-split apply) */
 } chefsi_params;
 
 const char* chefsi_last_error(void);
