@@ -14,8 +14,12 @@
 //   * the epilogue warps read D with tcgen05.ld (lane = vector) and scatter-add
 //     scalar * D / 2^s into the output rows with red.global.add.f32 -- for every cell row the
 //     32 lanes of a warp hit 32 consecutive floats, one 128-byte line per instruction. The
-//     scatter is the kernel's critical path: per-role cycle counters show the epilogue busy
-//     ~95% of the time (float4 reductions after a lane-quad transpose were 1.6x slower).
+//     scatter's instruction stream is the kernel's critical path (per-role cycle counters
+//     show the epilogue busy ~95% of the time), so two warps share each tensor-memory lane
+//     quarter and drain half of the columns each (8 epilogue warps: 1.10x faster than 4).
+//     Measured and rejected: float4 reductions after a lane-quad transpose (1.6x slower),
+//     plain load + store for the rows only one cell touches (more latency on the same
+//     critical path, 1.08x slower), L2 prefetch of the output rows (1.07x slower).
 // An mbarrier pipeline of up to 8 stages overlaps the TMA, the MMAs and the scatter of the
 // previous unit. Every mbarrier wait is bounded: on expiry the CTA records
 // CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own TMA copies, frees its
@@ -124,14 +128,17 @@ __device__ __forceinline__ void cp_async_wait_n(int n) {
   }
 }
 
-// named barrier 2 among the 128 epilogue threads with an AND-reduction of v
+// epilogue warps: two per tensor-memory lane quarter, each draining half of the columns
+constexpr int kEpiWarps = 8;
+
+// named barrier 2 among the epilogue threads with an AND-reduction of v
 __device__ __forceinline__ bool epilogue_sync_and(bool v) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 2, 128, pi;\n"
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 2, %2, pi;\n"
       " selp.u32 %0, 1, 0, po;\n}\n"
       : "=r"(r)
-      : "r"((uint32_t)v)
+      : "r"((uint32_t)v), "n"(kEpiWarps * 32)
       : "memory");
   return r != 0;
 }
@@ -162,11 +169,11 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 //   warps 2..5    X rows: cp.async of 16-byte pieces of the hi and lo rows of the K-block's
 //                 32 dofs (dof-map entries loaded one K-block ahead) straight into the
 //                 128B-swizzled MN-major tile, `lookahead` K-blocks in flight; no conversion
-//   warps 6..9    epilogue: tcgen05.ld of a finished accumulator (lane = vector) and
+//   warps 6..13   epilogue: tcgen05.ld of a finished accumulator (lane = vector) and
 //                 red.global.add.f32 into the output rows (one 128-byte line per warp
 //                 instruction; row offsets staged in shared memory once per unit),
 //                 overlapped with the MMAs of the next unit
-constexpr int kThreads3 = 320;
+constexpr int kThreads3 = 192 + 32 * kEpiWarps;
 
 __global__ void __launch_bounds__(kThreads3, 1)
     cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
@@ -182,7 +189,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
   uint64_t* x_full = bars + 2 * S;      // [SX] 4 producer-warp arrivals (their copies landed)
   uint64_t* x_empty = bars + 2 * S + SX;   // [SX] MMA finished reading the X stage
   uint64_t* acc_full = bars + 2 * S + 2 * SX;       // [2] accumulator ready for the epilogue
-  uint64_t* acc_empty = acc_full + 2;               // [2] accumulator drained (4 warp arrivals)
+  uint64_t* acc_empty = acc_full + 2;               // [2] accumulator drained (one arrival per epilogue warp)
   uint64_t* mma_done = acc_full + 4;                // final MMA completion
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(acc_full + 6);
@@ -207,7 +214,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);   // one arrival per epilogue warp
+      mbar_init(&acc_empty[b], kEpiWarps);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -371,8 +378,11 @@ __global__ void __launch_bounds__(kThreads3, 1)
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
-    // ---------------- epilogue warps 6..9
+    // ---------------- epilogue warps 6..6 + kEpiWarps - 1
     const int q = warp & 3;                  // tensor-memory lane quarter of this warp
+    // this warp's 16-column groups of the accumulator: part (warp - 6) / 4 of kEpiWarps / 4
+    const int ng = args.n_half >> 4, part = (warp - 6) >> 2, nparts = kEpiWarps / 4;
+    const int c_beg = (ng * part / nparts) * 16, c_end = (ng * (part + 1) / nparts) * 16;
     for (int64_t it = 0; it < my_units; ++it) {
       const int buf = (int)(it & 1);
       const uint32_t ph = (uint32_t)((it >> 1) & 1);
@@ -381,20 +391,20 @@ __global__ void __launch_bounds__(kThreads3, 1)
       const Unit w = unit_at(it, first, step, args);
       const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
       const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
-      // the unit's output-row offsets (dof * ldd), staged once by the four warps; rows past
-      // nrows get an offset no lane uses (they are skipped)
+      // the unit's output-row offsets (dof * ldd), staged once by the epilogue warps; rows
+      // past nrows get an offset no lane uses (they are skipped)
       int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + buf * 256;
       if (okw)
-        for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += 128)
+        for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += kEpiWarps * 32)
           offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
-      // the four warps continue or stop together (a named barrier with an AND-reduction)
+      // the epilogue warps continue or stop together (a named barrier with an AND-reduction)
       if (!epilogue_sync_and(okw)) break;
       const int gb = w.chunk * kVec + q * 32 + lane;
       const bool vok = gb < args.B;
       float* dstb = args.dst + gb;
       const float osc = args.out_scale;
       const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
-      for (int c0 = 0; c0 < args.n_half; c0 += 16) {
+      for (int c0 = c_beg; c0 < c_end; c0 += 16) {
         float vals[16];
         tmem_ld16(tq + c0, vals);
         if (vok) {

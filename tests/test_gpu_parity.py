@@ -70,6 +70,24 @@ def test_hx_reduced_precision(chefsi, prec, p, n, B):
     assert rel(Y.double().cpu().numpy(), ref) < 2e-6
 
 
+@pytest.mark.parametrize("p,n,B", [(4, 3, 40), (6, 2, 128), (3, 1, 16)])
+def test_hx_tc_accumulates_into_owned_and_shared_rows(chefsi, p, n, B):
+    """dst += scalar * A X on the tensor path: rows owned by one cell (plain load + store)
+    and rows shared by several cells (reductions) both keep dst's previous value. n = 1 is a
+    single periodic cell whose own nodes fold onto the same dofs (no owned face rows)."""
+    pr = small_problem(n=n, L=2.0 * n, p=p, wells=2, projectors=True)
+    op, ora = gpu_op(chefsi, pr), oracle_op(pr)
+    rng = np.random.default_rng(p + n)
+    X = rng.uniform(-1, 1, (pr.n_dofs, B))
+    D = rng.uniform(-1, 1, (pr.n_dofs, B))
+    Xt = torch.from_numpy(X).float().cuda()
+    Dt = torch.from_numpy(D).float().cuda()
+    op.HX(Xt, Dt, scalar=-0.61, scaleFlag=True, precision="mixed")
+    ref = ora.HX(Xt.double().cpu().numpy(), scalar=-0.61,
+                 dst=D.astype(np.float32).astype(np.float64), accumulate=True)
+    assert rel(Dt.double().cpu().numpy(), ref) < 2e-6
+
+
 def test_hx_complex_matches_oracle(chefsi):
     pr = small_problem(n=2, L=4.0, p=3, wells=2, kpoint=[0.2, -0.1, 0.3])
     op, ora = gpu_op(chefsi, pr), oracle_op(pr)
