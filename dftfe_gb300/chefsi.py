@@ -227,6 +227,22 @@ def axpby(a: float, x: torch.Tensor, b: float, y: torch.Tensor) -> torch.Tensor:
     return y
 
 
+def copyValueType1ArrToValueType2Arr(src: torch.Tensor, dst: torch.Tensor,
+                                     scale: float = 1.0) -> torch.Tensor:
+    """dst = scale * src with precision conversion (FP32 / FP64 device blocks, 1-D or 2-D with
+    unit column stride) through the library: a power-of-two scale is exact, one rounding."""
+    bits = {torch.float32: 32, torch.float64: 64}
+    rows = src.shape[0]
+    n = 1 if src.dim() == 1 else src.shape[1]
+    lds = n if src.dim() == 1 else src.stride(0)
+    ldd = n if dst.dim() == 1 else dst.stride(0)
+    if src.dim() == 1:
+        rows, n, lds, ldd = 1, src.shape[0], src.shape[0], dst.shape[0]
+    check(_lib.load().chefsi_convert_block(bits[src.dtype], _ptr(src), lds, bits[dst.dtype],
+                                           _ptr(dst), ldd, rows, n, float(scale), _stream()))
+    return dst
+
+
 def assemble_cell_hamiltonians(shape: torch.Tensor, stiffness: torch.Tensor,
                                v_jxw: torch.Tensor) -> torch.Tensor:
     """H_c = 1/2 K + N^T diag(v_jxw_c) N for every cell, on the GPU."""

@@ -156,8 +156,7 @@ void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* 
       throw Error(CHEFSI_ERR_INVALID, "tensor-core filter HX not applicable to this block");
     s->hx_mark(st);
   };
-  split_rows_f32(X, B, M, B, hi, lo, st);
-  copy_block<float, float>(X, B, Y, B, M, B, alpha1 * alpha2, st);
+  axpby_split_f32(X, Y, M, B, alpha1 * alpha2, 0.0, hi, lo, st);   // Y = a X, split(X)
   hx(X, Y, alpha1);
   float* x = X;
   float* y = Y;
@@ -899,6 +898,29 @@ int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(x && y && rows >= 0 && n_vec >= 1 && ldx >= n_vec && ldy >= n_vec, "bad argument");
   axpby_block<double>(x, ldx, y, ldy, rows, n_vec, a, b, as_stream(stream));
+  CHEFSI_API_END
+}
+
+int chefsi_convert_block(int32_t src_bits, const void* src, int64_t ld_src, int32_t dst_bits,
+                         void* dst, int64_t ld_dst, int64_t rows, int32_t n_vec, double scale,
+                         void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(src && dst && rows >= 0 && n_vec >= 1 && ld_src >= n_vec && ld_dst >= n_vec &&
+                     (src_bits == 32 || src_bits == 64) && (dst_bits == 32 || dst_bits == 64),
+                 "bad argument");
+  cudaStream_t st = as_stream(stream);
+  if (src_bits == 64 && dst_bits == 64)
+    copy_block<double, double>(static_cast<const double*>(src), ld_src, static_cast<double*>(dst),
+                               ld_dst, rows, n_vec, scale, st);
+  else if (src_bits == 64)
+    copy_block<double, float>(static_cast<const double*>(src), ld_src, static_cast<float*>(dst),
+                              ld_dst, rows, n_vec, scale, st);
+  else if (dst_bits == 64)
+    copy_block<float, double>(static_cast<const float*>(src), ld_src, static_cast<double*>(dst),
+                              ld_dst, rows, n_vec, scale, st);
+  else
+    copy_block<float, float>(static_cast<const float*>(src), ld_src, static_cast<float*>(dst),
+                             ld_dst, rows, n_vec, scale, st);
   CHEFSI_API_END
 }
 

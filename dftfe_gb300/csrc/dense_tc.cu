@@ -31,9 +31,11 @@
 // waits (bounded) for its own copies, frees its tensor memory and returns.
 #include "internal.h"
 #include "tc_common.cuh"
+#include "pow2.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 namespace chefsi {
 
@@ -45,15 +47,20 @@ constexpr int kKB = 32;                 // halves per K-block (64-byte rows)
 constexpr int kRows8K = 128 * kKB * 2;  // one 128-row operand tile: 8 KB
 
 // ======================================================================= conversions
+// column maxima of |X| as order-preserving keys (FP32 maxima in FP32, FP64 ones on the bit
+// patterns: no FP64 arithmetic per entry)
+__device__ __forceinline__ void col_max(float x, float& m) { m = fmaxf(m, fabsf(x)); }
+__device__ __forceinline__ void col_max(double x, unsigned long long& m) { m = max(m, abs_key(x)); }
+__device__ __forceinline__ unsigned long long col_key(float m) { return abs_key((double)m); }
+__device__ __forceinline__ unsigned long long col_key(unsigned long long m) { return m; }
 template <typename T>
 __global__ void k_col_absmax(const T* __restrict__ X, int64_t ld, int64_t M, int N,
                              unsigned long long* __restrict__ out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= N) return;
-  double m = 0.0;
-  for (int64_t r = blockIdx.y; r < M; r += gridDim.y) m = fmax(m, fabs((double)X[r * ld + j]));
-  // non-negative doubles order like their bit patterns
-  atomicMax(&out[j], (unsigned long long)__double_as_longlong(m));
+  typename std::conditional<std::is_same<T, float>::value, float, unsigned long long>::type m = 0;
+  for (int64_t r = blockIdx.y; r < M; r += gridDim.y) col_max(X[r * ld + j], m);
+  atomicMax(&out[j], col_key(m));
 }
 
 // e[j]: m 2^e in [2^14, 2^15) for the column maximum m (clamped to keep 2^e a normal double);
@@ -76,10 +83,11 @@ __device__ __forceinline__ void split_half(double v, __half& h, __half& l) {
   h = __double2half(v);
   l = __double2half(v - (double)__half2float(h));
 }
-// the same split from an FP32 value (the FP32 rounding keeps 24 bits, the split 22): one
-// FP64 multiply and one FP64 -> FP32 conversion per element, the rest on the FP32 pipe
-__device__ __forceinline__ float scaled_f32(double x, double sc) { return (float)(x * sc); }
-__device__ __forceinline__ float scaled_f32(float x, double sc) { return (float)((double)x * sc); }
+// the same split from an FP32 value (the FP32 rounding keeps 24 bits, the split 22): the
+// column scale 2^e is applied exactly on the bit patterns, (float)(x 2^e) with one rounding,
+// and the split runs on the FP32 pipe
+__device__ __forceinline__ float scaled_f32(double x, int e) { return narrow_ldexp(x, e); }
+__device__ __forceinline__ float scaled_f32(float x, int e) { return ldexpf_exact(x, e); }
 __device__ __forceinline__ void split_half_f32(float v, __half& h, __half& l) {
   h = __float2half_rn(v);
   l = __float2half_rn(v - __half2float(h));
@@ -88,7 +96,7 @@ __device__ __forceinline__ void split_half_f32(float v, __half& h, __half& l) {
 // [M][N] (ld) -> hi/lo [Np][Kp] (dof index fastest), column j scaled by sc[j]; zero padding
 template <typename T>
 __global__ void __launch_bounds__(256)
-    k_split_t(const T* __restrict__ X, int64_t ld, int64_t M, int N, const double* __restrict__ sc,
+    k_split_t(const T* __restrict__ X, int64_t ld, int64_t M, int N, const int* __restrict__ ex,
               int64_t Kp, __half* __restrict__ hi, __half* __restrict__ lo) {
   __shared__ float tile[64][65];  // [column][dof]
   const int64_t k0 = (int64_t)blockIdx.x * 64;
@@ -98,7 +106,7 @@ __global__ void __launch_bounds__(256)
     const int64_t k = k0 + r;
     const int j = j0 + c;
     float v = 0.f;
-    if (k < M && j < N) v = scaled_f32(X[k * ld + j], sc[j]);
+    if (k < M && j < N) v = scaled_f32(X[k * ld + j], ex[j]);
     tile[c][r] = v;
   }
   __syncthreads();
@@ -113,24 +121,29 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// [M][N] (ld) -> hi/lo [M][Kr] (row-major, columns zero-padded to Kr), column j scaled by sc[j]
+// [M][N] (ld) -> hi/lo [M][Kr] (row-major, columns zero-padded to Kr, Kr % 4 == 0), column j
+// scaled by 2^ex[j]. A block of 256 threads covers (256 / tpr) rows x tpr quads of columns
+// (tpr = 2^log_tpr), so no index needs an integer division.
 template <typename T>
 __global__ void k_split_r(const T* __restrict__ X, int64_t ld, int64_t M, int N,
-                          const double* __restrict__ sc, int Kr, __half* __restrict__ hi,
+                          const int* __restrict__ ex, int Kr, int log_tpr, __half* __restrict__ hi,
                           __half* __restrict__ lo) {
-  const int64_t pairs = (int64_t)(Kr / 2);
-  const int64_t total = M * pairs;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / pairs;
-    const int j = (int)(t % pairs) * 2;
-    const float v0 = j < N ? scaled_f32(X[r * ld + j], sc[j]) : 0.f;
-    const float v1 = j + 1 < N ? scaled_f32(X[r * ld + j + 1], sc[j + 1]) : 0.f;
-    __half h0, l0, h1, l1;
-    split_half_f32(v0, h0, l0);
-    split_half_f32(v1, h1, l1);
-    *reinterpret_cast<__half2*>(hi + r * Kr + j) = __halves2half2(h0, h1);
-    *reinterpret_cast<__half2*>(lo + r * Kr + j) = __halves2half2(l0, l1);
+  const int tpr = 1 << log_tpr;
+  const int q0 = threadIdx.x & (tpr - 1);
+  const int rpb = blockDim.x >> log_tpr;
+  for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < M;
+       r += (int64_t)gridDim.x * rpb) {
+    const T* xr = X + r * ld;
+    for (int q = q0; q < Kr / 4; q += tpr) {
+      const int j = 4 * q;
+      __half h[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split_half_f32(j + i < N ? scaled_f32(xr[j + i], ex[j + i]) : 0.f, h[i], l[i]);
+      __half2 hv[2] = {__halves2half2(h[0], h[1]), __halves2half2(h[2], h[3])};
+      __half2 lv[2] = {__halves2half2(l[0], l[1]), __halves2half2(l[2], l[3])};
+      *reinterpret_cast<uint2*>(hi + r * Kr + j) = *reinterpret_cast<const uint2*>(hv);
+      *reinterpret_cast<uint2*>(lo + r * Kr + j) = *reinterpret_cast<const uint2*>(lv);
+    }
   }
 }
 
@@ -615,7 +628,7 @@ void tc_split_transposed(const T* X, int64_t ld, int64_t M, int N, TcOperand& op
   op.lo.ensure(n);
   CHEFSI_REQUIRE(op.ld / 64 < (1ll << 31), "tensor-core split: too many rows");
   dim3 grid((unsigned)(op.ld / 64), (unsigned)(op.padded / 64));
-  k_split_t<T><<<grid, 256, 0, st>>>(X, ld, M, N, op.sc.ptr, op.ld, op.hi.ptr, op.lo.ptr);
+  k_split_t<T><<<grid, 256, 0, st>>>(X, ld, M, N, op.e.ptr, op.ld, op.hi.ptr, op.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -629,8 +642,11 @@ void tc_split_rows(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cuda
   const size_t n = (size_t)M * op.ld;
   op.hi.ensure(n);
   op.lo.ensure(n);
-  k_split_r<T><<<grid_for(M * (op.ld / 2), 256), 256, 0, st>>>(X, ld, M, N, op.sc.ptr, (int)op.ld,
-                                                                op.hi.ptr, op.lo.ptr);
+  int log_tpr = 0;
+  while (log_tpr < 8 && (1 << log_tpr) < op.ld / 4) ++log_tpr;
+  const int rpb = 256 >> log_tpr;
+  k_split_r<T><<<grid_for((M + rpb - 1) / rpb, 1), 256, 0, st>>>(X, ld, M, N, op.e.ptr, (int)op.ld,
+                                                                  log_tpr, op.hi.ptr, op.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
 }
 

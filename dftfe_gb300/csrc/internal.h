@@ -96,7 +96,7 @@ bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, co
                  cudaStream_t st);
 void split_rows_f32(const float* x, int64_t ldx, int64_t M, int B, __half* hi, __half* lo,
                     cudaStream_t st);
-// y = a x + b y on contiguous [M][B] blocks and (hi, lo) = split(x)
+// y = a x + b y on contiguous [M][B] blocks (b == 0: y is not read) and (hi, lo) = split(x)
 void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, double b, __half* hi,
                      __half* lo, cudaStream_t st);
 // W[a][j][b] = sum_r C[r][j] x[dof_r][b] for FP32 vectors (W zeroed here)

@@ -10,7 +10,9 @@
 // has no constraint rows (periodicity folded into the map), M^{-1/2} is folded into the cell
 // matrices and projectors at creation, so HX needs no scaling passes.
 #include "internal.h"
+#include "pow2.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -309,17 +311,6 @@ __global__ void k_finish(const T* __restrict__ y, int64_t ldy, T* __restrict__ d
 }
 
 template <typename T>
-__global__ void k_scale(T* x, int64_t ld, int64_t rows, int B, double s) {
-  const int64_t n = rows * B;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / B;
-    const int b = (int)(t % B);
-    x[i * ld + b] = (s == 0.0) ? Tr<T>::zero() : Tr<T>::scale(s, x[i * ld + b]);
-  }
-}
-
-template <typename T>
 __global__ void k_axpby(const T* __restrict__ x, int64_t ldx, T* __restrict__ y, int64_t ldy,
                         int64_t rows, int B, double a, double b_) {
   const int64_t n = rows * B;
@@ -331,47 +322,179 @@ __global__ void k_axpby(const T* __restrict__ x, int64_t ldx, T* __restrict__ y,
   }
 }
 
-template <typename Ts, typename Td>
-__global__ void k_copy(const Ts* __restrict__ src, int64_t lds, Td* __restrict__ dst, int64_t ldd,
-                       int64_t rows, int B, double s) {
-  const int64_t n = rows * B;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / B;
-    const int b = (int)(t % B);
-    dst[i * ldd + b] = (Td)(s * (double)src[i * lds + b]);
-  }
+// ---- streaming block kernels: dst = s * src (with precision conversion), x *= s, max |x|.
+// A scale s = 2^k is applied exactly on the bit patterns (pow2.cuh); any other s multiplies in
+// the destination's precision. Contiguous blocks run as flat float4-wide passes; strided
+// blocks run rows x columns with no integer division per entry (tpr threads per row, a
+// power of two).
+struct Scale {
+  double s;
+  int k;     // s == 2^k when p2
+  bool p2;
+};
+inline Scale make_scale(double s) {
+  Scale r{s, 0, false};
+  int e = 0;
+  const double f = std::frexp(s, &e);
+  if (f == 0.5 && e - 1 >= -1000 && e - 1 <= 1000) r.k = e - 1, r.p2 = true;
+  return r;
 }
-template <>
-__global__ void k_copy<cplx, cplx>(const cplx* __restrict__ src, int64_t lds, cplx* __restrict__ dst,
-                                   int64_t ldd, int64_t rows, int B, double s) {
-  const int64_t n = rows * B;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / B;
-    const int b = (int)(t % B);
-    const cplx v = src[i * lds + b];
-    dst[i * ldd + b] = {s * v.x, s * v.y};
+template <typename Ts, typename Td> struct Conv;
+template <> struct Conv<float, float> {
+  __device__ static float f(float x, const Scale& c) {
+    return c.p2 ? ldexpf_exact(x, c.k) : (float)c.s * x;
+  }
+};
+template <> struct Conv<double, float> {
+  __device__ static float f(double x, const Scale& c) {
+    return c.p2 ? narrow_ldexp(x, c.k) : (float)(c.s * x);
+  }
+};
+template <> struct Conv<float, double> {
+  __device__ static double f(float x, const Scale& c) {
+    return c.p2 ? widen_ldexp(x, c.k) : c.s * widen_ldexp(x, 0);
+  }
+};
+template <> struct Conv<double, double> {
+  __device__ static double f(double x, const Scale& c) { return c.p2 ? ldexp_exact(x, c.k) : c.s * x; }
+};
+template <> struct Conv<cplx, cplx> {
+  __device__ static cplx f(cplx x, const Scale& c) {
+    return {Conv<double, double>::f(x.x, c), Conv<double, double>::f(x.y, c)};
+  }
+};
+
+// four consecutive entries as one or two 16-byte accesses
+template <typename T> struct Quad { T v[4]; };
+template <typename T>
+__device__ __forceinline__ Quad<T> load_quad(const T* p) {
+  Quad<T> q;
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    q.v[0] = a.x, q.v[1] = a.y, q.v[2] = a.z, q.v[3] = a.w;
+  } else if constexpr (sizeof(T) == 8) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    q.v[0] = a.x, q.v[1] = a.y, q.v[2] = b.x, q.v[3] = b.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q.v[i] = p[i];
+  }
+  return q;
+}
+template <typename T>
+__device__ __forceinline__ void store_quad(T* p, const Quad<T>& q) {
+  if constexpr (sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
+  } else if constexpr (sizeof(T) == 8) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(q.v[0], q.v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(q.v[2], q.v[3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] = q.v[i];
   }
 }
 
-__global__ void k_absmax(const double* __restrict__ x, int64_t ld, int64_t rows, int B,
-                         unsigned long long* out) {
-  const int64_t n = rows * B;
-  double m = 0.0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+// flat pass over n entries (n % 4 == 0, both pointers 16-byte aligned)
+template <typename Ts, typename Td>
+__global__ void k_copy_flat(const Ts* __restrict__ src, Td* __restrict__ dst, int64_t n4, Scale c) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / B;
-    const int b = (int)(t % B);
-    m = fmax(m, fabs(x[i * ld + b]));
+    const Quad<Ts> a = load_quad(src + 4 * t);
+    Quad<Td> b;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) b.v[i] = Conv<Ts, Td>::f(a.v[i], c);
+    store_quad(dst + 4 * t, b);
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+// strided rows: block of 256 threads = (256 / tpr) rows x tpr columns
+template <typename Ts, typename Td>
+__global__ void k_copy_strided(const Ts* __restrict__ src, int64_t lds, Td* __restrict__ dst,
+                            int64_t ldd, int64_t rows, int B, int log_tpr, Scale c) {
+  const int tpr = 1 << log_tpr;
+  const int col0 = threadIdx.x & (tpr - 1);
+  const int rpb = blockDim.x >> log_tpr;
+  for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < rows;
+       r += (int64_t)gridDim.x * rpb)
+    for (int j = col0; j < B; j += tpr) dst[r * ldd + j] = Conv<Ts, Td>::f(src[r * lds + j], c);
+}
+
+template <typename T>
+__global__ void k_scale_flat(T* __restrict__ x, int64_t n4, Scale c, bool zero) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    Quad<T> a;
+    if (zero) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a.v[i] = Tr<T>::zero();
+    } else {
+      a = load_quad(x + 4 * t);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a.v[i] = Conv<T, T>::f(a.v[i], c);
+    }
+    store_quad(x + 4 * t, a);
+  }
+}
+template <typename T>
+__global__ void k_scale_strided(T* __restrict__ x, int64_t ld, int64_t rows, int B, int log_tpr,
+                                Scale c, bool zero) {
+  const int tpr = 1 << log_tpr;
+  const int col0 = threadIdx.x & (tpr - 1);
+  const int rpb = blockDim.x >> log_tpr;
+  for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < rows;
+       r += (int64_t)gridDim.x * rpb)
+    for (int j = col0; j < B; j += tpr)
+      x[r * ld + j] = zero ? Tr<T>::zero() : Conv<T, T>::f(x[r * ld + j], c);
+}
+
+// max |x| as the largest key of |x| (non-negative doubles order like their bit patterns)
+__device__ __forceinline__ void absmax_commit(unsigned long long m, unsigned long long* out) {
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+__global__ void k_absmax_flat(const double* __restrict__ x, int64_t n4, unsigned long long* out) {
+  unsigned long long m = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const Quad<double> q = load_quad(x + 4 * t);
+    m = max(m, max(max(abs_key(q.v[0]), abs_key(q.v[1])), max(abs_key(q.v[2]), abs_key(q.v[3]))));
+  }
+  absmax_commit(m, out);
+}
+__global__ void k_absmax_strided(const double* __restrict__ x, int64_t ld, int64_t rows, int B,
+                              int log_tpr, unsigned long long* out) {
+  const int tpr = 1 << log_tpr;
+  const int col0 = threadIdx.x & (tpr - 1);
+  const int rpb = blockDim.x >> log_tpr;
+  unsigned long long m = 0;
+  for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < rows;
+       r += (int64_t)gridDim.x * rpb)
+    for (int j = col0; j < B; j += tpr) m = max(m, abs_key(x[r * ld + j]));
+  absmax_commit(m, out);
+}
+
+// threads per row for the strided kernels: the power of two >= B, at most 256
+inline int log_threads_per_row(int B) {
+  int l = 0;
+  while (l < 8 && (1 << l) < B) ++l;
+  return l;
+}
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+inline int rows_grid(int64_t rows, int log_tpr) {
+  return grid_for((rows + (256 >> log_tpr) - 1) / (256 >> log_tpr), 1);
 }
 
 template <typename T>
 void scale_block(T* x, int64_t ld, int64_t rows, int B, double s, cudaStream_t st) {
-  k_scale<T><<<grid_for(rows * B, 256), 256, 0, st>>>(x, ld, rows, B, s);
+  if (rows <= 0 || B <= 0) return;
+  const Scale c = make_scale(s);
+  const int64_t n = rows * B;
+  if ((ld == B || rows == 1) && n % 4 == 0 && aligned16(x)) {
+    k_scale_flat<T><<<grid_for(n / 4, 256), 256, 0, st>>>(x, n / 4, c, s == 0.0);
+  } else {
+    const int l = log_threads_per_row(B);
+    k_scale_strided<T><<<rows_grid(rows, l), 256, 0, st>>>(x, ld, rows, B, l, c, s == 0.0);
+  }
   CHEFSI_CHECK_LAUNCH();
 }
 template void scale_block<double>(double*, int64_t, int64_t, int, double, cudaStream_t);
@@ -394,7 +517,15 @@ template void axpby_block<cplx>(const cplx*, int64_t, cplx*, int64_t, int64_t, i
 template <typename Ts, typename Td>
 void copy_block(const Ts* src, int64_t lds, Td* dst, int64_t ldd, int64_t rows, int B, double s,
                 cudaStream_t st) {
-  k_copy<Ts, Td><<<grid_for(rows * B, 256), 256, 0, st>>>(src, lds, dst, ldd, rows, B, s);
+  if (rows <= 0 || B <= 0) return;
+  const Scale c = make_scale(s);
+  const int64_t n = rows * B;
+  if (((lds == B && ldd == B) || rows == 1) && n % 4 == 0 && aligned16(src) && aligned16(dst)) {
+    k_copy_flat<Ts, Td><<<grid_for(n / 4, 256), 256, 0, st>>>(src, dst, n / 4, c);
+  } else {
+    const int l = log_threads_per_row(B);
+    k_copy_strided<Ts, Td><<<rows_grid(rows, l), 256, 0, st>>>(src, lds, dst, ldd, rows, B, l, c);
+  }
   CHEFSI_CHECK_LAUNCH();
 }
 template void copy_block<double, double>(const double*, int64_t, double*, int64_t, int64_t, int,
@@ -411,8 +542,15 @@ template void copy_block<cplx, cplx>(const cplx*, int64_t, cplx*, int64_t, int64
 void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
                       cudaStream_t st) {
   CHEFSI_CUDA(cudaMemsetAsync(out_dev, 0, sizeof(double), st));
-  k_absmax<<<grid_for(rows * B, 256, kNumSMs * 8), 256, 0, st>>>(
-      x, ld, rows, B, reinterpret_cast<unsigned long long*>(out_dev));
+  if (rows <= 0 || B <= 0) return;
+  unsigned long long* out = reinterpret_cast<unsigned long long*>(out_dev);
+  const int64_t n = rows * B;
+  if ((ld == B || rows == 1) && n % 4 == 0 && aligned16(x)) {
+    k_absmax_flat<<<grid_for(n / 4, 256, kNumSMs * 8), 256, 0, st>>>(x, n / 4, out);
+  } else {
+    const int l = log_threads_per_row(B);
+    k_absmax_strided<<<std::min(rows_grid(rows, l), kNumSMs * 8), 256, 0, st>>>(x, ld, rows, B, l, out);
+  }
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -495,86 +633,21 @@ void hx_f32(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
                     accumulate, st, cell_f32);
 }
 
-// W[a][j][b0..b0+128) = sum over all rows of atom a of C[r][j] x[dof_r][b]: one CTA per
-// (atom, 128-vector tile), 8 warps take interleaved rows (float4 loads, 4 vectors per lane),
-// partial sums reduced in shared memory -- no atomics.
-__global__ void __launch_bounds__(256)
-    nl_project_atom(const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
-                    const float* __restrict__ C, int P, const float* __restrict__ src, int64_t lds,
-                    float* __restrict__ W, int B) {
-  __shared__ float4 red[8][kMaxProj][32];
-  const int a = blockIdx.x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.y * 128 + lane * 4;
-  const int r0 = atom_ptr[a], r1 = atom_ptr[a + 1];
-  float4 acc[kMaxProj];
-#pragma unroll
-  for (int j = 0; j < kMaxProj; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (b < B) {
-    int r = r0 + warp;
-    for (; r + 24 < r1; r += 32) {
-      float4 x[4];
-      int rr[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        rr[u] = r + 8 * u;
-        x[u] = __ldg(reinterpret_cast<const float4*>(src + (int64_t)__ldg(dofs + rr[u]) * lds + b));
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int j = 0; j < kMaxProj; ++j) {
-          if (j >= P) break;
-          const float cv = __ldg(C + (size_t)rr[u] * P + j);
-          acc[j].x = fmaf(cv, x[u].x, acc[j].x);
-          acc[j].y = fmaf(cv, x[u].y, acc[j].y);
-          acc[j].z = fmaf(cv, x[u].z, acc[j].z);
-          acc[j].w = fmaf(cv, x[u].w, acc[j].w);
-        }
-    }
-    for (; r < r1; r += 8) {
-      const float4 x = __ldg(reinterpret_cast<const float4*>(src + (int64_t)__ldg(dofs + r) * lds + b));
-#pragma unroll
-      for (int j = 0; j < kMaxProj; ++j) {
-        if (j >= P) break;
-        const float cv = __ldg(C + (size_t)r * P + j);
-        acc[j].x = fmaf(cv, x.x, acc[j].x);
-        acc[j].y = fmaf(cv, x.y, acc[j].y);
-        acc[j].z = fmaf(cv, x.z, acc[j].z);
-        acc[j].w = fmaf(cv, x.w, acc[j].w);
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < kMaxProj; ++j)
-    if (j < P) red[warp][j][lane] = acc[j];
-  __syncthreads();
-  // 256 threads reduce P x 32 float4 across the 8 warps
-  for (int idx = threadIdx.x; idx < P * 32; idx += 256) {
-    const int j = idx / 32, l = idx % 32;
-    float4 sum = red[0][j][l];
-    for (int w2 = 1; w2 < 8; ++w2) {
-      const float4 v = red[w2][j][l];
-      sum.x += v.x, sum.y += v.y, sum.z += v.z, sum.w += v.w;
-    }
-    const int bb = blockIdx.y * 128 + l * 4;
-    if (bb < B) *reinterpret_cast<float4*>(&W[((size_t)a * P + j) * B + bb]) = sum;
-  }
-}
-
 // W[a][j][b] += sum over one kNlChunk-row chunk of atom a of C[r][j] x[dof_r][b]: one CTA per
 // (row chunk, 128-vector tile). The chunk's C rows and dofs are staged in shared memory, the 8
-// warps take interleaved rows with 8 gathered float4 loads in flight per lane, the warps'
+// warps take interleaved rows with U gathered float4 loads in flight per lane, the warps'
 // partial sums are reduced in shared memory and added to W with one float4 atomic per
 // (projector, lane). Many more CTAs than atoms x tiles, so the gather has enough loads in
-// flight to approach the memory bandwidth.
-__global__ void __launch_bounds__(256)
+// flight to approach the memory bandwidth. PP >= P is the compile-time projector capacity: the
+// accumulators are PP float4 registers, so a small PP keeps four CTAs resident per SM.
+template <int PP, int U>
+__global__ void __launch_bounds__(256, PP <= 8 ? 4 : 2)
     nl_project_chunk4(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
                       const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
                       const float* __restrict__ C, int P, const float* __restrict__ src,
                       int64_t lds, float* __restrict__ W, int B) {
   extern __shared__ float4 red_dyn[];                 // [8][P][32]
-  __shared__ float Cs[kNlChunk * kMaxProj];
+  __shared__ float Cs[kNlChunk * PP];
   __shared__ int Ds[kNlChunk];
   const int ch = blockIdx.x;
   const int a = chunk_atom[ch];
@@ -585,20 +658,20 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int b = blockIdx.y * 128 + lane * 4;
-  float4 acc[kMaxProj];
+  float4 acc[PP];
 #pragma unroll
-  for (int j = 0; j < kMaxProj; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j = 0; j < PP; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (b < B) {
     int r = warp;
-    for (; r + 56 < nr; r += 64) {
-      float4 xv[8];
+    for (; r + 8 * (U - 1) < nr; r += 8 * U) {
+      float4 xv[U];
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < U; ++u)
         xv[u] = __ldg(reinterpret_cast<const float4*>(src + (int64_t)Ds[r + 8 * u] * lds + b));
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int j = 0; j < kMaxProj; ++j) {
+        for (int j = 0; j < PP; ++j) {
           if (j >= P) break;
           const float cv = Cs[(r + 8 * u) * P + j];
           acc[j].x = fmaf(cv, xv[u].x, acc[j].x);
@@ -610,7 +683,7 @@ __global__ void __launch_bounds__(256)
     for (; r < nr; r += 8) {
       const float4 xv = __ldg(reinterpret_cast<const float4*>(src + (int64_t)Ds[r] * lds + b));
 #pragma unroll
-      for (int j = 0; j < kMaxProj; ++j) {
+      for (int j = 0; j < PP; ++j) {
         if (j >= P) break;
         const float cv = Cs[r * P + j];
         acc[j].x = fmaf(cv, xv.x, acc[j].x);
@@ -621,7 +694,7 @@ __global__ void __launch_bounds__(256)
     }
   }
 #pragma unroll
-  for (int j = 0; j < kMaxProj; ++j)
+  for (int j = 0; j < PP; ++j)
     if (j < P) red_dyn[(warp * P + j) * 32 + lane] = acc[j];
   __syncthreads();
   for (int t = threadIdx.x; t < P * 32; t += blockDim.x) {
@@ -636,19 +709,31 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <int PP, int U>
+static void launch_nl_project_chunk4(chefsi_operator_s* op, const float* x, int64_t ldx, float* W,
+                                     int B, cudaStream_t st) {
+  dim3 grid(op->nl_n_chunks, (B + 127) / 128);
+  const size_t red = sizeof(float4) * 8 * op->n_proj * 32;
+  CHEFSI_CUDA(cudaFuncSetAttribute(nl_project_chunk4<PP, U>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(float4) * 8 * PP * 32)));
+  nl_project_chunk4<PP, U><<<grid, 256, red, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
+                                                   op->nl_ptr.ptr, op->nl_dofs.ptr,
+                                                   op->nl_vals32.ptr, op->n_proj, x, ldx, W, B);
+}
+
 void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
                     cudaStream_t st) {
   if (op->n_atoms == 0) return;
   const bool vec = (B % 4 == 0) && (ldx % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
   if (vec) {
     CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * (size_t)op->n_atoms * op->n_proj * B, st));
-    dim3 grid(op->nl_n_chunks, (B + 127) / 128);
-    const size_t red = sizeof(float4) * 8 * op->n_proj * 32;
-    CHEFSI_CUDA(cudaFuncSetAttribute(nl_project_chunk4, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(sizeof(float4) * 8 * kMaxProj * 32)));
-    nl_project_chunk4<<<grid, 256, red, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
-                                              op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
-                                              op->n_proj, x, ldx, W, B);
+    if (op->n_proj <= 4)
+      launch_nl_project_chunk4<4, 8>(op, x, ldx, W, B, st);
+    else if (op->n_proj <= 8)
+      launch_nl_project_chunk4<8, 4>(op, x, ldx, W, B, st);
+    else
+      launch_nl_project_chunk4<kMaxProj, 4>(op, x, ldx, W, B, st);
   } else {
     CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * (size_t)op->n_atoms * op->n_proj * B, st));
     const int threads = 128;
@@ -660,13 +745,16 @@ void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W
   CHEFSI_CHECK_LAUNCH();
 }
 
-// y[dof_r][b..b+3] += scalar * sum_j C[r][j] V[a][j] W[a][j][b..b+3] (float4 atomics)
-__global__ void nl_apply_v4(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
-                            const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
-                            const float* __restrict__ C, int P, const double* __restrict__ V,
-                            const float* __restrict__ W, float* __restrict__ dst, int64_t ldd,
-                            int B, double scalar) {
-  __shared__ float Cs[kNlChunk * kMaxProj];
+// y[dof_r][b..b+3] += scalar * sum_j C[r][j] V[a][j] W[a][j][b..b+3] (float4 atomics); PP >= P
+// is the compile-time projector capacity (PP float4 registers of scaled W per thread)
+template <int PP>
+__global__ void __launch_bounds__(128, PP <= 8 ? 8 : 4)
+    nl_apply_v4(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
+                const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
+                const float* __restrict__ C, int P, const double* __restrict__ V,
+                const float* __restrict__ W, float* __restrict__ dst, int64_t ldd, int B,
+                float scalar) {
+  __shared__ float Cs[kNlChunk * PP];
   __shared__ int Ds[kNlChunk];
   const int ch = blockIdx.x;
   const int a = chunk_atom[ch];
@@ -678,18 +766,18 @@ __global__ void nl_apply_v4(const int* __restrict__ chunk_atom, const int* __res
   __syncthreads();
   const int b = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
   if (b >= B) return;
-  float4 w[kMaxProj];
+  float4 w[PP];
 #pragma unroll
-  for (int j = 0; j < kMaxProj; ++j) {
+  for (int j = 0; j < PP; ++j) {
     if (j >= P) break;
-    const float f = (float)(scalar * V[(size_t)a * P + j]);
+    const float f = scalar * (float)V[(size_t)a * P + j];
     const float4 x = *reinterpret_cast<const float4*>(&W[((size_t)a * P + j) * B + b]);
     w[j] = make_float4(f * x.x, f * x.y, f * x.z, f * x.w);
   }
   for (int r = 0; r < nr; ++r) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int j = 0; j < kMaxProj; ++j) {
+    for (int j = 0; j < PP; ++j) {
       if (j >= P) break;
       const float cv = Cs[r * P + j];
       acc.x = fmaf(cv, w[j].x, acc.x);
@@ -715,9 +803,17 @@ void apply_nonlocal_f32(chefsi_operator_s* op, const float* src, int64_t lds, fl
   nl_project_f32(op, src, lds, W, B, st);
   const int threads = 128;
   dim3 grid(op->nl_n_chunks, (B / 4 + threads - 1) / threads);
-  nl_apply_v4<<<grid, threads, 0, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
-                                        op->nl_ptr.ptr, op->nl_dofs.ptr, op->nl_vals32.ptr,
-                                        op->n_proj, op->couplings.ptr, W, dst, ldd, B, scalar);
+  auto launch = [&](auto kernel) {
+    kernel<<<grid, threads, 0, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr, op->nl_ptr.ptr,
+                                     op->nl_dofs.ptr, op->nl_vals32.ptr, op->n_proj,
+                                     op->couplings.ptr, W, dst, ldd, B, (float)scalar);
+  };
+  if (op->n_proj <= 4)
+    launch(nl_apply_v4<4>);
+  else if (op->n_proj <= 8)
+    launch(nl_apply_v4<8>);
+  else
+    launch(nl_apply_v4<kMaxProj>);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -482,14 +482,16 @@ __global__ void k_split_rows(const float* __restrict__ x, int64_t ldx, int64_t M
   }
 }
 
-// y = a x + b y on a contiguous [M][B] block, and (hi, lo) = split(x) (the step of the
-// Chebyshev recurrence that reads the vector the next HX multiplies)
+// y = a x + b y on a contiguous [M][B] block (b == 0: y = a x, y not read), and
+// (hi, lo) = split(x) (the step of the Chebyshev recurrence that reads the vector the next HX
+// multiplies)
 __global__ void k_axpby_split(const float* __restrict__ x, float* __restrict__ y, int64_t n,
                               float a, float b, __half* __restrict__ hi, __half* __restrict__ lo) {
+  const bool read_y = b != 0.f;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
        t += (int64_t)gridDim.x * blockDim.x) {
     const float4 xv = reinterpret_cast<const float4*>(x)[t];
-    float4 yv = reinterpret_cast<float4*>(y)[t];
+    float4 yv = read_y ? reinterpret_cast<float4*>(y)[t] : make_float4(0.f, 0.f, 0.f, 0.f);
     yv.x = a * xv.x + b * yv.x;
     yv.y = a * xv.y + b * yv.y;
     yv.z = a * xv.z + b * yv.z;

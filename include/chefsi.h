@@ -198,6 +198,17 @@ int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, dou
 int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,
                  double* y, int64_t ldy, void* stream);
 
+/* dst = scale * src with precision conversion on [rows][n_vec] device blocks (leading
+   dimensions ld_src, ld_dst); src_bits / dst_bits = 32 (FP32) or 64 (FP64). A power-of-two
+   scale is applied exactly and the result rounded once to the destination type; any other
+   scale multiplies in the destination's precision.
+   Replaces dftfe::utils::deviceKernelsGeneric::copyValueType1ArrToValueType2Arr
+   (include/deviceKernelsGeneric.h:53) and the scaled block copies of the mixed-precision
+   filter. */
+int chefsi_convert_block(int32_t src_bits, const void* src, int64_t ld_src, int32_t dst_bits,
+                         void* dst, int64_t ld_dst, int64_t rows, int32_t n_vec, double scale,
+                         void* stream);
+
 /* C = alpha op(A) op(B) + beta C, row-major device matrices, op = 'N' or 'T'. FP64, or FP32
    products with FP64 accumulation across K chunks (CHEFSI_PREC_MIXED / FP32). */
 int chefsi_gemm(char ta, char tb, int64_t M, int32_t N, int32_t K, double alpha, const double* A,
