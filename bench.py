@@ -522,7 +522,7 @@ def main():
     ap.add_argument("--hx-only", action="store_true",
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--rr-precision", default="fp32", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
     ap.add_argument("--fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -20,8 +20,8 @@ CHEFSI_ERR_TIMEOUT = 6
 CHEFSI_ERR_NAN = 7
 CHEFSI_ERR_UNSUPPORTED = 8
 
-PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "fp32": PREC_FP32}
+PREC_FP64, PREC_MIXED, PREC_FP32, PREC_FP32_TC = 0, 1, 2, 3
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "fp32": PREC_FP32, "fp32tc": PREC_FP32_TC}
 
 _ERRNAMES = {1: "INVALID", 2: "CUDA", 3: "NOT_SPD", 4: "NO_CONVERGENCE", 5: "ALLOC",
              6: "TIMEOUT", 7: "NAN", 8: "UNSUPPORTED"}

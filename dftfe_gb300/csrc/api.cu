@@ -361,27 +361,35 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   // X is rounded to FP32 once and the same rounded basis enters S (the mixed Gram converts on
   // load), HX and Hp, so the generalised problem stays consistent.
   double* HX = s->HX.ensure((size_t)M * N);
-  // rr_precision MIXED: the tensor-core (FP16-split) apply on X rounded to FP32 and scaled by
-  // a power of two into the split's range; FP32: the FP32 SIMT apply
-  const bool hxtc = is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_MIXED &&
-                    tc_split_usable(op, N);
-  const bool hx32 = is_mixed(prec) && (s->p.rr_precision == CHEFSI_PREC_FP32 || hxtc);
+  // rr_precision FP32_TC: X rounded to FP32 and applied with the three-term tensor-core split
+  // (exact FP32 operands, six products, FP32 accumulation; the FP32 SIMT apply where the tensor
+  // path does not apply). FP32: the FP32 SIMT apply. MIXED: the filter's two-term split (22
+  // bits). The tensor paths scale X by a power of two into the split's range.
+  const int rrp = s->p.rr_precision;
+  const bool tc3 = is_mixed(prec) && rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(op, N);
+  const bool tc2 = is_mixed(prec) && rrp == CHEFSI_PREC_MIXED && tc_split_usable(op, N);
+  const bool hx32 = is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC || tc2);
   float* y32 = nullptr;
   if (hx32) {
     float* x32 = s->Xb32.ensure((size_t)M * N);
     y32 = s->Yb32.ensure((size_t)M * N);
     double scale = 1.0;
-    if (hxtc) {
+    if (tc2 || tc3) {
       double* sc = s->scal.ensure(1);
       absmax_block_f64(X, ld, M, N, sc, st);
       double amax = 0.0;
       CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
       CHEFSI_CUDA(cudaStreamSynchronize(st));
-      if (amax > 0.0 && std::isfinite(amax)) scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, (tc3 ? 14 : 8) - (int)std::ceil(std::log2(amax)));
     }
     copy_block<double, float>(X, ld, x32, N, M, N, scale, st);
-    if (!(hxtc && hx_tc(op, x32, N, y32, N, N, 1.0 / scale, false, st)))
-      hx_f32(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    bool done = false;
+    if (tc3)
+      done = hx_tc3(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    else if (tc2)
+      done = hx_tc(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    if (!done) hx_f32(op, x32, N, y32, N, N, 1.0 / scale, false, st);
     // the tensor-core path reads the FP32 HX directly; its rotation writes the FP64 HX
     if (!tcd) copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
   } else {
@@ -518,15 +526,28 @@ int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, in
   }
   trtri_lower_c(S, N, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
-  // HX: FP64 complex, or (mixed with rr_precision FP32 on a folded operator) the FP32 apply
-  // of the real form on X rounded to FP32
+  // HX: FP64 complex, or (mixed with rr_precision FP32 / FP32_TC on a folded operator) the
+  // FP32 SIMT / three-term tensor-core apply of the real form on X rounded to FP32
   cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
-  if (is_mixed(prec) && s->p.rr_precision == CHEFSI_PREC_FP32 && op->folded) {
+  const int rrp = s->p.rr_precision;
+  if (is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC) && op->folded) {
     chefsi_operator_s* rv = realified(op, st);
     float* xr = s->Xb32.ensure((size_t)2 * M * N);
     float* yr = s->Yb32.ensure((size_t)2 * M * N);
-    complex_to_real_rows(X, ld, M, N, 1.0, xr, st);
-    hx_f32(rv, xr, N, yr, N, N, 1.0, false, st);
+    const bool tc3 = rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(rv, N);
+    double scale = 1.0;
+    if (tc3) {
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(reinterpret_cast<const double*>(X), 2 * ld, M, 2 * N, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, 14 - (int)std::ceil(std::log2(amax)));
+    }
+    complex_to_real_rows(X, ld, M, N, scale, xr, st);
+    if (!(tc3 && hx_tc3(rv, xr, N, yr, N, N, 1.0 / scale, false, st)))
+      hx_f32(rv, xr, N, yr, N, N, 1.0 / scale, false, st);
     real_rows_to_complex(yr, M, N, 1.0, HX, N, st);
   } else {
     const int Bmax = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
@@ -666,6 +687,30 @@ int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, in
     if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   } else if (precision == CHEFSI_PREC_FP32) {
     hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+  } else if (precision == CHEFSI_PREC_FP32_TC) {
+    // the three-term split wants max |src| < 2^15: a power-of-two scaled copy of src (undone
+    // through the scalar); the SIMT FP32 apply where the tensor path does not apply
+    const float* x = static_cast<const float*>(src);
+    bool done = false;
+    if (tc_split_usable(op, n_vec) && ld_dst % 4 == 0 &&
+        (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+      DeviceBuffer<double> sc(1);
+      absmax_block_f32(x, ld_src, op->n_dofs, n_vec, sc.ptr, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      const double scale = (amax > 0.0 && std::isfinite(amax))
+                               ? std::ldexp(1.0, 14 - (int)std::ceil(std::log2(amax)))
+                               : 1.0;
+      const int64_t ldx = (n_vec + 3) / 4 * 4;
+      float* xs = op->ws32x.ensure((size_t)op->n_dofs * ldx);
+      copy_block<float, float>(x, ld_src, xs, ldx, op->n_dofs, n_vec, scale, st);
+      done = hx_tc3(op, xs, ldx, (float*)dst, ld_dst, n_vec, scalar / scale, accumulate != 0, st);
+    }
+    if (!done)
+      hx_f32(op, x, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+    const int tc = tc_check_error(op, st);
+    if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   } else {
     throw Error(CHEFSI_ERR_INVALID, "unknown precision");
   }

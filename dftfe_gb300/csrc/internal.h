@@ -26,10 +26,12 @@ __device__ __forceinline__ cplx cscale(cplx a, double s) { return {a.x * s, a.y 
 // one 64-byte-swizzled operand tile.
 struct TensorCellMats {
   DeviceBuffer<__half> hi, lo;
+  DeviceBuffer<__half> lo3;  // third term of the three-term split (built on first use)
   int npad = 0;
   int kpad = 0;
   float scale = 1.f;   // power of two applied before the split
   bool ready = false;
+  bool lo3_ready = false;
 };
 
 }  // namespace chefsi
@@ -63,7 +65,7 @@ struct chefsi_operator_s {
 
 
   chefsi::DeviceBuffer<int> tc_err;       // timeout flag of the tensor-core kernel
-  chefsi::DeviceBuffer<__half> xs_hi, xs_lo;  // FP16 split of the HX input (chefsi_hx path)
+  chefsi::DeviceBuffer<__half> xs_hi, xs_lo, xs_lo3;  // FP16 split of the HX input (chefsi_hx path)
 
   // real form of a complex operator (2 n_dofs real unknowns, 2 n_e x 2 n_e real cell
   // matrices) for the FP32 / tensor-core filter; built on first use
@@ -71,7 +73,7 @@ struct chefsi_operator_s {
 
   // workspaces (grow-only)
   chefsi::DeviceBuffer<double> ws64a, ws64b, nlW64;
-  chefsi::DeviceBuffer<float> nlW32;
+  chefsi::DeviceBuffer<float> nlW32, ws32x;
 };
 
 namespace chefsi {
@@ -87,6 +89,11 @@ void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int6
 // tensor-core (FP16 split) apply on FP32 vectors; returns false if unavailable for this op
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st);
+// the same with the three-term split (33 bits: src exactly, the cell matrices to 2^-33; six
+// products, FP32 accumulation): the accuracy class of the FP32 apply. src must be scaled so
+// that max |src| < 2^15.
+bool hx_tc3(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+            double scalar, bool accumulate, cudaStream_t st);
 bool tc_usable(chefsi_operator_s* op);
 // the tensor-core apply reads the input as FP16 hi + lo rows [n_dofs][B] (B % 8 == 0);
 // src (FP32) feeds the nonlocal term
@@ -122,6 +129,8 @@ void copy_block(const Ts* src, int64_t lds, Td* dst, int64_t ldd, int64_t rows, 
                 cudaStream_t st);
 // max |x| over a block (device scalar out, as float bits via atomicMax)
 void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
+                      cudaStream_t st);
+void absmax_block_f32(const float* x, int64_t ld, int64_t rows, int B, double* out_dev,
                       cudaStream_t st);
 
 // ---- tensor-core dense products (dense_tc.cu) ---------------------------------------------

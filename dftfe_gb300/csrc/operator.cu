@@ -18,6 +18,7 @@
 #include <cstring>
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 
 namespace chefsi {
 
@@ -452,25 +453,38 @@ __device__ __forceinline__ void absmax_commit(unsigned long long m, unsigned lon
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
-__global__ void k_absmax_flat(const double* __restrict__ x, int64_t n4, unsigned long long* out) {
-  unsigned long long m = 0;
+// |x| keys: FP64 on the bit patterns; FP32 maxima taken in FP32 (exact) and keyed at the end
+__device__ __forceinline__ unsigned long long key_of(double x) { return abs_key(x); }
+__device__ __forceinline__ unsigned long long key_of(float x) { return abs_key((double)fabsf(x)); }
+__device__ __forceinline__ void key_max(unsigned long long& m, double x) { m = max(m, abs_key(x)); }
+__device__ __forceinline__ void key_max(float& m, float x) { m = fmaxf(m, fabsf(x)); }
+__device__ __forceinline__ unsigned long long key_final(unsigned long long m) { return m; }
+__device__ __forceinline__ unsigned long long key_final(float m) { return key_of(m); }
+template <typename T>
+using KeyAcc = typename std::conditional<std::is_same<T, float>::value, float, unsigned long long>::type;
+
+template <typename T>
+__global__ void k_absmax_flat(const T* __restrict__ x, int64_t n4, unsigned long long* out) {
+  KeyAcc<T> m = 0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const Quad<double> q = load_quad(x + 4 * t);
-    m = max(m, max(max(abs_key(q.v[0]), abs_key(q.v[1])), max(abs_key(q.v[2]), abs_key(q.v[3]))));
+    const Quad<T> q = load_quad(x + 4 * t);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) key_max(m, q.v[i]);
   }
-  absmax_commit(m, out);
+  absmax_commit(key_final(m), out);
 }
-__global__ void k_absmax_strided(const double* __restrict__ x, int64_t ld, int64_t rows, int B,
-                              int log_tpr, unsigned long long* out) {
+template <typename T>
+__global__ void k_absmax_strided(const T* __restrict__ x, int64_t ld, int64_t rows, int B,
+                                 int log_tpr, unsigned long long* out) {
   const int tpr = 1 << log_tpr;
   const int col0 = threadIdx.x & (tpr - 1);
   const int rpb = blockDim.x >> log_tpr;
-  unsigned long long m = 0;
+  KeyAcc<T> m = 0;
   for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < rows;
        r += (int64_t)gridDim.x * rpb)
-    for (int j = col0; j < B; j += tpr) m = max(m, abs_key(x[r * ld + j]));
-  absmax_commit(m, out);
+    for (int j = col0; j < B; j += tpr) key_max(m, x[r * ld + j]);
+  absmax_commit(key_final(m), out);
 }
 
 // threads per row for the strided kernels: the power of two >= B, at most 256
@@ -539,19 +553,29 @@ template void copy_block<float, float>(const float*, int64_t, float*, int64_t, i
 template void copy_block<cplx, cplx>(const cplx*, int64_t, cplx*, int64_t, int64_t, int, double,
                                      cudaStream_t);
 
-void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
-                      cudaStream_t st) {
+template <typename T>
+static void absmax_block(const T* x, int64_t ld, int64_t rows, int B, double* out_dev,
+                         cudaStream_t st) {
   CHEFSI_CUDA(cudaMemsetAsync(out_dev, 0, sizeof(double), st));
   if (rows <= 0 || B <= 0) return;
   unsigned long long* out = reinterpret_cast<unsigned long long*>(out_dev);
   const int64_t n = rows * B;
   if ((ld == B || rows == 1) && n % 4 == 0 && aligned16(x)) {
-    k_absmax_flat<<<grid_for(n / 4, 256, kNumSMs * 8), 256, 0, st>>>(x, n / 4, out);
+    k_absmax_flat<T><<<grid_for(n / 4, 256, kNumSMs * 8), 256, 0, st>>>(x, n / 4, out);
   } else {
     const int l = log_threads_per_row(B);
-    k_absmax_strided<<<std::min(rows_grid(rows, l), kNumSMs * 8), 256, 0, st>>>(x, ld, rows, B, l, out);
+    k_absmax_strided<T><<<std::min(rows_grid(rows, l), kNumSMs * 8), 256, 0, st>>>(x, ld, rows, B,
+                                                                                   l, out);
   }
   CHEFSI_CHECK_LAUNCH();
+}
+void absmax_block_f64(const double* x, int64_t ld, int64_t rows, int B, double* out_dev,
+                      cudaStream_t st) {
+  absmax_block<double>(x, ld, rows, B, out_dev, st);
+}
+void absmax_block_f32(const float* x, int64_t ld, int64_t rows, int B, double* out_dev,
+                      cudaStream_t st) {
+  absmax_block<float>(x, ld, rows, B, out_dev, st);
 }
 
 // ------------------------------------------------------------------ operator apply

@@ -65,6 +65,7 @@ constexpr int kXTile = 8192;         // 32 nodes x 128 vectors x 2 B
 struct TcArgs {
   const __half* xhi;
   const __half* xlo;
+  const __half* xlo3;  // third term of the three-term split (NS == 3)
   int64_t ldx;     // halves
   float* dst;
   int64_t ldd;
@@ -85,23 +86,24 @@ struct TcArgs {
   int* err;
 };
 
-// Two rings: the X tiles (xhi, xlo: 16 KB a stage) and the cell-matrix tiles (ahi, alo). The X
-// ring is the deeper one, since its rows come through the gather from HBM / L2 while a cell's
-// matrix halves are shared by the eight chunks processed at about the same time (L2).
+// Two rings: the X tiles (xhi, xlo [, xlo3]: 8 KB each a stage) and the cell-matrix tiles
+// (ahi, alo [, alo3]). The X ring is the deeper one, since its rows come through the gather
+// from HBM / L2 while a cell's matrix halves are shared by the eight chunks processed at about
+// the same time (L2). ns = number of split terms (2 or 3).
 struct Layout {
   int a_tile;   // n_half rows x 64 B, rounded to 1 KB
-  int xstage;   // xhi, xlo
-  int astage;   // ahi, alo
+  int xstage;   // ns X tiles
+  int astage;   // ns matrix tiles
   int aoff;     // start of the matrix ring
   int bars;     // barrier block
   int offs;     // epilogue row offsets: 2 x 256 int64 (one table per accumulator)
   int total;
 };
-__host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages) {
+__host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages, int ns) {
   Layout L;
   L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
-  L.xstage = 2 * kXTile;
-  L.astage = 2 * L.a_tile;
+  L.xstage = ns * kXTile;
+  L.astage = ns * L.a_tile;
   L.aoff = xstages * L.xstage;
   L.bars = L.aoff + stages * L.astage;
   L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 8);
@@ -175,14 +177,25 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 //                 overlapped with the MMAs of the next unit
 constexpr int kThreads3 = 192 + 32 * kEpiWarps;
 
+// NS = 2: the filter's split (hi + lo, 22 bits), products Xhi Ahi + Xhi Alo + Xlo Ahi.
+// NS = 3: hi + lo + lo3 (33 bits: an FP32 vector exactly, the cell matrix to 2^-33), products
+//         down to 2^-22 relative: + Xhi Alo3 + Xlo3 Ahi + Xlo Alo.
+// KCHUNK: every K-block (32 nodes) accumulates in a fresh tensor-memory accumulator and the
+//         epilogue adds the K-block results in FP32 registers (round to nearest) before the
+//         scatter. The tensor core's own FP32 accumulation over the ~130 MMA steps of a unit
+//         leaves errors ~5x those of an FP32 SIMT apply; over the 12 steps of one K-block it
+//         does not. Needs at most kChunkCols accumulator columns per epilogue warp.
+constexpr int kChunkCols = 96;
+template <int NS, bool KCHUNK>
 __global__ void __launch_bounds__(kThreads3, 1)
     cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
-                      const __grid_constant__ CUtensorMap tm_lo, TcArgs args) {
+                      const __grid_constant__ CUtensorMap tm_lo,
+                      const __grid_constant__ CUtensorMap tm_lo3, TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int S = args.stages, SX = args.xstages;
-  const Layout L = make_layout(args.n_half, S, SX);
+  const Layout L = make_layout(args.n_half, S, SX, NS);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] cell-matrix TMA bytes landed
   uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
@@ -229,7 +242,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
   if (warp == 0) {
     // ---------------- TMA producer of the cell-matrix K-blocks
     if (lane == 0) {
-      const uint32_t bytes = 2u * args.n_half * kRowBytes;
+      const uint32_t bytes = (uint32_t)NS * args.n_half * kRowBytes;
       int64_t issued = 0;
       int s = 0;
       uint32_t r = 0;
@@ -245,6 +258,9 @@ __global__ void __launch_bounds__(kThreads3, 1)
           mbar_arrive_expect_tx(&tma_full[s], bytes);
           tma_load_3d(st, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
           tma_load_3d(st + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
+          if (NS == 3)
+            tma_load_3d(st + 2 * L.a_tile, &tm_lo3, kb * kKB, w.half * args.n_half, w.cell,
+                        &tma_full[s]);
           ++issued;
           if (++s == S) s = 0, ++r;
         }
@@ -265,13 +281,26 @@ __global__ void __launch_bounds__(kThreads3, 1)
       bool ok = true;
       int s = 0, sx = 0;            // ring positions of the next K-block
       uint32_t r = 0, rx = 0;       // and their phases
+      int64_t g = 0;                // K-blocks issued (KCHUNK: accumulator sequence)
       for (int64_t it = 0; it < my_units && ok; ++it) {
-        const int buf = (int)(it & 1);
-        const uint32_t ph = (uint32_t)((it >> 1) & 1);
-        if (!mbar_wait(&acc_empty[buf], ph ^ 1, args.err, abort_flag)) break;
-        fence_after();
-        const uint32_t d = tmem + buf * args.buf_stride;
-        for (int kb = 0; kb < nkb; ++kb) {
+        int buf = (int)(it & 1);
+        uint32_t ph = (uint32_t)((it >> 1) & 1);
+        if (!KCHUNK) {
+          if (!mbar_wait(&acc_empty[buf], ph ^ 1, args.err, abort_flag)) break;
+          fence_after();
+        }
+        uint32_t d = tmem + buf * args.buf_stride;
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          if (KCHUNK) {
+            buf = (int)(g & 1);
+            ph = (uint32_t)((g >> 1) & 1);
+            if (!mbar_wait(&acc_empty[buf], ph ^ 1, args.err, abort_flag)) {
+              ok = false;
+              break;
+            }
+            fence_after();
+            d = tmem + buf * args.buf_stride;
+          }
           if (!mbar_wait(&tma_full[s], r & 1, args.err, abort_flag) ||
               !mbar_wait(&x_full[sx], rx & 1, args.err, abort_flag)) {
             ok = false;
@@ -280,24 +309,51 @@ __global__ void __launch_bounds__(kThreads3, 1)
           fence_after();
           const uint32_t xhi = smem_u32(smem + sx * L.xstage), xlo = xhi + kXTile;
           const uint32_t ahi = smem_u32(smem + L.aoff + s * L.astage), alo = ahi + L.a_tile;
+          if (NS == 2) {
 #pragma unroll
-          for (int ks = 0; ks < kKB / 16; ++ks) {
-            const uint32_t xoff = ks * 2 * kXGroupK;  // 16 nodes = two 8-node groups
-            const uint32_t koff = ks * 32;            // 16 halves of a K-major row
-            const uint32_t acc0 = (kb > 0 || ks > 0) ? 1u : 0u;
-            mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
-                    smem_desc_sw64(ahi + koff), idesc, acc0);
-            mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
-                    smem_desc_sw64(alo + koff), idesc, 1u);
-            mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
-                    smem_desc_sw64(ahi + koff), idesc, 1u);
+            for (int ks = 0; ks < kKB / 16; ++ks) {
+              const uint32_t xoff = ks * 2 * kXGroupK;  // 16 nodes = two 8-node groups
+              const uint32_t koff = ks * 32;            // 16 halves of a K-major row
+              const uint32_t acc0 = ((!KCHUNK && kb > 0) || ks > 0) ? 1u : 0u;
+              mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(ahi + koff), idesc, acc0);
+              mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(alo + koff), idesc, 1u);
+              mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(ahi + koff), idesc, 1u);
+            }
+          } else {
+            // small products of both K-steps first, the two hi * hi products last, so that
+            // the truncating FP32 accumulation adds few terms at the large magnitude
+            const uint32_t xlo3 = xhi + 2 * kXTile, alo3 = ahi + 2 * L.a_tile;
+#pragma unroll
+            for (int ks = 0; ks < kKB / 16; ++ks) {
+              const uint32_t xoff = ks * 2 * kXGroupK;
+              const uint32_t koff = ks * 32;
+              const uint32_t acc0 = ((!KCHUNK && kb > 0) || ks > 0) ? 1u : 0u;
+              mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(alo + koff), idesc, acc0);
+              mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(alo3 + koff), idesc, 1u);
+              mma_f16(d, smem_desc_mn_sw128(xlo3 + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(ahi + koff), idesc, 1u);
+              mma_f16(d, smem_desc_mn_sw128(xhi + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(alo + koff), idesc, 1u);
+              mma_f16(d, smem_desc_mn_sw128(xlo + xoff, kXAtomM, kXGroupK),
+                      smem_desc_sw64(ahi + koff), idesc, 1u);
+            }
+#pragma unroll
+            for (int ks = 0; ks < kKB / 16; ++ks)
+              mma_f16(d, smem_desc_mn_sw128(xhi + ks * 2 * kXGroupK, kXAtomM, kXGroupK),
+                      smem_desc_sw64(ahi + ks * 32), idesc, 1u);
           }
           mma_commit(&a_empty[s]);
           mma_commit(&x_empty[sx]);
+          if (KCHUNK) mma_commit(&acc_full[buf]);
           if (++s == S) s = 0, ++r;
           if (++sx == SX) sx = 0, ++rx;
         }
-        if (ok) mma_commit(&acc_full[buf]);
+        if (!KCHUNK && ok) mma_commit(&acc_full[buf]);
       }
       // every MMA must be complete before tensor memory is freed, also on the abort path
       mma_commit(mma_done);
@@ -358,6 +414,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
           const uint32_t d = st + dst_base + j * kXGroupK;
           cp_async16(d, args.xhi + off, ok);
           cp_async16(d + kXTile, args.xlo + off, ok);
+          if (NS == 3) cp_async16(d + 2 * kXTile, args.xlo3 + off, ok);
         }
       }
       cp_async_commit();
@@ -383,41 +440,99 @@ __global__ void __launch_bounds__(kThreads3, 1)
     // this warp's 16-column groups of the accumulator: part (warp - 6) / 4 of kEpiWarps / 4
     const int ng = args.n_half >> 4, part = (warp - 6) >> 2, nparts = kEpiWarps / 4;
     const int c_beg = (ng * part / nparts) * 16, c_end = (ng * (part + 1) / nparts) * 16;
-    for (int64_t it = 0; it < my_units; ++it) {
-      const int buf = (int)(it & 1);
-      const uint32_t ph = (uint32_t)((it >> 1) & 1);
-      const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
-      fence_after();
-      const Unit w = unit_at(it, first, step, args);
-      const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
-      const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
-      // the unit's output-row offsets (dof * ldd), staged once by the epilogue warps; rows
-      // past nrows get an offset no lane uses (they are skipped)
-      int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + buf * 256;
-      if (okw)
+    if (KCHUNK) {
+      // per unit: stage the row offsets, then add the unit's nkb K-block accumulators into
+      // registers (this warp's columns [c_beg, c_end), at most kChunkCols), then scatter
+      int64_t g = 0;
+      bool okp = true;
+      for (int64_t it = 0; it < my_units; ++it) {
+        const Unit w = unit_at(it, first, step, args);
+        const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
+        const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
+        int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + (it & 1) * 256;
         for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += kEpiWarps * 32)
           offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
-      // the epilogue warps continue or stop together (a named barrier with an AND-reduction)
-      if (!epilogue_sync_and(okw)) break;
-      const int gb = w.chunk * kVec + q * 32 + lane;
-      const bool vok = gb < args.B;
-      float* dstb = args.dst + gb;
-      const float osc = args.out_scale;
-      const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
-      for (int c0 = c_beg; c0 < c_end; c0 += 16) {
-        float vals[16];
-        tmem_ld16(tq + c0, vals);
-        if (vok) {
+        if (!epilogue_sync_and(okp)) break;
+        float sum[kChunkCols];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int64_t o = offs[c0 + i];
-            if (o >= 0) atomicAdd(dstb + o, osc * vals[i]);
+        for (int i = 0; i < kChunkCols; ++i) sum[i] = 0.f;
+        bool ok = true;
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int buf = (int)(g & 1);
+          const uint32_t ph = (uint32_t)((g >> 1) & 1);
+          if (!__all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag))) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
+#pragma unroll
+          for (int gi = 0; gi < kChunkCols / 16; ++gi) {
+            if (c_beg + 16 * gi < c_end) {
+              float v[16];
+              tmem_ld16(tq + c_beg + 16 * gi, v);
+#pragma unroll
+              for (int i = 0; i < 16; ++i) sum[16 * gi + i] += v[i];
+            }
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acc_empty[buf]);
+        }
+        okp = ok;
+        const int gb = w.chunk * kVec + q * 32 + lane;
+        if (ok && gb < args.B) {
+          float* dstb = args.dst + gb;
+          const float osc = args.out_scale;
+#pragma unroll
+          for (int gi = 0; gi < kChunkCols / 16; ++gi) {
+            if (c_beg + 16 * gi < c_end) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i) {
+                const int64_t o = offs[c_beg + 16 * gi + i];
+                if (o >= 0) atomicAdd(dstb + o, osc * sum[16 * gi + i]);
+              }
+            }
           }
         }
       }
-      fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[buf]);
+    } else {
+      for (int64_t it = 0; it < my_units; ++it) {
+        const int buf = (int)(it & 1);
+        const uint32_t ph = (uint32_t)((it >> 1) & 1);
+        const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
+        fence_after();
+        const Unit w = unit_at(it, first, step, args);
+        const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
+        const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
+        // the unit's output-row offsets (dof * ldd), staged once by the epilogue warps; rows
+        // past nrows get an offset no lane uses (they are skipped)
+        int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + buf * 256;
+        if (okw)
+          for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += kEpiWarps * 32)
+            offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
+        // the epilogue warps continue or stop together (a named barrier with an AND-reduction)
+        if (!epilogue_sync_and(okw)) break;
+        const int gb = w.chunk * kVec + q * 32 + lane;
+        const bool vok = gb < args.B;
+        float* dstb = args.dst + gb;
+        const float osc = args.out_scale;
+        const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
+        for (int c0 = c_beg; c0 < c_end; c0 += 16) {
+          float vals[16];
+          tmem_ld16(tq + c0, vals);
+          if (vok) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int64_t o = offs[c0 + i];
+              if (o >= 0) atomicAdd(dstb + o, osc * vals[i]);
+            }
+          }
+        }
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
+      }
     }
   }
   fence_before();
@@ -459,10 +574,55 @@ void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows)
     throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
+// third term of the three-term split of the cell matrices: lo3 = fp16(v - hi - lo) with
+// v = 2^s A_e, hi = fp16(v), lo = fp16(v - hi) (the two-term arrays)
+__global__ void k_split_mats_lo3(const double* __restrict__ mats, int n_cells, int n_e, int npad,
+                                 double scale, __half* __restrict__ lo3) {
+  const int64_t n = (int64_t)n_cells * npad * npad;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / ((int64_t)npad * npad);
+    const int r = (int)(t % ((int64_t)npad * npad));
+    const int I = r / npad, J = r % npad;
+    double v = 0.0;
+    if (I < n_e && J < n_e) v = scale * mats[(c * n_e + I) * n_e + J];
+    const double h = (double)__half2float(__double2half(v));
+    const double l = (double)__half2float(__double2half(v - h));
+    lo3[t] = __double2half(v - h - l);
+  }
+}
+
 // FP32 -> FP16 hi + lo (22 significant bits; the vectors are pre-scaled into FP16's range)
 __device__ __forceinline__ void split_f32(float a, __half& h, __half& l) {
   h = __float2half_rn(a);
   l = __float2half_rn(a - __half2float(h));
+}
+
+// FP32 -> FP16 hi + lo + lo3, exact: x - hi and (x - hi) - lo are exact in FP32 and the last
+// term holds the remaining <= 2 significant bits of the 24
+__device__ __forceinline__ void split3_f32(float a, __half& h, __half& l, __half& l3) {
+  h = __float2half_rn(a);
+  const float r = a - __half2float(h);
+  l = __float2half_rn(r);
+  l3 = __float2half_rn(r - __half2float(l));
+}
+// (hi, lo, lo3)[r][j] = split3(x[r][j]) for a [M][B] block (x leading dimension ldx, splits ld B)
+__global__ void k_split_rows3(const float* __restrict__ x, int64_t ldx, int64_t M, int B,
+                              __half* __restrict__ hi, __half* __restrict__ lo,
+                              __half* __restrict__ lo3) {
+  const int64_t n = M * (int64_t)(B / 2);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / (B / 2);
+    const int j = (int)(t % (B / 2)) * 2;
+    const float2 v = *reinterpret_cast<const float2*>(x + r * ldx + j);
+    __half h0, l0, m0, h1, l1, m1;
+    split3_f32(v.x, h0, l0, m0);
+    split3_f32(v.y, h1, l1, m1);
+    *reinterpret_cast<__half2*>(hi + r * B + j) = __halves2half2(h0, h1);
+    *reinterpret_cast<__half2*>(lo + r * B + j) = __halves2half2(l0, l1);
+    *reinterpret_cast<__half2*>(lo3 + r * B + j) = __halves2half2(m0, m1);
+  }
 }
 
 // (hi, lo)[r][j] = split(x[r][j]) for a [M][B] block (x leading dimension ldx, splits ld B)
@@ -513,7 +673,7 @@ struct TcPlan {
   int npad, n_half, n_halves, buf_stride, tmem_cols, stages, xstages, smem;
 };
 
-TcPlan plan_for(int n_e) {
+TcPlan plan_for(int n_e, int ns) {
   TcPlan p{};
   p.npad = (n_e + 31) / 32 * 32;
   if (p.npad <= 256) {
@@ -525,13 +685,15 @@ TcPlan plan_for(int n_e) {
   }
   p.buf_stride = p.n_half <= 128 ? 128 : 256;
   p.tmem_cols = 2 * p.buf_stride;
-  // three matrix stages, then as many X stages as fit (at most 8)
+  // three matrix stages, then as many X stages as fit (at most 8, at least 3); two matrix
+  // stages when three leave no room for three X stages
   const int budget = 220 * 1024;
   p.stages = 3;
   p.xstages = 8;
-  while (p.xstages > 3 && make_layout(p.n_half, p.stages, p.xstages).total + 1024 > budget)
-    --p.xstages;
-  p.smem = make_layout(p.n_half, p.stages, p.xstages).total + 1024;
+  auto total = [&] { return make_layout(p.n_half, p.stages, p.xstages, ns).total + 1024; };
+  while (p.xstages > 3 && total() > budget) --p.xstages;
+  if (total() > budget) p.stages = 2;
+  p.smem = total();
   return p;
 }
 
@@ -586,7 +748,7 @@ void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
   auto& tc = op->tc;
   if (tc.ready || op->is_complex || !op->folded) return;
   const int n_e = op->n_e;
-  const TcPlan p = plan_for(n_e);
+  const TcPlan p = plan_for(n_e, 2);
   CHEFSI_REQUIRE(p.n_half <= 256 && p.n_half % 16 == 0, "cell too large for the tensor path");
   // power-of-two scale: largest |A_e| -> [2^14, 2^15)
   DeviceBuffer<double> amax(1);
@@ -605,6 +767,20 @@ void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
                                                           std::ldexp(1.0, e), tc.hi.ptr, tc.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
   tc.ready = true;
+  tc.lo3_ready = false;
+}
+
+// the third split term of the cell matrices, for the three-term apply
+static void prepare_tensor_mats_lo3(chefsi_operator_s* op, cudaStream_t st) {
+  prepare_tensor_mats(op, st);
+  auto& tc = op->tc;
+  if (tc.lo3_ready) return;
+  const size_t n = (size_t)op->n_cells * tc.npad * tc.npad;
+  tc.lo3.reset(n);
+  k_split_mats_lo3<<<grid_for((int64_t)n, 256), 256, 0, st>>>(
+      op->mats64.ptr, op->n_cells, op->n_e, tc.npad, (double)tc.scale, tc.lo3.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  tc.lo3_ready = true;
 }
 
 bool tc_usable(chefsi_operator_s* op) {
@@ -612,20 +788,27 @@ bool tc_usable(chefsi_operator_s* op) {
   return tcgen05_device();
 }
 
-// launch the persistent tensor-core kernel on the split rows (xhi, xlo: [rows][ldx] FP16)
+// launch the persistent tensor-core kernel on the split rows (xhi, xlo [, xlo3]: [rows][ldx]
+// FP16); ns = number of split terms (2, or 3 with xlo3)
 static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const __half* xlo,
-                      int64_t ldx, float* dst, int64_t ldd, int B, cudaStream_t st) {
-  prepare_tensor_mats(op, st);
-  const TcPlan p = plan_for(op->n_e);
+                      const __half* xlo3, int64_t ldx, float* dst, int64_t ldd, int B, int ns,
+                      cudaStream_t st) {
+  if (ns == 3)
+    prepare_tensor_mats_lo3(op, st);
+  else
+    prepare_tensor_mats(op, st);
+  const TcPlan p = plan_for(op->n_e, ns);
   if (!op->tc_err.ptr) {
     op->tc_err.reset(1);
     CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
   }
-  CUtensorMap mhi, mlo;
+  CUtensorMap mhi, mlo, mlo3;
   make_map(&mhi, op->tc.hi.ptr, op->n_cells, p.npad, p.n_half);
   make_map(&mlo, op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
+  make_map(&mlo3, ns == 3 ? op->tc.lo3.ptr : op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
   a.xhi = xhi;
   a.xlo = xlo;
+  a.xlo3 = ns == 3 ? xlo3 : xlo;
   a.ldx = ldx;
   a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
   a.dst = dst;
@@ -645,15 +828,16 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const
   a.err = op->tc_err.ptr;
   CHEFSI_REQUIRE(op->n_dofs < (1ll << 31), "tensor-core HX: too many dofs for 32-bit map entries");
   CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(xhi) & 15) == 0 && (reinterpret_cast<uintptr_t>(xlo) & 15) == 0 &&
-                     ldx % 8 == 0 && B % 8 == 0,
+                     (reinterpret_cast<uintptr_t>(a.xlo3) & 15) == 0 && ldx % 8 == 0 && B % 8 == 0,
                  "tensor-core HX: split rows must be 16-byte aligned");
-  CHEFSI_CUDA(cudaFuncSetAttribute(cell_hx_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   227 * 1024));
+  CHEFSI_REQUIRE(ns == 2 || ns == 3, "tensor-core HX: two or three split terms");
+  auto kernel = ns == 3 ? cell_hx_tc_kernel<3, true> : cell_hx_tc_kernel<2, false>;
+  CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   int dev = 0, sms = kNumSMs;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t grid = std::min<int64_t>(sms, a.n_units / p.n_halves);
-  cell_hx_tc_kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(mhi, mlo, a);
+  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(mhi, mlo, mlo3, a);
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -686,7 +870,7 @@ bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, co
   prepare_tensor_mats(op, st);
   TcArgs a{};
   a.out_scale = (float)(scalar / op->tc.scale);
-  launch_tc(op, a, xhi, xlo, B, dst, ldd, B, st);
+  launch_tc(op, a, xhi, xlo, nullptr, B, dst, ldd, B, 2, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
 }
@@ -700,6 +884,30 @@ bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int
   __half* lo = op->xs_lo.ensure((size_t)op->n_dofs * B);
   split_rows_f32(src, lds, op->n_dofs, B, hi, lo, st);
   return hx_tc_split(op, hi, lo, src, lds, dst, ldd, B, scalar, accumulate, st);
+}
+
+bool hx_tc3(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
+            double scalar, bool accumulate, cudaStream_t st) {
+  if (!tc_split_usable(op, B) || lds % 2 != 0 || ldd % 4 != 0 ||
+      (reinterpret_cast<uintptr_t>(dst) & 15) != 0)
+    return false;
+  // the K-block-chunked epilogue holds each warp's accumulator columns in registers
+  const int ng = plan_for(op->n_e, 3).n_half / 16;
+  if ((ng + kEpiWarps / 4 - 1) / (kEpiWarps / 4) * 16 > kChunkCols) return false;
+  const size_t n = (size_t)op->n_dofs * B;
+  __half* hi = op->xs_hi.ensure(n);
+  __half* lo = op->xs_lo.ensure(n);
+  __half* lo3 = op->xs_lo3.ensure(n);
+  k_split_rows3<<<grid_for(op->n_dofs * (B / 2), 256), 256, 0, st>>>(src, lds, op->n_dofs, B, hi,
+                                                                      lo, lo3);
+  CHEFSI_CHECK_LAUNCH();
+  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  prepare_tensor_mats_lo3(op, st);
+  TcArgs a{};
+  a.out_scale = (float)(scalar / op->tc.scale);
+  launch_tc(op, a, hi, lo, lo3, B, dst, ldd, B, 3, st);
+  apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
+  return true;
 }
 
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st) {

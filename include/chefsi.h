@@ -50,10 +50,14 @@
  *   - Handles are not thread-safe: one host thread per handle.
  *   - Precision: CHEFSI_PREC_FP64 computes everything in FP64. CHEFSI_PREC_MIXED runs the
  *     filter HX on the tensor cores with FP16-split operands (hi+lo, three products,
- *     FP32 accumulation) on FP32 block vectors, and the Gram / rotation GEMMs in FP32 with
- *     FP64 accumulation across K chunks; the HX feeding the projected Hamiltonian, the
- *     Cholesky, the projected eigensolve and the residual norms stay in FP64.
- *     CHEFSI_PREC_FP32 is the SIMT FP32 filter (no tensor cores), kept for comparison.
+ *     FP32 accumulation) on FP32 block vectors, and the overlap / projected-Hamiltonian Gram
+ *     products and the rotations on the tensor cores with the same split of column-scaled
+ *     operands (FP32 accumulation over 128-dof chunks, compensated sums across chunks); the
+ *     HX feeding the projected Hamiltonian follows rr_precision; the Cholesky, the projected
+ *     eigensolve and the residual norms stay in FP64. CHEFSI_PREC_FP32 is the SIMT FP32
+ *     apply (no tensor cores), kept for comparison. CHEFSI_PREC_FP32_TC (chefsi_hx and
+ *     rr_precision) is the FP32-accurate tensor-core apply: three-term FP16 split (FP32
+ *     operands exactly, cell matrices to 2^-33), six products, FP32 accumulation.
  */
 #ifndef CHEFSI_GB300_H
 #define CHEFSI_GB300_H
@@ -79,6 +83,7 @@ extern "C" {
 #define CHEFSI_PREC_FP64 0
 #define CHEFSI_PREC_MIXED 1
 #define CHEFSI_PREC_FP32 2
+#define CHEFSI_PREC_FP32_TC 3
 
 typedef struct chefsi_operator_s* chefsi_operator;
 typedef struct chefsi_solver_s* chefsi_solver;
@@ -123,7 +128,10 @@ typedef struct {
   int32_t keep_hx;              /* 1: keep H X from the RR step for the residuals */
   int32_t rr_precision;         /* precision of the H X feeding X^T H X in mixed mode:
                                    CHEFSI_PREC_FP64 (default), CHEFSI_PREC_FP32 (FP32 SIMT
-                                   apply) or CHEFSI_PREC_MIXED (tensor-core FP16-split apply) */
+                                   apply), CHEFSI_PREC_FP32_TC (tensor-core apply with the
+                                   three-term FP16 split: FP32 operands exactly, FP32
+                                   accumulation) or CHEFSI_PREC_MIXED (the filter's two-term
+                                   split) */
 } chefsi_params;
 
 const char* chefsi_last_error(void);
@@ -137,7 +145,8 @@ int chefsi_operator_info(chefsi_operator op, int64_t* n_dofs, int32_t* n_cells,
                          int32_t* nodes_per_cell, int32_t* is_complex);
 
 /* dst = (accumulate ? dst : 0) + scalar * A src over n_vec vectors (DFT-FE's HX with
-   scaleFlag == accumulate). Real: src/dst FP64 (precision FP64) or FP32 (FP32 / MIXED).
+   scaleFlag == accumulate). Real: src/dst FP64 (precision FP64) or FP32 (FP32 / FP32_TC /
+   MIXED).
    Complex: interleaved complex FP64 only. ld_* are leading dimensions in elements. */
 int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, int64_t ld_dst,
               int32_t n_vec, double scalar, int32_t accumulate, int32_t precision, void* stream);

@@ -73,7 +73,7 @@ def test_rayleigh_ritz_complex_matches_oracle(C, prec, tol):
 
 
 @pytest.mark.parametrize("mixed,tol,rr", [(False, 1e-10, "fp64"), (True, 1e-6, "fp64"),
-                                          (True, 1e-6, "fp32")])
+                                          (True, 1e-6, "fp32"), (True, 1e-6, "fp32tc")])
 def test_solve_complex_matches_oracle(C, mixed, tol, rr):
     pr = small_problem(n=3, L=6.0, p=2, wells=3, nwfc=12, seed=7, kpoint=K)
     op, ora = C.KohnShamOperator.from_problem(pr), oracle_op(pr)

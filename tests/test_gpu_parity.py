@@ -1,7 +1,8 @@
 """GPU parity tests: every CheFSI stage through the C ABI against the FP64 oracle.
 
 Tolerances (written per test): FP64 stages <= 1e-12 relative (HX) / 1e-10 (filter, Ritz);
-FP32 SIMT HX <= 2e-6 relative; the mixed (FP16-split tensor-core) HX <= 2e-6 relative;
+FP32 SIMT HX <= 2e-6 relative; the mixed (FP16-split tensor-core) HX and the three-term split
+(fp32tc) HX <= 2e-6 relative;
 mixed CheFSI Ritz values <= 1e-6 Ha.
 """
 import os
@@ -53,7 +54,9 @@ def test_hx_scaleflag_semantics(chefsi):
 
 @pytest.mark.parametrize("prec,p,n,B", [("fp32", 4, 2, 96), ("mixed", 4, 2, 96),
                                          ("mixed", 6, 2, 136), ("mixed", 2, 3, 8),
-                                         ("mixed", 5, 2, 256)])
+                                         ("mixed", 5, 2, 256), ("fp32tc", 4, 2, 96),
+                                         ("fp32tc", 6, 2, 136), ("fp32tc", 2, 3, 8),
+                                         ("fp32tc", 5, 2, 256)])
 def test_hx_reduced_precision(chefsi, prec, p, n, B):
     """FP32 SIMT and tensor-core (FP16-split) HX: cell sizes with one K-block (p = 2), one
     row half (p = 4, 5) and two row halves (p = 6); partial and several 128-vector chunks."""
@@ -68,6 +71,27 @@ def test_hx_reduced_precision(chefsi, prec, p, n, B):
         pytest.fail(f"{prec} HX failed: {e}")
     ref = ora.HX(Xt.double().cpu().numpy())
     assert rel(Y.double().cpu().numpy(), ref) < 2e-6
+
+
+@pytest.mark.parametrize("p,n,B", [(6, 2, 128), (4, 3, 64)])
+def test_hx_tc_three_term_split_is_fp32_class(chefsi, p, n, B):
+    """The three-term split apply (FP32 operands exactly, six products, FP32 accumulation) is
+    as accurate as the FP32 SIMT apply: both against the FP64 oracle on the FP32-rounded
+    input, with inputs spanning three decades per vector."""
+    pr = small_problem(n=n, L=2.0 * n, p=p, wells=2, projectors=True)
+    op, ora = gpu_op(chefsi, pr), oracle_op(pr)
+    rng = np.random.default_rng(11)
+    X = rng.uniform(-1, 1, (pr.n_dofs, B)) * 10.0 ** rng.uniform(-3, 0, B)[None, :]
+    Xt = torch.from_numpy(X).float().cuda()
+    ref = ora.HX(Xt.double().cpu().numpy())
+    errs = {}
+    for prec in ("fp32", "fp32tc", "mixed"):
+        Y = torch.zeros_like(Xt)
+        op.HX(Xt, Y, precision=prec)
+        d = Y.double().cpu().numpy() - ref
+        errs[prec] = float(np.sqrt((d ** 2).mean()) / np.sqrt((ref ** 2).mean()))
+    assert errs["fp32tc"] <= 2.0 * errs["fp32"] + 1e-8, errs
+    assert errs["fp32tc"] < errs["mixed"], errs
 
 
 @pytest.mark.parametrize("p,n,B", [(4, 3, 40), (6, 2, 128), (3, 1, 16)])
