@@ -106,6 +106,14 @@ def build_workload(name, seed):
     return problems.workload(name, seed=seed)
 
 
+def first_bounds(chefsi, op, n_wfc):
+    """First-call bounds of the reference (chefsi.initial_bounds). Its bLow = a0 + (b - a0) N/M
+    200 passes b when N/M > 1/200 (small meshes with many wavefunctions); there it is capped at
+    the midpoint of [a0, b]. The large workloads (N/M < 1/200) are unchanged."""
+    lo, blow, up = chefsi.initial_bounds(op, n_wfc)
+    return lo, min(blow, lo + 0.5 * (up - lo)), up
+
+
 def cpu_sample(pr, m, N, max_seconds=25.0):
     """Time the CPU oracle's HX on a bounded block of vectors and extrapolate one CheFSI
     iteration: (m + 2) HX over all N vectors + the dense RR products (numpy BLAS, timed on
@@ -182,7 +190,7 @@ def run_ours(args):
     pr = build_workload(args.workload, args.seed + rank)   # independent replica per rank
     N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
     op = chefsi.KohnShamOperator.from_problem(pr)
-    lo, blow, up = chefsi.initial_bounds(op, N)
+    lo, blow, up = first_bounds(chefsi, op, N)
     params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=N,
                                  mixed_precision="mixed", rr_precision=args.rr_precision)
     solver = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params)
@@ -331,7 +339,7 @@ def run_ritz_check(args):
     pr = build_workload(args.workload, args.seed)
     N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
     op = chefsi.KohnShamOperator.from_problem(pr)
-    lo, blow, up = chefsi.initial_bounds(op, N)
+    lo, blow, up = first_bounds(chefsi, op, N)
     mk = lambda: chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
         chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=min(N, 512), mixed_precision="mixed",
         rr_precision=args.rr_precision))
@@ -451,12 +459,7 @@ def run_bloch(args):
     prs = problems.bloch_set(args.batch, seed=args.seed)
     ops = [chefsi.KohnShamOperator.from_problem(p) for p in prs]
     X0 = [torch.from_numpy(p.initial_vectors()).to(dev) for p in prs]
-    # first-call bounds of the reference; its bLow = a0 + (b - a0) N/M 200 passes b when
-    # N/M > 1/200 (the small meshes with 512 wavefunctions), so it is capped at the midpoint
-    bounds = []
-    for op, p in zip(ops, prs):
-        lo, blow, up = chefsi.initial_bounds(op, p.n_wfc)
-        bounds.append((lo, min(blow, lo + 0.5 * (up - lo)), up))
+    bounds = [first_bounds(chefsi, op, p.n_wfc) for op, p in zip(ops, prs)]
 
     def fresh():
         solvers = []

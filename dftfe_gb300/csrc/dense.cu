@@ -175,24 +175,29 @@ void gram_c64(const cplx* A, int64_t lda, const cplx* B, int64_t ldb, int64_t K,
 
 // ======================================================================= GEMM
 // C[M][N] = alpha op(A) op(B) + beta C, row-major. op(A)[m][k] = ta=='N' ? A[m][k] : A[k][m].
+// Split K (part != nullptr): CTA z sums k in [z kc, (z+1) kc) and writes the raw sum to
+// part[z][M][N]; k_splitk_reduce forms C.
 template <typename Tc>
 __global__ void __launch_bounds__(256)
     gemm_kernel(int ta, int tb, int64_t M, int N, int K, double alpha,
                 const double* __restrict__ A, int64_t lda, const double* __restrict__ B,
-                int64_t ldb, double beta, double* __restrict__ C, int64_t ldc, int chunk) {
+                int64_t ldb, double beta, double* __restrict__ C, int64_t ldc, int chunk,
+                int kc = 0, double* __restrict__ part = nullptr) {
   __shared__ Tc As[GK][GT + 1];
   __shared__ Tc Bs[GK][GT];
   const int64_t m0 = (int64_t)blockIdx.x * GT;
   const int n0 = blockIdx.y * GT;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   double acc[4][4];
-  Tc part[4][4];
+  Tc partc[4][4];
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
-    for (int s = 0; s < 4; ++s) acc[r][s] = 0.0, part[r][s] = (Tc)0;
+    for (int s = 0; s < 4; ++s) acc[r][s] = 0.0, partc[r][s] = (Tc)0;
   int since = 0;
-  for (int k0 = 0; k0 < K; k0 += GK) {
+  const int kbeg = part ? blockIdx.z * kc : 0;
+  const int kend = part ? min(K, kbeg + kc) : K;
+  for (int k0 = kbeg; k0 < kend; k0 += GK) {
     for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
       int k, mm;
       if (ta) {  // A is [K][M]: contiguous along m
@@ -203,7 +208,7 @@ __global__ void __launch_bounds__(256)
       const int64_t gm = m0 + mm;
       const int gk = k0 + k;
       double v = 0.0;
-      if (gm < M && gk < K) v = ta ? A[(int64_t)gk * lda + gm] : A[gm * lda + gk];
+      if (gm < M && gk < kend) v = ta ? A[(int64_t)gk * lda + gm] : A[gm * lda + gk];
       As[k][mm] = (Tc)v;
     }
     for (int idx = threadIdx.x; idx < GK * GT; idx += 256) {
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(256)
       }
       const int gn = n0 + nn, gk = k0 + k;
       double v = 0.0;
-      if (gn < N && gk < K) v = tb ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn];
+      if (gn < N && gk < kend) v = tb ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn];
       Bs[k][nn] = (Tc)v;
     }
     __syncthreads();
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int s = 0; s < 4; ++s) part[r][s] = fma(a[r], b[s], part[r][s]);
+        for (int s = 0; s < 4; ++s) partc[r][s] = fma(a[r], b[s], partc[r][s]);
     }
     __syncthreads();
     since += GK;
@@ -237,7 +242,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int s = 0; s < 4; ++s) acc[r][s] += (double)part[r][s], part[r][s] = (Tc)0;
+        for (int s = 0; s < 4; ++s) acc[r][s] += (double)partc[r][s], partc[r][s] = (Tc)0;
       since = 0;
     }
   }
@@ -248,11 +253,29 @@ __global__ void __launch_bounds__(256)
       const int64_t m = m0 + ty + 16 * r;
       const int n = n0 + tx + 16 * s;
       if (m < M && n < N) {
-        const double v = alpha * (acc[r][s] + (double)part[r][s]);
-        double* c = &C[m * ldc + n];
-        *c = (beta == 0.0) ? v : v + beta * *c;
+        if (part) {
+          part[((int64_t)blockIdx.z * M + m) * N + n] = acc[r][s] + (double)partc[r][s];
+        } else {
+          const double v = alpha * (acc[r][s] + (double)partc[r][s]);
+          double* c = &C[m * ldc + n];
+          *c = (beta == 0.0) ? v : v + beta * *c;
+        }
       }
     }
+}
+
+// C = alpha sum_z part[z] + beta C (fixed order over the K slices)
+__global__ void k_splitk_reduce(const double* __restrict__ part, int S, int64_t M, int N,
+                                double alpha, double beta, double* __restrict__ C, int64_t ldc) {
+  const int64_t n = M * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int z = 0; z < S; ++z) v += part[z * n + t];
+    const int64_t m = t / N;
+    double* c = &C[m * ldc + (t - m * N)];
+    *c = (beta == 0.0) ? alpha * v : alpha * v + beta * *c;
+  }
 }
 
 void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const double* A, int64_t lda,
@@ -264,6 +287,28 @@ void gemm_f64(char ta, char tb, int64_t M, int N, int K, double alpha, const dou
   const int ita = (ta == 'T' || ta == 't' || ta == 'C' || ta == 'c');
   const int itb = (tb == 'T' || tb == 't' || tb == 'C' || tb == 'c');
   if (prec == CHEFSI_PREC_FP64) {
+    // a 64 x 64 tile runs its whole K loop on one SM (~2 FP64 FMAs per clock): with few tiles
+    // and a long K, the K range is split over CTAs and the slices are summed in fixed order
+    const int64_t tiles = (int64_t)grid.x * grid.y;
+    int S = 1;
+    if (tiles < kNumSMs / 2 && K >= 8 * GK) {
+      S = (int)std::min<int64_t>((2 * kNumSMs) / tiles, K / (4 * GK));
+      S = std::max(1, std::min(S, 64));
+    }
+    if (S > 1) {
+      const int kc = ((K + S - 1) / S + GK - 1) / GK * GK;
+      S = (K + kc - 1) / kc;
+      double* part = nullptr;
+      CHEFSI_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&part), sizeof(double) * S * M * N, st));
+      dim3 g3(grid.x, grid.y, (unsigned)S);
+      gemm_kernel<double><<<g3, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
+                                              ldc, 1 << 30, kc, part);
+      CHEFSI_CHECK_LAUNCH();
+      k_splitk_reduce<<<grid_for(M * N, 256), 256, 0, st>>>(part, S, M, N, alpha, beta, C, ldc);
+      CHEFSI_CHECK_LAUNCH();
+      CHEFSI_CUDA(cudaFreeAsync(part, st));
+      return;
+    }
     gemm_kernel<double><<<grid, 256, 0, st>>>(ita, itb, M, N, K, alpha, A, lda, B, ldb, beta, C,
                                               ldc, 1 << 30);
     CHEFSI_CHECK_LAUNCH();

@@ -10,13 +10,20 @@
 
 namespace chefsi {
 
+// The rare cases run out of line behind a branch: inlined, the compiler evaluates them for
+// every entry under a predicate, on the FP64 pipe.
+static __device__ __noinline__ double ldexp_slow(double x, int k) { return ldexp(x, k); }
+static __device__ __noinline__ float ldexpf_slow(float x, int k) {
+  return static_cast<float>(ldexp(static_cast<double>(x), k));
+}
+
 // x * 2^k (exact when the result is a normal double)
 __device__ __forceinline__ double ldexp_exact(double x, int k) {
   const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
   if ((u << 1) == 0) return x;  // +-0
   const int e = static_cast<int>((u >> 52) & 0x7ff);
   const int ne = e + k;
-  if (e == 0 || e == 0x7ff || ne <= 0 || ne >= 0x7ff) return ldexp(x, k);
+  if (__builtin_expect(e == 0 || e == 0x7ff || ne <= 0 || ne >= 0x7ff, 0)) return ldexp_slow(x, k);
   return __longlong_as_double(
       static_cast<long long>((u & 0x800fffffffffffffull) | (static_cast<unsigned long long>(ne) << 52)));
 }
@@ -27,7 +34,7 @@ __device__ __forceinline__ float ldexpf_exact(float x, int k) {
   if ((u << 1) == 0) return x;
   const int e = static_cast<int>((u >> 23) & 0xff);
   const int ne = e + k;
-  if (e == 0 || e == 0xff || ne <= 0 || ne >= 0xff) return static_cast<float>(ldexp(static_cast<double>(x), k));
+  if (__builtin_expect(e == 0 || e == 0xff || ne <= 0 || ne >= 0xff, 0)) return ldexpf_slow(x, k);
   return __uint_as_float((u & 0x807fffffu) | (static_cast<uint32_t>(ne) << 23));
 }
 
@@ -39,7 +46,8 @@ __device__ __forceinline__ double widen_ldexp(float x, int k) {
   if ((u << 1) == 0) return __longlong_as_double(static_cast<long long>(sign));
   const int e = static_cast<int>((u >> 23) & 0xff);
   const int ne = e + 896 + k;
-  if (e == 0 || e == 0xff || ne <= 0 || ne >= 0x7ff) return ldexp(static_cast<double>(x), k);
+  if (__builtin_expect(e == 0 || e == 0xff || ne <= 0 || ne >= 0x7ff, 0))
+    return ldexp_slow(static_cast<double>(x), k);
   return __longlong_as_double(static_cast<long long>(
       sign | (static_cast<unsigned long long>(ne) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
