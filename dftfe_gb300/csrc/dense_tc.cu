@@ -200,7 +200,8 @@ struct GramArgs {
   int* err;
 };
 
-constexpr int kGramThreads = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
+constexpr int kGramEpiWarps = 16;  // four per tensor-memory lane quarter, 32 columns each
+constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // warp 0 TMA, warp 1 MMA, then epilogue
 constexpr int kGramAcc = 3;        // chunk accumulators (128 columns each); columns 384.. hold
                                    // the TwoSum low parts
 constexpr int kGramStage = 4 * kRows8K;
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
   uint64_t* full = bars;                 // [S] TMA bytes landed
   uint64_t* empty = bars + S;            // [S] MMAs done reading the stage
   uint64_t* acc_full = bars + 2 * S;     // [kGramAcc]
-  uint64_t* acc_empty = bars + 2 * S + 4;  // [kGramAcc] 8 epilogue-warp arrivals
+  uint64_t* acc_empty = bars + 2 * S + 4;  // [kGramAcc] one arrival per epilogue warp
   uint64_t* mma_done = bars + 2 * S + 8;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 9);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * S + 10);
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     }
     for (int b = 0; b < kGramAcc; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 8);   // one arrival per epilogue warp
+      mbar_init(&acc_empty[b], kGramEpiWarps);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -337,18 +338,20 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     }
   } else {
     // epilogue: warp w owns tensor-memory lanes 32*(w%4).. (row i) and accumulator columns
-    // 64*((w-2)/4).. It keeps the sum of its 64 entries as FP32 pairs (sh + sl, TwoSum: the
-    // exact error of every addition goes to sl): sh in registers, sl in tensor memory.
+    // 32*((w-2)/4).. It keeps the sum of its 32 entries as FP32 pairs (sh + sl, TwoSum: the
+    // exact error of every addition goes to sl): sh in registers, sl in tensor memory. Four
+    // warps share a lane quarter, so their tensor-memory round trips overlap.
     const int q = warp & 3, hcol = (warp - 2) >> 2;
+    constexpr int kCols = 128 / (kGramEpiWarps / 4);
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-    const uint32_t tl = tmem + 128 * kGramAcc + hcol * 64 + lane_off;
-    float sh[64];
+    const uint32_t tl = tmem + 128 * kGramAcc + hcol * kCols + lane_off;
+    float sh[kCols];
 #pragma unroll
-    for (int c = 0; c < 64; ++c) sh[c] = 0.f;
+    for (int c = 0; c < kCols; ++c) sh[c] = 0.f;
     {
       const uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 8) tmem_st8(tl + c0, z);
+      for (int c0 = 0; c0 < kCols; c0 += 8) tmem_st8(tl + c0, z);
       tmem_wait_st();
     }
     bool ok = true;
@@ -359,10 +362,9 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, a.err, abort_flag));
       if (!ok) break;
       fence_after();
-      const uint32_t tv = tmem + buf * 128 + hcol * 64 + lane_off;
+      const uint32_t tv = tmem + buf * 128 + hcol * kCols + lane_off;
 #pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16) {
-        // 16 columns per tensor-memory round trip (the load latency is the epilogue's cost)
+      for (int c0 = 0; c0 < kCols; c0 += 16) {
         uint32_t rv[16], rl[16];
         tmem_ld16_async(tv + c0, rv);
         tmem_ld16_async(tl + c0, rl);
@@ -387,9 +389,10 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     // the partial in scaled units over the whole (padded) tile; the reduction reads the
     // valid part and undoes the column scalings
     const int i = ti * 128 + q * 32 + lane;
-    double* prow = a.part + (int64_t)slice * a.pstride + (int64_t)i * a.ldp + tj * 128 + hcol * 64;
+    double* prow =
+        a.part + (int64_t)slice * a.pstride + (int64_t)i * a.ldp + tj * 128 + hcol * kCols;
 #pragma unroll
-    for (int c0 = 0; c0 < 64; c0 += 8) {
+    for (int c0 = 0; c0 < kCols; c0 += 8) {
       uint32_t rl[8];
       tmem_ld8_async(tl + c0, rl);
       tmem_wait_ld();

@@ -52,9 +52,22 @@ __device__ __forceinline__ double widen_ldexp(float x, int k) {
       sign | (static_cast<unsigned long long>(ne) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
 
-// (float)(x * 2^k), one rounding
+static __device__ __noinline__ float narrow_slow(double x, int k) {
+  return static_cast<float>(ldexp(x, k));
+}
+
+// (float)(x * 2^k), one rounding. When x and x 2^k both lie in FP32's normal range
+// (unbiased exponent in [-125, 126]), rounding commutes with the scaling: f = fp32(x) is a
+// normal FP32 of exponent e or e + 1 and f 2^k is the exponent field plus k. Everything else
+// (zeros, subnormal or out-of-range values) takes the exact out-of-line path.
 __device__ __forceinline__ float narrow_ldexp(double x, int k) {
-  return static_cast<float>(ldexp_exact(x, k));
+  const int e = ((__double2hiint(x) >> 20) & 0x7ff) - 1023;
+  const float f = __double2float_rn(x);
+  if (__builtin_expect(e < -125 || e > 126 || e + k < -125 || e + k > 126, 0)) {
+    if ((static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0) return f;  // +-0
+    return narrow_slow(x, k);
+  }
+  return __uint_as_float(__float_as_uint(f) + (static_cast<uint32_t>(k) << 23));
 }
 
 // |x| as an order-preserving integer key (non-negative doubles order like their bit patterns)

@@ -83,6 +83,9 @@ struct TcArgs {
   int lookahead;   // K-blocks of X copies in flight per producer thread
   int64_t n_units; // n_cells * n_chunks * n_halves
   float out_scale; // scalar / 2^s
+  const __half* ahi;   // cell-matrix tiles in their shared-memory image (see TensorCellMats)
+  const __half* alo;
+  const __half* alo3;
   int* err;
 };
 
@@ -188,9 +191,7 @@ constexpr int kThreads3 = 192 + 32 * kEpiWarps;
 constexpr int kChunkCols = 96;
 template <int NS, bool KCHUNK>
 __global__ void __launch_bounds__(kThreads3, 1)
-    cell_hx_tc_kernel(const __grid_constant__ CUtensorMap tm_hi,
-                      const __grid_constant__ CUtensorMap tm_lo,
-                      const __grid_constant__ CUtensorMap tm_lo3, TcArgs args) {
+    cell_hx_tc_kernel(TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -256,11 +257,13 @@ __global__ void __launch_bounds__(kThreads3, 1)
           }
           uint8_t* st = smem + L.aoff + s * L.astage;
           mbar_arrive_expect_tx(&tma_full[s], bytes);
-          tma_load_3d(st, &tm_hi, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
-          tma_load_3d(st + L.a_tile, &tm_lo, kb * kKB, w.half * args.n_half, w.cell, &tma_full[s]);
-          if (NS == 3)
-            tma_load_3d(st + 2 * L.a_tile, &tm_lo3, kb * kKB, w.half * args.n_half, w.cell,
-                        &tma_full[s]);
+          // one contiguous block per split term: the (cell, half, K-block) tile, stored in
+          // its swizzled shared-memory image
+          const int64_t tix = ((int64_t)w.cell * args.n_halves + w.half) * nkb + kb;
+          const int64_t toff = tix * (args.n_half * (kRowBytes / 2));
+          bulk_load(st, args.ahi + toff, bytes / NS, &tma_full[s]);
+          bulk_load(st + L.a_tile, args.alo + toff, bytes / NS, &tma_full[s]);
+          if (NS == 3) bulk_load(st + 2 * L.a_tile, args.alo3 + toff, bytes / NS, &tma_full[s]);
           ++issued;
           if (++s == S) s = 0, ++r;
         }
@@ -544,48 +547,52 @@ __global__ void __launch_bounds__(kThreads3, 1)
 }
 
 // ---------------------------------------------------------------- host side
-__global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n_e, int npad,
-                             double scale, __half* __restrict__ hi, __half* __restrict__ lo) {
-  const int64_t n = (int64_t)n_cells * npad * npad;
+// Tensor-core copy of the cell matrices, tile by tile: tile (cell, half, kb) holds rows
+// [half n_half, (half + 1) n_half) and columns [32 kb, 32 kb + 32) of 2^s A_e (zero outside
+// n_e) as n_half rows of 64 bytes in the 64-byte-swizzled shared-memory image, so that the
+// kernel loads a K-block with one bulk copy. Entry t of the array (in storage order) maps to
+// (cell c, row I, column J) of the padded matrix:
+__device__ __forceinline__ void tile_entry(int64_t t, int n_half, int n_halves, int nkb, int& c,
+                                           int& I, int& J) {
+  const int64_t tile_elems = (int64_t)n_half * 32;
+  const int64_t tix = t / tile_elems;
+  const uint32_t p = (uint32_t)(t - tix * tile_elems);
+  const uint32_t o = sw64_offset(0, 2 * p);  // the swizzle is its own inverse
+  const int kb = (int)(tix % nkb);
+  const int64_t ch = tix / nkb;
+  I = (int)(ch % n_halves) * n_half + (int)(o / 64);
+  J = kb * 32 + (int)(o % 64) / 2;
+  c = (int)(ch / n_halves);
+}
+__global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
+                             int n_halves, double scale, __half* __restrict__ hi,
+                             __half* __restrict__ lo) {
+  const int nkb = n_half * n_halves / 32;
+  const int64_t n = (int64_t)n_cells * n_half * n_halves * n_half * n_halves;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = t / ((int64_t)npad * npad);
-    const int r = (int)(t % ((int64_t)npad * npad));
-    const int I = r / npad, J = r % npad;
+    int c, I, J;
+    tile_entry(t, n_half, n_halves, nkb, c, I, J);
     double v = 0.0;
-    if (I < n_e && J < n_e) v = scale * mats[(c * n_e + I) * n_e + J];
+    if (I < n_e && J < n_e) v = scale * mats[((int64_t)c * n_e + I) * n_e + J];
     const __half h = __double2half(v);
     hi[t] = h;
     lo[t] = __double2half(v - (double)__half2float(h));
   }
 }
 
-void make_map(CUtensorMap* m, __half* base, int n_cells, int npad, int box_rows) {
-  EncodeTiledFn enc = get_encode();
-  if (!enc) throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[3] = {(cuuint64_t)npad, (cuuint64_t)npad, (cuuint64_t)n_cells};
-  cuuint64_t strides[2] = {(cuuint64_t)npad * 2, (cuuint64_t)npad * npad * 2};
-  cuuint32_t box[3] = {(cuuint32_t)kKB, (cuuint32_t)box_rows, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, base, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS)
-    throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-}
-
 // third term of the three-term split of the cell matrices: lo3 = fp16(v - hi - lo) with
-// v = 2^s A_e, hi = fp16(v), lo = fp16(v - hi) (the two-term arrays)
-__global__ void k_split_mats_lo3(const double* __restrict__ mats, int n_cells, int n_e, int npad,
-                                 double scale, __half* __restrict__ lo3) {
-  const int64_t n = (int64_t)n_cells * npad * npad;
+// v = 2^s A_e, hi = fp16(v), lo = fp16(v - hi) (the two-term arrays), in the same tile layout
+__global__ void k_split_mats_lo3(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
+                                 int n_halves, double scale, __half* __restrict__ lo3) {
+  const int nkb = n_half * n_halves / 32;
+  const int64_t n = (int64_t)n_cells * n_half * n_halves * n_half * n_halves;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = t / ((int64_t)npad * npad);
-    const int r = (int)(t % ((int64_t)npad * npad));
-    const int I = r / npad, J = r % npad;
+    int c, I, J;
+    tile_entry(t, n_half, n_halves, nkb, c, I, J);
     double v = 0.0;
-    if (I < n_e && J < n_e) v = scale * mats[(c * n_e + I) * n_e + J];
+    if (I < n_e && J < n_e) v = scale * mats[((int64_t)c * n_e + I) * n_e + J];
     const double h = (double)__half2float(__double2half(v));
     const double l = (double)__half2float(__double2half(v - h));
     lo3[t] = __double2half(v - h - l);
@@ -763,8 +770,9 @@ void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st) {
   const size_t n = (size_t)op->n_cells * p.npad * p.npad;
   tc.hi.reset(n);
   tc.lo.reset(n);
-  k_split_mats<<<grid_for((int64_t)n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, n_e, p.npad,
-                                                          std::ldexp(1.0, e), tc.hi.ptr, tc.lo.ptr);
+  k_split_mats<<<grid_for((int64_t)n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, n_e, p.n_half,
+                                                          p.n_halves, std::ldexp(1.0, e), tc.hi.ptr,
+                                                          tc.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
   tc.ready = true;
   tc.lo3_ready = false;
@@ -777,8 +785,9 @@ static void prepare_tensor_mats_lo3(chefsi_operator_s* op, cudaStream_t st) {
   if (tc.lo3_ready) return;
   const size_t n = (size_t)op->n_cells * tc.npad * tc.npad;
   tc.lo3.reset(n);
+  const TcPlan p = plan_for(op->n_e, 2);
   k_split_mats_lo3<<<grid_for((int64_t)n, 256), 256, 0, st>>>(
-      op->mats64.ptr, op->n_cells, op->n_e, tc.npad, (double)tc.scale, tc.lo3.ptr);
+      op->mats64.ptr, op->n_cells, op->n_e, p.n_half, p.n_halves, (double)tc.scale, tc.lo3.ptr);
   CHEFSI_CHECK_LAUNCH();
   tc.lo3_ready = true;
 }
@@ -802,10 +811,9 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const
     op->tc_err.reset(1);
     CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
   }
-  CUtensorMap mhi, mlo, mlo3;
-  make_map(&mhi, op->tc.hi.ptr, op->n_cells, p.npad, p.n_half);
-  make_map(&mlo, op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
-  make_map(&mlo3, ns == 3 ? op->tc.lo3.ptr : op->tc.lo.ptr, op->n_cells, p.npad, p.n_half);
+  a.ahi = op->tc.hi.ptr;
+  a.alo = op->tc.lo.ptr;
+  a.alo3 = ns == 3 ? op->tc.lo3.ptr : op->tc.lo.ptr;
   a.xhi = xhi;
   a.xlo = xlo;
   a.xlo3 = ns == 3 ? xlo3 : xlo;
@@ -837,7 +845,7 @@ static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t grid = std::min<int64_t>(sms, a.n_units / p.n_halves);
-  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(mhi, mlo, mlo3, a);
+  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -72,6 +72,25 @@ static __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap*
       : "memory");
 }
 
+// one contiguous global block -> shared memory (cp.async.bulk; 16-byte aligned addresses, size
+// a multiple of 16), completing transaction bytes on the mbarrier
+static __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                                 uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// byte offset of (row r, byte b) of a K-major tile of 64-byte rows in the 64-byte-swizzled
+// shared-memory image (the layout TMA writes with SWIZZLE_64B): the 16-byte chunk index
+// (bits 4-5) is XORed with bits 7-8 of the offset
+static __host__ __device__ __forceinline__ uint32_t sw64_offset(uint32_t r, uint32_t b) {
+  const uint32_t o = r * 64u + b;
+  return o ^ (((o >> 7) & 3u) << 4);
+}
+
 // tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512 B apart
 static __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
   uint64_t d = 0;
