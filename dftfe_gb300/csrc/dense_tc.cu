@@ -93,7 +93,9 @@ __device__ __forceinline__ void split_half_f32(float v, __half& h, __half& l) {
   l = __float2half_rn(v - __half2float(h));
 }
 
-// [M][N] (ld) -> hi/lo [Np][Kp] (dof index fastest), column j scaled by sc[j]; zero padding
+// [M][N] (ld) -> hi/lo, column j scaled by 2^ex[j], zero padding to Np columns and Kp dofs,
+// stored as tiles of 128 columns x 32 dofs ([Np / 128][Kp / 32][4096 halves]), each tile the
+// 64-byte-swizzled shared-memory image of a K-major operand (one bulk copy per tile)
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_split_t(const T* __restrict__ X, int64_t ld, int64_t M, int N, const int* __restrict__ ex,
@@ -115,7 +117,11 @@ __global__ void __launch_bounds__(256)
     __half h0, l0, h1, l1;
     split_half_f32(tile[c][2 * p], h0, l0);
     split_half_f32(tile[c][2 * p + 1], h1, l1);
-    const int64_t o = (int64_t)(j0 + c) * Kp + k0 + 2 * p;
+    // tile (panel of 128 columns, K-block of 32 dofs), 64-byte-swizzled image, 4096 halves
+    const int jj = j0 + c;
+    const int64_t k = k0 + 2 * p;
+    const int64_t o = (((int64_t)(jj >> 7) * (Kp / 32) + (k >> 5)) << 12) +
+                      (sw64_offset((uint32_t)(jj & 127), 2u * (uint32_t)(k & 31)) >> 1);
     *reinterpret_cast<__half2*>(hi + o) = __halves2half2(h0, h1);
     *reinterpret_cast<__half2*>(lo + o) = __halves2half2(l0, l1);
   }
@@ -196,6 +202,10 @@ struct GramArgs {
   int stages;
   int n1, n2;    // valid output rows / columns
   double* part;  // [kslices][padded n1][ldp = padded n2], scaled units
+  const __half* a_hi;  // operand tiles [panel][K-block][4096 halves]
+  const __half* a_lo;
+  const __half* b_hi;
+  const __half* b_lo;
   int64_t ldp, pstride;
   int* err;
 };
@@ -220,9 +230,7 @@ __device__ __forceinline__ void gram_tile(int t, const GramArgs& a, int& ti, int
 }
 
 __global__ void __launch_bounds__(kGramThreads, 1)
-    gram_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_constant__ CUtensorMap ma_lo,
-                   const __grid_constant__ CUtensorMap mb_hi, const __grid_constant__ CUtensorMap mb_lo,
-                   GramArgs a) {
+    gram_tc_kernel(GramArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -277,11 +285,13 @@ __global__ void __launch_bounds__(kGramThreads, 1)
           }
           uint8_t* st = smem + s * kGramStage;
           mbar_arrive_expect_tx(&full[s], diag ? 2 * kRows8K : 4 * kRows8K);
-          tma_load_2d(st, &ma_hi, kb * kKB, ti * 128, &full[s]);
-          tma_load_2d(st + kRows8K, &ma_lo, kb * kKB, ti * 128, &full[s]);
+          const int64_t ta = ((int64_t)ti * a.nkb + kb) * (kRows8K / 2);
+          bulk_load(st, a.a_hi + ta, kRows8K, &full[s]);
+          bulk_load(st + kRows8K, a.a_lo + ta, kRows8K, &full[s]);
           if (!diag) {
-            tma_load_2d(st + 2 * kRows8K, &mb_hi, kb * kKB, tj * 128, &full[s]);
-            tma_load_2d(st + 3 * kRows8K, &mb_lo, kb * kKB, tj * 128, &full[s]);
+            const int64_t tb = ((int64_t)tj * a.nkb + kb) * (kRows8K / 2);
+            bulk_load(st + 2 * kRows8K, a.b_hi + tb, kRows8K, &full[s]);
+            bulk_load(st + 3 * kRows8K, a.b_lo + tb, kRows8K, &full[s]);
           }
           ++g;
           if (++s == S) s = 0, ++r;
@@ -683,13 +693,11 @@ void tc_gram(const TcOperand& A, const TcOperand* B, double* C, int64_t ldc, boo
   const int64_t pstride = (int64_t)A.padded * ldp;
   double* part = w.part.ensure((size_t)kslices * pstride);
 
-  CUtensorMap ahi, alo, bhi, blo;
-  make_map_2d(&ahi, A.hi.ptr, A.ld, A.padded, A.ld, kKB, 128);
-  make_map_2d(&alo, A.lo.ptr, A.ld, A.padded, A.ld, kKB, 128);
-  make_map_2d(&bhi, Bo.hi.ptr, Bo.ld, Bo.padded, Bo.ld, kKB, 128);
-  make_map_2d(&blo, Bo.lo.ptr, Bo.ld, Bo.padded, Bo.ld, kKB, 128);
-
   GramArgs g{};
+  g.a_hi = A.hi.ptr;
+  g.a_lo = A.lo.ptr;
+  g.b_hi = Bo.hi.ptr;
+  g.b_lo = Bo.lo.ptr;
   g.n_tiles = n_tiles;
   g.tiles_j = tj_n;
   g.lower = lower ? 1 : 0;
@@ -708,7 +716,7 @@ void tc_gram(const TcOperand& A, const TcOperand* B, double* C, int64_t ldc, boo
   CHEFSI_CUDA(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   const int64_t grid = (int64_t)n_tiles * kslices;
   CHEFSI_REQUIRE(grid < (1ll << 31), "tensor-core Gram: grid too large");
-  gram_tc_kernel<<<(unsigned)grid, kGramThreads, smem, st>>>(ahi, alo, bhi, blo, g);
+  gram_tc_kernel<<<(unsigned)grid, kGramThreads, smem, st>>>(g);
   CHEFSI_CHECK_LAUNCH();
   k_gram_reduce<<<grid_for((int64_t)n1 * n2, 256), 256, 0, st>>>(
       part, kslices, pstride, ldp, n1, n2, lower ? 1 : 0, A.e.ptr, Bo.e.ptr, C, ldc);

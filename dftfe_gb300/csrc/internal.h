@@ -135,8 +135,10 @@ void absmax_block_f32(const float* x, int64_t ld, int64_t rows, int B, double* o
 
 // ---- tensor-core dense products (dense_tc.cu) ---------------------------------------------
 // FP16 hi/lo split of a block of vectors, each column scaled by 2^e[j] (max |entry| in
-// [2^14, 2^15)). Transposed layout [padded columns][ld = padded rows] feeds the Gram
-// products; row layout [rows][ld = padded columns] feeds the rotation.
+// [2^14, 2^15)). The transposed split (ld = rows padded to 64) is stored as tiles of 128
+// columns x 32 rows, each the swizzled shared-memory image of a K-major Gram operand
+// ([padded / 128][ld / 32][4096 halves]); the row split [rows][ld = padded columns] feeds the
+// rotation.
 struct TcOperand {
   DeviceBuffer<__half> hi, lo;
   DeviceBuffer<int> e;                     // column exponents
