@@ -26,9 +26,13 @@
 //     Y^T. Tiles are 128 output columns x 256 dofs, persistent CTAs, double-buffered
 //     accumulators; the epilogue writes FP64 rows of Y with 256-byte coalesced stores. The
 //     FP16 copy of X is read, so Y may be X itself (in-place rotation).
-// Operands are staged by TMA (64-byte swizzle, K-major) through an mbarrier ring; one lane
-// issues the MMAs. Every wait is bounded: on expiry the CTA records CHEFSI_ERR_TIMEOUT,
-// waits (bounded) for its own copies, frees its tensor memory and returns.
+// The split kernels store every operand as tiles (128 or 256 rows x 32 K entries) that are
+// already the 64-byte-swizzled, K-major shared-memory image the MMA descriptors read, so a
+// K-block stage is a few bulk copies (cp.async.bulk) through an mbarrier ring. Tensor-map
+// (TMA tensor) loads of the same boxes fetch 128 or 256 rows of 64 bytes each, and their row
+// rate bounded the Gram at ~0.4 rows per clock per SM (28 ms at config 1 vs 7.5 ms with the
+// tiles). One lane issues the MMAs. Every wait is bounded: on expiry the CTA records
+// CHEFSI_ERR_TIMEOUT, waits (bounded) for its own copies, frees its tensor memory and returns.
 #include "internal.h"
 #include "tc_common.cuh"
 #include "pow2.cuh"
@@ -127,33 +131,41 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// [M][N] (ld) -> hi/lo [M][Kr] (row-major, columns zero-padded to Kr, Kr % 4 == 0), column j
-// scaled by 2^ex[j]. A block of 256 threads covers (256 / tpr) rows x tpr quads of columns
-// (tpr = 2^log_tpr), so no index needs an integer division.
+// [M][N] (ld) -> hi/lo, column j scaled by 2^ex[j], columns zero-padded to Kr (Kr % 32 == 0)
+// and rows to Mp (a multiple of 256), stored as tiles of 256 rows x 32 columns
+// ([Mp / 256][Kr / 32][8192 halves]), each the 64-byte-swizzled shared-memory image of a
+// K-major rotation operand. A warp handles 4 rows x one 32-column K-block per step (lane =
+// row 4 + 4-column quad): it writes 4 whole 64-byte tile rows, 256 contiguous bytes.
 template <typename T>
-__global__ void k_split_r(const T* __restrict__ X, int64_t ld, int64_t M, int N,
-                          const int* __restrict__ ex, int Kr, int log_tpr, __half* __restrict__ hi,
+__global__ void k_split_r(const T* __restrict__ X, int64_t ld, int64_t M, int64_t Mp, int N,
+                          const int* __restrict__ ex, int Kr, __half* __restrict__ hi,
                           __half* __restrict__ lo) {
-  const int tpr = 1 << log_tpr;
-  const int q0 = threadIdx.x & (tpr - 1);
-  const int rpb = blockDim.x >> log_tpr;
-  for (int64_t r = (int64_t)blockIdx.x * rpb + (threadIdx.x >> log_tpr); r < M;
-       r += (int64_t)gridDim.x * rpb) {
-    const T* xr = X + r * ld;
-    for (int q = q0; q < Kr / 4; q += tpr) {
-      const int j = 4 * q;
-      __half h[4], l[4];
+  const int lane = threadIdx.x & 31;
+  const int rr = lane >> 3, qq = lane & 7;
+  const int nkb = Kr / 32;
+  const int64_t items = (Mp / 4) * nkb;
+  const int64_t wstep = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < items;
+       w += wstep) {
+    const int64_t rb = w / nkb;
+    const int kb = (int)(w - rb * nkb);
+    const int64_t r = rb * 4 + rr;
+    const int j = kb * 32 + qq * 4;
+    __half h[4], l[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) split_half_f32(j + i < N ? scaled_f32(xr[j + i], ex[j + i]) : 0.f, h[i], l[i]);
-      __half2 hv[2] = {__halves2half2(h[0], h[1]), __halves2half2(h[2], h[3])};
-      __half2 lv[2] = {__halves2half2(l[0], l[1]), __halves2half2(l[2], l[3])};
-      *reinterpret_cast<uint2*>(hi + r * Kr + j) = *reinterpret_cast<const uint2*>(hv);
-      *reinterpret_cast<uint2*>(lo + r * Kr + j) = *reinterpret_cast<const uint2*>(lv);
-    }
+    for (int i = 0; i < 4; ++i)
+      split_half_f32(r < M && j + i < N ? scaled_f32(X[r * ld + j + i], ex[j + i]) : 0.f, h[i], l[i]);
+    __half2 hv[2] = {__halves2half2(h[0], h[1]), __halves2half2(h[2], h[3])};
+    __half2 lv[2] = {__halves2half2(l[0], l[1]), __halves2half2(l[2], l[3])};
+    const int64_t o = (((r >> 8) * nkb + kb) << 13) +
+                      (sw64_offset((uint32_t)(r & 255), 8u * (uint32_t)qq) >> 1);
+    *reinterpret_cast<uint2*>(hi + o) = *reinterpret_cast<const uint2*>(hv);
+    *reinterpret_cast<uint2*>(lo + o) = *reinterpret_cast<const uint2*>(lv);
   }
 }
 
-// Rotation operand: Wt[m][k] = W[k][m] 2^(t_m - e_k) as FP16 hi/lo [Mp][Kr] (W is K x n_out),
+// Rotation operand: Wt[m][k] = W[k][m] 2^(t_m - e_k) as FP16 hi/lo tiles of 128 m x 32 k
+// ([Mp / 128][Kr / 32][4096 halves], swizzled shared-memory images; W is K x n_out),
 // with t_m the exponent that puts column m of diag(2^-e) W into [2^14, 2^15). One block per
 // output column.
 __global__ void __launch_bounds__(256)
@@ -185,8 +197,11 @@ __global__ void __launch_bounds__(256)
     const double v = (m < n_out && k < K) ? ldexp(W[(int64_t)k * ldw + m], tm - e[k]) : 0.0;
     __half h, l;
     split_half(v, h, l);
-    hi[(int64_t)m * Kr + k] = h;
-    lo[(int64_t)m * Kr + k] = l;
+    // tile (128 output columns, 32 k), 64-byte-swizzled image of 4096 halves
+    const int64_t o = (((int64_t)(m >> 7) * (Kr / 32) + (k >> 5)) << 12) +
+                      (sw64_offset((uint32_t)(m & 127), 2u * (uint32_t)(k & 31)) >> 1);
+    hi[o] = h;
+    lo[o] = l;
   }
 }
 
@@ -211,7 +226,7 @@ struct GramArgs {
 };
 
 constexpr int kGramEpiWarps = 16;  // four per tensor-memory lane quarter, 32 columns each
-constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // warp 0 TMA, warp 1 MMA, then epilogue
+constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // warp 0 copies, warp 1 MMA, then epilogue
 constexpr int kGramAcc = 3;        // chunk accumulators (128 columns each); columns 384.. hold
                                    // the TwoSum low parts
 constexpr int kGramStage = 4 * kRows8K;
@@ -236,7 +251,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int S = a.stages;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * kGramStage);
-  uint64_t* full = bars;                 // [S] TMA bytes landed
+  uint64_t* full = bars;                 // [S] stage bytes landed
   uint64_t* empty = bars + S;            // [S] MMAs done reading the stage
   uint64_t* acc_full = bars + 2 * S;     // [kGramAcc]
   uint64_t* acc_empty = bars + 2 * S + 4;  // [kGramAcc] one arrival per epilogue warp
@@ -445,15 +460,17 @@ struct RotArgs {
   double* Y;
   int64_t ldy;
   int* err;
+  const __half* w_hi;  // W' tiles [m panel][K-block][4096 halves]
+  const __half* w_lo;
+  const __half* x_hi;  // X row-split tiles [256-row panel][K-block][8192 halves]
+  const __half* x_lo;
 };
 
-constexpr int kRotThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int kRotThreads = 192;  // warp 0 copies, warp 1 MMA, warps 2..5 epilogue
 constexpr int kRotStage = 2 * kRows8K + 4 * kRows8K;  // A hi/lo (128 rows), B hi/lo (256 rows)
 
 __global__ void __launch_bounds__(kRotThreads, 1)
-    rotate_tc_kernel(const __grid_constant__ CUtensorMap mw_hi, const __grid_constant__ CUtensorMap mw_lo,
-                     const __grid_constant__ CUtensorMap mx_hi, const __grid_constant__ CUtensorMap mx_lo,
-                     RotArgs a) {
+    rotate_tc_kernel(RotArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -506,10 +523,13 @@ __global__ void __launch_bounds__(kRotThreads, 1)
           }
           uint8_t* st = smem + s * kRotStage;
           mbar_arrive_expect_tx(&full[s], kRotStage);
-          tma_load_2d(st, &mw_hi, kb * kKB, mt * 128, &full[s]);
-          tma_load_2d(st + kRows8K, &mw_lo, kb * kKB, mt * 128, &full[s]);
-          tma_load_2d(st + 2 * kRows8K, &mx_hi, kb * kKB, nt * 256, &full[s]);
-          tma_load_2d(st + 4 * kRows8K, &mx_lo, kb * kKB, nt * 256, &full[s]);
+          // one bulk copy per operand tile (swizzled shared-memory images)
+          const int64_t tw = ((int64_t)mt * a.nkb + kb) * (kRows8K / 2);
+          const int64_t tx = ((int64_t)nt * a.nkb + kb) * kRows8K;
+          bulk_load(st, a.w_hi + tw, kRows8K, &full[s]);
+          bulk_load(st + kRows8K, a.w_lo + tw, kRows8K, &full[s]);
+          bulk_load(st + 2 * kRows8K, a.x_hi + tx, 2 * kRows8K, &full[s]);
+          bulk_load(st + 4 * kRows8K, a.x_lo + tx, 2 * kRows8K, &full[s]);
           ++g;
           if (++s == S) s = 0, ++r;
         }
@@ -652,14 +672,13 @@ void tc_split_rows(const T* X, int64_t ld, int64_t M, int N, TcOperand& op, cuda
   op.transposed = false;
   op.ld = (N + 63) / 64 * 64;                 // Kr: columns, zero-padded
   op.padded = (int)op.ld;
-  const size_t n = (size_t)M * op.ld;
+  const int64_t Mp = (M + 255) / 256 * 256;   // rows, zero-padded to whole 256-row tiles
+  const size_t n = (size_t)Mp * op.ld;
   op.hi.ensure(n);
   op.lo.ensure(n);
-  int log_tpr = 0;
-  while (log_tpr < 8 && (1 << log_tpr) < op.ld / 4) ++log_tpr;
-  const int rpb = 256 >> log_tpr;
-  k_split_r<T><<<grid_for((M + rpb - 1) / rpb, 1), 256, 0, st>>>(X, ld, M, N, op.e.ptr, (int)op.ld,
-                                                                  log_tpr, op.hi.ptr, op.lo.ptr);
+  const int64_t items = (Mp / 4) * (op.ld / 32);   // one per warp step (8 warps a block)
+  k_split_r<T><<<grid_for((items + 7) / 8, 1), 256, 0, st>>>(X, ld, M, Mp, N, op.e.ptr,
+                                                              (int)op.ld, op.hi.ptr, op.lo.ptr);
   CHEFSI_CHECK_LAUNCH();
 }
 
@@ -742,13 +761,11 @@ void tc_rotate(const TcOperand& Xr, const double* W, int64_t ldw, int n_out, dou
                                       w.wlo.ptr);
   CHEFSI_CHECK_LAUNCH();
 
-  CUtensorMap whi, wlo, xhi, xlo;
-  make_map_2d(&whi, w.whi.ptr, Kr, Mp, Kr, kKB, 128);
-  make_map_2d(&wlo, w.wlo.ptr, Kr, Mp, Kr, kKB, 128);
-  make_map_2d(&xhi, Xr.hi.ptr, Kr, Xr.rows, Kr, kKB, 256);
-  make_map_2d(&xlo, Xr.lo.ptr, Kr, Xr.rows, Kr, kKB, 256);
-
   RotArgs r{};
+  r.w_hi = w.whi.ptr;
+  r.w_lo = w.wlo.ptr;
+  r.x_hi = Xr.hi.ptr;
+  r.x_lo = Xr.lo.ptr;
   r.m_tiles = Mp / 128;
   r.n_tiles = ((Xr.rows + 255) / 256) * r.m_tiles;
   r.nkb = Kr / kKB;
@@ -762,7 +779,7 @@ void tc_rotate(const TcOperand& Xr, const double* W, int64_t ldw, int n_out, dou
   const int smem = rot_smem(r.stages);
   CHEFSI_CUDA(cudaFuncSetAttribute(rotate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   const int64_t grid = std::min<int64_t>(device_sms(), r.n_tiles);
-  rotate_tc_kernel<<<(unsigned)grid, kRotThreads, smem, st>>>(whi, wlo, xhi, xlo, r);
+  rotate_tc_kernel<<<(unsigned)grid, kRotThreads, smem, st>>>(r);
   CHEFSI_CHECK_LAUNCH();
 }
 

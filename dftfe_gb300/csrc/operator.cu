@@ -1074,12 +1074,25 @@ chefsi_operator_s* create_operator(const chefsi_operator_desc* d) {
       k_to_f32<<<grid_for(op->nl_nnz * d->n_proj, 256), 256>>>(
           op->nl_vals64.ptr, op->nl_vals32.ptr, op->nl_nnz * d->n_proj);
       CHEFSI_CHECK_LAUNCH();
-      std::vector<int> ca, cr;
+      // chunks of kNlChunk rows of one atom, ordered by their smallest dof: with spatially
+      // ordered dofs, the chunks of overlapping projector supports then run at about the same
+      // time and the rows they share (1.4 supports per row in dense wells) are re-read and
+      // re-reduced in L2 instead of HBM
+      std::vector<std::pair<int, std::pair<int, int>>> chunks;
       for (int a = 0; a < d->n_atoms; ++a)
         for (int r = d->atom_dof_ptr[a]; r < d->atom_dof_ptr[a + 1]; r += kNlChunk) {
-          ca.push_back(a);
-          cr.push_back(r);
+          const int r1 = std::min(r + kNlChunk, d->atom_dof_ptr[a + 1]);
+          int dmin = d->atom_dofs[r];
+          for (int i = r + 1; i < r1; ++i) dmin = std::min(dmin, d->atom_dofs[i]);
+          chunks.push_back({dmin, {a, r}});
         }
+      std::stable_sort(chunks.begin(), chunks.end(),
+                       [](const auto& x, const auto& y) { return x.first < y.first; });
+      std::vector<int> ca, cr;
+      for (const auto& c : chunks) {
+        ca.push_back(c.second.first);
+        cr.push_back(c.second.second);
+      }
       op->nl_n_chunks = (int)ca.size();
       upload(op->nl_chunk_atom, ca.data(), ca.size());
       upload(op->nl_chunk_row0, cr.data(), cr.size());

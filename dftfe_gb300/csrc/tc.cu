@@ -7,8 +7,9 @@
 // rows (written by the recurrence step that reads them anyway), and one CTA owns one
 // (cell, 128-vector chunk, half of the cell's rows) at a time:
 //   * producer warps copy the chunk's X rows through the cell's dof map (cp.async, 16-byte
-//     pieces) into a 128B-swizzled, MN-major tile, and TMA loads the cell-matrix K-block
-//     (FP16 hi and lo of 2^s A_e, K-major, 64B-swizzled);
+//     pieces) into a 128B-swizzled, MN-major tile, and one bulk copy per split term loads
+//     the cell-matrix K-block (FP16 hi and lo of 2^s A_e, stored tile by tile as the K-major,
+//     64B-swizzled shared-memory image);
 //   * one lane issues tcgen05.mma kind::f16 with M = 128 vectors, N = the half's rows
 //     (<= 256), K = 16:  D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T  (lo*lo is below 2^-22);
 //   * the epilogue warps read D with tcgen05.ld (lane = vector) and scatter-add
@@ -20,18 +21,15 @@
 //     Measured and rejected: float4 reductions after a lane-quad transpose (1.6x slower),
 //     plain load + store for the rows only one cell touches (more latency on the same
 //     critical path, 1.08x slower), L2 prefetch of the output rows (1.07x slower).
-// An mbarrier pipeline of up to 8 stages overlaps the TMA, the MMAs and the scatter of the
+// An mbarrier pipeline of up to 8 stages overlaps the copies, the MMAs and the scatter of the
 // previous unit. Every mbarrier wait is bounded: on expiry the CTA records
-// CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own TMA copies, frees its
+// CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own bulk copies, frees its
 // tensor memory and returns.
 #include "internal.h"
 #include "tc_common.cuh"
 
-#include <cuda.h>
-
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 #include <vector>
 
 namespace chefsi {
@@ -167,7 +165,7 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 // Persistent warp-specialised kernel, one CTA per SM. Work unit = (cell, 128-vector chunk,
 // row half of the cell matrix). The filter keeps its vectors also as FP16 hi + lo rows
 // [dof][vectors], which are exactly the rows of an MN-major A operand (M = vectors):
-//   warp 0        TMA of the cell-matrix K-blocks (hi, lo; K-major, 64B-swizzled)
+//   warp 0        bulk copies of the cell-matrix K-block tiles (hi, lo; K-major, 64B-swizzled)
 //   warp 1        tcgen05.mma issue (one lane): D[vector][row] += Xhi Ahi + Xhi Alo + Xlo Ahi,
 //                 M = 128 vectors, N = the half's rows, K = 16; two accumulators in tensor
 //                 memory
@@ -198,7 +196,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
   const int S = args.stages, SX = args.xstages;
   const Layout L = make_layout(args.n_half, S, SX, NS);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
-  uint64_t* tma_full = bars;            // [S] cell-matrix TMA bytes landed
+  uint64_t* tma_full = bars;            // [S] cell-matrix tile bytes landed
   uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
   uint64_t* x_full = bars + 2 * S;      // [SX] 4 producer-warp arrivals (their copies landed)
   uint64_t* x_empty = bars + 2 * S + SX;   // [SX] MMA finished reading the X stage
@@ -241,7 +239,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    // ---------------- TMA producer of the cell-matrix K-blocks
+    // ---------------- bulk-copy producer of the cell-matrix K-blocks
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)NS * args.n_half * kRowBytes;
       int64_t issued = 0;
@@ -707,43 +705,7 @@ TcPlan plan_for(int n_e, int ns) {
 }  // namespace
 
 namespace tcx {
-EncodeTiledFn get_encode() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-    else
-      cudaGetLastError();
-  });
-  return fn;
-}
-
-void make_map_2d(CUtensorMap* m, const __half* base, int64_t inner, int64_t rows, int64_t ld,
-                 int box_inner, int box_rows) {
-  EncodeTiledFn enc = get_encode();
-  if (!enc) throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(base) & 15) == 0 && (ld * 2) % 16 == 0 &&
-                     (box_inner * 2) % 16 == 0 && box_rows <= 256 && box_inner <= 256,
-                 "tensor map: unaligned base, row stride or box");
-  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half*>(base), dims, strides,
-                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS)
-    throw Error(CHEFSI_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-}
-
 bool tcgen05_device() {
-  if (!get_encode()) return false;
   int dev = 0, major = 0;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));

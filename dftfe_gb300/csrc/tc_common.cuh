@@ -3,7 +3,6 @@
 
 #include "common.cuh"
 
-#include <cuda.h>
 #include <cuda_fp16.h>
 
 namespace chefsi {
@@ -61,15 +60,6 @@ static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
   atomicExch(err, CHEFSI_ERR_TIMEOUT);
   *abort_flag = 1;
   return false;
-}
-
-static __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
 }
 
 // one contiguous global block -> shared memory (cp.async.bulk; 16-byte aligned addresses, size
@@ -214,15 +204,6 @@ static __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-static __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
 static __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t cols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                    smem_u32(slot)),
@@ -234,16 +215,7 @@ static __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t col
 }
 
 // ---- host side
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn get_encode();
-// 2D FP16 tensor map [rows][inner] with row stride ld (elements), box [box_rows][box_inner],
-// 64-byte swizzle (box_inner = 32 halves)
-void make_map_2d(CUtensorMap* m, const __half* base, int64_t inner, int64_t rows, int64_t ld,
-                 int box_inner, int box_rows);
-// true on an sm_100-family device with the tensor-map encoder available
+// true on an sm_100-family device (tcgen05, tensor memory, bulk async copies)
 bool tcgen05_device();
 
 }  // namespace tcx
