@@ -87,7 +87,7 @@ class ClockSampler:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one cell_hx_tc_kernel launch (ncu capture of
 # `bench.py --workload mixed --hx-only`, summarised in profiles/cell_hx_tc_mixed_traffic.md)
-TC_TRAFFIC_BYTES = {"mixed": 20.99e9 + 8.29e9}
+TC_TRAFFIC_BYTES = {"mixed": 20.33e9 + 8.20e9}
 
 
 def hx_algorithmic(pr, B, s_h=4, s_x=4):

@@ -1186,12 +1186,11 @@ static void back_transform_wy(const double* V, const double* tau, int N, double*
   for (int end = nrefl; end > 0; end -= kWY) {
     const int k0 = std::max(0, end - kWY), nb = end - k0;
     const double* Vb = Vc.ptr + k0;
-    CHEFSI_CUDA(cudaMemsetAsync(G.ptr, 0, sizeof(double) * nb * nb, st));
-    gram_f64(Vb, N, Vb, N, N, nb, nb, G.ptr, nb, CHEFSI_PREC_FP64, false, st);
+    // the two long-K products (K = N) of the block: the split-K FP64 GEMM
+    gemm_f64('T', 'N', nb, nb, N, 1.0, Vb, N, Vb, N, 0.0, G.ptr, nb, CHEFSI_PREC_FP64, st);
     k_build_t<<<1, kWY, 0, st>>>(G.ptr, tau + k0, nb, T.ptr);
     CHEFSI_CHECK_LAUNCH();
-    CHEFSI_CUDA(cudaMemsetAsync(W1.ptr, 0, sizeof(double) * nb * N, st));
-    gram_f64(Vb, N, Z, N, N, nb, N, W1.ptr, N, CHEFSI_PREC_FP64, false, st);        // Vb^T Z
+    gemm_f64('T', 'N', nb, N, N, 1.0, Vb, N, Z, N, 0.0, W1.ptr, N, CHEFSI_PREC_FP64, st);  // Vb^T Z
     gemm_f64('N', 'N', nb, N, nb, 1.0, T.ptr, nb, W1.ptr, N, 0.0, W2.ptr, N,
              CHEFSI_PREC_FP64, st);                                                   // T (Vb^T Z)
     gemm_f64('N', 'N', N, N, nb, -1.0, Vb, N, W2.ptr, N, 1.0, Z, N, CHEFSI_PREC_FP64, st);
