@@ -623,14 +623,14 @@ __global__ void __launch_bounds__(kRotThreads, 1)
 int gram_smem(int stages) { return stages * kGramStage + 8 * (2 * stages + 12) + 1024; }
 int rot_smem(int stages) { return stages * kRotStage + 8 * (2 * stages + 8) + 1024; }
 
+}  // namespace
+
 int device_sms() {
   int dev = 0, sms = kNumSMs;
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   return sms;
 }
-
-}  // namespace
 
 // ======================================================================= host API
 bool dense_tc_available() { return tcgen05_device(); }

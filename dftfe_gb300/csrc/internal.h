@@ -89,6 +89,27 @@ void hx_c64(chefsi_operator_s* op, const cplx* src, int64_t lds, cplx* dst, int6
 // tensor-core (FP16 split) apply on FP32 vectors; returns false if unavailable for this op
 bool hx_tc(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, int64_t ldd, int B,
            double scalar, bool accumulate, cudaStream_t st);
+// One member of a grouped tensor-core apply: dst += scalar * A src (local part only), the
+// input given by its FP16 split rows [n_dofs][B] (xlo3 for the three-term split).
+struct TcGroupItem {
+  chefsi_operator_s* op;
+  const __half* xhi;
+  const __half* xlo;
+  const __half* xlo3;
+  float* dst;
+  int64_t ldd;
+  int B;
+  double scalar;
+};
+// pipeline shape of the tensor-core apply (X-ring depth, K-blocks of copies in flight)
+struct TcPipeline {
+  int xstages;
+  int lookahead;
+};
+// one persistent launch over up to 32 applies of operators with the same cell type
+void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipeline* pipe,
+                        cudaStream_t st);
+int device_sms();
 // the same with the three-term split (33 bits: src exactly, the cell matrices to 2^-33; six
 // products, FP32 accumulation): the accuracy class of the FP32 apply. src must be scaled so
 // that max |src| < 2^15.

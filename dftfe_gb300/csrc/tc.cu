@@ -60,18 +60,34 @@ constexpr uint32_t kXAtomM = 1024;   // byte step between the two 64-vector atom
 constexpr uint32_t kXGroupK = 2048;  // byte step between 8-node groups
 constexpr int kXTile = 8192;         // 32 nodes x 128 vectors x 2 B
 
-struct TcArgs {
-  const __half* xhi;
+// One operator applied to one block of vectors. A launch takes a group of these (operators of
+// the same cell type: the same n_e and tile shapes), so many Hamiltonians of uneven mesh and
+// block sizes share one persistent launch; a single apply is a group of one.
+struct TcProblem {
+  const __half* xhi;   // split rows [rows][ldx]
   const __half* xlo;
   const __half* xlo3;  // third term of the three-term split (NS == 3)
-  int64_t ldx;     // halves
-  float* dst;
+  float* dst;          // output rows [rows][ldd]
+  const int* map;      // [n_cells][n_e]
+  const __half* ahi;   // cell-matrix tiles in their shared-memory image (see TensorCellMats)
+  const __half* alo;
+  const __half* alo3;
+  int64_t ldx;         // halves
   int64_t ldd;
-  const int* map;
+  int64_t pair_begin;  // first (cell, chunk) pair of this problem in the group's enumeration
+  int B;               // vectors
+  int n_chunks;        // 128-vector chunks
+  float out_scale;     // scalar / 2^s
+  int pad_;
+};
+constexpr int kMaxGroup = 32;
+
+struct TcArgs {
+  TcProblem prob[kMaxGroup];
+  int n_probs;
+  int64_t n_pairs; // (cell, chunk) pairs over the group
   int n_e;
   int nkb;         // K-blocks of 32 nodes
-  int B;
-  int n_chunks;    // 128-vector chunks
   int n_half;      // cell rows per work unit (= MMA N)
   int n_halves;    // row halves per cell (1 or 2)
   int buf_stride;  // tensor-memory column offset of accumulator 1
@@ -79,13 +95,9 @@ struct TcArgs {
   int stages;      // cell-matrix ring depth
   int xstages;     // X ring depth
   int lookahead;   // K-blocks of X copies in flight per producer thread
-  int64_t n_units; // n_cells * n_chunks * n_halves
-  float out_scale; // scalar / 2^s
-  const __half* ahi;   // cell-matrix tiles in their shared-memory image (see TensorCellMats)
-  const __half* alo;
-  const __half* alo3;
   int* err;
 };
+static_assert(sizeof(TcArgs) <= 4096, "kernel parameters above 4 KB");
 
 // Two rings: the X tiles (xhi, xlo [, xlo3]: 8 KB each a stage) and the cell-matrix tiles
 // (ahi, alo [, alo3]). The X ring is the deeper one, since its rows come through the gather
@@ -147,7 +159,7 @@ __device__ __forceinline__ bool epilogue_sync_and(bool v) {
 }
 
 struct Unit {
-  int cell, chunk, half;
+  int cell, chunk, half, p;
 };
 // The CTA's it-th unit: (cell, chunk) pairs are dealt round-robin over the CTAs and a CTA
 // runs both row halves of its pair back to back, so the second gather of the chunk's X rows
@@ -157,8 +169,14 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
   Unit w;
   w.half = (int)(it % a.n_halves);
   const int64_t cc = first + (it / a.n_halves) * step;
-  w.chunk = (int)(cc % a.n_chunks);
-  w.cell = (int)(cc / a.n_chunks);
+  int p = 0;
+  for (int q = 1; q < a.n_probs; ++q)
+    if (cc >= a.prob[q].pair_begin) p = q;   // problems in ascending pair order
+  const int64_t lc = cc - a.prob[p].pair_begin;
+  const int nch = a.prob[p].n_chunks;
+  w.chunk = (int)(lc % nch);
+  w.cell = (int)(lc / nch);
+  w.p = p;
   return w;
 }
 
@@ -209,7 +227,7 @@ __global__ void __launch_bounds__(kThreads3, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t first = blockIdx.x;
   const int64_t step = gridDim.x;
-  const int64_t n_pairs = args.n_units / args.n_halves;   // (cell, chunk) pairs
+  const int64_t n_pairs = args.n_pairs;   // (cell, chunk) pairs over the group
   const int64_t my_units =
       first < n_pairs ? ((n_pairs - first + step - 1) / step) * args.n_halves : 0;
   const int nkb = args.nkb;
@@ -259,9 +277,10 @@ __global__ void __launch_bounds__(kThreads3, 1)
           // its swizzled shared-memory image
           const int64_t tix = ((int64_t)w.cell * args.n_halves + w.half) * nkb + kb;
           const int64_t toff = tix * (args.n_half * (kRowBytes / 2));
-          bulk_load(st, args.ahi + toff, bytes / NS, &tma_full[s]);
-          bulk_load(st + L.a_tile, args.alo + toff, bytes / NS, &tma_full[s]);
-          if (NS == 3) bulk_load(st + 2 * L.a_tile, args.alo3 + toff, bytes / NS, &tma_full[s]);
+          const TcProblem& pr = args.prob[w.p];
+          bulk_load(st, pr.ahi + toff, bytes / NS, &tma_full[s]);
+          bulk_load(st + L.a_tile, pr.alo + toff, bytes / NS, &tma_full[s]);
+          if (NS == 3) bulk_load(st + 2 * L.a_tile, pr.alo3 + toff, bytes / NS, &tma_full[s]);
           ++issued;
           if (++s == S) s = 0, ++r;
         }
@@ -373,23 +392,25 @@ __global__ void __launch_bounds__(kThreads3, 1)
     // cursor over this CTA's K-blocks (no per-block divisions): unit it, K-block kb
     int64_t c_it = 0;
     int c_kb = 0;
-    Unit c_w = my_units > 0 ? unit_at(0, first, step, args) : Unit{0, 0, 0};
+    Unit c_w = my_units > 0 ? unit_at(0, first, step, args) : Unit{0, 0, 0, 0};
     struct Pending {
       int rows[4];
       int vb;
+      int p;
       bool valid;
     } nxt;
     // dof-map entries of the cursor's K-block (one K-block ahead of the copies)
     auto load_next = [&]() {
       nxt.valid = c_it < my_units;
       if (nxt.valid) {
-        const int* mrow = args.map + (int64_t)c_w.cell * args.n_e;
+        const int* mrow = args.prob[c_w.p].map + (int64_t)c_w.cell * args.n_e;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int J = c_kb * kKB + j * 8 + rsub;
           nxt.rows[j] = J < args.n_e ? __ldg(mrow + J) : -1;
         }
         nxt.vb = c_w.chunk * kVec + cc * 8;
+        nxt.p = c_w.p;
         if (++c_kb == nkb) {
           c_kb = 0;
           if (++c_it < my_units) c_w = unit_at(c_it, first, step, args);
@@ -406,16 +427,17 @@ __global__ void __launch_bounds__(kThreads3, 1)
         // warp-uniform decision: the warp arrives on x_full as one
         if (!__all_sync(0xffffffffu, mbar_wait(&x_empty[s_iss], (r_iss & 1) ^ 1, args.err, abort_flag)))
           return false;
-        const bool vok = cur.vb < args.B;
+        const TcProblem& pr = args.prob[cur.p];
+        const bool vok = cur.vb < pr.B;
         const uint32_t st = smem_u32(smem + s_iss * L.xstage);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const bool ok = vok && cur.rows[j] >= 0;
-          const int64_t off = ok ? (int64_t)cur.rows[j] * args.ldx + cur.vb : 0;
+          const int64_t off = ok ? (int64_t)cur.rows[j] * pr.ldx + cur.vb : 0;
           const uint32_t d = st + dst_base + j * kXGroupK;
-          cp_async16(d, args.xhi + off, ok);
-          cp_async16(d + kXTile, args.xlo + off, ok);
-          if (NS == 3) cp_async16(d + 2 * kXTile, args.xlo3 + off, ok);
+          cp_async16(d, pr.xhi + off, ok);
+          cp_async16(d + kXTile, pr.xlo + off, ok);
+          if (NS == 3) cp_async16(d + 2 * kXTile, pr.xlo3 + off, ok);
         }
       }
       cp_async_commit();
@@ -448,11 +470,12 @@ __global__ void __launch_bounds__(kThreads3, 1)
       bool okp = true;
       for (int64_t it = 0; it < my_units; ++it) {
         const Unit w = unit_at(it, first, step, args);
-        const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
+        const TcProblem& pr = args.prob[w.p];
+        const int* mrow = pr.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
         const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
         int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + (it & 1) * 256;
         for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += kEpiWarps * 32)
-          offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
+          offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * pr.ldd : -1;
         if (!epilogue_sync_and(okp)) break;
         float sum[kChunkCols];
 #pragma unroll
@@ -482,9 +505,9 @@ __global__ void __launch_bounds__(kThreads3, 1)
         }
         okp = ok;
         const int gb = w.chunk * kVec + q * 32 + lane;
-        if (ok && gb < args.B) {
-          float* dstb = args.dst + gb;
-          const float osc = args.out_scale;
+        if (ok && gb < pr.B) {
+          float* dstb = pr.dst + gb;
+          const float osc = pr.out_scale;
 #pragma unroll
           for (int gi = 0; gi < kChunkCols / 16; ++gi) {
             if (c_beg + 16 * gi < c_end) {
@@ -504,20 +527,21 @@ __global__ void __launch_bounds__(kThreads3, 1)
         const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
         fence_after();
         const Unit w = unit_at(it, first, step, args);
-        const int* mrow = args.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
+        const TcProblem& pr = args.prob[w.p];
+        const int* mrow = pr.map + (int64_t)w.cell * args.n_e + w.half * args.n_half;
         const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
         // the unit's output-row offsets (dof * ldd), staged once by the epilogue warps; rows
         // past nrows get an offset no lane uses (they are skipped)
         int64_t* offs = reinterpret_cast<int64_t*>(smem + L.offs) + buf * 256;
         if (okw)
           for (int I = (warp - 6) * 32 + lane; I < args.n_half; I += kEpiWarps * 32)
-            offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * args.ldd : -1;
+            offs[I] = I < nrows ? (int64_t)__ldg(mrow + I) * pr.ldd : -1;
         // the epilogue warps continue or stop together (a named barrier with an AND-reduction)
         if (!epilogue_sync_and(okw)) break;
         const int gb = w.chunk * kVec + q * 32 + lane;
-        const bool vok = gb < args.B;
-        float* dstb = args.dst + gb;
-        const float osc = args.out_scale;
+        const bool vok = gb < pr.B;
+        float* dstb = pr.dst + gb;
+        const float osc = pr.out_scale;
         const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
         for (int c0 = c_beg; c0 < c_end; c0 += 16) {
           float vals[16];
@@ -759,56 +783,85 @@ bool tc_usable(chefsi_operator_s* op) {
   return tcgen05_device();
 }
 
-// launch the persistent tensor-core kernel on the split rows (xhi, xlo [, xlo3]: [rows][ldx]
-// FP16); ns = number of split terms (2, or 3 with xlo3)
-static void launch_tc(chefsi_operator_s* op, TcArgs& a, const __half* xhi, const __half* xlo,
-                      const __half* xlo3, int64_t ldx, float* dst, int64_t ldd, int B, int ns,
-                      cudaStream_t st) {
-  if (ns == 3)
-    prepare_tensor_mats_lo3(op, st);
-  else
-    prepare_tensor_mats(op, st);
-  const TcPlan p = plan_for(op->n_e, ns);
-  if (!op->tc_err.ptr) {
-    op->tc_err.reset(1);
-    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
-  }
-  a.ahi = op->tc.hi.ptr;
-  a.alo = op->tc.lo.ptr;
-  a.alo3 = ns == 3 ? op->tc.lo3.ptr : op->tc.lo.ptr;
-  a.xhi = xhi;
-  a.xlo = xlo;
-  a.xlo3 = ns == 3 ? xlo3 : xlo;
-  a.ldx = ldx;
-  a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
-  a.dst = dst;
-  a.ldd = ldd;
-  a.map = op->map.ptr;
-  a.n_e = op->n_e;
+// Launch the persistent tensor-core kernel over a group of applies of operators with the same
+// cell type: dst_i += scalar_i A_i src_i for the split rows (xhi, xlo [, xlo3]: [rows][B_i]
+// FP16) of each item; ns = number of split terms (2, or 3 with xlo3). pipe (optional)
+// overrides the X-ring depth and the copy lookahead of the default plan.
+void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipeline* pipe,
+                        cudaStream_t st) {
+  CHEFSI_REQUIRE(n >= 1 && n <= kMaxGroup, "tensor-core HX group: 1.." + std::to_string(kMaxGroup) + " items");
+  CHEFSI_REQUIRE(ns == 2 || ns == 3, "tensor-core HX: two or three split terms");
+  chefsi_operator_s* op0 = items[0].op;
+  const int n_e = op0->n_e;
+  TcPlan p = plan_for(n_e, ns);
+  TcArgs a{};
+  a.n_probs = n;
+  a.n_e = n_e;
   a.nkb = p.npad / kKB;
-  a.B = B;
-  a.n_chunks = (B + kVec - 1) / kVec;
   a.n_half = p.n_half;
   a.n_halves = p.n_halves;
   a.buf_stride = p.buf_stride;
   a.tmem_cols = p.tmem_cols;
   a.stages = p.stages;
   a.xstages = p.xstages;
-  a.n_units = (int64_t)op->n_cells * a.n_chunks * p.n_halves;
-  a.err = op->tc_err.ptr;
-  CHEFSI_REQUIRE(op->n_dofs < (1ll << 31), "tensor-core HX: too many dofs for 32-bit map entries");
-  CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(xhi) & 15) == 0 && (reinterpret_cast<uintptr_t>(xlo) & 15) == 0 &&
-                     (reinterpret_cast<uintptr_t>(a.xlo3) & 15) == 0 && ldx % 8 == 0 && B % 8 == 0,
-                 "tensor-core HX: split rows must be 16-byte aligned");
-  CHEFSI_REQUIRE(ns == 2 || ns == 3, "tensor-core HX: two or three split terms");
+  a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
+  if (pipe && pipe->xstages >= 3 && pipe->xstages <= p.xstages) {
+    a.xstages = pipe->xstages;
+    p.smem = make_layout(p.n_half, p.stages, a.xstages, ns).total + 1024;
+    a.lookahead = std::max(1, std::min(pipe->lookahead, a.xstages - 2));
+  }
+  if (!op0->tc_err.ptr) {
+    op0->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op0->tc_err.ptr, 0, sizeof(int), st));
+  }
+  a.err = op0->tc_err.ptr;
+  int64_t pairs = 0;
+  for (int i = 0; i < n; ++i) {
+    const TcGroupItem& it = items[i];
+    chefsi_operator_s* op = it.op;
+    CHEFSI_REQUIRE(op->n_e == n_e && tc_usable(op), "tensor-core HX group: operators of one cell type");
+    CHEFSI_REQUIRE(op->n_dofs < (1ll << 31), "tensor-core HX: too many dofs for 32-bit map entries");
+    const __half* x3 = ns == 3 ? it.xlo3 : it.xlo;
+    CHEFSI_REQUIRE((reinterpret_cast<uintptr_t>(it.xhi) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(it.xlo) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(x3) & 15) == 0 && it.B % 8 == 0 &&
+                       it.ldd % 4 == 0 && (reinterpret_cast<uintptr_t>(it.dst) & 15) == 0,
+                   "tensor-core HX: split rows and output rows must be 16-byte aligned");
+    if (ns == 3)
+      prepare_tensor_mats_lo3(op, st);
+    else
+      prepare_tensor_mats(op, st);
+    TcProblem& pr = a.prob[i];
+    pr.xhi = it.xhi;
+    pr.xlo = it.xlo;
+    pr.xlo3 = x3;
+    pr.dst = it.dst;
+    pr.map = op->map.ptr;
+    pr.ahi = op->tc.hi.ptr;
+    pr.alo = op->tc.lo.ptr;
+    pr.alo3 = ns == 3 ? op->tc.lo3.ptr : op->tc.lo.ptr;
+    pr.ldx = it.B;
+    pr.ldd = it.ldd;
+    pr.B = it.B;
+    pr.n_chunks = (it.B + kVec - 1) / kVec;
+    pr.out_scale = (float)(it.scalar / op->tc.scale);
+    pr.pair_begin = pairs;
+    pairs += (int64_t)op->n_cells * pr.n_chunks;
+  }
+  a.n_pairs = pairs;
   auto kernel = ns == 3 ? cell_hx_tc_kernel<3, true> : cell_hx_tc_kernel<2, false>;
   CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  int dev = 0, sms = kNumSMs;
-  CHEFSI_CUDA(cudaGetDevice(&dev));
-  CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t grid = std::min<int64_t>(sms, a.n_units / p.n_halves);
+  const int64_t grid = std::min<int64_t>(device_sms(), pairs);
   kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
   CHEFSI_CHECK_LAUNCH();
+}
+
+// one apply: a group of one
+static void launch_tc(chefsi_operator_s* op, const __half* xhi, const __half* xlo,
+                      const __half* xlo3, float* dst, int64_t ldd, int B, double scalar, int ns,
+                      cudaStream_t st) {
+  TcGroupItem it{op, xhi, xlo, xlo3, dst, ldd, B, scalar};
+  hx_tc_group_launch(&it, 1, ns, nullptr, st);
 }
 
 bool tc_split_usable(chefsi_operator_s* op, int B) { return tc_usable(op) && B % 8 == 0; }
@@ -837,10 +890,7 @@ bool hx_tc_split(chefsi_operator_s* op, const __half* xhi, const __half* xlo, co
   if (!tc_split_usable(op, B) || ldd % 4 != 0 || (reinterpret_cast<uintptr_t>(dst) & 15) != 0)
     return false;
   if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
-  prepare_tensor_mats(op, st);
-  TcArgs a{};
-  a.out_scale = (float)(scalar / op->tc.scale);
-  launch_tc(op, a, xhi, xlo, nullptr, B, dst, ldd, B, 2, st);
+  launch_tc(op, xhi, xlo, nullptr, dst, ldd, B, scalar, 2, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
 }
@@ -872,10 +922,7 @@ bool hx_tc3(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
                                                                       lo, lo3);
   CHEFSI_CHECK_LAUNCH();
   if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
-  prepare_tensor_mats_lo3(op, st);
-  TcArgs a{};
-  a.out_scale = (float)(scalar / op->tc.scale);
-  launch_tc(op, a, hi, lo, lo3, B, dst, ldd, B, 3, st);
+  launch_tc(op, hi, lo, lo3, dst, ldd, B, scalar, 3, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
 }
