@@ -121,7 +121,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solver_set_profiling": ([vp, i32], ctypes.c_int),
         "chefsi_solver_hx_stats": ([vp, vp, vp], ctypes.c_int),
         "chefsi_solve": ([vp, vp, vp, i32, vp, vp, i32, i32, vp], ctypes.c_int),
-        "chefsi_solve_batched": ([i32, vp, vp, vp, vp, vp, vp, i32, i32, i32], ctypes.c_int),
+        "chefsi_solve_batched": ([i32, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32], ctypes.c_int),
         "chefsi_solve_no_rr": ([vp, vp, vp, i32, i32, i32, vp], ctypes.c_int),
         "chefsi_chebyshev_order": ([f64], i32),
     }

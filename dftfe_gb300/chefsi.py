@@ -383,9 +383,11 @@ def initial_bounds(op: KohnShamOperator, n_wfc: int, k: int = 20, reproducible: 
 
 
 def solve_batched(solvers, operators, Xs, useMixedPrec: bool = False,
-                  computeResidual: bool = True, isFirstScf: bool = False, n_streams: int = 0):
+                  computeResidual: bool = True, isFirstScf: bool = False, n_streams: int = 0,
+                  group: bool = True):
     """One CheFSI iteration on each independent problem (k-points, spins, Bloch Hamiltonians)
-    through chefsi_solve_batched; returns (list of eigenvalues, list of residual norms)."""
+    through chefsi_solve_batched; returns (list of eigenvalues, list of residual norms).
+    group: filter the eligible problems together (grouped launches in a CUDA graph)."""
     count = len(Xs)
     if not (len(solvers) == len(operators) == count):
         raise ValueError("solvers, operators and Xs must have the same length")
@@ -401,5 +403,5 @@ def solve_batched(solvers, operators, Xs, useMixedPrec: bool = False,
     rn_p = (vp * count)(*[r.ctypes.data for r in rns])
     torch.cuda.synchronize()  # the worker streams do not order after the caller's stream
     check(lib.chefsi_solve_batched(count, hs, ops, xs, ns, ev_p, rn_p, int(computeResidual),
-                                   int(isFirstScf), int(n_streams)))
+                                   int(isFirstScf), int(n_streams), int(group)))
     return evs, rns

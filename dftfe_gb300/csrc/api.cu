@@ -13,6 +13,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <random>
@@ -1103,17 +1104,11 @@ static int degree_for(chefsi_solver_s* s, int is_first_scf) {
   return std::max(1, m);
 }
 
-int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
-                 double* res_host, int32_t compute_residual, int32_t is_first_scf, void* stream) {
-  CHEFSI_API_BEGIN
-  CHEFSI_REQUIRE(s && op && X && eig_host && N >= 1, "bad argument");
-  CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
-  cudaStream_t st = as_stream(stream);
+// everything of one CheFSI iteration after the filter: Rayleigh-Ritz (Cholesky-GS, X^T H X,
+// projected eigensolve, rotation), residual norms, eigenvalues / residuals to the host
+static int solve_after_filter(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N,
+                       double* eig_host, double* res_host, int compute_residual, cudaStream_t st) {
   const int prec = s->p.precision;
-  const int m = degree_for(s, is_first_scf);
-  s->last_degree = m;
-  CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
-  filter_all(s, op, X, N, m, prec, st);
   const int64_t M = op->n_dofs;
   double* res = s->resid.ensure(N);
   if (op->is_complex) {
@@ -1139,12 +1134,218 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
   s->times[5] = elapsed(s->ev[5], s->ev[6]);
   s->times[6] = elapsed(s->ev[0], s->ev[6]);
   s->hx_collect();
+  return CHEFSI_OK;
+}
+
+int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
+                 double* res_host, int32_t compute_residual, int32_t is_first_scf, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s && op && X && eig_host && N >= 1, "bad argument");
+  CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
+  cudaStream_t st = as_stream(stream);
+  const int m = degree_for(s, is_first_scf);
+  s->last_degree = m;
+  CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
+  filter_all(s, op, X, N, m, s->p.precision, st);
+  const int rc = solve_after_filter(s, op, X, N, eig_host, res_host, compute_residual, st);
+  if (rc != CHEFSI_OK) return rc;
   CHEFSI_API_END
 }
 
+// ---------------------------------------------------------------- batched (grouped) filter
+// Problems of a batch whose mixed filter runs on the tensor cores in one block are filtered
+// together: per Chebyshev degree one grouped recurrence step and one persistent tensor-core
+// HX launch cover every problem of a cell type (their per-problem coefficients ride in the
+// kernel parameters), and the whole lockstep recurrence is captured in a CUDA graph.
+namespace {
+
+struct GroupMember {
+  int idx;                     // batch entry
+  chefsi_solver_s* s;
+  chefsi_operator_s* op;       // the caller's operator
+  chefsi_operator_s* tcop;     // the operator the tensor cores apply (op, or its real form)
+  void* X;
+  int N;
+  int64_t rows;                // FP32 rows: n_dofs, or 2 n_dofs for the real form
+  float* x;
+  float* y;
+  __half* hi;
+  __half* lo;
+  double scale;
+  int m;
+  float* result;
+};
+
+// Autotuner of the grouped apply: the X-ring depth and the K-blocks of gathers in flight
+// (the pipeline shape of a cell tile), chosen per (cell type, work size) by timing each
+// candidate on the group's own operands once; the choice is kept for the process.
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, TcPipeline> g_tune_cache;
+
+TcPipeline autotune_pipeline(const std::vector<TcGroupItem>& items, cudaStream_t st) {
+  int64_t pairs = 0;
+  for (const auto& it : items) pairs += (int64_t)it.op->n_cells * ((it.B + 127) / 128);
+  int bucket = 0;
+  while ((1ll << (bucket + 1)) <= pairs) ++bucket;
+  const std::pair<int, int> key{items[0].op->n_e, bucket};
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto f = g_tune_cache.find(key);
+    if (f != g_tune_cache.end()) return f->second;
+  }
+  const TcPipeline cand[] = {{8, 6}, {8, 4}, {6, 4}, {6, 2}, {4, 2}};
+  cudaEvent_t e0, e1;
+  CHEFSI_CUDA(cudaEventCreate(&e0));
+  CHEFSI_CUDA(cudaEventCreate(&e1));
+  TcPipeline best = cand[0];
+  float best_ms = 1e30f;
+  try {
+    for (const TcPipeline& c : cand) {
+      hx_tc_group_launch(items.data(), (int)items.size(), 2, &c, st);   // warm-up
+      CHEFSI_CUDA(cudaEventRecord(e0, st));
+      hx_tc_group_launch(items.data(), (int)items.size(), 2, &c, st);
+      CHEFSI_CUDA(cudaEventRecord(e1, st));
+      CHEFSI_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CHEFSI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) best_ms = ms, best = c;
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune_cache[key] = best;
+  return best;
+}
+
+// the filter of one group (same cell type), lockstep over the degrees, captured in a graph
+void cheb_filter_group(std::vector<GroupMember*>& g, cudaStream_t st) {
+  const int n = (int)g.size();
+  struct Rec {
+    double e, c, sigma, gamma;
+  };
+  std::vector<Rec> r(n);
+  int mmax = 0;
+  for (int i = 0; i < n; ++i) {
+    chefsi_solver_s* s = g[i]->s;
+    const double e = (s->b_up - s->b_low) / 2.0, c = (s->b_up + s->b_low) / 2.0;
+    const double sigma = e / (s->a0 - c);
+    r[i] = Rec{e, c, sigma, 2.0 / sigma};
+    mmax = std::max(mmax, g[i]->m);
+  }
+  auto hx_items = [&](const std::vector<int>& act, const std::vector<double>& scal,
+                      bool first) {
+    std::vector<TcGroupItem> it;
+    for (size_t k = 0; k < act.size(); ++k) {
+      GroupMember* gm = g[act[k]];
+      it.push_back(TcGroupItem{gm->tcop, gm->hi, gm->lo, nullptr, first ? gm->y : gm->x, gm->N,
+                               gm->N, scal[k]});
+    }
+    return it;
+  };
+  // the step-1 applies, also used by the autotuner (before step 1 writes y without reading it)
+  std::vector<int> all(n);
+  std::iota(all.begin(), all.end(), 0);
+  std::vector<double> a1(n);
+  for (int i = 0; i < n; ++i) a1[i] = r[i].sigma / r[i].e;
+  std::vector<TcPipeline> pipes;
+  for (int i0 = 0; i0 < n; i0 += 32) {
+    std::vector<int> part(all.begin() + i0, all.begin() + std::min(n, i0 + 32));
+    std::vector<double> sc(a1.begin() + i0, a1.begin() + std::min(n, i0 + 32));
+    pipes.push_back(autotune_pipeline(hx_items(part, sc, true), st));
+  }
+  // apply the active members in launches of at most 32
+  auto launch = [&](const std::vector<int>& act, const std::vector<double>& scal,
+                    const std::vector<double>& aa, const std::vector<double>& bb, bool first) {
+    for (size_t k0 = 0; k0 < act.size(); k0 += 32) {
+      const size_t k1 = std::min(act.size(), k0 + 32);
+      std::vector<AxpbyGroupItem> ax;
+      for (size_t k = k0; k < k1; ++k) {
+        GroupMember* gm = g[act[k]];
+        // step 1: y = a x, split(x); later: x = a y + b x, split(y)
+        if (first)
+          ax.push_back(AxpbyGroupItem{gm->x, gm->y, gm->hi, gm->lo, gm->rows * gm->N, aa[k], 0.0});
+        else
+          ax.push_back(AxpbyGroupItem{gm->y, gm->x, gm->hi, gm->lo, gm->rows * gm->N, aa[k], bb[k]});
+      }
+      axpby_split_group(ax.data(), (int)ax.size(), st);
+      std::vector<int> part(act.begin() + k0, act.begin() + k1);
+      std::vector<double> sc(scal.begin() + k0, scal.begin() + k1);
+      const auto it = hx_items(part, sc, first);
+      hx_tc_group_launch(it.data(), (int)it.size(), 2, &pipes[std::min<size_t>(k0 / 32, pipes.size() - 1)], st);
+      for (size_t k = k0; k < k1; ++k) {
+        GroupMember* gm = g[act[k]];
+        if (gm->tcop->n_atoms)
+          apply_nonlocal_f32(gm->tcop, first ? gm->x : gm->y, gm->N, first ? gm->y : gm->x, gm->N,
+                             gm->N, scal[k], st);
+      }
+    }
+  };
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CHEFSI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    std::vector<double> aa(n), bb(n, 0.0);
+    for (int i = 0; i < n; ++i) aa[i] = a1[i] * (-r[i].c);
+    launch(all, a1, aa, bb, true);
+    for (int degree = 2; degree <= mmax; ++degree) {
+      std::vector<int> act;
+      std::vector<double> sc, ca, cb;
+      for (int i = 0; i < n; ++i) {
+        if (g[i]->m < degree) continue;
+        const double sigma2 = 1.0 / (r[i].gamma - r[i].sigma);
+        const double alpha1 = 2.0 * sigma2 / r[i].e, alpha2 = -(r[i].sigma * sigma2);
+        act.push_back(i);
+        sc.push_back(alpha1);
+        ca.push_back(-r[i].c * alpha1);
+        cb.push_back(alpha2);
+        r[i].sigma = sigma2;
+      }
+      launch(act, sc, ca, cb, false);
+      for (int i : act) std::swap(g[i]->x, g[i]->y);
+    }
+  } catch (...) {
+    cudaStreamEndCapture(st, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  CHEFSI_CUDA(cudaStreamEndCapture(st, &graph));
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    CHEFSI_CUDA(ie);
+  }
+  const cudaError_t le = cudaGraphLaunch(exec, st);
+  const cudaError_t se = le == cudaSuccess ? cudaStreamSynchronize(st) : le;
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  CHEFSI_CUDA(se);
+  for (int i = 0; i < n; ++i) g[i]->result = g[i]->y;
+}
+
+// a batch entry whose filter can join a group: mixed precision, one block, tensor-core apply
+chefsi_operator_s* group_operator(chefsi_solver_s* s, chefsi_operator_s* op, int N,
+                                  cudaStream_t st) {
+  if (s->p.precision != CHEFSI_PREC_MIXED) return nullptr;
+  if (s->p.cheby_wfc_block > 0 && s->p.cheby_wfc_block < N) return nullptr;
+  if (op->is_complex) {
+    if (!op->folded) return nullptr;
+    chefsi_operator_s* rv = realified(op, st);
+    return tc_split_usable(rv, N) ? rv : nullptr;
+  }
+  return tc_split_usable(op, N) ? op : nullptr;
+}
+
+}  // namespace
+
 int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator* ops, void** X,
                          const int32_t* N, double** eig_host, double** res_host,
-                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams) {
+                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams,
+                         int32_t group_filter) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(count >= 0 && (count == 0 || (solvers && ops && X && N && eig_host)),
                  "bad argument");
@@ -1169,6 +1370,82 @@ int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator*
   workers = std::max(1, std::min(workers, count));
   int dev = 0;
   CHEFSI_CUDA(cudaGetDevice(&dev));
+
+  // grouped filter of the entries that can share launches (two or more)
+  std::vector<GroupMember> mem;
+  std::vector<int> member_of(count, -1);
+  {
+    cudaStream_t st0 = nullptr;
+    CHEFSI_CUDA(cudaStreamCreateWithFlags(&st0, cudaStreamNonBlocking));
+    try {
+      for (int k = 0; k < count && group_filter; ++k) {
+        const int i = order[k];
+        chefsi_operator_s* tcop = group_operator(solvers[i], ops[i], N[i], st0);
+        if (!tcop) continue;
+        GroupMember gm{};
+        gm.idx = i;
+        gm.s = solvers[i];
+        gm.op = ops[i];
+        gm.tcop = tcop;
+        gm.X = X[i];
+        gm.N = N[i];
+        gm.rows = tcop->n_dofs;
+        gm.m = degree_for(solvers[i], is_first_scf);
+        mem.push_back(gm);
+      }
+      if (mem.size() < 2) mem.clear();
+      std::vector<double> amax(mem.size(), 0.0);
+      for (size_t k = 0; k < mem.size(); ++k) {
+        GroupMember& gm = mem[k];
+        gm.s->last_degree = gm.m;
+        CHEFSI_CUDA(cudaEventRecord(gm.s->ev[0], st0));
+        double* sc = gm.s->scal.ensure(1);
+        const int64_t M = gm.op->n_dofs;
+        if (gm.op->is_complex)
+          absmax_block_f64(reinterpret_cast<const double*>(gm.X), 2 * (int64_t)gm.N, M, 2 * gm.N, sc, st0);
+        else
+          absmax_block_f64(reinterpret_cast<const double*>(gm.X), gm.N, M, gm.N, sc, st0);
+        CHEFSI_CUDA(cudaMemcpyAsync(&amax[k], sc, sizeof(double), cudaMemcpyDeviceToHost, st0));
+      }
+      CHEFSI_CUDA(cudaStreamSynchronize(st0));
+      std::map<int, std::vector<GroupMember*>> by_type;
+      for (size_t k = 0; k < mem.size(); ++k) {
+        GroupMember& gm = mem[k];
+        // FP32 rows scaled by a power of two (max |x| ~ 2^8, the FP16 split's range)
+        gm.scale = (amax[k] > 0.0 && std::isfinite(amax[k]))
+                       ? std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax[k])))
+                       : 1.0;
+        const size_t n = (size_t)gm.rows * gm.N;
+        gm.x = gm.s->Xb32.ensure(n);
+        gm.y = gm.s->Yb32.ensure(n);
+        gm.hi = gm.s->xs_hi.ensure(n);
+        gm.lo = gm.s->xs_lo.ensure(n);
+        if (gm.op->is_complex)
+          complex_to_real_rows(reinterpret_cast<const cplx*>(gm.X), gm.N, gm.op->n_dofs, gm.N,
+                               gm.scale, gm.x, st0);
+        else
+          copy_block<double, float>(reinterpret_cast<const double*>(gm.X), gm.N, gm.x, gm.N,
+                                    gm.rows, gm.N, gm.scale, st0);
+        // everything the captured launches need, allocated before the capture
+        prepare_tensor_mats(gm.tcop, st0);
+        if (gm.tcop->n_atoms) gm.tcop->nlW32.ensure((size_t)gm.tcop->n_atoms * gm.tcop->n_proj * gm.N);
+        by_type[gm.tcop->n_e].push_back(&gm);
+        member_of[gm.idx] = (int)k;
+      }
+      for (auto& kv : by_type) {
+        cheb_filter_group(kv.second, st0);
+        const int tc = tc_check_error(kv.second[0]->tcop, st0);
+        if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
+      }
+    } catch (...) {
+      cudaStreamSynchronize(st0);
+      cudaStreamDestroy(st0);
+      throw;
+    }
+    CHEFSI_CUDA(cudaStreamSynchronize(st0));
+    CHEFSI_CUDA(cudaStreamDestroy(st0));
+  }
+
   std::atomic<int> next{0};
   std::mutex mu;
   int first_rc = CHEFSI_OK;
@@ -1188,13 +1465,35 @@ int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator*
         if (first_rc != CHEFSI_OK) break;
       }
       const int i = order[k];
-      const int rc = chefsi_solve(solvers[i], ops[i], X[i], N[i], eig_host[i],
-                                  res_host ? res_host[i] : nullptr, compute_residual,
-                                  is_first_scf, st);
+      int rc = CHEFSI_OK;
+      std::string msg;
+      if (member_of[i] >= 0) {
+        // filtered in its group: back to the caller's block, then the rest of the iteration
+        GroupMember& gm = mem[member_of[i]];
+        try {
+          if (gm.op->is_complex)
+            real_rows_to_complex(gm.result, gm.op->n_dofs, gm.N, 1.0 / gm.scale,
+                                 reinterpret_cast<cplx*>(gm.X), gm.N, st);
+          else
+            copy_block<float, double>(gm.result, gm.N, reinterpret_cast<double*>(gm.X), gm.N,
+                                      gm.rows, gm.N, 1.0 / gm.scale, st);
+          rc = solve_after_filter(gm.s, gm.op, gm.X, gm.N, eig_host[i],
+                                  res_host ? res_host[i] : nullptr, compute_residual, st);
+          if (rc != CHEFSI_OK) msg = chefsi_last_error();
+        } catch (const Error& e) {
+          rc = e.code, msg = e.what();
+        } catch (const std::exception& e) {
+          rc = CHEFSI_ERR_INVALID, msg = e.what();
+        }
+      } else {
+        rc = chefsi_solve(solvers[i], ops[i], X[i], N[i], eig_host[i],
+                          res_host ? res_host[i] : nullptr, compute_residual, is_first_scf, st);
+        if (rc != CHEFSI_OK) msg = chefsi_last_error();
+      }
       if (rc != CHEFSI_OK) {
         std::lock_guard<std::mutex> g(mu);
         if (first_rc == CHEFSI_OK)
-          first_rc = rc, first_msg = "batch entry " + std::to_string(i) + ": " + chefsi_last_error();
+          first_rc = rc, first_msg = "batch entry " + std::to_string(i) + ": " + msg;
       }
     }
     cudaStreamSynchronize(st);

@@ -106,6 +106,16 @@ struct TcPipeline {
   int xstages;
   int lookahead;
 };
+// one block of a grouped recurrence step: y = a x + b y (b == 0: y not read), (hi, lo) = split(x)
+struct AxpbyGroupItem {
+  const float* x;
+  float* y;
+  __half* hi;
+  __half* lo;
+  int64_t n;  // entries (a multiple of 4)
+  double a, b;
+};
+void axpby_split_group(const AxpbyGroupItem* items, int n, cudaStream_t st);
 // one persistent launch over up to 32 applies of operators with the same cell type
 void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipeline* pipe,
                         cudaStream_t st);

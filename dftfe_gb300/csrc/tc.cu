@@ -698,6 +698,54 @@ __global__ void k_axpby_split(const float* __restrict__ x, float* __restrict__ y
   }
 }
 
+// The recurrence step for a group of blocks (up to 32): y_i = a_i x_i + b_i y_i and
+// (hi_i, lo_i) = split(x_i), over the concatenation of the blocks in float4 units; the block of
+// an index is found by binary search over the ascending begins.
+struct AxpbyItem {
+  const float* x;
+  float* y;
+  __half* hi;
+  __half* lo;
+  int64_t n4;      // float4 entries
+  int64_t begin4;  // first float4 index of this block in the concatenation
+  float a, b;
+};
+struct AxpbyGroupArgs {
+  AxpbyItem it[kMaxGroup];
+  int n;
+  int64_t total4;
+};
+static_assert(sizeof(AxpbyGroupArgs) <= 4096, "kernel parameters above 4 KB");
+
+__global__ void k_axpby_split_group(const __grid_constant__ AxpbyGroupArgs g) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.total4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = g.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (t >= g.it[mid].begin4) lo = mid; else hi = mid - 1;
+    }
+    const AxpbyItem& it = g.it[lo];
+    const int64_t u = t - it.begin4;
+    const float4 xv = reinterpret_cast<const float4*>(it.x)[u];
+    float4 yv = it.b != 0.f ? reinterpret_cast<float4*>(it.y)[u] : make_float4(0.f, 0.f, 0.f, 0.f);
+    yv.x = it.a * xv.x + it.b * yv.x;
+    yv.y = it.a * xv.y + it.b * yv.y;
+    yv.z = it.a * xv.z + it.b * yv.z;
+    yv.w = it.a * xv.w + it.b * yv.w;
+    reinterpret_cast<float4*>(it.y)[u] = yv;
+    __half h[4], l[4];
+    split_f32(xv.x, h[0], l[0]);
+    split_f32(xv.y, h[1], l[1]);
+    split_f32(xv.z, h[2], l[2]);
+    split_f32(xv.w, h[3], l[3]);
+    reinterpret_cast<__half2*>(it.hi)[2 * u] = __halves2half2(h[0], h[1]);
+    reinterpret_cast<__half2*>(it.hi)[2 * u + 1] = __halves2half2(h[2], h[3]);
+    reinterpret_cast<__half2*>(it.lo)[2 * u] = __halves2half2(l[0], l[1]);
+    reinterpret_cast<__half2*>(it.lo)[2 * u + 1] = __halves2half2(l[2], l[3]);
+  }
+}
+
 struct TcPlan {
   int npad, n_half, n_halves, buf_stride, tmem_cols, stages, xstages, smem;
 };
@@ -870,6 +918,27 @@ void split_rows_f32(const float* x, int64_t ldx, int64_t M, int B, __half* hi, _
                     cudaStream_t st) {
   CHEFSI_REQUIRE(B % 2 == 0 && ldx % 2 == 0, "split rows: even widths only");
   k_split_rows<<<grid_for(M * (B / 2), 256), 256, 0, st>>>(x, ldx, M, B, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void axpby_split_group(const AxpbyGroupItem* items, int n, cudaStream_t st) {
+  CHEFSI_REQUIRE(n >= 1 && n <= kMaxGroup, "grouped recurrence step: 1..32 blocks");
+  AxpbyGroupArgs g{};
+  g.n = n;
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    const AxpbyGroupItem& it = items[i];
+    CHEFSI_REQUIRE(it.n % 4 == 0 && (reinterpret_cast<uintptr_t>(it.x) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(it.y) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(it.hi) & 7) == 0 &&
+                       (reinterpret_cast<uintptr_t>(it.lo) & 7) == 0,
+                   "grouped recurrence step: 16-byte aligned blocks with a multiple of 4 entries");
+    g.it[i] = AxpbyItem{it.x, it.y, it.hi, it.lo, it.n / 4, total, (float)it.a, (float)it.b};
+    total += it.n / 4;
+  }
+  g.total4 = total;
+  if (total == 0) return;
+  k_axpby_split_group<<<grid_for(total, 256), 256, 0, st>>>(g);
   CHEFSI_CHECK_LAUNCH();
 }
 

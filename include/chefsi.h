@@ -278,12 +278,19 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
    dftClass::kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:507-655, which calls
    solve() once per (k, spin)): problem i is (solvers[i], ops[i], X[i], N[i]) with its
    eigenvalues (and residual norms) written to eig_host[i] (res_host[i]); res_host may be
-   null. Every entry needs its own solver (bounds and workspaces). The problems run
+   null. Every entry needs its own solver (bounds and workspaces).
+   With group_filter != 0, the entries whose mixed filter runs on the tensor cores in one
+   block (chebyWfcBlockSize >= N) are filtered together: per Chebyshev degree one grouped
+   recurrence launch and one persistent tensor-core HX launch cover all problems of a cell
+   type, with their own coefficients, and the lockstep recurrence is captured and replayed as
+   a CUDA graph; the HX pipeline shape is chosen by a built-in autotuner (timed once per cell
+   type and work size). The Rayleigh-Ritz steps (and every other entry) then run
    concurrently on n_streams CUDA streams (n_streams <= 0: min(count, 8)), each driven by a
    host worker thread, largest problems first. Returns the first failing entry's status. */
 int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator* ops, void** X,
                          const int32_t* N, double** eig_host, double** res_host,
-                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams);
+                         int32_t compute_residual, int32_t is_first_scf, int32_t n_streams,
+                         int32_t group_filter);
 
 /* Filter only (no Rayleigh-Ritz), solveNoRR. */
 int chefsi_solve_no_rr(chefsi_solver s, chefsi_operator op, void* X, int32_t N,

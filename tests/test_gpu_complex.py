@@ -139,6 +139,47 @@ def test_solve_batched_matches_sequential(C, mixed):
             assert np.abs(a - b).max() < tol
 
 
+def test_solve_batched_grouped_uneven_bloch(C):
+    """Bloch Hamiltonians of uneven mesh (2^3 and 3^3 cells) and block size (8 and 16
+    wavefunctions), different bounds and degrees: the batched solve filters them together
+    (grouped recurrence and tensor-core launches in one CUDA graph) and gives the same Ritz
+    values as one-by-one solves of the same iterations (mixed tolerance: FP32 atomics)."""
+    from dftfe_gb300 import problems
+    probs = problems.bloch_set(6, seed=11, small=True)
+    ops = [C.KohnShamOperator.from_problem(p) for p in probs]
+    X0 = [p.initial_vectors() for p in probs]
+
+    bounds = []
+    for op, p in zip(ops, probs):
+        lo, blow, up = C.initial_bounds(op, p.n_wfc)
+        bounds.append((lo, min(blow, lo + 0.5 * (up - lo)), up))
+
+    def make():
+        out = []
+        for i, b in enumerate(bounds):
+            s = C.ChebyshevOrthogonalizedSubspaceIterationSolver(
+                C.SolverParams(chebyshevOrder=8 + 2 * (i % 3), mixed_precision="mixed",
+                               rr_precision="fp32"))
+            s.reinitSpectrumBounds(*b)
+            out.append(s)
+        return out
+
+    seq, bat = make(), make()
+    Xs = [torch.from_numpy(x.copy()).cuda() for x in X0]
+    Xb = [torch.from_numpy(x.copy()).cuda() for x in X0]
+    for _ in range(2):
+        ev_s = []
+        for s, op, X in zip(seq, ops, Xs):
+            ev, _ = s.solve(op, X, useMixedPrec=True)
+            ev_s.append(ev)
+        ev_b, _ = C.solve_batched(bat, ops, Xb, useMixedPrec=True, n_streams=3)
+        for a, b in zip(ev_s, ev_b):
+            assert np.abs(a - b).max() < 1e-5 * max(1.0, np.abs(a).max())
+        for s1, s2, a, b, bd in zip(seq, bat, ev_s, ev_b, bounds):
+            s1.reinitSpectrumBounds(a[0], a[-1], bd[2])
+            s2.reinitSpectrumBounds(b[0], b[-1], bd[2])
+
+
 def test_lanczos_bounds_complex_match_oracle(C):
     pr = small_problem(n=2, L=4.0, p=3, wells=2, kpoint=K)
     op, ora = C.KohnShamOperator.from_problem(pr), oracle_op(pr)
