@@ -353,6 +353,8 @@ def run_ritz_check(args):
         s.reinitSpectrumBounds(ev[0], ev[-1], up)
     bounds = (ev[0], ev[-1], up)
     out = {}
+    nocc = pr.n_occupied
+    occ = {}
     for mode in ("fp64", "mixed"):
         sv = mk()
         sv.reinitSpectrumBounds(*bounds)
@@ -362,9 +364,13 @@ def run_ritz_check(args):
         e, r = sv.solve(op, Xc, useMixedPrec=(mode == "mixed"))
         torch.cuda.synchronize()
         out[mode] = (e.copy(), r.copy(), time.perf_counter() - t0, sv.timings(mode == "mixed"))
+        occ[mode] = Xc[:, :nocc].contiguous()
         del Xc
+    # largest principal angle between the occupied Ritz subspaces (both blocks orthonormal)
+    sv_q = np.linalg.svd((occ["fp64"].T @ occ["mixed"]).cpu().numpy(), compute_uv=False)
+    angle = float(np.arccos(np.clip(sv_q.min(), -1.0, 1.0)))
+    del occ
     e64, e32 = out["fp64"][0], out["mixed"][0]
-    nocc = pr.n_occupied
     d = np.abs(e32 - e64)
     print(json.dumps({
         "metric": "mixed vs FP64 Ritz error (one iteration from the same block)",
@@ -374,7 +380,8 @@ def run_ritz_check(args):
         "speedup_mixed_vs_fp64": out["fp64"][2] / out["mixed"][2],
         "fp64_phases_ms": out["fp64"][3], "mixed_phases_ms": out["mixed"][3],
         "res_occ_max_fp64": float(out["fp64"][1][:nocc].max()),
-        "res_occ_max_mixed": float(out["mixed"][1][:nocc].max())}))
+        "res_occ_max_mixed": float(out["mixed"][1][:nocc].max()),
+        "subspace_angle_occupied_rad": angle}))
     return 0
 
 
