@@ -1043,63 +1043,76 @@ __device__ double block_sum(double v, double* red) {
   return t;
 }
 
+// One cooperative launch for the whole tridiagonalisation, two grid barriers per reflector.
+// Step k: every active CTA loads column k below the diagonal into shared memory and forms the
+// reflector itself (norm, alpha, tau: no separate vector phase), the CTAs' warps compute
+// p = tau A22 v one row per warp; after a barrier every CTA forms f = tau/2 v^T p and updates
+// its rows of A22 -= v w^T + w v^T (w = p - f v); barrier. CTA 0 also stores the reflector,
+// tau, d and e. A CTA leaves once the trailing size needs fewer CTAs (one row per warp), so
+// the late barriers have fewer participants; every barrier is bounded.
 __global__ void __launch_bounds__(256)
     k_tridiag_fused(double* A, int N, double* V, double* tau, double* d, double* e, double* p,
                     GridSync gs) {
+  extern __shared__ double vs[];     // [N] the current reflector
   __shared__ double red[32];
-  const unsigned int nb = gridDim.x;
-  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  const int lane = threadIdx.x & 31;
+  const int warps_per_cta = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = 0; k + 2 < N; ++k) {
     const int n = N - k - 1;
-    double* v = V + (int64_t)k * N + k + 1;
+    const unsigned int active =
+        min(gridDim.x, (unsigned)max(1, (n + warps_per_cta - 1) / warps_per_cta));
+    if (blockIdx.x >= active) return;   // never needed again: active does not grow
+    // the reflector from column k (rows k+1..N-1), in every CTA
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double x = A[(int64_t)(k + 1 + i) * N + k];
+      vs[i] = x;
+      s += x * x;
+    }
+    const double nrm2 = block_sum(s, red);
+    const double x0 = vs[0];
+    const double nrm = sqrt(nrm2);
+    const double alpha = (x0 >= 0.0) ? -nrm : nrm;
+    const double vtv = 2.0 * (nrm2 - alpha * x0);
+    const bool skip = !(vtv > 0.0) || nrm == 0.0;
+    const double tk = skip ? 0.0 : 2.0 / vtv;
+    __syncthreads();
+    if (threadIdx.x == 0) vs[0] = skip ? 0.0 : x0 - alpha;
+    if (skip)
+      for (int i = threadIdx.x + 1; i < n; i += blockDim.x) vs[i] = 0.0;
+    __syncthreads();
     if (blockIdx.x == 0) {
-      double s = 0.0;
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double x = A[(int64_t)(k + 1 + i) * N + k];
-        s += x * x;
-      }
-      const double nrm2 = block_sum(s, red);
-      const double x0 = A[(int64_t)(k + 1) * N + k];
-      const double nrm = sqrt(nrm2);
-      const double alpha = (x0 >= 0.0) ? -nrm : nrm;
-      const double vtv = 2.0 * (nrm2 - alpha * x0);
-      const bool skip = !(vtv > 0.0) || nrm == 0.0;
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double x = A[(int64_t)(k + 1 + i) * N + k];
-        v[i] = skip ? 0.0 : (i == 0 ? x - alpha : x);
-      }
+      double* v = V + (int64_t)k * N + k + 1;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = vs[i];
       if (threadIdx.x == 0) {
-        tau[k] = skip ? 0.0 : 2.0 / vtv;
+        tau[k] = tk;
         d[k] = A[(int64_t)k * N + k];
         e[k] = skip ? x0 : alpha;
       }
     }
-    if (!grid_barrier(gs, nb)) return;
-    const double tk = tau[k];
     // p = tau A22 v, one warp per row
-    for (int i = gwarp; i < n; i += nwarps) {
+    const int nwarps = (int)active * warps_per_cta;
+    for (int i = (int)blockIdx.x * warps_per_cta + wid; i < n; i += nwarps) {
       const double* row = A + (int64_t)(k + 1 + i) * N + k + 1;
-      double s = 0.0;
-      for (int j = lane; j < n; j += 32) s += row[j] * v[j];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) p[i] = tk * s;
+      double t = 0.0;
+      for (int j = lane; j < n; j += 32) t += row[j] * vs[j];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) p[i] = tk * t;
     }
-    if (!grid_barrier(gs, nb)) return;
+    if (!grid_barrier(gs, active)) return;
     // f = (tau/2) v^T p in every CTA; A22 -= v w^T + w v^T with w = p - f v
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i] * v[i];
-    const double f = 0.5 * tk * block_sum(s, red);
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-      const double vi = v[i], wi = p[i] - f * vi;
+    double q = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) q += p[i] * vs[i];
+    const double f = 0.5 * tk * block_sum(q, red);
+    for (int i = blockIdx.x; i < n; i += active) {
+      const double vi = vs[i], wi = p[i] - f * vi;
       double* row = A + (int64_t)(k + 1 + i) * N + k + 1;
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double vj = v[j], wj = p[j] - f * vj;
+        const double vj = vs[j], wj = p[j] - f * vj;
         row[j] -= vi * wj + wi * vj;
       }
     }
-    if (!grid_barrier(gs, nb)) return;
+    if (!grid_barrier(gs, active)) return;
   }
 }
 
@@ -1111,7 +1124,11 @@ static void tridiagonalise(double* A, int N, double* V, double* tau, double* d, 
   CHEFSI_CUDA(cudaGetDevice(&dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   CHEFSI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  CHEFSI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_fused, 256, 0));
+  if (sizeof(double) * N > 48 * 1024)
+    CHEFSI_CUDA(cudaFuncSetAttribute(k_tridiag_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(double) * N)));
+  CHEFSI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag_fused, 256,
+                                                            sizeof(double) * N));
   if (coop && per_sm > 0 && N > 2) {
     DeviceBuffer<unsigned int> sync(2);
     DeviceBuffer<int> err(1);
@@ -1122,7 +1139,7 @@ static void tridiagonalise(double* A, int N, double* V, double* tau, double* d, 
     blocks = std::min(blocks, sms * per_sm);
     void* args[] = {&A, &N, &V, &tau, &d, &e, &p, &gs};
     CHEFSI_CUDA(cudaLaunchCooperativeKernel((const void*)k_tridiag_fused, dim3(blocks), dim3(256),
-                                            args, 0, st));
+                                            args, sizeof(double) * N, st));
     CHEFSI_CHECK_LAUNCH();
     int h = 0;
     CHEFSI_CUDA(cudaMemcpyAsync(&h, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
