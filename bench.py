@@ -385,6 +385,61 @@ def run_ritz_check(args):
     return 0
 
 
+def run_density_check(args):
+    """Density of the Ritz vectors at the quadrature points (chefsi_density, densityCalculator)
+    on the mixed workload: 1024 vectors with occupations 2 for the lowest 512, the (p+3)^3 Gauss
+    points of every cell. FP64. Timed with CUDA events; checked against a direct
+    interpolate-square-sum (numpy) on 16 seeded cells."""
+    import torch
+    from dftfe_gb300 import build, chefsi, fe
+    build.build()
+    pr = build_workload(args.workload, args.seed)
+    N, M, mesh = pr.n_wfc, pr.n_dofs, pr.mesh
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    nq1 = mesh.p + 3
+    xq, _ = fe.gauss_nodes_weights(nq1)
+    phi, _ = mesh.shape_1d(xq)
+    q = np.arange(nq1 ** 3)
+    qx, qy, qz = q % nq1, (q // nq1) % nq1, q // (nq1 * nq1)
+    i = np.arange(mesh.nodes_per_cell)
+    p1 = mesh.p + 1
+    shape = phi[qx][:, i % p1] * phi[qy][:, (i // p1) % p1] * phi[qz][:, i // (p1 * p1)]
+    _, w3 = mesh.quadrature(nq1)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 1)
+    X = torch.rand((M, N), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    occ = np.where(np.arange(N) < N // 2, 2.0, 0.0)
+    occ_d, shape_d = t(occ), t(shape)
+    jxw_d = t(np.broadcast_to(w3, (mesh.n_cells, len(w3))))
+    for _ in range(max(1, args.warmup)):
+        rho = chefsi.density(op, X, occ_d, shape_d, jxw_d)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.steps):
+        rho = chefsi.density(op, X, occ_d, shape_d, jxw_d)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.steps
+    # direct interpolate-square-sum on 16 seeded cells (FP64 numpy)
+    cells = np.random.default_rng(args.seed).choice(mesh.n_cells, 16, replace=False)
+    ref = np.empty((16, len(w3)))
+    for k, c in enumerate(cells):
+        dofs = pr.cell_map[c]
+        nodal = pr.inv_sqrt_mass[dofs][:, None] * X[torch.from_numpy(dofs).cuda()].cpu().numpy()
+        psi = shape @ nodal
+        ref[k] = ((psi * psi) @ occ) * w3
+    got = rho[torch.from_numpy(cells).cuda()].cpu().numpy()
+    ne, nq, nc = mesh.nodes_per_cell, len(w3), mesh.n_cells
+    flops = 2.0 * nc * ne * ne * N + 2.0 * nc * nq * ne * ne
+    print(json.dumps({"metric": "density at the quadrature points (FP64)", "value": ms, "unit": "ms",
+                      "workload": args.workload, "n_dofs": M, "n_wfc": N, "n_q": nq,
+                      "gflops": flops / (ms * 1e-3) / 1e9,
+                      "max_rel_err_vs_direct_16_cells": float(np.abs(got - ref).max() / np.abs(ref).max())}))
+    return 0
+
+
 def run_adjoint_check(args):
     """Adjoint workload: 10^3 cells, degree 4, 256 wavefunctions, loss = sum of the lowest 128
     Ritz values after 5 CheFSI iterations (degree 24, checkpoints every 6); the gradient w.r.t.
@@ -543,6 +598,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
     ap.add_argument("--fp64-compare", action="store_true")
+    ap.add_argument("--density-check", action="store_true",
+                    help="time chefsi_density on the workload and check 16 cells against a direct sum")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -555,6 +612,8 @@ def main():
         return run_hx_only(args)
     if args.adjoint_check:
         return run_adjoint_check(args)
+    if args.density_check:
+        return run_density_check(args)
     if args.ritz_check:
         return run_ritz_check(args)
     return run_ours(args)

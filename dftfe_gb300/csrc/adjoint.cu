@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_cell_outer(const int* __restrict__ map, int n_e, const double* __restrict__ d,
                  const double* __restrict__ u, const double* __restrict__ w, int64_t ld, int B,
-                 double alpha, double* __restrict__ G, int nt) {
+                 const double* __restrict__ wt, double alpha, double* __restrict__ G, int nt) {
   __shared__ double Ui[16][T + 1];
   __shared__ double Wj[16][T + 1];
   __shared__ int gi[T], gj[T];
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256)
       const int bb = idx % 16, k = idx / 16;
       const int b = b0 + bb;
       Ui[bb][k] = (b < B && gi[k] >= 0) ? u[(int64_t)gi[k] * ld + b] : 0.0;
-      Wj[bb][k] = (b < B && gj[k] >= 0) ? w[(int64_t)gj[k] * ld + b] : 0.0;
+      Wj[bb][k] = (b < B && gj[k] >= 0) ? w[(int64_t)gj[k] * ld + b] * (wt ? wt[b] : 1.0) : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256)
 // out[c][q] = jxw[c][q] * sum_I N[q][I] sum_J G[c][I][J] N[q][J]
 __global__ void k_quad_contract(int n_cells, int n_e, int n_q, const double* __restrict__ N,
                                 const double* __restrict__ G, const double* __restrict__ jxw,
-                                double* __restrict__ out) {
+                                double* __restrict__ out, int accumulate) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= (int64_t)n_cells * n_q) return;
   const int c = (int)(t / n_q), q = (int)(t % n_q);
@@ -114,7 +114,8 @@ __global__ void k_quad_contract(int n_cells, int n_e, int n_q, const double* __r
     for (int J = 0; J < n_e; ++J) s = fma(gr[J], Nq[J], s);
     acc = fma(Nq[I], s, acc);
   }
-  out[t] = (jxw ? jxw[t] : 1.0) * acc;
+  const double v = (jxw ? jxw[t] : 1.0) * acc;
+  out[t] = accumulate ? out[t] + v : v;
 }
 
 }  // namespace
@@ -129,19 +130,20 @@ void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double
 }
 
 void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
-                double alpha, double* G, cudaStream_t st) {
+                double alpha, double* G, cudaStream_t st, const double* weights) {
   const int nt = (op->n_e + T - 1) / T;
   const int64_t blocks = (int64_t)op->n_cells * nt * nt;
   CHEFSI_REQUIRE(blocks < (1ll << 31), "cell outer grid too large");
   k_cell_outer<<<(unsigned)blocks, 256, 0, st>>>(op->map.ptr, op->n_e, op->inv_sqrt_mass.ptr, u,
-                                                 w, ld, B, alpha, G, nt);
+                                                 w, ld, B, weights, alpha, G, nt);
   CHEFSI_CHECK_LAUNCH();
 }
 
 void quad_contract(int n_cells, int n_e, int n_q, const double* N, const double* G,
-                   const double* jxw, double* out, cudaStream_t st) {
+                   const double* jxw, double* out, cudaStream_t st, bool accumulate) {
   const int64_t n = (int64_t)n_cells * n_q;
-  k_quad_contract<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n_cells, n_e, n_q, N, G, jxw, out);
+  k_quad_contract<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n_cells, n_e, n_q, N, G, jxw, out,
+                                                               accumulate ? 1 : 0);
   CHEFSI_CHECK_LAUNCH();
 }
 

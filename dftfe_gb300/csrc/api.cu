@@ -1015,6 +1015,22 @@ int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int
   CHEFSI_API_END
 }
 
+int chefsi_density(chefsi_operator op, const double* X, int64_t ld, int32_t N,
+                   const double* occupation, int32_t n_q, const double* shape, const double* jxw,
+                   double* rho, int32_t accumulate, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && occupation && shape && rho && N >= 1 && ld >= N && n_q >= 1,
+                 "bad argument");
+  CHEFSI_REQUIRE(!op->is_complex, "density: real operators only");
+  cudaStream_t st = as_stream(stream);
+  const size_t ng = (size_t)op->n_cells * op->n_e * op->n_e;
+  double* G = op->ws64a.ensure(ng);
+  CHEFSI_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * ng, st));
+  cell_outer(op, X, X, ld, N, 1.0, G, st, occupation);
+  quad_contract(op->n_cells, op->n_e, n_q, shape, G, jxw, rho, st, accumulate != 0);
+  CHEFSI_API_END
+}
+
 int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,
                           const double* eig_host, double* res_host, void* stream) {
   CHEFSI_API_BEGIN

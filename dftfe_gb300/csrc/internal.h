@@ -245,10 +245,12 @@ void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaS
 // adjoint / assembly building blocks (adjoint.cu)
 void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
                     const double* v, double* out, cudaStream_t st);
+// G_c += alpha * sum_b weights[b] (D u_b)_c (D w_b)_c^T (weights null: 1), D = M^{-1/2}
 void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
-                double alpha, double* G, cudaStream_t st);
+                double alpha, double* G, cudaStream_t st, const double* weights = nullptr);
+// out[c][q] (+)= jxw[c][q] * sum_IJ N[q][I] G[c][I][J] N[q][J]
 void quad_contract(int n_cells, int n_e, int n_q, const double* N, const double* G,
-                   const double* jxw, double* out, cudaStream_t st);
+                   const double* jxw, double* out, cudaStream_t st, bool accumulate = false);
 // replace the operator's cell matrices (device, unscaled) and refresh the derived copies
 void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStream_t st);
 // the real form of a folded complex operator (cached in op->rv)

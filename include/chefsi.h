@@ -248,6 +248,18 @@ int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int
                                     const double* shape, const double* G, const double* jxw,
                                     double* out, void* stream);
 
+/* Electron density of the Ritz vectors at the quadrature points:
+   rho[c][q] (+)= jxw[c][q] * sum_i occupation[i] |psi_i(x_q)|^2, with psi_i = M^{-1/2} x_i
+   interpolated by the cell's shape functions shape[q][I] ([n_q][nodes_per_cell], device) and
+   occupation (device, N entries) carrying the occupation, spin and k-point weights; jxw may be
+   null (weight 1); accumulate != 0 adds to rho (the sum over k-points and spins). Real
+   operators, FP64. Replaces the per-(k, spin) density accumulation of densityCalculator
+   (src/dft/densityCalculator.cc:39; densityCalculatorDeviceKernels.cc:34-86): here through the
+   occupation-weighted cell outer products sum_i f_i psi_c,i psi_c,i^T and one contraction. */
+int chefsi_density(chefsi_operator op, const double* X, int64_t ld, int32_t N,
+                   const double* occupation, int32_t n_q, const double* shape, const double* jxw,
+                   double* rho, int32_t accumulate, void* stream);
+
 /* residual norms r_i = || A x_i - lambda_i x_i || (host arrays eig, res). */
 int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,
                           const double* eig_host, double* res_host, void* stream);

@@ -13,6 +13,8 @@ FP64 restatement of DFT-FE's CPU CheFSI. The operator apply and the Chebyshev fi
                           src/solvers/eigenSolvers/chebyshevOrthogonalizedSubspaceIterationSolver.cc:116-607
 * ``chebyshev_order``  -- the degree lookup table, same file :24-56
 * bounds update       -- kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:335-365,489-498
+* ``density``          -- densityCalculator, src/dft/densityCalculator.cc:39
+                          (densityCalculatorDeviceKernels.cc:34-86)
 
 Parity status: the reference ships no golden vectors at this boundary (its tests pin total
 energies only) and cannot be built here (deal.II, MPI, ELPA absent), so parity with the
@@ -169,6 +171,23 @@ def cell_hamiltonians_direct(K: np.ndarray, N: np.ndarray, vjxw: np.ndarray) -> 
     lib().oracle_cell_hamiltonians(ctypes.c_int32(nc), ctypes.c_int32(ne), ctypes.c_int32(nq),
                                    _p(K), _p(N), _p(v), _p(H))
     return H
+
+
+def density(cell_map: np.ndarray, inv_sqrt_mass: np.ndarray, shape: np.ndarray, X: np.ndarray,
+            occupation: np.ndarray, jxw: np.ndarray | None = None) -> np.ndarray:
+    """rho[c][q] = jxw[c][q] sum_i f_i |psi_i(x_q)|^2 with psi_i = M^{-1/2} x_i interpolated by
+    the cell's shape functions: the density of densityCalculator (src/dft/densityCalculator.cc:39;
+    the device path densityCalculatorDeviceKernels.cc:34-86 interpolates the cell's nodal
+    values with the shape-function matrix, squares and sums with the occupations)."""
+    nc = cell_map.shape[0]
+    rho = np.empty((nc, shape.shape[0]))
+    for c in range(nc):
+        nodal = inv_sqrt_mass[cell_map[c]][:, None] * X[cell_map[c]]   # [n_e][N]
+        psi = shape @ nodal                                              # [n_q][N]
+        rho[c] = (psi * psi) @ occupation
+    if jxw is not None:
+        rho *= jxw
+    return rho
 
 
 # ---------------------------------------------------------------------------- dense steps

@@ -161,3 +161,26 @@ def test_golden_fixture_reproduces():
     out = build_case()
     for k in g.files:
         assert np.allclose(out[k], g[k], rtol=1e-11, atol=1e-12), k
+
+
+def test_oracle_density_of_a_constant_state():
+    """psi = M^{-1/2} x = 1 at every node (x = M^{1/2} 1) interpolates to 1 at every Gauss
+    point, so rho = sum_i f_i there and its integral is sum_i f_i times the volume."""
+    pr = small_problem(n=2, L=4.0, p=3, wells=2)
+    mesh = pr.mesh
+    nq1 = mesh.p + 3
+    xq, _ = fe.gauss_nodes_weights(nq1)
+    phi, _ = mesh.shape_1d(xq)
+    q = np.arange(nq1 ** 3)
+    qx, qy, qz = q % nq1, (q // nq1) % nq1, q // (nq1 * nq1)
+    i = np.arange(mesh.nodes_per_cell)
+    p1 = mesh.p + 1
+    N = phi[qx][:, i % p1] * phi[qy][:, (i // p1) % p1] * phi[qz][:, i // (p1 * p1)]
+    _, w3 = mesh.quadrature(nq1)
+    jxw = np.broadcast_to(w3, (mesh.n_cells, len(w3))).copy()
+    X = np.repeat((1.0 / pr.inv_sqrt_mass)[:, None], 2, axis=1)
+    occ = np.array([2.0, 0.5])
+    rho = orc.density(pr.cell_map, pr.inv_sqrt_mass, N, X, occ)
+    assert np.abs(rho - occ.sum()).max() < 1e-12
+    rho_w = orc.density(pr.cell_map, pr.inv_sqrt_mass, N, X, occ, jxw)
+    assert abs(rho_w.sum() - occ.sum() * 4.0 ** 3) < 1e-9
