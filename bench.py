@@ -412,16 +412,21 @@ def run_density_check(args):
     occ = np.where(np.arange(N) < N // 2, 2.0, 0.0)
     occ_d, shape_d = t(occ), t(shape)
     jxw_d = t(np.broadcast_to(w3, (mesh.n_cells, len(w3))))
-    for _ in range(max(1, args.warmup)):
-        rho = chefsi.density(op, X, occ_d, shape_d, jxw_d)
-    torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record()
-    for _ in range(args.steps):
-        rho = chefsi.density(op, X, occ_d, shape_d, jxw_d)
-    e.record()
-    torch.cuda.synchronize()
-    ms = s.elapsed_time(e) / args.steps
+    def timed(prec):
+        for _ in range(max(1, args.warmup)):
+            r = chefsi.density(op, X, occ_d, shape_d, jxw_d, precision=prec)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(args.steps):
+            r = chefsi.density(op, X, occ_d, shape_d, jxw_d, precision=prec)
+        e.record()
+        torch.cuda.synchronize()
+        return r, s.elapsed_time(e) / args.steps
+
+    rho_m, ms_m = timed("mixed")
+    rho, ms = timed("fp64")
+    mixed_err = float((rho_m - rho).abs().max() / rho.abs().max())
     # direct interpolate-square-sum on 16 seeded cells (FP64 numpy)
     cells = np.random.default_rng(args.seed).choice(mesh.n_cells, 16, replace=False)
     ref = np.empty((16, len(w3)))
@@ -436,6 +441,8 @@ def run_density_check(args):
     print(json.dumps({"metric": "density at the quadrature points (FP64)", "value": ms, "unit": "ms",
                       "workload": args.workload, "n_dofs": M, "n_wfc": N, "n_q": nq,
                       "gflops": flops / (ms * 1e-3) / 1e9,
+                      "mixed_ms": ms_m, "mixed_max_rel_err_vs_fp64": mixed_err,
+                      "mixed_interp_tflops": 2.0 * nc * nq * ne * N / (ms_m * 1e-3) / 1e12,
                       "max_rel_err_vs_direct_16_cells": float(np.abs(got - ref).max() / np.abs(ref).max())}))
     return 0
 

@@ -108,7 +108,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
                          vp, i64, i32, vp], ctypes.c_int),
         "chefsi_axpby": ([i64, i32, f64, vp, i64, f64, vp, i64, vp], ctypes.c_int),
         "chefsi_convert_block": ([i32, vp, i64, i32, vp, i64, i64, i32, f64, vp], ctypes.c_int),
-        "chefsi_density": ([vp, vp, i64, i32, vp, i32, vp, vp, vp, i32, vp], ctypes.c_int),
+        "chefsi_density": ([vp, vp, i64, i32, vp, i32, vp, vp, vp, i32, i32, vp], ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians": ([i32, i32, i32, vp, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_operator_update_cell_matrices": ([vp, vp, vp], ctypes.c_int),
         "chefsi_cell_outer_accumulate": ([vp, vp, vp, i64, i32, f64, vp, vp], ctypes.c_int),

@@ -155,7 +155,8 @@ fillOverlapMatrix = KohnShamOperator.overlap
 
 def density(op: "KohnShamOperator", X: torch.Tensor, occupation: torch.Tensor,
             shape: torch.Tensor, jxw: torch.Tensor | None = None,
-            rho: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
+            rho: torch.Tensor | None = None, accumulate: bool = False,
+            precision: str = "fp64") -> torch.Tensor:
     """rho[c][q] (+)= jxw[c][q] sum_i f_i |psi_i(x_q)|^2 (densityCalculator: the density of the
     Ritz vectors at the quadrature points; psi = M^{-1/2} x interpolated by shape [n_q][n_e])."""
     nq = shape.shape[0]
@@ -163,7 +164,8 @@ def density(op: "KohnShamOperator", X: torch.Tensor, occupation: torch.Tensor,
         rho = torch.zeros((op.n_cells, nq), dtype=torch.float64, device=X.device)
     occ = occupation.to(device=X.device, dtype=torch.float64).contiguous()
     check(_lib.load().chefsi_density(op.handle, _ptr(X), X.stride(0), X.shape[1], _ptr(occ), nq,
-                                     _ptr(shape), _ptr(jxw), _ptr(rho), int(accumulate), _stream()))
+                                     _ptr(shape), _ptr(jxw), _ptr(rho), int(accumulate),
+                                     _prec(precision), _stream()))
     return rho
 
 

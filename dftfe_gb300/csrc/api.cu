@@ -1017,12 +1017,15 @@ int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int
 
 int chefsi_density(chefsi_operator op, const double* X, int64_t ld, int32_t N,
                    const double* occupation, int32_t n_q, const double* shape, const double* jxw,
-                   double* rho, int32_t accumulate, void* stream) {
+                   double* rho, int32_t accumulate, int32_t precision, void* stream) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op && X && occupation && shape && rho && N >= 1 && ld >= N && n_q >= 1,
                  "bad argument");
   CHEFSI_REQUIRE(!op->is_complex, "density: real operators only");
   cudaStream_t st = as_stream(stream);
+  if (precision == CHEFSI_PREC_MIXED &&
+      density_tc(op, X, ld, N, occupation, n_q, shape, jxw, rho, accumulate != 0, st))
+    return CHEFSI_OK;
   const size_t ng = (size_t)op->n_cells * op->n_e * op->n_e;
   double* G = op->ws64a.ensure(ng);
   CHEFSI_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * ng, st));

@@ -120,6 +120,11 @@ void axpby_split_group(const AxpbyGroupItem* items, int n, cudaStream_t st);
 void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipeline* pipe,
                         cudaStream_t st);
 int device_sms();
+// the density on tensor cores (FP16 split of M^{-1/2} x and of the shape functions, FP32 sums):
+// rho[c][q] (+)= jxw * sum_v occ_v psi_v(x_q)^2; false if the tensor path does not apply
+bool density_tc(chefsi_operator_s* op, const double* X, int64_t ld, int B, const double* occ,
+                int n_q, const double* shape, const double* jxw, double* rho, bool accumulate,
+                cudaStream_t st);
 // the same with the three-term split (33 bits: src exactly, the cell matrices to 2^-33; six
 // products, FP32 accumulation): the accuracy class of the FP32 apply. src must be scaled so
 // that max |src| < 2^15.

@@ -78,7 +78,9 @@ struct TcProblem {
   int B;               // vectors
   int n_chunks;        // 128-vector chunks
   float out_scale;     // scalar / 2^s
-  int pad_;
+  int a_shared;        // 1: one matrix for every cell (the density's shape functions)
+  const float* occ;    // density: per-vector weights (occupations, scales folded in)
+  float* rho;          // density: [n_cells][n_rows] sums of occ_v D[v][row]^2
 };
 constexpr int kMaxGroup = 32;
 
@@ -87,6 +89,7 @@ struct TcArgs {
   int n_probs;
   int64_t n_pairs; // (cell, chunk) pairs over the group
   int n_e;
+  int n_rows;      // matrix rows (= n_e for H; quadrature points for the density)
   int nkb;         // K-blocks of 32 nodes
   int n_half;      // cell rows per work unit (= MMA N)
   int n_halves;    // row halves per cell (1 or 2)
@@ -205,7 +208,11 @@ constexpr int kThreads3 = 192 + 32 * kEpiWarps;
 //         leaves errors ~5x those of an FP32 SIMT apply; over the 12 steps of one K-block it
 //         does not. Needs at most kChunkCols accumulator columns per epilogue warp.
 constexpr int kChunkCols = 96;
-template <int NS, bool KCHUNK>
+// DENS: the density mode. The matrix is the shape-function matrix N[q][node] (one for all
+//       cells, rows = quadrature points in parts of n_half), so D[v][q] = psi_v(x_q) for the
+//       gathered vectors; the epilogue adds occ_v D[v][q]^2 over the vectors into rho[c][q]
+//       (warp butterfly reduction, one FP32 atomic per quadrature point and warp).
+template <int NS, bool KCHUNK, bool DENS = false>
 __global__ void __launch_bounds__(kThreads3, 1)
     cell_hx_tc_kernel(TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
@@ -275,7 +282,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
           mbar_arrive_expect_tx(&tma_full[s], bytes);
           // one contiguous block per split term: the (cell, half, K-block) tile, stored in
           // its swizzled shared-memory image
-          const int64_t tix = ((int64_t)w.cell * args.n_halves + w.half) * nkb + kb;
+          const TcProblem& pa = args.prob[w.p];
+          const int64_t tix = ((int64_t)(pa.a_shared ? 0 : w.cell) * args.n_halves + w.half) * nkb + kb;
           const int64_t toff = tix * (args.n_half * (kRowBytes / 2));
           const TcProblem& pr = args.prob[w.p];
           bulk_load(st, pr.ahi + toff, bytes / NS, &tma_full[s]);
@@ -519,6 +527,46 @@ __global__ void __launch_bounds__(kThreads3, 1)
             }
           }
         }
+      }
+    } else if (DENS) {
+      for (int64_t it = 0; it < my_units; ++it) {
+        const int buf = (int)(it & 1);
+        const uint32_t ph = (uint32_t)((it >> 1) & 1);
+        const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
+        fence_after();
+        if (!epilogue_sync_and(okw)) break;
+        const Unit w = unit_at(it, first, step, args);
+        const TcProblem& pr = args.prob[w.p];
+        const int nrows = min(args.n_half, args.n_rows - w.half * args.n_half);
+        const int gb = w.chunk * kVec + q * 32 + lane;
+        const float f = gb < pr.B ? __ldg(pr.occ + gb) : 0.f;
+        float* rrow = pr.rho + (int64_t)w.cell * args.n_rows + w.half * args.n_half;
+        const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
+        for (int c0 = c_beg; c0 < c_end; c0 += 16) {
+          float v[16];
+          tmem_ld16(tq + c0, v);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) v[i] = f * v[i] * v[i];
+          // butterfly: each step a lane keeps half of its values and adds its partner's
+          // matching half; after offsets 16, 8, 4, 2 lane l holds value (l >> 1) & 15 summed
+          // over 16 lanes, the last exchange adds the other 16
+#pragma unroll
+          for (int sh = 4, half = 8; sh >= 1; --sh, half >>= 1) {
+            const bool up = (lane >> sh) & 1;
+#pragma unroll
+            for (int j = 0; j < half; ++j) {
+              const float send = up ? v[j] : v[j + half];
+              const float keep = up ? v[j + half] : v[j];
+              v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 1 << sh);
+            }
+          }
+          const float tot = v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+          const int col = c0 + ((lane >> 1) & 15);
+          if ((lane & 1) == 0 && col < nrows) atomicAdd(rrow + col, tot);
+        }
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
       }
     } else {
       for (int64_t it = 0; it < my_units; ++it) {
@@ -845,6 +893,7 @@ void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipelin
   TcArgs a{};
   a.n_probs = n;
   a.n_e = n_e;
+  a.n_rows = n_e;
   a.nkb = p.npad / kKB;
   a.n_half = p.n_half;
   a.n_halves = p.n_halves;
@@ -993,6 +1042,155 @@ bool hx_tc3(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
   if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
   launch_tc(op, hi, lo, lo3, dst, ldd, B, scalar, 3, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
+  return true;
+}
+
+// ---------------------------------------------------------------- density on tensor cores
+// (hi, lo)[r][j] = split(fp32(x[r][j]) * fp32(d[r] 2^s)): the vectors M^{-1/2} x, scaled into
+// the FP16 split's range
+__global__ void k_split_rows_dscaled(const double* __restrict__ x, int64_t ldx, int64_t M, int B,
+                                     const double* __restrict__ d, double s,
+                                     __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int64_t n = M * (int64_t)(B / 2);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / (B / 2);
+    const int j = (int)(t % (B / 2)) * 2;
+    const float dr = (float)(d[r] * s);
+    __half h0, l0, h1, l1;
+    split_f32((float)x[r * ldx + j] * dr, h0, l0);
+    split_f32((float)x[r * ldx + j + 1] * dr, h1, l1);
+    *reinterpret_cast<__half2*>(hi + r * B + j) = __halves2half2(h0, h1);
+    *reinterpret_cast<__half2*>(lo + r * B + j) = __halves2half2(l0, l1);
+  }
+}
+
+// shape-function tiles: part h, K-block kb = rows [h n_half, ...) x nodes [32 kb, ...) of
+// 2^s N, zero outside (n_q, n_e), each tile the 64B-swizzled K-major shared-memory image
+__global__ void k_split_shape(const double* __restrict__ N, int n_q, int n_e, int n_half,
+                              int n_parts, int nkb, double s, __half* __restrict__ hi,
+                              __half* __restrict__ lo) {
+  const int64_t tile_elems = (int64_t)n_half * 32;
+  const int64_t n = (int64_t)n_parts * nkb * tile_elems;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t tix = t / tile_elems;
+    const uint32_t o = sw64_offset(0, 2u * (uint32_t)(t - tix * tile_elems));
+    const int kb = (int)(tix % nkb), h = (int)(tix / nkb);
+    const int I = h * n_half + (int)(o / 64), J = kb * 32 + (int)(o % 64) / 2;
+    const double v = (I < n_q && J < n_e) ? s * N[(int64_t)I * n_e + J] : 0.0;
+    const __half hh = __double2half(v);
+    hi[t] = hh;
+    lo[t] = __double2half(v - (double)__half2float(hh));
+  }
+}
+
+__global__ void k_density_weights(const double* __restrict__ occ, int B, double s,
+                                  float* __restrict__ w) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < B) w[j] = (float)(occ[j] * s);
+}
+
+// rho[t] (+)= jxw[t] * r32[t]
+__global__ void k_density_finish(const float* __restrict__ r32, const double* __restrict__ jxw,
+                                 int64_t n, int accumulate, double* __restrict__ rho) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (jxw ? jxw[t] : 1.0) * (double)r32[t];
+    rho[t] = accumulate ? rho[t] + v : v;
+  }
+}
+
+bool density_tc(chefsi_operator_s* op, const double* X, int64_t ld, int B, const double* occ,
+                int n_q, const double* shape, const double* jxw, double* rho, bool accumulate,
+                cudaStream_t st) {
+  if (!tc_usable(op) || B % 8 != 0) return false;
+  const int n_e = op->n_e;
+  const int npad_k = (n_e + 31) / 32 * 32;
+  const int nkb = npad_k / kKB;
+  const int n_parts = (n_q + 255) / 256;
+  const int n_half = ((n_q + n_parts - 1) / n_parts + 15) / 16 * 16;
+  const int64_t M = op->n_dofs;
+  // scales: max |M^{-1/2} x| <= max|x| max|d| -> 2^8, max |N| -> [2^14, 2^15)
+  DeviceBuffer<double> mx(2);
+  absmax_block_f64(X, ld, M, B, mx.ptr, st);
+  absmax_block_f64(op->inv_sqrt_mass.ptr, 1, M, 1, mx.ptr + 1, st);
+  double h[2] = {0.0, 0.0};
+  CHEFSI_CUDA(cudaMemcpyAsync(h, mx.ptr, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  DeviceBuffer<double> nmax(1);
+  absmax_block_f64(shape, n_e, n_q, n_e, nmax.ptr, st);
+  double hn = 0.0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&hn, nmax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  const double amax = h[0] * h[1];
+  const int ex = (amax > 0 && std::isfinite(amax)) ? 8 - (int)std::ceil(std::log2(amax)) : 0;
+  const int en = (hn > 0 && std::isfinite(hn)) ? 14 - (int)std::floor(std::log2(hn)) : 0;
+  const size_t nx = (size_t)M * B;
+  __half* xh = op->xs_hi.ensure(nx);
+  __half* xl = op->xs_lo.ensure(nx);
+  k_split_rows_dscaled<<<grid_for(M * (B / 2), 256), 256, 0, st>>>(
+      X, ld, M, B, op->inv_sqrt_mass.ptr, std::ldexp(1.0, ex), xh, xl);
+  CHEFSI_CHECK_LAUNCH();
+  const int64_t nt = (int64_t)n_parts * nkb * n_half * 32;
+  DeviceBuffer<__half> sh(nt), sl(nt);
+  k_split_shape<<<grid_for(nt, 256), 256, 0, st>>>(shape, n_q, n_e, n_half, n_parts, nkb,
+                                                    std::ldexp(1.0, en), sh.ptr, sl.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  DeviceBuffer<float> w(B);
+  k_density_weights<<<(B + 255) / 256, 256, 0, st>>>(occ, B, std::ldexp(1.0, -2 * (ex + en)), w.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  const int64_t nr = (int64_t)op->n_cells * n_q;
+  DeviceBuffer<float> r32(nr);
+  CHEFSI_CUDA(cudaMemsetAsync(r32.ptr, 0, sizeof(float) * nr, st));
+  // the launch: rows = quadrature points in n_parts parts of n_half
+  TcArgs a{};
+  a.n_probs = 1;
+  a.n_e = n_e;
+  a.n_rows = n_q;
+  a.nkb = nkb;
+  a.n_half = n_half;
+  a.n_halves = n_parts;
+  a.buf_stride = n_half <= 128 ? 128 : 256;
+  a.tmem_cols = 2 * a.buf_stride;
+  a.stages = 3;
+  a.xstages = 8;
+  while (a.xstages > 3 && make_layout(n_half, a.stages, a.xstages, 2).total + 1024 > 220 * 1024)
+    --a.xstages;
+  a.lookahead = std::max(1, std::min(a.xstages - 2, 6));
+  const int smem = make_layout(n_half, a.stages, a.xstages, 2).total + 1024;
+  if (!op->tc_err.ptr) {
+    op->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  }
+  a.err = op->tc_err.ptr;
+  TcProblem& pr = a.prob[0];
+  pr.xhi = xh;
+  pr.xlo = xl;
+  pr.xlo3 = xl;
+  pr.dst = nullptr;
+  pr.map = op->map.ptr;
+  pr.ahi = sh.ptr;
+  pr.alo = sl.ptr;
+  pr.alo3 = sl.ptr;
+  pr.ldx = B;
+  pr.ldd = B;
+  pr.B = B;
+  pr.n_chunks = (B + kVec - 1) / kVec;
+  pr.out_scale = 1.f;
+  pr.a_shared = 1;
+  pr.occ = w.ptr;
+  pr.rho = r32.ptr;
+  pr.pair_begin = 0;
+  a.n_pairs = (int64_t)op->n_cells * pr.n_chunks;
+  auto kernel = cell_hx_tc_kernel<2, false, true>;
+  CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
+  kernel<<<(unsigned)grid, kThreads3, smem, st>>>(a);
+  CHEFSI_CHECK_LAUNCH();
+  k_density_finish<<<grid_for(nr, 256), 256, 0, st>>>(r32.ptr, jxw, nr, accumulate ? 1 : 0, rho);
+  CHEFSI_CHECK_LAUNCH();
+  const int tc = tc_check_error(op, st);   // synchronises: the temporaries live until here
+  if (tc != CHEFSI_OK) throw Error(tc, "tensor-core density: a bounded device wait expired");
   return true;
 }
 

@@ -253,12 +253,15 @@ int chefsi_cell_quadrature_contract(int32_t n_cells, int32_t nodes_per_cell, int
    interpolated by the cell's shape functions shape[q][I] ([n_q][nodes_per_cell], device) and
    occupation (device, N entries) carrying the occupation, spin and k-point weights; jxw may be
    null (weight 1); accumulate != 0 adds to rho (the sum over k-points and spins). Real
-   operators, FP64. Replaces the per-(k, spin) density accumulation of densityCalculator
-   (src/dft/densityCalculator.cc:39; densityCalculatorDeviceKernels.cc:34-86): here through the
-   occupation-weighted cell outer products sum_i f_i psi_c,i psi_c,i^T and one contraction. */
+   operators. precision CHEFSI_PREC_FP64: the occupation-weighted cell outer products
+   sum_i f_i psi_c,i psi_c,i^T and one contraction with the shape functions, FP64.
+   CHEFSI_PREC_MIXED: tensor cores interpolate psi at the quadrature points (FP16 split of
+   M^{-1/2} x and of the shape functions, FP32 accumulation) and add f_i psi^2 in FP32.
+   Replaces the per-(k, spin) density accumulation of densityCalculator
+   (src/dft/densityCalculator.cc:39; densityCalculatorDeviceKernels.cc:34-86). */
 int chefsi_density(chefsi_operator op, const double* X, int64_t ld, int32_t N,
                    const double* occupation, int32_t n_q, const double* shape, const double* jxw,
-                   double* rho, int32_t accumulate, void* stream);
+                   double* rho, int32_t accumulate, int32_t precision, void* stream);
 
 /* residual norms r_i = || A x_i - lambda_i x_i || (host arrays eig, res). */
 int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t N,

@@ -1,5 +1,6 @@
 """Electron density of the Ritz vectors at the quadrature points (`chefsi_density`, DFT-FE's
-densityCalculator) against the oracle's direct interpolate-square-sum, FP64 to 1e-12."""
+densityCalculator) against the oracle's direct interpolate-square-sum: FP64 to 1e-12, the
+tensor-core path to 2e-5 of the largest value."""
 import numpy as np
 import pytest
 import torch
@@ -44,6 +45,27 @@ def test_density_matches_oracle(cuda, p, n, N):
     ref2 = ref + orc.density(pr.cell_map, pr.inv_sqrt_mass, shape, X2, occ, jxw)
     rho2 = C.density(op, t(X2), t(occ), t(shape), t(jxw), rho=t(rho), accumulate=True)
     assert np.abs(rho2.cpu().numpy() - ref2).max() <= 1e-12 * np.abs(ref2).max()
+
+
+@pytest.mark.parametrize("p,n,N", [(2, 3, 8), (4, 2, 136), (6, 2, 256)])
+def test_density_tensor_cores_match_oracle(cuda, p, n, N):
+    """The tensor-core density (FP16 split of M^{-1/2} x and of the shape functions, FP32
+    accumulation; quadrature points in one, two or three row parts): within 2e-5 of the
+    largest density value of the FP64 oracle."""
+    from dftfe_gb300 import chefsi as C
+    pr = small_problem(n=n, L=2.0 * n, p=p, wells=2)
+    op = C.KohnShamOperator.from_problem(pr)
+    rng = np.random.default_rng(3 * p + n)
+    X = rng.standard_normal((pr.n_dofs, N))
+    occ = rng.uniform(0.0, 2.0, N)
+    shape, jxw = quadrature(pr)
+    ref = orc.density(pr.cell_map, pr.inv_sqrt_mass, shape, X, occ, jxw)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    rho = C.density(op, t(X), t(occ), t(shape), t(jxw), precision="mixed").cpu().numpy()
+    assert np.abs(rho - ref).max() <= 2e-5 * np.abs(ref).max()
+    rho2 = C.density(op, t(X), t(occ), t(shape), t(jxw), rho=t(rho), accumulate=True,
+                     precision="mixed").cpu().numpy()
+    assert np.abs(rho2 - 2 * ref).max() <= 4e-5 * np.abs(ref).max()
 
 
 def test_density_integrates_to_the_electron_count(cuda):
