@@ -385,6 +385,84 @@ def run_ritz_check(args):
     return 0
 
 
+def run_spectrum_split_check(args):
+    """Spectrum-split Rayleigh-Ritz (rayleighRitzGEPSpectrumSplitDirect) on the workload, with
+    the core-state count of DFT-FE's FAST mode on a device (0.8 of the occupied states, floored
+    to a multiple of the 128-vector block). After three mixed iterations from X0, (1) one mixed
+    CheFSI iteration with the full and with the spectrum-split RR from the same block and
+    bounds, phases timed; (2) the RR step alone in FP64 and in mixed precision (fractional
+    block FP64, and reduced) on the same filtered block: fractional Ritz values compared with
+    the FP64 ones, XFrac spans compared."""
+    import torch
+    from dftfe_gb300 import build, chefsi
+    build.build()
+    pr = build_workload(args.workload, args.seed)
+    N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
+    blk = 128
+    n_core = int(0.8 * pr.n_occupied) // blk * blk
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    lo, blow, up = first_bounds(chefsi, op, N)
+    mk = lambda reduced=False: chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(
+        chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=blk,
+                            mixed_precision="mixed", rr_precision=args.rr_precision,
+                            spectrum_split_frac_reduced=reduced))
+    s = mk()
+    s.reinitSpectrumBounds(lo, blow, up)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 1)
+    X = torch.rand((M, N), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    for _ in range(3):
+        ev, _ = s.solve(op, X, useMixedPrec=True)
+        s.reinitSpectrumBounds(ev[0], ev[-1], up)
+    bounds = (ev[0], ev[-1], up)
+    it = {}
+    for mode in ("full", "split_frac_fp64", "split_frac_reduced"):
+        sv = mk(mode == "split_frac_reduced")
+        sv.reinitSpectrumBounds(*bounds)
+        Xc = X.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if mode == "full":
+            e, r = sv.solve(op, Xc, useMixedPrec=True)
+        else:
+            e, r, XF = sv.solveSpectrumSplit(op, Xc, n_core, useMixedPrec=True)
+            del XF
+        torch.cuda.synchronize()
+        it[mode] = {"iter_s": time.perf_counter() - t0, "phases_ms": sv.timings(True),
+                    "res_max_fractional": float(r[-(N - n_core):].max())}
+        del Xc
+    Xf = X.clone()
+    chefsi.chebyshevFilter(op, Xf, m, bounds[1], bounds[2], bounds[0], precision="mixed")
+    rr = {}
+    spans = {}
+    for key, prec, reduced in (("fp64", "fp64", False), ("mixed_frac_fp64", "mixed", False),
+                               ("mixed_frac_reduced", "mixed", True)):
+        Xc = Xf.clone()
+        XF = torch.empty((M, N - n_core), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = chefsi.rayleighRitzGEPSpectrumSplitDirect(op, Xc, XF, n_core, precision=prec,
+                                                      frac_reduced=reduced)
+        torch.cuda.synchronize()
+        rr[key] = {"ev": e, "s": time.perf_counter() - t0}
+        spans[key] = XF
+        del Xc
+    out = {}
+    for key in ("mixed_frac_fp64", "mixed_frac_reduced"):
+        d = np.abs(rr[key]["ev"] - rr["fp64"]["ev"])
+        sv_q = np.linalg.svd((spans["fp64"].T @ spans[key]).cpu().numpy(), compute_uv=False)
+        out[key] = {"rr_s": rr[key]["s"], "max_abs_err_Ha": float(d.max()),
+                    "subspace_angle_rad": float(np.arccos(np.clip(sv_q.min(), -1.0, 1.0)))}
+    print(json.dumps({
+        "metric": "spectrum-split Rayleigh-Ritz: iteration time and fractional Ritz error",
+        "workload": args.workload, "n_dofs": M, "n_wfc": N, "occupied": pr.n_occupied,
+        "core_states": n_core, "fractional_states": N - n_core,
+        "iteration_full_rr": it["full"], "iteration_split_frac_fp64": it["split_frac_fp64"],
+        "iteration_split_frac_reduced": it["split_frac_reduced"],
+        "rr_fp64_s": rr["fp64"]["s"], "rr_mixed": out}))
+    return 0
+
+
 def run_density_check(args):
     """Density of the Ritz vectors at the quadrature points (chefsi_density, densityCalculator)
     on the mixed workload: 1024 vectors with occupations 2 for the lowest 512, the (p+3)^3 Gauss
@@ -607,6 +685,8 @@ def main():
     ap.add_argument("--fp64-compare", action="store_true")
     ap.add_argument("--density-check", action="store_true",
                     help="time chefsi_density on the workload and check 16 cells against a direct sum")
+    ap.add_argument("--spectrum-split-check", action="store_true",
+                    help="full vs spectrum-split RR iteration; split RR in FP64 vs mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -621,6 +701,8 @@ def main():
         return run_adjoint_check(args)
     if args.density_check:
         return run_density_check(args)
+    if args.spectrum_split_check:
+        return run_spectrum_split_check(args)
     if args.ritz_check:
         return run_ritz_check(args)
     return run_ours(args)

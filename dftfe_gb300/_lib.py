@@ -32,10 +32,11 @@ EXPORTS = [
     "chefsi_operator_info", "chefsi_hx", "chefsi_overlap", "chefsi_xthx",
     "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_heevd", "chefsi_syevd_noalloc",
     "chefsi_cholesky_gs",
-    "chefsi_rayleigh_ritz", "chefsi_residual_norms", "chefsi_solver_create",
+    "chefsi_rayleigh_ritz", "chefsi_rayleigh_ritz_spectrum_split", "chefsi_residual_norms",
+    "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
-    "chefsi_solve", "chefsi_solve_batched", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
+    "chefsi_solve", "chefsi_solve_spectrum_split", "chefsi_solve_batched", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
     "chefsi_axpby", "chefsi_convert_block", "chefsi_density", "chefsi_assemble_cell_hamiltonians", "chefsi_operator_update_cell_matrices",
     "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract",
 ]
@@ -68,7 +69,7 @@ class Params(ctypes.Structure):
         ("wfc_block", ctypes.c_int32), ("precision", ctypes.c_int32),
         ("lanczos_steps", ctypes.c_int32), ("reproducible", ctypes.c_int32),
         ("first_scf_degree_scale", ctypes.c_double), ("keep_hx", ctypes.c_int32),
-        ("rr_precision", ctypes.c_int32),
+        ("rr_precision", ctypes.c_int32), ("ss_frac_reduced", ctypes.c_int32),
     ]
 
 
@@ -104,6 +105,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_syevd_noalloc": ([i32, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_cholesky_gs": ([vp, vp, i64, i32, i32, vp], ctypes.c_int),
         "chefsi_rayleigh_ritz": ([vp, vp, i64, i32, vp, vp, vp, i32, vp], ctypes.c_int),
+        "chefsi_rayleigh_ritz_spectrum_split": ([vp, vp, i64, i32, i32, vp, i64, vp, vp, i32, i32,
+                                                 vp], ctypes.c_int),
         "chefsi_gemm": ([ctypes.c_char, ctypes.c_char, i64, i32, i32, f64, vp, i64, vp, i64, f64,
                          vp, i64, i32, vp], ctypes.c_int),
         "chefsi_axpby": ([i64, i32, f64, vp, i64, f64, vp, i64, vp], ctypes.c_int),
@@ -122,6 +125,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solver_set_profiling": ([vp, i32], ctypes.c_int),
         "chefsi_solver_hx_stats": ([vp, vp, vp], ctypes.c_int),
         "chefsi_solve": ([vp, vp, vp, i32, vp, vp, i32, i32, vp], ctypes.c_int),
+        "chefsi_solve_spectrum_split": ([vp, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp],
+                                        ctypes.c_int),
         "chefsi_solve_batched": ([i32, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32], ctypes.c_int),
         "chefsi_solve_no_rr": ([vp, vp, vp, i32, i32, i32, vp], ctypes.c_int),
         "chefsi_chebyshev_order": ([f64], i32),

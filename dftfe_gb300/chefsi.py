@@ -219,6 +219,24 @@ def rayleighRitzGEP(op: KohnShamOperator, X: torch.Tensor, precision="fp64", wan
     return out[0] if len(out) == 1 else tuple(out)
 
 
+def rayleighRitzGEPSpectrumSplitDirect(op: KohnShamOperator, X: torch.Tensor, XFrac: torch.Tensor,
+                                       Noc: int, precision="fp64", want_hx=False,
+                                       frac_reduced=False):
+    """Spectrum-split Rayleigh-Ritz (linearAlgebraOperationsDevice.h:279-298): X [n_dofs, N]
+    is orthonormalised in place, XFrac [n_dofs, N - Noc] receives X Q_fr; returns the N - Noc
+    eigenvalues (ascending), and H XFrac when want_hx."""
+    N = X.shape[1]
+    nfr = N - Noc
+    if XFrac.shape != (X.shape[0], nfr) or XFrac.dtype != X.dtype:
+        raise ValueError("XFrac must be [n_dofs, N - Noc] of X's dtype")
+    ev = np.zeros(nfr)
+    HXF = torch.empty_like(XFrac) if want_hx else None
+    check(_lib.load().chefsi_rayleigh_ritz_spectrum_split(
+        op.handle, _ptr(X), X.stride(0), N, int(Noc), _ptr(XFrac), XFrac.stride(0), _np_ptr(ev),
+        _ptr(HXF), _prec(precision), int(bool(frac_reduced)), _stream()))
+    return (ev, HXF) if want_hx else ev
+
+
 def gemm(A: torch.Tensor, B: torch.Tensor, ta: str = "N", tb: str = "N", alpha: float = 1.0,
          beta: float = 0.0, C: torch.Tensor | None = None, precision="fp64") -> torch.Tensor:
     """C = alpha op(A) op(B) + beta C on the GPU (row-major FP64)."""
@@ -307,6 +325,9 @@ class SolverParams:
     chebyshevFilterPolyDegreeFirstScfScalingFactor: float = 1.34
     keep_hx: bool = True
     rr_precision: str = "fp64"         # HX precision feeding X^T H X in mixed mode
+    # spectrum split in mixed mode: the block of X^T H X coupling the fractional states from
+    # an FP64 H X (False, useMixedPrecXTHXSpectrumSplit's map) or from the rr_precision H X
+    spectrum_split_frac_reduced: bool = False
 
 
 class ChebyshevOrthogonalizedSubspaceIterationSolver:
@@ -330,6 +351,7 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
             p.first_scf_degree_scale = self.params.chebyshevFilterPolyDegreeFirstScfScalingFactor
             p.keep_hx = int(self.params.keep_hx)
             p.rr_precision = _prec(self.params.rr_precision)
+            p.ss_frac_reduced = int(self.params.spectrum_split_frac_reduced)
             h = ctypes.c_void_p()
             check(self._lib.chefsi_solver_create(ctypes.byref(p), ctypes.byref(h)))
             self._h[key] = h
@@ -361,6 +383,22 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
         check(self._lib.chefsi_solve(h, operatorMatrix.handle, _ptr(X), N, _np_ptr(ev),
                                      _np_ptr(rn), int(computeResidual), int(isFirstScf), _stream()))
         return ev, rn
+
+    def solveSpectrumSplit(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, Noc: int,
+                           XFrac: torch.Tensor | None = None, computeResidual: bool = True,
+                           useMixedPrec: bool = False, isFirstScf: bool = False):
+        """solve() with N - Noc wanted eigenvalues: filter, spectrum-split Rayleigh-Ritz.
+        X is left orthonormalised; returns (eigenValues, residualNorms, XFrac)."""
+        N = X.shape[1]
+        nfr = N - Noc
+        if XFrac is None:
+            XFrac = torch.empty((X.shape[0], nfr), dtype=X.dtype, device=X.device)
+        ev, rn = np.zeros(nfr), np.zeros(nfr)
+        h = self._handle(useMixedPrec)
+        check(self._lib.chefsi_solve_spectrum_split(
+            h, operatorMatrix.handle, _ptr(X), N, int(Noc), _ptr(XFrac), _np_ptr(ev), _np_ptr(rn),
+            int(computeResidual), int(isFirstScf), _stream()))
+        return ev, rn, XFrac
 
     def solveNoRR(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, numberPasses: int = 1,
                   useMixedPrec: bool = False, isFirstScf: bool = False):

@@ -33,6 +33,7 @@ struct chefsi_solver_s {
   double a0 = 0.0, b_low = 0.0, b_up = 0.0;
   int last_degree = 0;
   DeviceBuffer<double> Xb64, Yb64, S, Hp, T1, Z, W, evals, HX, rot, resid, scal;
+  DeviceBuffer<double> HXf, HXF;  // spectrum split: FP64 H X of the fractional columns, H XFrac
   DeviceBuffer<double> G2, W2;  // 2N x 2N real views for the complex tensor-core products
   DeviceBuffer<float> Xb32, Yb32;
   TcOperand tx, th;      // FP16 splits of X and HX for the tensor-core RR products
@@ -444,6 +445,171 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   return CHEFSI_OK;
 }
 
+// Spectrum-split Rayleigh-Ritz (rayleighRitzGEPSpectrumSplitDirect,
+// src/linAlg/rayleighRitzDevice.cc:822-1455) for a real operator:
+//   S = X^T X = L L^T;  X <- X L^{-T} (Cholesky-GS, X stays in this orthonormal basis);
+//   Hp = X^T H X;  the top n_fr = N - n_occ eigenpairs (Q_fr, eigenvalues ascending) only;
+//   XFrac = X Q_fr ([M][n_fr], ldf);  with want_hxf, H XFrac = (H X) Q_fr into s->HXF.
+// Precision map of X^T H X in the mixed mode (XtHXMixedPrecOverlapComputeCommun,
+// src/dftOperator/kohnShamDFTOperatorDevice.cc:4553): the column blocks of wfc_block vectors
+// that lie inside the first n_occ vectors use the reduced-precision H X (rr_precision), and
+// the trailing square from the block that holds vector n_occ on, i.e. the block that couples
+// the fractionally occupied states, is recomputed from an FP64 H X and an FP64 Gram product
+// (unless ss_frac_reduced). rr_precision FP64 keeps every H X in FP64.
+int rayleigh_ritz_ss_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int N,
+                          int n_occ, double* XF, int64_t ldf, int prec, bool want_hxf,
+                          cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const int nfr = N - n_occ;
+  const bool tcd = prec == CHEFSI_PREC_MIXED && dense_tc_available();
+  double* S = s->S.ensure((size_t)N * N);
+  double* Hp = s->Hp.ensure((size_t)N * N);
+  double* T1 = s->T1.ensure((size_t)N * N);
+  double* Z = s->Z.ensure((size_t)N * nfr);
+  double* W = s->W.ensure((size_t)N * N);
+  double* w = s->evals.ensure(N);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  // S = X^T X, Cholesky, L^{-1}; X <- X L^{-T}
+  CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+  if (tcd) {
+    tc_exponents<double>(X, ld, M, N, s->tx, st);
+    tc_split_transposed<double>(X, ld, M, N, s->tx, st);
+    tc_gram(s->tx, nullptr, S, N, true, s->tcw, st);
+  } else {
+    gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+  }
+  symmetrize_lower(S, N, st);
+  if (fault_injected("not_spd")) {
+    k_negate_diag0<<<1, 1, 0, st>>>(S);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower(S, N, st);
+  k_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);
+  CHEFSI_CHECK_LAUNCH();
+  rotate_rows(s, X, ld, M, N, W, prec, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  // H X of the orthonormal X (same precision choices as the full Rayleigh-Ritz step)
+  double* HX = s->HX.ensure((size_t)M * N);
+  const int rrp = s->p.rr_precision;
+  const bool tc3 = is_mixed(prec) && rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(op, N);
+  const bool tc2 = is_mixed(prec) && rrp == CHEFSI_PREC_MIXED && tc_split_usable(op, N);
+  const bool hx32 = is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC || tc2);
+  float* y32 = nullptr;
+  if (hx32) {
+    float* x32 = s->Xb32.ensure((size_t)M * N);
+    y32 = s->Yb32.ensure((size_t)M * N);
+    double scale = 1.0;
+    if (tc2 || tc3) {
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(X, ld, M, N, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, (tc3 ? 14 : 8) - (int)std::ceil(std::log2(amax)));
+    }
+    copy_block<double, float>(X, ld, x32, N, M, N, scale, st);
+    bool done = false;
+    if (tc3)
+      done = hx_tc3(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    else if (tc2)
+      done = hx_tc(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    if (!done) hx_f32(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    if (!tcd) copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
+  } else {
+    hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
+  }
+  // Hp = X^T (H X), lower triangle
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
+  if (tcd) {
+    tc_exponents<double>(X, ld, M, N, s->tx, st);
+    tc_split_transposed<double>(X, ld, M, N, s->tx, st);
+    if (hx32) {
+      tc_exponents<float>(y32, N, M, N, s->th, st);
+      tc_split_transposed<float>(y32, N, M, N, s->th, st);
+    } else {
+      tc_exponents<double>(HX, N, M, N, s->th, st);
+      tc_split_transposed<double>(HX, N, M, N, s->th, st);
+    }
+    tc_gram(s->tx, &s->th, Hp, N, true, s->tcw, st);
+  } else {
+    gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
+  }
+  if (hx32 && !s->p.ss_frac_reduced) {
+    // the trailing square from the wfc block holding vector n_occ on, in FP64
+    const int blk = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
+    const int n_lo = (n_occ / blk) * blk;
+    const int nf = N - n_lo;
+    double* HXf = s->HXf.ensure((size_t)M * nf);
+    hx_all_f64(op, X + n_lo, ld, nf, HXf, s->p.wfc_block, st);
+    CHEFSI_CUDA(cudaMemsetAsync(T1, 0, sizeof(double) * nf * nf, st));
+    gram_f64(X + n_lo, ld, HXf, nf, M, nf, nf, T1, nf, CHEFSI_PREC_FP64, true, st);
+    copy_block<double, double>(T1, nf, Hp + (int64_t)n_lo * N + n_lo, N, nf, nf, 1.0, st);
+  }
+  symmetrize_lower(Hp, N, st);
+  // Mixed mode: the reduced-precision rotation leaves X^T X = I + O(2^-22 cond(L)), and a
+  // filtered block has a large cond(L); the projected problem is then solved in the
+  // generalised form with this well-conditioned Gram (S2 = L2 L2^T, C = L2^{-1} Hp L2^{-T},
+  // Ritz coefficients L2^{-T} Q) instead of taking the basis as exactly orthonormal. One more
+  // Gram product of the split already made for Hp; FP64 mode keeps the standard form.
+  const bool reproject = is_mixed(prec);
+  if (reproject) {
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+    if (tcd)
+      tc_gram(s->tx, nullptr, S, N, true, s->tcw, st);
+    else
+      gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+    symmetrize_lower(S, N, st);
+    rc = cholesky_lower(S, N, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("Gram matrix of the orthonormalised basis is not positive definite");
+      return rc;
+    }
+    trtri_lower(S, N, st);
+    gemm_f64('N', 'N', N, N, N, 1.0, S, N, Hp, N, 0.0, T1, N, CHEFSI_PREC_FP64, st);
+    gemm_f64('N', 'T', N, N, N, 1.0, T1, N, S, N, 0.0, Hp, N, CHEFSI_PREC_FP64, st);
+    symmetrize_lower(Hp, N, st);
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  // the top n_fr eigenpairs of the standard problem (eigenpairs_hermitian_by_index (Noc, N-1))
+  rc = syevd_range(Hp, N, n_occ, nfr, w, Z, st);
+  if (rc != CHEFSI_OK) return rc;
+  const double* R = Z;   // Ritz coefficients [N][n_fr]
+  if (reproject) {
+    gemm_f64('T', 'N', N, nfr, N, 1.0, S, N, Z, nfr, 0.0, W, nfr, CHEFSI_PREC_FP64, st);
+    R = W;
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  // XFrac = X Q_fr (subspaceRotationSpectrumSplitScalapack); H XFrac = (H X) Q_fr
+  double* HXF = want_hxf ? s->HXF.ensure((size_t)M * nfr) : nullptr;
+  if (tcd) {
+    tc_split_rows<double>(X, ld, M, N, s->tx, st);
+    tc_rotate(s->tx, R, nfr, nfr, XF, ldf, s->tcw, st);
+    if (want_hxf) {
+      if (hx32)
+        tc_split_rows<float>(y32, N, M, N, s->th, st);
+      else
+        tc_split_rows<double>(HX, N, M, N, s->th, st);
+      tc_rotate(s->th, R, nfr, nfr, HXF, nfr, s->tcw, st);
+    }
+    rc = tc_dense_check_error(s->tcw, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("tensor-core spectrum-split rotation: a bounded device wait expired");
+      return rc;
+    }
+  } else {
+    gemm_f64('N', 'N', M, nfr, N, 1.0, X, ld, R, nfr, 0.0, XF, ldf, prec, st);
+    if (want_hxf) gemm_f64('N', 'N', M, nfr, N, 1.0, HX, N, R, nfr, 0.0, HXF, nfr, prec, st);
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  return CHEFSI_OK;
+}
+
 // X[M][N] <- X W for complex blocks (row blocks through a temporary)
 void rotate_rows_c(chefsi_solver_s* s, cplx* X, int64_t ld, int64_t M, int N, const cplx* W,
                    cudaStream_t st) {
@@ -624,6 +790,7 @@ chefsi_params default_params() {
   p.first_scf_degree_scale = 1.34;
   p.keep_hx = 1;
   p.rr_precision = CHEFSI_PREC_FP64;
+  p.ss_frac_reduced = 0;
   return p;
 }
 
@@ -939,6 +1106,32 @@ int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, dou
   CHEFSI_API_END
 }
 
+int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld, int32_t N,
+                                        int32_t n_occ, void* XFrac, int64_t ld_frac,
+                                        double* eig_host, void* HXFrac_out, int32_t precision,
+                                        int32_t frac_reduced, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op && X && XFrac && eig_host && N >= 1 && ld >= N, "bad argument");
+  CHEFSI_REQUIRE(n_occ >= 0 && n_occ < N, "need 0 <= n_occ < N");
+  CHEFSI_REQUIRE(ld_frac >= N - n_occ, "ld_frac below N - n_occ");
+  CHEFSI_REQUIRE(!op->is_complex, "spectrum-split Rayleigh-Ritz: real operators only");
+  cudaStream_t st = as_stream(stream);
+  chefsi_solver_s s;
+  s.p = default_params();
+  s.p.rr_precision = precision == CHEFSI_PREC_MIXED ? CHEFSI_PREC_FP32_TC : CHEFSI_PREC_FP64;
+  s.p.ss_frac_reduced = frac_reduced;
+  const int nfr = N - n_occ;
+  int rc = rayleigh_ritz_ss_real(&s, op, (double*)X, ld, N, n_occ, (double*)XFrac, ld_frac,
+                                 precision, HXFrac_out != nullptr, st);
+  if (rc != CHEFSI_OK) return rc;
+  if (HXFrac_out)
+    CHEFSI_CUDA(cudaMemcpyAsync(HXFrac_out, s.HXF.ptr, sizeof(double) * op->n_dofs * nfr,
+                                cudaMemcpyDeviceToDevice, st));
+  CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
 int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,
                  double* y, int64_t ldy, void* stream) {
   CHEFSI_API_BEGIN
@@ -1168,6 +1361,42 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
   filter_all(s, op, X, N, m, s->p.precision, st);
   const int rc = solve_after_filter(s, op, X, N, eig_host, res_host, compute_residual, st);
   if (rc != CHEFSI_OK) return rc;
+  CHEFSI_API_END
+}
+
+// One CheFSI iteration with the spectrum-split Rayleigh-Ritz step: the solve() branch taken
+// when fewer eigenvalues than vectors are wanted
+// (chebyshevOrthogonalizedSubspaceIterationSolverDevice.cc:584-605, residuals of the
+// fractional vectors at :675-690).
+int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, int32_t N,
+                                int32_t n_occ, void* XFrac, double* eig_host, double* res_host,
+                                int32_t compute_residual, int32_t is_first_scf, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(s && op && X && XFrac && eig_host && N >= 1, "bad argument");
+  CHEFSI_REQUIRE(n_occ >= 0 && n_occ < N, "need 0 <= n_occ < N");
+  CHEFSI_REQUIRE(!op->is_complex, "spectrum-split Rayleigh-Ritz: real operators only");
+  CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
+  cudaStream_t st = as_stream(stream);
+  const int m = degree_for(s, is_first_scf);
+  s->last_degree = m;
+  const int nfr = N - n_occ;
+  const int64_t M = op->n_dofs;
+  CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
+  filter_all(s, op, X, N, m, s->p.precision, st);
+  int rc = rayleigh_ritz_ss_real(s, op, (double*)X, N, N, n_occ, (double*)XFrac, nfr,
+                                 s->p.precision, compute_residual != 0, st);
+  if (rc != CHEFSI_OK) return rc;
+  double* res = s->resid.ensure(nfr);
+  if (compute_residual)
+    residual_norms_f64((const double*)XFrac, nfr, s->HXF.ptr, nfr, M, nfr, s->evals.ptr, res, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[6], st));
+  CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s->evals.ptr, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));
+  if (compute_residual && res_host)
+    CHEFSI_CUDA(cudaMemcpyAsync(res_host, res, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < 6; ++i) s->times[i] = elapsed(s->ev[i], s->ev[i + 1]);
+  s->times[6] = elapsed(s->ev[0], s->ev[6]);
+  s->hx_collect();
   CHEFSI_API_END
 }
 

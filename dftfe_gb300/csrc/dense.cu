@@ -842,10 +842,13 @@ __device__ int sturm_count(const double* d, const double* e, int n, double x, do
 // lanes evaluate Sturm counts at 32 interior points of the current interval, which then
 // shrinks to the sub-interval holding eigenvalue idx (a factor 33 per step, ~11 steps to
 // full precision instead of ~55 bisection steps; every Sturm count is an FP64-division chain).
-__global__ void k_bisect_warp(const double* d, const double* e, int n, double* w) {
-  const int idx = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+// Eigenvalues idx0 .. idx0+count-1 (ascending) go to w[0 .. count).
+__global__ void k_bisect_warp(const double* d, const double* e, int n, int idx0, int count,
+                              double* w) {
+  const int sub = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (idx >= n) return;  // uniform within the warp
+  if (sub >= count) return;  // uniform within the warp
+  const int idx = idx0 + sub;
   double lo = 1e300, hi = -1e300, emax = 0.0;
   for (int j = lane; j < n; j += 32) {
     const double r = (j > 0 ? fabs(e[j - 1]) : 0.0) + (j < n - 1 ? fabs(e[j]) : 0.0);
@@ -873,7 +876,7 @@ __global__ void k_bisect_warp(const double* d, const double* e, int n, double* w
     lo = nlo;
     hi = nhi;
   }
-  if (lane == 0) w[idx] = 0.5 * (lo + hi);
+  if (lane == 0) w[sub] = 0.5 * (lo + hi);
 }
 
 // Inverse iteration for the eigenvectors of the tridiagonal (d, e): Gaussian elimination with
@@ -881,16 +884,20 @@ __global__ void k_bisect_warp(const double* d, const double* e, int n, double* w
 // second super-diagonal where rows were swapped), five iterations from a deterministic start
 // vector, modified Gram-Schmidt against earlier members of the same cluster (eigenvalues
 // closer than ortol). One thread owns a whole cluster. Workspace per vector: 5n doubles.
+// w holds count eigenvalues (ascending), eigenvalues idx0 .. idx0+count-1 of the whole
+// tridiagonal; their vectors go to columns 0 .. count-1 of Z. The start vector depends on the
+// global index, so a subset reproduces the columns of the full solve outside clusters that
+// straddle the subset's edge.
 __global__ void k_inverse_iteration(const double* d, const double* e,
-                                    int n, const double* w, double* Z,
+                                    int n, const double* w, int count, int idx0, double* Z,
                                     int ldz, double* work, unsigned char* swaps,
                                     double ortol) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n) return;
+  if (idx >= count) return;
   // only the first member of a cluster works; it handles the whole cluster sequentially
   if (idx > 0 && w[idx] - w[idx - 1] <= ortol) return;
   int last = idx;
-  while (last + 1 < n && w[last + 1] - w[last] <= ortol) ++last;
+  while (last + 1 < count && w[last + 1] - w[last] <= ortol) ++last;
   double tnorm = 0.0;
   for (int j = 0; j < n; ++j)
     tnorm = fmax(tnorm, fabs(d[j]) + (j > 0 ? fabs(e[j - 1]) : 0.0) + (j < n - 1 ? fabs(e[j]) : 0.0));
@@ -933,7 +940,7 @@ __global__ void k_inverse_iteration(const double* d, const double* e,
     }
     if (a[n - 1] == 0.0) a[n - 1] = tiny;
     // deterministic start vector
-    unsigned int s = 2654435761u * (unsigned)(t + 1);
+    unsigned int s = 2654435761u * (unsigned)(idx0 + t + 1);
     for (int j = 0; j < n; ++j) {
       s = s * 1664525u + 1013904223u;
       x[j] = ((double)(s >> 8) / 16777216.0) - 0.5 + 1e-3;
@@ -1190,13 +1197,15 @@ __global__ void k_transpose_sq(const double* A, double* B, int N) {
 }
 
 // Z <- H_0 H_1 ... H_{N-3} Z with the reflectors in rows of V (V[k][k+1:N], tau[k]), applied
-// as compact-WY blocks of kWY reflectors, last block first: Z -= Vb (T (Vb^T Z)).
+// as compact-WY blocks of kWY reflectors, last block first: Z -= Vb (T (Vb^T Z)). Z is N x
+// ncols (row-major, ld ncols): all eigenvectors, or the subset of a partial solve.
 constexpr int kWY = 64;
-static void back_transform_wy(const double* V, const double* tau, int N, double* Z, cudaStream_t st) {
+static void back_transform_wy(const double* V, const double* tau, int N, double* Z, int ncols,
+                              cudaStream_t st) {
   const int nrefl = N - 2;
   if (nrefl <= 0) return;
   DeviceBuffer<double> Vc((size_t)N * N), G((size_t)kWY * kWY), T((size_t)kWY * kWY),
-      W1((size_t)kWY * N), W2((size_t)kWY * N);
+      W1((size_t)kWY * ncols), W2((size_t)kWY * ncols);
   // Vc[i][k] = V[k][i]: block k0.. of reflectors is the row-major N x nb slice Vc + k0
   k_transpose_sq<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(V, Vc.ptr, N);
   CHEFSI_CHECK_LAUNCH();
@@ -1207,15 +1216,23 @@ static void back_transform_wy(const double* V, const double* tau, int N, double*
     gemm_f64('T', 'N', nb, nb, N, 1.0, Vb, N, Vb, N, 0.0, G.ptr, nb, CHEFSI_PREC_FP64, st);
     k_build_t<<<1, kWY, 0, st>>>(G.ptr, tau + k0, nb, T.ptr);
     CHEFSI_CHECK_LAUNCH();
-    gemm_f64('T', 'N', nb, N, N, 1.0, Vb, N, Z, N, 0.0, W1.ptr, N, CHEFSI_PREC_FP64, st);  // Vb^T Z
-    gemm_f64('N', 'N', nb, N, nb, 1.0, T.ptr, nb, W1.ptr, N, 0.0, W2.ptr, N,
-             CHEFSI_PREC_FP64, st);                                                   // T (Vb^T Z)
-    gemm_f64('N', 'N', N, N, nb, -1.0, Vb, N, W2.ptr, N, 1.0, Z, N, CHEFSI_PREC_FP64, st);
+    gemm_f64('T', 'N', nb, ncols, N, 1.0, Vb, N, Z, ncols, 0.0, W1.ptr, ncols, CHEFSI_PREC_FP64,
+             st);                                                                       // Vb^T Z
+    gemm_f64('N', 'N', nb, ncols, nb, 1.0, T.ptr, nb, W1.ptr, ncols, 0.0, W2.ptr, ncols,
+             CHEFSI_PREC_FP64, st);                                                // T (Vb^T Z)
+    gemm_f64('N', 'N', N, ncols, nb, -1.0, Vb, N, W2.ptr, ncols, 1.0, Z, ncols, CHEFSI_PREC_FP64,
+             st);
   }
 }
 
-int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
+// Eigenpairs il .. il+count-1 (ascending order) of the symmetric row-major A (destroyed):
+// tridiagonalisation, multisection for the wanted eigenvalues only, inverse iteration for
+// their vectors, back-transformation of count columns. w[count], Z[N][count].
+// count == N is the full solve (syevd); a partial solve is the eigenpairs_hermitian_by_index
+// step of the spectrum-split Rayleigh-Ritz (the top N - Noc pairs).
+int syevd_range(double* A, int N, int il, int count, double* w, double* Z, cudaStream_t st) {
   CHEFSI_REQUIRE(N >= 1, "syevd: N must be positive");
+  CHEFSI_REQUIRE(il >= 0 && count >= 1 && il + count <= N, "syevd: eigenpair range out of bounds");
   DeviceBuffer<double> V((size_t)N * N), tau(N), d(N), e(N), p(N);
   CHEFSI_CUDA(cudaMemsetAsync(V.ptr, 0, sizeof(double) * N * N, st));
   CHEFSI_CUDA(cudaMemsetAsync(tau.ptr, 0, sizeof(double) * N, st));
@@ -1223,7 +1240,7 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
   tridiagonalise(A, N, V.ptr, tau.ptr, d.ptr, e.ptr, p.ptr, st);
   k_tail<<<1, 32, 0, st>>>(A, N, d.ptr, e.ptr);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d.ptr, e.ptr, N, w);
+  k_bisect_warp<<<(count + 3) / 4, 128, 0, st>>>(d.ptr, e.ptr, N, il, count, w);
   CHEFSI_CHECK_LAUNCH();
   // cluster tolerance relative to the tridiagonal's scale
   std::vector<double> hd(N), he(N);
@@ -1235,14 +1252,18 @@ int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
     tn = std::max(tn, std::fabs(hd[j]) + (j > 0 ? std::fabs(he[j - 1]) : 0.0) +
                           (j < N - 1 ? std::fabs(he[j]) : 0.0));
   const double ortol = 1e-5 * std::max(tn, 1e-300);
-  DeviceBuffer<double> work((size_t)N * 5 * N);
-  DeviceBuffer<unsigned char> swaps((size_t)N * N);
-  k_inverse_iteration<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, e.ptr, N, w, Z, N, work.ptr, swaps.ptr,
-                                                    ortol);
+  DeviceBuffer<double> work((size_t)count * 5 * N);
+  DeviceBuffer<unsigned char> swaps((size_t)count * N);
+  k_inverse_iteration<<<(count + 31) / 32, 32, 0, st>>>(d.ptr, e.ptr, N, w, count, il, Z, count,
+                                                        work.ptr, swaps.ptr, ortol);
   CHEFSI_CHECK_LAUNCH();
-  back_transform_wy(V.ptr, tau.ptr, N, Z, st);
+  back_transform_wy(V.ptr, tau.ptr, N, Z, count, st);
   CHEFSI_CUDA(cudaStreamSynchronize(st));
   return CHEFSI_OK;
+}
+
+int syevd(double* A, int N, double* w, double* Z, cudaStream_t st) {
+  return syevd_range(A, N, 0, N, w, Z, st);
 }
 
 // ======================================================================= residuals, dots

@@ -351,7 +351,7 @@ int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
   CHEFSI_CHECK_LAUNCH();
   k_tridiag_phases<<<1, 32, 0, st>>>(e.ptr, N, er.ptr, phi.ptr);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d.ptr, er.ptr, N, w);
+  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d.ptr, er.ptr, N, 0, N, w);
   CHEFSI_CHECK_LAUNCH();
   std::vector<double> hd(N), he(N);
   CHEFSI_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
@@ -364,7 +364,7 @@ int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
   const double ortol = 1e-5 * std::max(tn, 1e-300);
   DeviceBuffer<double> work((size_t)N * 5 * N);
   DeviceBuffer<unsigned char> swaps((size_t)N * N);
-  k_inverse_iteration<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, er.ptr, N, w, Zr.ptr, N, work.ptr,
+  k_inverse_iteration<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, er.ptr, N, w, N, 0, Zr.ptr, N, work.ptr,
                                                     swaps.ptr, ortol);
   CHEFSI_CHECK_LAUNCH();
   k_phase_rows<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(Zr.ptr, phi.ptr, N, Z);

@@ -235,6 +235,7 @@ void trtri_lower(double* L, int N, cudaStream_t st);
 // symmetric eigensolve (Householder tridiagonalisation, bisection, inverse iteration,
 // back-transformation); A overwritten; eigenvalues ascending in w; vectors in columns of Z.
 int syevd(double* A, int N, double* w, double* Z, cudaStream_t st);
+int syevd_range(double* A, int N, int il, int count, double* w, double* Z, cudaStream_t st);
 // complex Hermitian counterparts (dense_c.cu)
 int cholesky_lower_c(cplx* A, int N, cudaStream_t st);
 void trtri_lower_c(cplx* L, int N, cudaStream_t st);
@@ -273,10 +274,11 @@ __global__ void k_hh_symv(const double* A, int N, int k, const double* V, const 
 __global__ void k_hh_w(int N, int k, const double* V, const double* tau, double* p);
 __global__ void k_hh_rank2(double* A, int N, int k, const double* V, const double* w);
 __global__ void k_tail(const double* A, int N, double* d, double* e);
-__global__ void k_bisect_warp(const double* d, const double* e, int n, double* w);
+__global__ void k_bisect_warp(const double* d, const double* e, int n, int idx0, int count,
+                              double* w);
 __global__ void k_inverse_iteration(const double* d, const double* e, int n, const double* w,
-                                    double* Z, int ldz, double* work, unsigned char* swaps,
-                                    double ortol);
+                                    int count, int idx0, double* Z, int ldz, double* work,
+                                    unsigned char* swaps, double ortol);
 __global__ void k_bt_dot(const double* V, int N, int k, const double* Z, double* r);
 __global__ void k_bt_update(const double* V, int N, int k, const double* tau, double* Z,
                             const double* r);

@@ -100,14 +100,14 @@ int syevd_noalloc(double* A, int N, double* w, double* Z, cudaStream_t st) {
   }
   k_tail<<<1, 32, 0, st>>>(A, N, d, e);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d, e, N, w);
+  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d, e, N, 0, N, w);
   CHEFSI_CHECK_LAUNCH();
   k_cluster_tol<<<1, 32, 0, st>>>(d, e, N, tol);
   CHEFSI_CHECK_LAUNCH();
   double ortol = 0.0;
   CHEFSI_CUDA(cudaMemcpyAsync(&ortol, tol, sizeof(double), cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
-  k_inverse_iteration<<<(N + 63) / 64, 64, 0, st>>>(d, e, N, w, Z, N, work, swaps, ortol);
+  k_inverse_iteration<<<(N + 63) / 64, 64, 0, st>>>(d, e, N, w, N, 0, Z, N, work, swaps, ortol);
   CHEFSI_CHECK_LAUNCH();
   for (int k = N - 3; k >= 0; --k) {
     k_bt_dot<<<(N + 127) / 128, 128, 0, st>>>(V, N, k, Z, p);

@@ -26,6 +26,11 @@
  *                    pseudoGramSchmidtOrthogonalization (src/linAlg/pseudoGSDevice.cc:82-463)
  *   chefsi_rayleigh_ritz
  *                    rayleighRitzGEP (src/linAlg/rayleighRitzDevice.cc:356-819)
+ *   chefsi_rayleigh_ritz_spectrum_split / chefsi_solve_spectrum_split
+ *                    rayleighRitzGEPSpectrumSplitDirect
+ *                    (include/linearAlgebraOperationsDevice.h:279-298,
+ *                    src/linAlg/rayleighRitzDevice.cc:822-1455) and the solve() branch that
+ *                    calls it (chebyshevOrthogonalizedSubspaceIterationSolverDevice.cc:584-690)
  *   chefsi_residual_norms
  *                    computeEigenResidualNorm (src/linAlg/linearAlgebraOperationsDevice.cc:4611-)
  *   chefsi_solver_create / _reinit_spectrum_bounds / chefsi_solve / chefsi_solve_no_rr
@@ -132,6 +137,11 @@ typedef struct {
                                    three-term FP16 split: FP32 operands exactly, FP32
                                    accumulation) or CHEFSI_PREC_MIXED (the filter's two-term
                                    split) */
+  int32_t ss_frac_reduced;      /* spectrum-split Rayleigh-Ritz in mixed mode: 0 (default)
+                                   recomputes the block of X^T H X that couples the
+                                   fractionally occupied states from an FP64 H X (the
+                                   precision map of useMixedPrecXTHXSpectrumSplit); 1 keeps
+                                   the rr_precision H X there too */
 } chefsi_params;
 
 const char* chefsi_last_error(void);
@@ -202,6 +212,19 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
    W_out is non-null it receives the N x N coefficient matrix W = L^{-T} Q (X_rot = X W). */
 int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
                          double* HX_out, double* W_out, int32_t precision, void* stream);
+
+/* Spectrum-split Rayleigh-Ritz (real operators). X ([n_dofs][N], ld) is orthonormalised in
+   place by Cholesky-GS (X <- X L^{-T}, X^T X = L L^T) and stays in that basis; the projected
+   Hamiltonian X^T H X of the orthonormal X is diagonalised for its top n_fr = N - n_occ
+   eigenpairs only, and XFrac ([n_dofs][n_fr], ld_frac) = X Q_fr. eig_host receives the n_fr
+   eigenvalues in ascending order; HXFrac_out, if non-null, H XFrac ([n_dofs][n_fr] FP64).
+   precision MIXED: tensor-core Gram and rotation products, the three-term tensor-core H X
+   for the occupied column blocks and, unless frac_reduced, an FP64 H X and Gram product for
+   the block that couples the fractional states. */
+int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld, int32_t N,
+                                        int32_t n_occ, void* XFrac, int64_t ld_frac,
+                                        double* eig_host, void* HXFrac_out, int32_t precision,
+                                        int32_t frac_reduced, void* stream);
 
 /* y = a x + b y on [rows][n_vec] FP64 device blocks (leading dimensions ldx, ldy). */
 int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,
@@ -288,6 +311,15 @@ int chefsi_solver_hx_stats(chefsi_solver s, int32_t* launches, double* total_ms)
 int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double* eig_host,
                  double* res_host, int32_t compute_residual, int32_t is_first_scf,
                  void* stream);
+
+/* One CheFSI iteration whose Rayleigh-Ritz step is the spectrum-split one (the solve()
+   branch taken when N - n_occ < N eigenvalues are wanted): filter all N vectors of X, then
+   X <- orthonormalised X, XFrac ([n_dofs][N - n_occ], ld N - n_occ, device) = X Q_fr.
+   eig_host / res_host receive the N - n_occ eigenvalues and the residual norms of the
+   XFrac columns (H XFrac - lambda XFrac, with H XFrac = (H X) Q_fr). Real operators. */
+int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, int32_t N,
+                                int32_t n_occ, void* XFrac, double* eig_host, double* res_host,
+                                int32_t compute_residual, int32_t is_first_scf, void* stream);
 
 /* One CheFSI iteration on each of count independent problems (the k-point / spin loop of
    dftClass::kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:507-655, which calls

@@ -255,6 +255,25 @@ def rayleigh_ritz_gep(op: OracleOperator, X: np.ndarray):
     return ev, X @ W, HX @ W
 
 
+def rayleigh_ritz_spectrum_split(op: OracleOperator, X: np.ndarray, n_occ: int):
+    """Spectrum-split RR (rayleighRitzGEPSpectrumSplitDirect, rayleighRitzDevice.cc:822-1455).
+
+    S = X^T X = L L^T and X <- X L^{-T} (:870-1115); Hp = X^T H X with the lower triangle
+    mirrored (:1183-1279); the top N - n_occ eigenpairs of Hp (by index (Noc, N-1), :1370-1407);
+    XFrac = X Q_fr (:1425-1439). Returns (eigenvalues, orthonormalised X, XFrac, H XFrac).
+    """
+    Xc = X.conj() if op.is_complex else X
+    L = np.linalg.cholesky(Xc.T @ X)
+    Xo = X @ np.tril(np.linalg.inv(L)).conj().T
+    HX = op.HX(Xo)
+    Hp = (Xo.conj() if op.is_complex else Xo).T @ HX
+    Hl = np.tril(Hp)
+    Hp = Hl + np.tril(Hl, -1).conj().T
+    ev, Q = np.linalg.eigh(Hp, UPLO='L')
+    Qf = Q[:, n_occ:]
+    return ev[n_occ:], Xo, Xo @ Qf, HX @ Qf
+
+
 @dataclass
 class SolverState:
     a0: float

@@ -184,3 +184,17 @@ def test_oracle_density_of_a_constant_state():
     assert np.abs(rho - occ.sum()).max() < 1e-12
     rho_w = orc.density(pr.cell_map, pr.inv_sqrt_mass, N, X, occ, jxw)
     assert abs(rho_w.sum() - occ.sum() * 4.0 ** 3) < 1e-9
+
+
+def test_oracle_spectrum_split_is_the_top_of_the_full_rayleigh_ritz():
+    """The spectrum-split RR returns the top N - Noc Ritz pairs of the generalised RR on the
+    same X: equal eigenvalues, XFrac spanning the top rotated vectors, X left orthonormal."""
+    pr = small_problem(projectors=True)
+    ora = oracle_op(pr)
+    X = np.random.default_rng(9).standard_normal((pr.n_dofs, 20))
+    ev, Xr, HXr = orc.rayleigh_ritz_gep(ora, X)
+    ev_s, Xo, XF, HXF = orc.rayleigh_ritz_spectrum_split(ora, X, 14)
+    assert np.abs(ev_s - ev[14:]).max() < 1e-11 * np.abs(ev).max()
+    assert np.abs(Xo.T @ Xo - np.eye(20)).max() < 1e-12
+    assert np.abs(XF @ XF.T - Xr[:, 14:] @ Xr[:, 14:].T).max() < 1e-10
+    assert np.abs(HXF - dense_operator(pr) @ XF).max() < 1e-10 * np.abs(ev).max()
