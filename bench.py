@@ -463,6 +463,60 @@ def run_spectrum_split_check(args):
     return 0
 
 
+def run_dm_response_check(args):
+    """First-order density-matrix response (densityMatrixEigenBasisFirstOrderResponse) on the
+    workload: the Ritz vectors of three mixed CheFSI iterations from X0, their Ritz values, the
+    Fermi energy between the occupied states and the next, T = 500 K. H' applies dense cell
+    matrices of the workload's shape (the workload's own local cell matrices, without the
+    nonlocal part: the cost of a first-order potential operator). FP64 and mixed timed with
+    CUDA events (one warm-up call each); the mixed X P' is compared with the FP64 one."""
+    import torch
+    from dftfe_gb300 import build, chefsi
+    build.build()
+    pr = build_workload(args.workload, args.seed)
+    N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
+    op = chefsi.KohnShamOperator.from_problem(pr)
+    op_prime = chefsi.KohnShamOperator(pr.cell_map, pr.cell_mats, pr.sqrt_mass,
+                                       pr.inv_sqrt_mass, pr.n_dofs)
+    lo, blow, up = first_bounds(chefsi, op, N)
+    s = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
+        chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=min(N, 512), mixed_precision="mixed",
+        rr_precision=args.rr_precision))
+    s.reinitSpectrumBounds(lo, blow, up)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 1)
+    X = torch.rand((M, N), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    for _ in range(3):
+        ev, _ = s.solve(op, X, useMixedPrec=True)
+        s.reinitSpectrumBounds(ev[0], ev[-1], up)
+    nocc = pr.n_occupied
+    mu = 0.5 * (ev[nocc - 1] + ev[nocc])
+    res = {}
+    for prec in ("fp64", "mixed"):
+        Xc = X.clone()
+        chefsi.densityMatrixEigenBasisFirstOrderResponse(op_prime, Xc, ev, mu, 500.0,
+                                                         precision=prec)
+        Xc.copy_(X)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dmu = chefsi.densityMatrixEigenBasisFirstOrderResponse(op_prime, Xc, ev, mu, 500.0,
+                                                               precision=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        res[prec] = (Xc, e0.elapsed_time(e1), dmu)
+    err = float((res["mixed"][0] - res["fp64"][0]).abs().max() / res["fp64"][0].abs().max())
+    print(json.dumps({
+        "metric": "first-order density-matrix response (X^T H' X, recursive Fermi-operator "
+                  "expansion, X <- X P')", "workload": args.workload, "n_dofs": M, "n_wfc": N,
+        "fermi_energy": mu, "temperature_K": 500.0, "fp64_ms": res["fp64"][1],
+        "mixed_ms": res["mixed"][1], "speedup_mixed_vs_fp64": res["fp64"][1] / res["mixed"][1],
+        "mixed_max_rel_err_vs_fp64": err,
+        "dmu_max_rel_diff": float(np.abs(res["mixed"][2] - res["fp64"][2]).max()
+                                  / np.abs(res["fp64"][2]).max())}))
+    return 0
+
+
 def run_density_check(args):
     """Density of the Ritz vectors at the quadrature points (chefsi_density, densityCalculator)
     on the mixed workload: 1024 vectors with occupations 2 for the lowest 512, the (p+3)^3 Gauss
@@ -687,6 +741,8 @@ def main():
                     help="time chefsi_density on the workload and check 16 cells against a direct sum")
     ap.add_argument("--spectrum-split-check", action="store_true",
                     help="full vs spectrum-split RR iteration; split RR in FP64 vs mixed")
+    ap.add_argument("--dm-response-check", action="store_true",
+                    help="time the first-order density-matrix response in FP64 and mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -703,6 +759,8 @@ def main():
         return run_density_check(args)
     if args.spectrum_split_check:
         return run_spectrum_split_check(args)
+    if args.dm_response_check:
+        return run_dm_response_check(args)
     if args.ritz_check:
         return run_ritz_check(args)
     return run_ours(args)

@@ -32,7 +32,8 @@ EXPORTS = [
     "chefsi_operator_info", "chefsi_hx", "chefsi_overlap", "chefsi_xthx",
     "chefsi_chebyshev_filter", "chefsi_lanczos_bounds", "chefsi_syevd", "chefsi_heevd", "chefsi_syevd_noalloc",
     "chefsi_cholesky_gs",
-    "chefsi_rayleigh_ritz", "chefsi_rayleigh_ritz_spectrum_split", "chefsi_residual_norms",
+    "chefsi_rayleigh_ritz", "chefsi_rayleigh_ritz_spectrum_split",
+    "chefsi_density_matrix_first_order_response", "chefsi_residual_norms",
     "chefsi_solver_create",
     "chefsi_solver_destroy", "chefsi_solver_reinit_spectrum_bounds", "chefsi_solver_get_bounds",
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
@@ -124,6 +125,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solver_timings": ([vp, vp], ctypes.c_int),
         "chefsi_solver_set_profiling": ([vp, i32], ctypes.c_int),
         "chefsi_solver_hx_stats": ([vp, vp, vp], ctypes.c_int),
+        "chefsi_density_matrix_first_order_response": ([vp, vp, i64, i32, vp, f64, f64, vp, i32,
+                                                        vp], ctypes.c_int),
         "chefsi_solve": ([vp, vp, vp, i32, vp, vp, i32, i32, vp], ctypes.c_int),
         "chefsi_solve_spectrum_split": ([vp, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp],
                                         ctypes.c_int),

@@ -237,6 +237,24 @@ def rayleighRitzGEPSpectrumSplitDirect(op: KohnShamOperator, X: torch.Tensor, XF
     return (ev, HXF) if want_hx else ev
 
 
+def densityMatrixEigenBasisFirstOrderResponse(opPrime: KohnShamOperator, X: torch.Tensor,
+                                              eigenValues, fermiEnergy: float, TVal: float,
+                                              precision="fp64") -> np.ndarray:
+    """First-order density-matrix response (linearAlgebraOperationsDevice.h:302-322): X
+    [n_dofs, N] (orthonormal eigenvectors) becomes X P' in place, P' the first-order response
+    of the recursive Fermi-operator expansion to the perturbation opPrime applies; returns
+    densityMatDerFermiEnergy (N values)."""
+    N = X.shape[1]
+    ev = np.ascontiguousarray(eigenValues, dtype=np.float64)
+    if ev.shape != (N,):
+        raise ValueError("eigenValues must have N entries")
+    dmu = np.zeros(N)
+    check(_lib.load().chefsi_density_matrix_first_order_response(
+        opPrime.handle, _ptr(X), X.stride(0), N, _np_ptr(ev), float(fermiEnergy), float(TVal),
+        _np_ptr(dmu), _prec(precision), _stream()))
+    return dmu
+
+
 def gemm(A: torch.Tensor, B: torch.Tensor, ta: str = "N", tb: str = "N", alpha: float = 1.0,
          beta: float = 0.0, C: torch.Tensor | None = None, precision="fp64") -> torch.Tensor:
     """C = alpha op(A) op(B) + beta C on the GPU (row-major FP64)."""

@@ -610,6 +610,132 @@ int rayleigh_ritz_ss_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, 
   return CHEFSI_OK;
 }
 
+// ---------------------------------------------------------------- density-matrix response
+// First-order response of the density matrix in the eigenbasis
+// (densityMatrixEigenBasisFirstOrderResponse, src/linAlg/rayleighRitzDevice.cc:1455-1721).
+// The recursive Fermi-operator expansion X_{k+1} = Y_k X_k^2, Y_k = (2 X_k (X_k - 1) + 1)^{-1},
+// from X_0 = 1/2 - c (H - mu), c = 2^{-2-m} beta, is diagonal in the eigenbasis; its first-order
+// part P (from P_0 = -c H') obeys, entry by entry, with i the row and j the column,
+//   T = P X0_i + P X0_j;  P <- (Y0_i T - 2 (T X0'_j) Y0_i) + 2 (P X0'_j) Y0_i
+// (X0' the updated diagonal): the reference's sequence of row / column scalings of dense
+// matrices, which here is one pass over the entries of the lower triangle (row >= column)
+// with the diagonal sequences precomputed; the upper triangle is its mirror.
+constexpr int kDmforSteps = 10;
+
+// X0[k][i] (k = 0..m), Y0[k][i] (k = 0..m-1); dmu[i] = beta X0_m (1 - X0_m). Every operation
+// is an explicitly rounded one (no FMA contraction), in the reference's order: near the
+// occupied end 1 - X0 is a difference of nearly equal numbers and carries the rounding of
+// every step into densityMatDerFermiEnergy.
+__global__ void k_dmfor_diag(const double* __restrict__ eig, int N, double mu, double beta,
+                             double c, double* __restrict__ X0, double* __restrict__ Y0,
+                             double* __restrict__ dmu) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double x = __dsub_rn(0.5, __dmul_rn(c, __dsub_rn(eig[i], mu)));
+  X0[i] = x;
+  for (int k = 0; k < kDmforSteps; ++k) {
+    const double y =
+        __ddiv_rn(1.0, __dadd_rn(__dmul_rn(__dmul_rn(2.0, x), __dsub_rn(x, 1.0)), 1.0));
+    x = __dmul_rn(__dmul_rn(y, x), x);
+    Y0[(int64_t)k * N + i] = y;
+    X0[(int64_t)(k + 1) * N + i] = x;
+  }
+  dmu[i] = __dmul_rn(__dmul_rn(beta, x), __dsub_rn(1.0, x));
+}
+
+// P[i][j] <- first-order density-matrix response from Hp[i][j] (full symmetric input;
+// the entry of row max(i, j), column min(i, j) is computed and written to both places)
+__global__ void k_dmfor_apply(double* __restrict__ P, int N, double c,
+                              const double* __restrict__ X0, const double* __restrict__ Y0) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (j > i) continue;  // row i >= column j
+    double p = __dmul_rn(-c, P[t]);
+    for (int k = 0; k < kDmforSteps; ++k) {
+      const double xi = X0[(int64_t)k * N + i], xj = X0[(int64_t)k * N + j];
+      const double y = Y0[(int64_t)k * N + i];
+      const double xn = X0[(int64_t)(k + 1) * N + j];
+      const double T = __dadd_rn(__dmul_rn(p, xi), __dmul_rn(p, xj));
+      const double a = __dsub_rn(__dmul_rn(T, y), __dmul_rn(2.0, __dmul_rn(__dmul_rn(T, xn), y)));
+      p = __dadd_rn(a, __dmul_rn(2.0, __dmul_rn(__dmul_rn(p, xn), y)));
+    }
+    P[t] = p;
+    P[(int64_t)j * N + i] = p;
+  }
+}
+
+// Hp' = X^T H' X (lower triangle mirrored), P' by the recursion, X <- X P'. dmu (device, N)
+// receives densityMatDerFermiEnergy. Mixed: the three-term tensor-core H X, tensor-core Gram
+// and rotation (the reference's singlePrecLRD path runs every block of X^T H' X in FP32).
+int dm_first_order_response_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld,
+                                 int N, const double* eig, double mu, double beta, double* dmu,
+                                 int prec, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const bool tcd = prec == CHEFSI_PREC_MIXED && dense_tc_available();
+  double* Hp = s->Hp.ensure((size_t)N * N);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  const bool tc3 = is_mixed(prec) && tc_split_usable(op, N);
+  float* y32 = nullptr;
+  double* HX = nullptr;
+  if (is_mixed(prec)) {
+    float* x32 = s->Xb32.ensure((size_t)M * N);
+    y32 = s->Yb32.ensure((size_t)M * N);
+    double scale = 1.0;
+    if (tc3) {
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(X, ld, M, N, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, 14 - (int)std::ceil(std::log2(amax)));
+    }
+    copy_block<double, float>(X, ld, x32, N, M, N, scale, st);
+    if (!(tc3 && hx_tc3(op, x32, N, y32, N, N, 1.0 / scale, false, st)))
+      hx_f32(op, x32, N, y32, N, N, 1.0 / scale, false, st);
+    const int tc = tc_check_error(op, st);
+    if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
+    if (!tcd) {
+      HX = s->HX.ensure((size_t)M * N);
+      copy_block<float, double>(y32, N, HX, N, M, N, 1.0, st);
+    }
+  } else {
+    HX = s->HX.ensure((size_t)M * N);
+    hx_all_f64(op, X, ld, N, HX, s->p.wfc_block, st);
+  }
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
+  if (tcd) {
+    tc_exponents<double>(X, ld, M, N, s->tx, st);
+    tc_split_transposed<double>(X, ld, M, N, s->tx, st);
+    tc_exponents<float>(y32, N, M, N, s->th, st);
+    tc_split_transposed<float>(y32, N, M, N, s->th, st);
+    tc_gram(s->tx, &s->th, Hp, N, true, s->tcw, st);
+    const int rc = tc_dense_check_error(s->tcw, st);
+    if (rc != CHEFSI_OK) {
+      set_last_error("tensor-core Gram product: a bounded device wait expired");
+      return rc;
+    }
+  } else {
+    gram_f64(X, ld, HX, N, M, N, N, Hp, N, prec, true, st);
+  }
+  symmetrize_lower(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  const double c = std::ldexp(1.0, -2 - kDmforSteps) * beta;
+  double* X0 = s->T1.ensure((size_t)(2 * kDmforSteps + 1) * N);
+  double* Y0 = X0 + (size_t)(kDmforSteps + 1) * N;
+  k_dmfor_diag<<<(N + 127) / 128, 128, 0, st>>>(eig, N, mu, beta, c, X0, Y0, dmu);
+  CHEFSI_CHECK_LAUNCH();
+  k_dmfor_apply<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(Hp, N, c, X0, Y0);
+  CHEFSI_CHECK_LAUNCH();
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  // Y = X P' (P' symmetric: the reference rotates by its conjugate transpose)
+  rotate_rows(s, X, ld, M, N, Hp, prec, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  return CHEFSI_OK;
+}
+
 // X[M][N] <- X W for complex blocks (row blocks through a temporary)
 void rotate_rows_c(chefsi_solver_s* s, cplx* X, int64_t ld, int64_t M, int N, const cplx* W,
                    cudaStream_t st) {
@@ -1128,6 +1254,31 @@ int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld,
     CHEFSI_CUDA(cudaMemcpyAsync(HXFrac_out, s.HXF.ptr, sizeof(double) * op->n_dofs * nfr,
                                 cudaMemcpyDeviceToDevice, st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
+int chefsi_density_matrix_first_order_response(chefsi_operator op_prime, void* X, int64_t ld,
+                                               int32_t N, const double* eig_host,
+                                               double fermi_energy, double temperature,
+                                               double* dmu_host, int32_t precision,
+                                               void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(op_prime && X && eig_host && dmu_host && N >= 1 && ld >= N, "bad argument");
+  CHEFSI_REQUIRE(temperature > 0.0, "temperature must be positive (Kelvin)");
+  CHEFSI_REQUIRE(!op_prime->is_complex,
+                 "density-matrix first-order response: real operators only");
+  cudaStream_t st = as_stream(stream);
+  chefsi_solver_s s;
+  s.p = default_params();
+  DeviceBuffer<double> eig(N), dmu(N);
+  CHEFSI_CUDA(cudaMemcpyAsync(eig.ptr, eig_host, sizeof(double) * N, cudaMemcpyHostToDevice, st));
+  // beta = 1 / k_B / T, k_B in Hartree per Kelvin (include/constants.h:30)
+  const double beta = 1.0 / 3.166811429e-06 / temperature;
+  int rc = dm_first_order_response_real(&s, op_prime, (double*)X, ld, N, eig.ptr, fermi_energy,
+                                        beta, dmu.ptr, precision, st);
+  if (rc != CHEFSI_OK) return rc;
+  CHEFSI_CUDA(cudaMemcpyAsync(dmu_host, dmu.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
   CHEFSI_API_END
 }

@@ -26,6 +26,10 @@
  *                    pseudoGramSchmidtOrthogonalization (src/linAlg/pseudoGSDevice.cc:82-463)
  *   chefsi_rayleigh_ritz
  *                    rayleighRitzGEP (src/linAlg/rayleighRitzDevice.cc:356-819)
+ *   chefsi_density_matrix_first_order_response
+ *                    densityMatrixEigenBasisFirstOrderResponse
+ *                    (include/linearAlgebraOperationsDevice.h:302-322,
+ *                    src/linAlg/rayleighRitzDevice.cc:1455-1721)
  *   chefsi_rayleigh_ritz_spectrum_split / chefsi_solve_spectrum_split
  *                    rayleighRitzGEPSpectrumSplitDirect
  *                    (include/linearAlgebraOperationsDevice.h:279-298,
@@ -225,6 +229,20 @@ int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld,
                                         int32_t n_occ, void* XFrac, int64_t ld_frac,
                                         double* eig_host, void* HXFrac_out, int32_t precision,
                                         int32_t frac_reduced, void* stream);
+
+/* First-order response of the density matrix in the eigenbasis (real operators). op_prime
+   applies the perturbation H' only (DFT-FE's onlyHPrimePart apply: build it from the cell
+   matrices of the first-order potential). X ([n_dofs][N], ld) holds the N orthonormal
+   eigenvectors (Loewdin basis, as the solve works on) with eigenvalues eig_host[N]:
+   Hp' = X^T H' X; P' from 10 steps of the first-order recursive Fermi-operator expansion at
+   beta = 1 / (k_B temperature) (Kelvin; k_B = 3.166811429e-6 Ha/K) around fermi_energy;
+   X <- X P' in place; dmu_host[N] receives densityMatDerFermiEnergy = beta X0 (1 - X0).
+   precision MIXED: tensor-core H X, Gram and rotation (the reference's singlePrecLRD). */
+int chefsi_density_matrix_first_order_response(chefsi_operator op_prime, void* X, int64_t ld,
+                                               int32_t N, const double* eig_host,
+                                               double fermi_energy, double temperature,
+                                               double* dmu_host, int32_t precision,
+                                               void* stream);
 
 /* y = a x + b y on [rows][n_vec] FP64 device blocks (leading dimensions ldx, ldy). */
 int chefsi_axpby(int64_t rows, int32_t n_vec, double a, const double* x, int64_t ldx, double b,

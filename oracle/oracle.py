@@ -274,6 +274,46 @@ def rayleigh_ritz_spectrum_split(op: OracleOperator, X: np.ndarray, n_occ: int):
     return ev[n_occ:], Xo, Xo @ Qf, HX @ Qf
 
 
+K_B_HARTREE_PER_KELVIN = 3.166811429e-06   # include/constants.h:30
+
+
+def density_matrix_first_order_response(op_prime: OracleOperator, X: np.ndarray, eig: np.ndarray,
+                                        fermi_energy: float, temperature: float, m: int = 10):
+    """densityMatrixEigenBasisFirstOrderResponse (rayleighRitzDevice.cc:1455-1721).
+
+    Hp' = X^T H' X, lower triangle kept (:1498-1545); the recursive Fermi-operator expansion's
+    first-order part by its row / column scalings (:1556-1633): X1 = diag(X0) P + P diag(X0),
+    Y0 = 1 / (2 X0 (X0 - 1) + 1), X0 <- Y0 X0 X0, P <- diag(Y0) X1 - 2 diag(Y0) X1 diag(X0)
+    + 2 diag(Y0) P diag(X0); P + P^T with the diagonal halved (:1656-1682); X <- X P.
+    Returns (X P, densityMatDerFermiEnergy = beta X0 (1 - X0)).
+    """
+    beta = 1.0 / K_B_HARTREE_PER_KELVIN / temperature
+    c = 2.0 ** (-2 - m) * beta
+    Hp = np.tril(X.T @ op_prime.HX(X))
+    X0 = 0.5 - c * (np.asarray(eig, dtype=np.float64) - fermi_energy)
+    P = -c * Hp
+    for _ in range(m):
+        X1 = P * X0[:, None] + P * X0[None, :]
+        Y0 = 1.0 / (2.0 * X0 * (X0 - 1.0) + 1.0)
+        X0 = Y0 * X0 * X0
+        X1c = (X1 * X0[None, :]) * Y0[:, None]
+        X1 = X1 * Y0[:, None] - 2.0 * X1c
+        Xb = (P * X0[None, :]) * Y0[:, None]
+        P = X1 + 2.0 * Xb
+    P = P + P.T
+    P[np.diag_indices_from(P)] *= 0.5
+    return X @ P, beta * X0 * (1.0 - X0)
+
+
+def fermi_recursion_scalar(x: np.ndarray, fermi_energy: float, temperature: float, m: int = 10):
+    """The scalar function the recursion applies to an eigenvalue (the zeroth-order part)."""
+    beta = 1.0 / K_B_HARTREE_PER_KELVIN / temperature
+    X0 = 0.5 - 2.0 ** (-2 - m) * beta * (np.asarray(x, dtype=np.float64) - fermi_energy)
+    for _ in range(m):
+        X0 = X0 * X0 / (2.0 * X0 * (X0 - 1.0) + 1.0)
+    return X0
+
+
 @dataclass
 class SolverState:
     a0: float

@@ -198,3 +198,36 @@ def test_oracle_spectrum_split_is_the_top_of_the_full_rayleigh_ritz():
     assert np.abs(Xo.T @ Xo - np.eye(20)).max() < 1e-12
     assert np.abs(XF @ XF.T - Xr[:, 14:] @ Xr[:, 14:].T).max() < 1e-10
     assert np.abs(HXF - dense_operator(pr) @ XF).max() < 1e-10 * np.abs(ev).max()
+
+
+def test_oracle_density_matrix_response_is_the_divided_difference():
+    """The first-order recursion gives the derivative of the matrix function g(H) that the
+    zeroth-order recursion applies: in the eigenbasis, P'_ij = g[e_i, e_j] H'_ij (divided
+    difference; g'(e_i) on the diagonal), and g is close to the Fermi-Dirac occupation f.
+    densityMatDerFermiEnergy is beta g (1 - g), the Fermi-Dirac identity -f' = beta f (1 - f)
+    evaluated with g, so it matches -g' to the accuracy of g ~ f."""
+    pr = small_problem(projectors=False)
+    ora = oracle_op(pr)
+    A = dense_operator(pr)
+    w, Q = np.linalg.eigh(A)
+    N = 24
+    X = Q[:, :N]
+    eig = w[:N]
+    mu, T = 0.5 * (eig[10] + eig[11]), 5000.0
+    XP, dmu = orc.density_matrix_first_order_response(ora, X, eig, mu, T)
+    P = X.T @ XP
+    Hp = X.T @ A @ X
+    g = lambda x: orc.fermi_recursion_scalar(x, mu, T)
+    h = 1e-6
+    D = np.empty((N, N))
+    for i in range(N):
+        for j in range(N):
+            if abs(eig[i] - eig[j]) > 1e-4:
+                D[i, j] = (g(eig[i]) - g(eig[j])) / (eig[i] - eig[j])
+            else:
+                D[i, j] = (g(eig[i] + h) - g(eig[i] - h)) / (2 * h)
+    assert np.abs(P - D * Hp).max() < 1e-6 * np.abs(D * Hp).max()
+    assert np.abs(-np.diag(D) - dmu).max() < 1e-4 * np.abs(dmu).max()
+    beta = 1.0 / orc.K_B_HARTREE_PER_KELVIN / T
+    fd = 1.0 / (1.0 + np.exp(beta * (eig - mu)))
+    assert np.abs(g(eig) - fd).max() < 1e-3
