@@ -643,6 +643,23 @@ __global__ void k_dmfor_diag(const double* __restrict__ eig, int N, double mu, d
   dmu[i] = __dmul_rn(__dmul_rn(beta, x), __dsub_rn(1.0, x));
 }
 
+// The recursion of entry (row i, column j) on one real component (the factors are real, so a
+// complex entry runs it on its real and imaginary parts separately)
+__device__ __forceinline__ double dmfor_entry(double h, int i, int j, int N, double c,
+                                              const double* __restrict__ X0,
+                                              const double* __restrict__ Y0) {
+  double p = __dmul_rn(-c, h);
+  for (int k = 0; k < kDmforSteps; ++k) {
+    const double xi = X0[(int64_t)k * N + i], xj = X0[(int64_t)k * N + j];
+    const double y = Y0[(int64_t)k * N + i];
+    const double xn = X0[(int64_t)(k + 1) * N + j];
+    const double T = __dadd_rn(__dmul_rn(p, xi), __dmul_rn(p, xj));
+    const double a = __dsub_rn(__dmul_rn(T, y), __dmul_rn(2.0, __dmul_rn(__dmul_rn(T, xn), y)));
+    p = __dadd_rn(a, __dmul_rn(2.0, __dmul_rn(__dmul_rn(p, xn), y)));
+  }
+  return p;
+}
+
 // P[i][j] <- first-order density-matrix response from Hp[i][j] (full symmetric input;
 // the entry of row max(i, j), column min(i, j) is computed and written to both places)
 __global__ void k_dmfor_apply(double* __restrict__ P, int N, double c,
@@ -652,17 +669,25 @@ __global__ void k_dmfor_apply(double* __restrict__ P, int N, double c,
        t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t / N), j = (int)(t % N);
     if (j > i) continue;  // row i >= column j
-    double p = __dmul_rn(-c, P[t]);
-    for (int k = 0; k < kDmforSteps; ++k) {
-      const double xi = X0[(int64_t)k * N + i], xj = X0[(int64_t)k * N + j];
-      const double y = Y0[(int64_t)k * N + i];
-      const double xn = X0[(int64_t)(k + 1) * N + j];
-      const double T = __dadd_rn(__dmul_rn(p, xi), __dmul_rn(p, xj));
-      const double a = __dsub_rn(__dmul_rn(T, y), __dmul_rn(2.0, __dmul_rn(__dmul_rn(T, xn), y)));
-      p = __dadd_rn(a, __dmul_rn(2.0, __dmul_rn(__dmul_rn(p, xn), y)));
-    }
+    const double p = dmfor_entry(P[t], i, j, N, c, X0, Y0);
     P[t] = p;
     P[(int64_t)j * N + i] = p;
+  }
+}
+
+// complex Hermitian P: the lower entry from the recursion, the upper one its conjugate
+__global__ void k_dmfor_apply_c(cplx* __restrict__ P, int N, double c,
+                                const double* __restrict__ X0, const double* __restrict__ Y0) {
+  const int64_t n = (int64_t)N * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / N), j = (int)(t % N);
+    if (j > i) continue;
+    const cplx h = P[t];
+    const double re = dmfor_entry(h.x, i, j, N, c, X0, Y0);
+    const double im = i == j ? 0.0 : dmfor_entry(h.y, i, j, N, c, X0, Y0);
+    P[t] = {re, im};
+    P[(int64_t)j * N + i] = {re, -im};
   }
 }
 
@@ -780,6 +805,42 @@ __global__ void k_realify_w(const cplx* W, int N, double* Wr) {
   }
 }
 
+// H X ([M][N], ld N) of a complex block for the Rayleigh-Ritz products: FP64 complex, or (mixed
+// with rr_precision FP32 / FP32_TC on a folded operator) the FP32 SIMT / three-term tensor-core
+// apply of the real form on X rounded to FP32. Returns true when the reduced apply ran.
+bool hx_complex_block(chefsi_solver_s* s, chefsi_operator_s* op, const cplx* X, int64_t ld, int N,
+                      int prec, cplx* HX, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const int rrp = s->p.rr_precision;
+  if (is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC) && op->folded) {
+    chefsi_operator_s* rv = realified(op, st);
+    float* xr = s->Xb32.ensure((size_t)2 * M * N);
+    float* yr = s->Yb32.ensure((size_t)2 * M * N);
+    const bool tc3 = rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(rv, N);
+    double scale = 1.0;
+    if (tc3) {
+      double* sc = s->scal.ensure(1);
+      absmax_block_f64(reinterpret_cast<const double*>(X), 2 * ld, M, 2 * N, sc, st);
+      double amax = 0.0;
+      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (amax > 0.0 && std::isfinite(amax))
+        scale = std::ldexp(1.0, 14 - (int)std::ceil(std::log2(amax)));
+    }
+    complex_to_real_rows(X, ld, M, N, scale, xr, st);
+    if (!(tc3 && hx_tc3(rv, xr, N, yr, N, N, 1.0 / scale, false, st)))
+      hx_f32(rv, xr, N, yr, N, N, 1.0 / scale, false, st);
+    real_rows_to_complex(yr, M, N, 1.0, HX, N, st);
+    return true;
+  }
+  const int Bmax = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
+  for (int j0 = 0; j0 < N; j0 += Bmax) {
+    const int B = std::min(Bmax, N - j0);
+    hx_c64(op, X + j0, ld, HX + j0, N, B, 1.0, false, st);
+  }
+  return false;
+}
+
 // Rayleigh-Ritz for a complex (Bloch) operator: the generalised form with Hermitian S and Hp.
 int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, int64_t ld, int N,
                           int prec, bool want_hx, cudaStream_t st) {
@@ -819,36 +880,8 @@ int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, in
   }
   trtri_lower_c(S, N, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
-  // HX: FP64 complex, or (mixed with rr_precision FP32 / FP32_TC on a folded operator) the
-  // FP32 SIMT / three-term tensor-core apply of the real form on X rounded to FP32
   cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
-  const int rrp = s->p.rr_precision;
-  if (is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC) && op->folded) {
-    chefsi_operator_s* rv = realified(op, st);
-    float* xr = s->Xb32.ensure((size_t)2 * M * N);
-    float* yr = s->Yb32.ensure((size_t)2 * M * N);
-    const bool tc3 = rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(rv, N);
-    double scale = 1.0;
-    if (tc3) {
-      double* sc = s->scal.ensure(1);
-      absmax_block_f64(reinterpret_cast<const double*>(X), 2 * ld, M, 2 * N, sc, st);
-      double amax = 0.0;
-      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
-      CHEFSI_CUDA(cudaStreamSynchronize(st));
-      if (amax > 0.0 && std::isfinite(amax))
-        scale = std::ldexp(1.0, 14 - (int)std::ceil(std::log2(amax)));
-    }
-    complex_to_real_rows(X, ld, M, N, scale, xr, st);
-    if (!(tc3 && hx_tc3(rv, xr, N, yr, N, N, 1.0 / scale, false, st)))
-      hx_f32(rv, xr, N, yr, N, N, 1.0 / scale, false, st);
-    real_rows_to_complex(yr, M, N, 1.0, HX, N, st);
-  } else {
-    const int Bmax = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
-    for (int j0 = 0; j0 < N; j0 += Bmax) {
-      const int B = std::min(Bmax, N - j0);
-      hx_c64(op, X + j0, ld, HX + j0, N, B, 1.0, false, st);
-    }
-  }
+  hx_complex_block(s, op, X, ld, N, prec, HX, st);
   double* HXv = reinterpret_cast<double*>(HX);
   if (tcd) {
     tc_exponents<double>(HXv, N2, M, N2, s->th, st);
@@ -893,6 +926,96 @@ int rayleigh_ritz_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, in
     if (want_hx) rotate_rows_c(s, HX, N, M, N, W, st);
   }
   CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  return CHEFSI_OK;
+}
+
+// Spectrum-split Rayleigh-Ritz for a complex (Bloch) operator: the steps of
+// rayleigh_ritz_ss_real with Hermitian products (S = X^H X = L L^H, X <- X L^{-H}, Hp = X^H H X,
+// XFrac = X Q_fr). The dense products are FP64 complex GEMMs in every mode (the Bloch blocks
+// are small); the mixed mode changes the H X (the real form's reduced apply, as the full
+// step) and, unless ss_frac_reduced, recomputes the fractional block from an FP64 H X.
+int rayleigh_ritz_ss_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X, int64_t ld,
+                             int N, int n_occ, cplx* XF, int64_t ldf, int prec, bool want_hxf,
+                             cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const int nfr = N - n_occ;
+  cplx* S = reinterpret_cast<cplx*>(s->S.ensure((size_t)N * N * 2));
+  cplx* Hp = reinterpret_cast<cplx*>(s->Hp.ensure((size_t)N * N * 2));
+  cplx* T1 = reinterpret_cast<cplx*>(s->T1.ensure((size_t)N * N * 2));
+  cplx* Z = reinterpret_cast<cplx*>(s->Z.ensure((size_t)N * nfr * 2));
+  cplx* W = reinterpret_cast<cplx*>(s->W.ensure((size_t)N * N * 2));
+  double* w = s->evals.ensure(N);
+  const cplx one = {1.0, 0.0}, zero = {0.0, 0.0};
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(cplx) * N * N, st));
+  gram_c64(X, ld, X, ld, M, N, N, S, N, true, st);
+  symmetrize_lower_c(S, N, st);
+  int rc = cholesky_lower_c(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower_c(S, N, st);
+  k_conj_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);
+  CHEFSI_CHECK_LAUNCH();
+  rotate_rows_c(s, X, ld, M, N, W, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
+  const bool reduced = hx_complex_block(s, op, X, ld, N, prec, HX, st);
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(cplx) * N * N, st));
+  gram_c64(X, ld, HX, N, M, N, N, Hp, N, true, st);
+  if (reduced && !s->p.ss_frac_reduced) {
+    const int blk = std::max(1, std::min(s->p.wfc_block > 0 ? s->p.wfc_block : N, N));
+    const int n_lo = (n_occ / blk) * blk;
+    const int nf = N - n_lo;
+    cplx* HXf = reinterpret_cast<cplx*>(s->HXf.ensure((size_t)M * nf * 2));
+    for (int j0 = 0; j0 < nf; j0 += blk) {
+      const int B = std::min(blk, nf - j0);
+      hx_c64(op, X + n_lo + j0, ld, HXf + j0, nf, B, 1.0, false, st);
+    }
+    CHEFSI_CUDA(cudaMemsetAsync(T1, 0, sizeof(cplx) * nf * nf, st));
+    gram_c64(X + n_lo, ld, HXf, nf, M, nf, nf, T1, nf, true, st);
+    copy_block<cplx, cplx>(T1, nf, Hp + (int64_t)n_lo * N + n_lo, N, nf, nf, 1.0, st);
+  }
+  symmetrize_lower_c(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  rc = heevd_range(Hp, N, n_occ, nfr, w, Z, st);
+  if (rc != CHEFSI_OK) return rc;
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  gemm_c64('N', 'N', M, nfr, N, one, X, ld, Z, nfr, zero, XF, ldf, st);
+  if (want_hxf) {
+    cplx* HXF = reinterpret_cast<cplx*>(s->HXF.ensure((size_t)M * nfr * 2));
+    gemm_c64('N', 'N', M, nfr, N, one, HX, N, Z, nfr, zero, HXF, nfr, st);
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  return CHEFSI_OK;
+}
+
+// First-order density-matrix response for a complex operator: Hp' = X^H H' X (FP64 complex
+// Gram), the recursion on the real and imaginary parts of the lower triangle, the upper
+// triangle its conjugate, X <- X P'.
+int dm_first_order_response_complex(chefsi_solver_s* s, chefsi_operator_s* op, cplx* X,
+                                    int64_t ld, int N, const double* eig, double mu, double beta,
+                                    double* dmu, int prec, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  cplx* Hp = reinterpret_cast<cplx*>(s->Hp.ensure((size_t)N * N * 2));
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  cplx* HX = reinterpret_cast<cplx*>(s->HX.ensure((size_t)M * N * 2));
+  hx_complex_block(s, op, X, ld, N, prec, HX, st);
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(cplx) * N * N, st));
+  gram_c64(X, ld, HX, N, M, N, N, Hp, N, true, st);
+  symmetrize_lower_c(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  const double c = std::ldexp(1.0, -2 - kDmforSteps) * beta;
+  double* X0 = s->T1.ensure((size_t)(2 * kDmforSteps + 1) * N);
+  double* Y0 = X0 + (size_t)(kDmforSteps + 1) * N;
+  k_dmfor_diag<<<(N + 127) / 128, 128, 0, st>>>(eig, N, mu, beta, c, X0, Y0, dmu);
+  CHEFSI_CHECK_LAUNCH();
+  k_dmfor_apply_c<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(Hp, N, c, X0, Y0);
+  CHEFSI_CHECK_LAUNCH();
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  rotate_rows_c(s, X, ld, M, N, Hp, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
   return CHEFSI_OK;
 }
 
@@ -1240,18 +1363,21 @@ int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld,
   CHEFSI_REQUIRE(op && X && XFrac && eig_host && N >= 1 && ld >= N, "bad argument");
   CHEFSI_REQUIRE(n_occ >= 0 && n_occ < N, "need 0 <= n_occ < N");
   CHEFSI_REQUIRE(ld_frac >= N - n_occ, "ld_frac below N - n_occ");
-  CHEFSI_REQUIRE(!op->is_complex, "spectrum-split Rayleigh-Ritz: real operators only");
   cudaStream_t st = as_stream(stream);
   chefsi_solver_s s;
   s.p = default_params();
   s.p.rr_precision = precision == CHEFSI_PREC_MIXED ? CHEFSI_PREC_FP32_TC : CHEFSI_PREC_FP64;
   s.p.ss_frac_reduced = frac_reduced;
   const int nfr = N - n_occ;
-  int rc = rayleigh_ritz_ss_real(&s, op, (double*)X, ld, N, n_occ, (double*)XFrac, ld_frac,
-                                 precision, HXFrac_out != nullptr, st);
+  const int cw = op->is_complex ? 2 : 1;
+  int rc = op->is_complex
+               ? rayleigh_ritz_ss_complex(&s, op, (cplx*)X, ld, N, n_occ, (cplx*)XFrac, ld_frac,
+                                          precision, HXFrac_out != nullptr, st)
+               : rayleigh_ritz_ss_real(&s, op, (double*)X, ld, N, n_occ, (double*)XFrac,
+                                       ld_frac, precision, HXFrac_out != nullptr, st);
   if (rc != CHEFSI_OK) return rc;
   if (HXFrac_out)
-    CHEFSI_CUDA(cudaMemcpyAsync(HXFrac_out, s.HXF.ptr, sizeof(double) * op->n_dofs * nfr,
+    CHEFSI_CUDA(cudaMemcpyAsync(HXFrac_out, s.HXF.ptr, sizeof(double) * op->n_dofs * nfr * cw,
                                 cudaMemcpyDeviceToDevice, st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s.evals.ptr, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
@@ -1266,8 +1392,6 @@ int chefsi_density_matrix_first_order_response(chefsi_operator op_prime, void* X
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(op_prime && X && eig_host && dmu_host && N >= 1 && ld >= N, "bad argument");
   CHEFSI_REQUIRE(temperature > 0.0, "temperature must be positive (Kelvin)");
-  CHEFSI_REQUIRE(!op_prime->is_complex,
-                 "density-matrix first-order response: real operators only");
   cudaStream_t st = as_stream(stream);
   chefsi_solver_s s;
   s.p = default_params();
@@ -1275,8 +1399,11 @@ int chefsi_density_matrix_first_order_response(chefsi_operator op_prime, void* X
   CHEFSI_CUDA(cudaMemcpyAsync(eig.ptr, eig_host, sizeof(double) * N, cudaMemcpyHostToDevice, st));
   // beta = 1 / k_B / T, k_B in Hartree per Kelvin (include/constants.h:30)
   const double beta = 1.0 / 3.166811429e-06 / temperature;
-  int rc = dm_first_order_response_real(&s, op_prime, (double*)X, ld, N, eig.ptr, fermi_energy,
-                                        beta, dmu.ptr, precision, st);
+  int rc = op_prime->is_complex
+               ? dm_first_order_response_complex(&s, op_prime, (cplx*)X, ld, N, eig.ptr,
+                                                 fermi_energy, beta, dmu.ptr, precision, st)
+               : dm_first_order_response_real(&s, op_prime, (double*)X, ld, N, eig.ptr,
+                                              fermi_energy, beta, dmu.ptr, precision, st);
   if (rc != CHEFSI_OK) return rc;
   CHEFSI_CUDA(cudaMemcpyAsync(dmu_host, dmu.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
@@ -1525,7 +1652,6 @@ int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, in
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(s && op && X && XFrac && eig_host && N >= 1, "bad argument");
   CHEFSI_REQUIRE(n_occ >= 0 && n_occ < N, "need 0 <= n_occ < N");
-  CHEFSI_REQUIRE(!op->is_complex, "spectrum-split Rayleigh-Ritz: real operators only");
   CHEFSI_REQUIRE(s->b_up > s->b_low, "spectrum bounds not set (call reinit_spectrum_bounds)");
   cudaStream_t st = as_stream(stream);
   const int m = degree_for(s, is_first_scf);
@@ -1534,11 +1660,17 @@ int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, in
   const int64_t M = op->n_dofs;
   CHEFSI_CUDA(cudaEventRecord(s->ev[0], st));
   filter_all(s, op, X, N, m, s->p.precision, st);
-  int rc = rayleigh_ritz_ss_real(s, op, (double*)X, N, N, n_occ, (double*)XFrac, nfr,
-                                 s->p.precision, compute_residual != 0, st);
+  int rc = op->is_complex
+               ? rayleigh_ritz_ss_complex(s, op, (cplx*)X, N, N, n_occ, (cplx*)XFrac, nfr,
+                                          s->p.precision, compute_residual != 0, st)
+               : rayleigh_ritz_ss_real(s, op, (double*)X, N, N, n_occ, (double*)XFrac, nfr,
+                                       s->p.precision, compute_residual != 0, st);
   if (rc != CHEFSI_OK) return rc;
   double* res = s->resid.ensure(nfr);
-  if (compute_residual)
+  if (compute_residual && op->is_complex)
+    residual_norms_c64((const cplx*)XFrac, nfr, (const cplx*)s->HXF.ptr, nfr, M, nfr, s->evals.ptr,
+                       res, st);
+  else if (compute_residual)
     residual_norms_f64((const double*)XFrac, nfr, s->HXF.ptr, nfr, M, nfr, s->evals.ptr, res, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[6], st));
   CHEFSI_CUDA(cudaMemcpyAsync(eig_host, s->evals.ptr, sizeof(double) * nfr, cudaMemcpyDeviceToHost, st));

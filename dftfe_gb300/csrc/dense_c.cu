@@ -228,12 +228,12 @@ __global__ void k_tridiag_phases(const cplx* e, int N, double* er, cplx* phi) {
   er[N - 1] = 0.0;
 }
 
-// Z[j][t] = phi_j Zr[j][t]
-__global__ void k_phase_rows(const double* Zr, const cplx* phi, int N, cplx* Z) {
-  const int64_t n = (int64_t)N * N;
+// Z[j][t] = phi_j Zr[j][t] (N rows of ncols)
+__global__ void k_phase_rows(const double* Zr, const cplx* phi, int N, int ncols, cplx* Z) {
+  const int64_t n = (int64_t)N * ncols;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x)
-    Z[t] = cscale(phi[t / N], Zr[t]);
+    Z[t] = cscale(phi[t / ncols], Zr[t]);
 }
 
 // compact-WY T of a block of complex reflectors (forward, columnwise) from G = V^H V
@@ -264,12 +264,13 @@ __global__ void k_transpose_sq_c(const cplx* A, cplx* B, int N) {
 
 constexpr int kWYc = 64;
 
-// Z <- H_0 ... H_{N-3} Z with H_k = I - tau_k v_k v_k^H, v_k in row k of V
-void back_transform_wy_c(const cplx* V, const double* tau, int N, cplx* Z, cudaStream_t st) {
+// Z <- H_0 ... H_{N-3} Z with H_k = I - tau_k v_k v_k^H, v_k in row k of V; Z is N x ncols
+void back_transform_wy_c(const cplx* V, const double* tau, int N, cplx* Z, int ncols,
+                         cudaStream_t st) {
   const int nrefl = N - 2;
   if (nrefl <= 0) return;
   DeviceBuffer<cplx> Vc((size_t)N * N), G((size_t)kWYc * kWYc), T((size_t)kWYc * kWYc),
-      W1((size_t)kWYc * N), W2((size_t)kWYc * N);
+      W1((size_t)kWYc * ncols), W2((size_t)kWYc * ncols);
   k_transpose_sq_c<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(V, Vc.ptr, N);
   CHEFSI_CHECK_LAUNCH();
   const cplx one = {1.0, 0.0}, zero = {0.0, 0.0}, mone = {-1.0, 0.0};
@@ -280,10 +281,10 @@ void back_transform_wy_c(const cplx* V, const double* tau, int N, cplx* Z, cudaS
     gram_c64(Vb, N, Vb, N, N, nb, nb, G.ptr, nb, false, st);               // Vb^H Vb
     k_build_t_c<<<1, kWYc, 0, st>>>(G.ptr, tau + k0, nb, T.ptr);
     CHEFSI_CHECK_LAUNCH();
-    CHEFSI_CUDA(cudaMemsetAsync(W1.ptr, 0, sizeof(cplx) * nb * N, st));
-    gram_c64(Vb, N, Z, N, N, nb, N, W1.ptr, N, false, st);                 // Vb^H Z
-    gemm_c64('N', 'N', nb, N, nb, one, T.ptr, nb, W1.ptr, N, zero, W2.ptr, N, st);
-    gemm_c64('N', 'N', N, N, nb, mone, Vb, N, W2.ptr, N, one, Z, N, st);
+    CHEFSI_CUDA(cudaMemsetAsync(W1.ptr, 0, sizeof(cplx) * nb * ncols, st));
+    gram_c64(Vb, N, Z, ncols, N, nb, ncols, W1.ptr, ncols, false, st);     // Vb^H Z
+    gemm_c64('N', 'N', nb, ncols, nb, one, T.ptr, nb, W1.ptr, ncols, zero, W2.ptr, ncols, st);
+    gemm_c64('N', 'N', N, ncols, nb, mone, Vb, N, W2.ptr, ncols, one, Z, ncols, st);
   }
 }
 
@@ -329,10 +330,13 @@ void trtri_lower_c(cplx* L, int N, cudaStream_t st) {
   }
 }
 
-int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
+// Eigenpairs il .. il+count-1 (ascending) of the Hermitian row-major A (destroyed); w[count],
+// Z[N][count]. count == N is the full solve.
+int heevd_range(cplx* A, int N, int il, int count, double* w, cplx* Z, cudaStream_t st) {
   CHEFSI_REQUIRE(N >= 1, "heevd: N must be positive");
+  CHEFSI_REQUIRE(il >= 0 && count >= 1 && il + count <= N, "heevd: eigenpair range out of bounds");
   DeviceBuffer<cplx> V((size_t)N * N), e(N), p(N), phi(N);
-  DeviceBuffer<double> tau(N), d(N), er(N), Zr((size_t)N * N);
+  DeviceBuffer<double> tau(N), d(N), er(N), Zr((size_t)N * count);
   CHEFSI_CUDA(cudaMemsetAsync(V.ptr, 0, sizeof(cplx) * N * N, st));
   CHEFSI_CUDA(cudaMemsetAsync(tau.ptr, 0, sizeof(double) * N, st));
   CHEFSI_CUDA(cudaMemsetAsync(e.ptr, 0, sizeof(cplx) * N, st));
@@ -351,7 +355,7 @@ int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
   CHEFSI_CHECK_LAUNCH();
   k_tridiag_phases<<<1, 32, 0, st>>>(e.ptr, N, er.ptr, phi.ptr);
   CHEFSI_CHECK_LAUNCH();
-  k_bisect_warp<<<(N + 3) / 4, 128, 0, st>>>(d.ptr, er.ptr, N, 0, N, w);
+  k_bisect_warp<<<(count + 3) / 4, 128, 0, st>>>(d.ptr, er.ptr, N, il, count, w);
   CHEFSI_CHECK_LAUNCH();
   std::vector<double> hd(N), he(N);
   CHEFSI_CUDA(cudaMemcpyAsync(hd.data(), d.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
@@ -362,16 +366,20 @@ int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
     tn = std::max(tn, std::fabs(hd[j]) + (j > 0 ? std::fabs(he[j - 1]) : 0.0) +
                           (j < N - 1 ? std::fabs(he[j]) : 0.0));
   const double ortol = 1e-5 * std::max(tn, 1e-300);
-  DeviceBuffer<double> work((size_t)N * 5 * N);
-  DeviceBuffer<unsigned char> swaps((size_t)N * N);
-  k_inverse_iteration<<<(N + 31) / 32, 32, 0, st>>>(d.ptr, er.ptr, N, w, N, 0, Zr.ptr, N, work.ptr,
-                                                    swaps.ptr, ortol);
+  DeviceBuffer<double> work((size_t)count * 5 * N);
+  DeviceBuffer<unsigned char> swaps((size_t)count * N);
+  k_inverse_iteration<<<(count + 31) / 32, 32, 0, st>>>(d.ptr, er.ptr, N, w, count, il, Zr.ptr,
+                                                        count, work.ptr, swaps.ptr, ortol);
   CHEFSI_CHECK_LAUNCH();
-  k_phase_rows<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(Zr.ptr, phi.ptr, N, Z);
+  k_phase_rows<<<grid_for((int64_t)N * count, 256), 256, 0, st>>>(Zr.ptr, phi.ptr, N, count, Z);
   CHEFSI_CHECK_LAUNCH();
-  back_transform_wy_c(V.ptr, tau.ptr, N, Z, st);
+  back_transform_wy_c(V.ptr, tau.ptr, N, Z, count, st);
   CHEFSI_CUDA(cudaStreamSynchronize(st));
   return CHEFSI_OK;
+}
+
+int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st) {
+  return heevd_range(A, N, 0, N, w, Z, st);
 }
 
 }  // namespace chefsi

@@ -240,6 +240,7 @@ int syevd_range(double* A, int N, int il, int count, double* w, double* Z, cudaS
 int cholesky_lower_c(cplx* A, int N, cudaStream_t st);
 void trtri_lower_c(cplx* L, int N, cudaStream_t st);
 int heevd(cplx* A, int N, double* w, cplx* Z, cudaStream_t st);
+int heevd_range(cplx* A, int N, int il, int count, double* w, cplx* Z, cudaStream_t st);
 // residual norms of columns: out[j] = || HX[:,j] - lam[j] X[:,j] ||
 void residual_norms_f64(const double* X, int64_t ldx, const double* HX, int64_t ldh, int64_t M,
                         int N, const double* lam_dev, double* out_dev, cudaStream_t st);

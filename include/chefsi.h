@@ -217,27 +217,30 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
 int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
                          double* HX_out, double* W_out, int32_t precision, void* stream);
 
-/* Spectrum-split Rayleigh-Ritz (real operators). X ([n_dofs][N], ld) is orthonormalised in
-   place by Cholesky-GS (X <- X L^{-T}, X^T X = L L^T) and stays in that basis; the projected
-   Hamiltonian X^T H X of the orthonormal X is diagonalised for its top n_fr = N - n_occ
+/* Spectrum-split Rayleigh-Ritz. X ([n_dofs][N], ld) is orthonormalised in place by
+   Cholesky-GS (X <- X L^{-H}, X^H X = L L^H) and stays in that basis; the projected
+   Hamiltonian X^H H X of the orthonormal X is diagonalised for its top n_fr = N - n_occ
    eigenpairs only, and XFrac ([n_dofs][n_fr], ld_frac) = X Q_fr. eig_host receives the n_fr
    eigenvalues in ascending order; HXFrac_out, if non-null, H XFrac ([n_dofs][n_fr] FP64).
-   precision MIXED: tensor-core Gram and rotation products, the three-term tensor-core H X
-   for the occupied column blocks and, unless frac_reduced, an FP64 H X and Gram product for
-   the block that couples the fractional states. */
+   precision MIXED: the reduced-precision H X (three-term tensor-core split) for the occupied
+   column blocks and, unless frac_reduced, an FP64 H X and Gram product for the block that
+   couples the fractional states; real operators also take the Gram and rotation products
+   to the tensor cores (complex operators keep them in FP64). */
 int chefsi_rayleigh_ritz_spectrum_split(chefsi_operator op, void* X, int64_t ld, int32_t N,
                                         int32_t n_occ, void* XFrac, int64_t ld_frac,
                                         double* eig_host, void* HXFrac_out, int32_t precision,
                                         int32_t frac_reduced, void* stream);
 
-/* First-order response of the density matrix in the eigenbasis (real operators). op_prime
+/* First-order response of the density matrix in the eigenbasis. op_prime
    applies the perturbation H' only (DFT-FE's onlyHPrimePart apply: build it from the cell
    matrices of the first-order potential). X ([n_dofs][N], ld) holds the N orthonormal
    eigenvectors (Loewdin basis, as the solve works on) with eigenvalues eig_host[N]:
-   Hp' = X^T H' X; P' from 10 steps of the first-order recursive Fermi-operator expansion at
+   Hp' = X^H H' X; P' from 10 steps of the first-order recursive Fermi-operator expansion at
    beta = 1 / (k_B temperature) (Kelvin; k_B = 3.166811429e-6 Ha/K) around fermi_energy;
    X <- X P' in place; dmu_host[N] receives densityMatDerFermiEnergy = beta X0 (1 - X0).
-   precision MIXED: tensor-core H X, Gram and rotation (the reference's singlePrecLRD). */
+   precision MIXED: tensor-core H X, Gram and rotation for real operators (the reference's
+   singlePrecLRD), the reduced H X of the real form with FP64 complex products for complex
+   ones. */
 int chefsi_density_matrix_first_order_response(chefsi_operator op_prime, void* X, int64_t ld,
                                                int32_t N, const double* eig_host,
                                                double fermi_energy, double temperature,
@@ -334,7 +337,7 @@ int chefsi_solve(chefsi_solver s, chefsi_operator op, void* X, int32_t N, double
    branch taken when N - n_occ < N eigenvalues are wanted): filter all N vectors of X, then
    X <- orthonormalised X, XFrac ([n_dofs][N - n_occ], ld N - n_occ, device) = X Q_fr.
    eig_host / res_host receive the N - n_occ eigenvalues and the residual norms of the
-   XFrac columns (H XFrac - lambda XFrac, with H XFrac = (H X) Q_fr). Real operators. */
+   XFrac columns (H XFrac - lambda XFrac, with H XFrac = (H X) Q_fr). */
 int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, int32_t N,
                                 int32_t n_occ, void* XFrac, double* eig_host, double* res_host,
                                 int32_t compute_residual, int32_t is_first_scf, void* stream);

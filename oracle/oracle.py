@@ -289,7 +289,8 @@ def density_matrix_first_order_response(op_prime: OracleOperator, X: np.ndarray,
     """
     beta = 1.0 / K_B_HARTREE_PER_KELVIN / temperature
     c = 2.0 ** (-2 - m) * beta
-    Hp = np.tril(X.T @ op_prime.HX(X))
+    Xc = X.conj() if op_prime.is_complex else X
+    Hp = np.tril(Xc.T @ op_prime.HX(X))
     X0 = 0.5 - c * (np.asarray(eig, dtype=np.float64) - fermi_energy)
     P = -c * Hp
     for _ in range(m):
@@ -300,7 +301,7 @@ def density_matrix_first_order_response(op_prime: OracleOperator, X: np.ndarray,
         X1 = X1 * Y0[:, None] - 2.0 * X1c
         Xb = (P * X0[None, :]) * Y0[:, None]
         P = X1 + 2.0 * Xb
-    P = P + P.T
+    P = P + P.conj().T
     P[np.diag_indices_from(P)] *= 0.5
     return X @ P, beta * X0 * (1.0 - X0)
 
