@@ -55,6 +55,76 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Bloch cell Hamiltonians for n_k k-points (the k-point form of hamMatrixKernelLDA,
+// src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:119-280), as the matrix applied
+// to the cell vector (the transpose of the reference's flattened layout, whose complex HX
+// multiplies with op = T):
+//   Re out[k][c][I][J] = 0.5 K[I][J] + sum_q v[c][q] N_qI N_qJ + |k|^2/2 sum_q w[c][q] N_qI N_qJ
+//   Im out[k][c][I][J] = -sum_d k_d sum_q w[c][q] N_qI dN_d[q][J]
+// (w = JxW, dN_d the real-space shape-function gradients). The five cell sums are formed once
+// per cell tile and combined for every k-point in the epilogue.
+__global__ void __launch_bounds__(256)
+    k_assemble_bloch(int n_cells, int n_e, int n_q, const double* __restrict__ N,
+                     const double* __restrict__ dN, const double* __restrict__ K,
+                     const double* __restrict__ v, const double* __restrict__ w, int n_k,
+                     const double* __restrict__ kpts, double2* __restrict__ out, int nt) {
+  __shared__ double Av[16][T + 1];
+  __shared__ double Aw[16][T + 1];
+  __shared__ double Bn[16][T + 1];
+  __shared__ double Bd[3][16][T + 1];
+  const int64_t blk = blockIdx.x;
+  const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
+  const int c = (int)(blk / ((int64_t)nt * nt));
+  const int i0 = ti * T, j0 = tj * T;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 per thread
+  double sv[2][2] = {}, sm[2][2] = {}, sg[3][2][2] = {};
+  const double* vc = v + (int64_t)c * n_q;
+  const double* wc = w + (int64_t)c * n_q;
+  for (int q0 = 0; q0 < n_q; q0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * T; idx += 256) {
+      const int qq = idx / T, k = idx % T;
+      const int q = q0 + qq;
+      const bool okq = q < n_q;
+      const bool oki = okq && i0 + k < n_e, okj = okq && j0 + k < n_e;
+      const double ni = oki ? N[(int64_t)q * n_e + i0 + k] : 0.0;
+      Av[qq][k] = oki ? ni * vc[q] : 0.0;
+      Aw[qq][k] = oki ? ni * wc[q] : 0.0;
+      Bn[qq][k] = okj ? N[(int64_t)q * n_e + j0 + k] : 0.0;
+      for (int d = 0; d < 3; ++d)
+        Bd[d][qq][k] = okj ? dN[((int64_t)d * n_q + q) * n_e + j0 + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int qq = 0; qq < 16; ++qq)
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const double av = Av[qq][ty + 16 * r], aw = Aw[qq][ty + 16 * r];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int jj = tx + 16 * s;
+          sv[r][s] = fma(av, Bn[qq][jj], sv[r][s]);
+          sm[r][s] = fma(aw, Bn[qq][jj], sm[r][s]);
+#pragma unroll
+          for (int d = 0; d < 3; ++d) sg[d][r][s] = fma(aw, Bd[d][qq][jj], sg[d][r][s]);
+        }
+      }
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int I = i0 + ty + 16 * r, J = j0 + tx + 16 * s;
+      if (I >= n_e || J >= n_e) continue;
+      const double base = 0.5 * K[(int64_t)I * n_e + J] + sv[r][s];
+      for (int kp = 0; kp < n_k; ++kp) {
+        const double k0 = kpts[3 * kp], k1 = kpts[3 * kp + 1], k2 = kpts[3 * kp + 2];
+        const double ksq = k0 * k0 + k1 * k1 + k2 * k2;
+        const double re = base + 0.5 * ksq * sm[r][s];
+        const double im = -(k0 * sg[0][r][s] + k1 * sg[1][r][s] + k2 * sg[2][r][s]);
+        out[(((int64_t)kp * n_cells + c) * n_e + I) * n_e + J] = make_double2(re, im);
+      }
+    }
+}
+
 // G[c][I][J] += alpha * sum_b d[gI] u[gI][b] d[gJ] w[gJ][b], g = map[c][.]
 __global__ void __launch_bounds__(256)
     k_cell_outer(const int* __restrict__ map, int n_e, const double* __restrict__ d,
@@ -126,6 +196,17 @@ void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double
   const int64_t blocks = (int64_t)n_cells * nt * nt;
   CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
   k_assemble_cells<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, K, v, out, nt);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                          const double* K, const double* v, const double* w, int n_k,
+                          const double* kpts, double* out, cudaStream_t st) {
+  const int nt = (n_e + T - 1) / T;
+  const int64_t blocks = (int64_t)n_cells * nt * nt;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
+  k_assemble_bloch<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w, n_k, kpts,
+                                                     reinterpret_cast<double2*>(out), nt);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -252,6 +252,9 @@ void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaS
 // adjoint / assembly building blocks (adjoint.cu)
 void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
                     const double* v, double* out, cudaStream_t st);
+void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                          const double* K, const double* v, const double* w, int n_k,
+                          const double* kpts, double* out, cudaStream_t st);
 // G_c += alpha * sum_b weights[b] (D u_b)_c (D w_b)_c^T (weights null: 1), D = M^{-1/2}
 void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
                 double alpha, double* G, cudaStream_t st, const double* weights = nullptr);

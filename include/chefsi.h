@@ -276,6 +276,20 @@ int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, i
                                       const double* shape, const double* stiffness,
                                       const double* v_jxw, double* out, void* stream);
 
+/* Bloch cell Hamiltonians for n_k k-points (the k-point form of hamMatrixKernelLDA,
+   src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:119-280), stored as the matrix
+   applied to the cell vector (interleaved complex, the layout chefsi_operator_create takes):
+   Re out[k][c][I][J] = 0.5 stiffness[I][J] + sum_q (v_jxw[c][q] + |k|^2/2 jxw[c][q]) N_qI N_qJ
+   Im out[k][c][I][J] = -sum_d k_d sum_q jxw[c][q] N_qI shape_grad[d][q][J].
+   shape [n_q][n_e], shape_grad [3][n_q][n_e] (real-space gradients), stiffness [n_e][n_e],
+   v_jxw and jxw [n_cells][n_q] on the device; kpoints_host [n_k][3] (Cartesian, 1/bohr) on
+   the host; out [n_k][n_cells][n_e][n_e] complex on the device. */
+int chefsi_assemble_cell_hamiltonians_bloch(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                            const double* shape, const double* shape_grad,
+                                            const double* stiffness, const double* v_jxw,
+                                            const double* jxw, int32_t n_k,
+                                            const double* kpoints_host, void* out, void* stream);
+
 /* Replace the operator's cell matrices with new unscaled ones (device pointer), as
    computeHamiltonianMatricesAllkpt does each SCF step; derived copies are refreshed. */
 int chefsi_operator_update_cell_matrices(chefsi_operator op, const double* cell_matrices,

@@ -173,6 +173,33 @@ def cell_hamiltonians_direct(K: np.ndarray, N: np.ndarray, vjxw: np.ndarray) -> 
     return H
 
 
+def cell_hamiltonians_bloch_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, vjxw: np.ndarray,
+                                   jxw: np.ndarray, kpoints: np.ndarray) -> np.ndarray:
+    """Bloch cell matrices by the q-loop of the k-point hamMatrixKernelLDA
+    (hamiltonianMatrixCalculatorFlattenedDevice.cc:119-280): per cell the sums val, valRealKpt
+    and valImagKpt[d] over the quadrature points, combined per k-point as
+    0.5 K + val + |k|^2/2 valRealKpt + i k . valImagKpt, then transposed to the matrix applied to
+    the cell vector. Returns [n_k, n_cells, n_e, n_e] complex."""
+    nc, nq = vjxw.shape
+    ne = K.shape[0]
+    kp = np.asarray(kpoints, dtype=np.float64).reshape(-1, 3)
+    out = np.empty((len(kp), nc, ne, ne), dtype=np.complex128)
+    for c in range(nc):
+        val = np.zeros((ne, ne))
+        val_m = np.zeros((ne, ne))
+        val_g = np.zeros((3, ne, ne))
+        for q in range(nq):
+            nn = np.outer(N[q], N[q])
+            val += vjxw[c, q] * nn
+            val_m += jxw[c, q] * nn
+            for d in range(3):
+                val_g[d] -= jxw[c, q] * np.outer(dN[d, q], N[q])   # [I][J]: dN_I N_J
+        for i, k in enumerate(kp):
+            ref = (0.5 * K + val + 0.5 * float(k @ k) * val_m) + 1j * np.tensordot(k, val_g, 1)
+            out[i, c] = ref.T
+    return out
+
+
 def density(cell_map: np.ndarray, inv_sqrt_mass: np.ndarray, shape: np.ndarray, X: np.ndarray,
             occupation: np.ndarray, jxw: np.ndarray | None = None) -> np.ndarray:
     """rho[c][q] = jxw[c][q] sum_i f_i |psi_i(x_q)|^2 with psi_i = M^{-1/2} x_i interpolated by

@@ -33,6 +33,25 @@ def unfolded_setup(pr):
     return emap, n_ext, (slaves, ptr, masters, w), mass_ext
 
 
+def shape_tables(mesh, nq1=None):
+    """Shape values N [n_q][n_e], real-space gradients dN [3][n_q][n_e] and JxW [n_q] at the
+    QGauss(nq1)^3 points of a uniform cell (q = qx + nq1 (qy + nq1 qz), I = a + p1 (b + p1 c))."""
+    nq1 = mesh.p + 3 if nq1 is None else nq1
+    xq, _ = fe.gauss_nodes_weights(nq1)
+    phi, dphi = mesh.shape_1d(xq)
+    q = np.arange(nq1 ** 3)
+    qx, qy, qz = q % nq1, (q // nq1) % nq1, q // (nq1 * nq1)
+    i = np.arange(mesh.nodes_per_cell)
+    p1 = mesh.p + 1
+    ia, ib, ic = i % p1, (i // p1) % p1, i // (p1 * p1)
+    fx, fy, fz = phi[qx][:, ia], phi[qy][:, ib], phi[qz][:, ic]
+    gx, gy, gz = dphi[qx][:, ia] / mesh.h, dphi[qy][:, ib] / mesh.h, dphi[qz][:, ic] / mesh.h
+    N = fx * fy * fz
+    dN = np.stack([gx * fy * fz, fx * gy * fz, fx * fy * gz])
+    _, w3 = mesh.quadrature(nq1)
+    return N, dN, w3
+
+
 def dense_operator(pr) -> np.ndarray:
     cm = pr.cell_map
     H = np.zeros((pr.n_dofs, pr.n_dofs), dtype=pr.cell_mats.dtype)

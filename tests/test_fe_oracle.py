@@ -231,3 +231,20 @@ def test_oracle_density_matrix_response_is_the_divided_difference():
     beta = 1.0 / orc.K_B_HARTREE_PER_KELVIN / T
     fd = 1.0 / (1.0 + np.exp(beta * (eig - mu)))
     assert np.abs(g(eig) - fd).max() < 1e-3
+
+
+def test_oracle_bloch_cell_matrices_match_fe_module():
+    """The direct q-loop of the k-point cell-matrix formula equals the sum-factorised
+    construction the workloads use (both restate hamMatrixKernelLDA's k-point form)."""
+    from tests.helpers import shape_tables
+    k = [0.2, -0.1, 0.3]
+    pr = small_problem(n=2, L=4.0, p=2, wells=2, kpoint=k)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    jxw = np.broadcast_to(w3, (mesh.n_cells, len(w3))).copy()
+    vjxw = pr.info["vjxw"]
+    H = orc.cell_hamiltonians_bloch_direct(mesh.stiffness_cell(), N, dN, vjxw, jxw,
+                                           np.array([k, [0.0, 0.0, 0.0]]))
+    assert np.abs(H[0] - pr.cell_mats).max() < 1e-12 * np.abs(pr.cell_mats).max()
+    real = fe.cell_hamiltonians(mesh, vjxw)
+    assert np.abs(H[1] - real).max() < 1e-12 * np.abs(real).max()
