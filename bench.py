@@ -229,10 +229,9 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     t_ms = start.elapsed_time(end) / args.steps
-    tm = torch.tensor([t_ms], device=dev)
     if world > 1:
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-    t_ms = float(tm.item())
+        from dftfe_gb300 import pools
+        t_ms = pools.max_over_ranks(t_ms)
     phases = solver.timings(True)
 
     # end to end through the public API with host buffers: H2D of X, solve, D2H of X and

@@ -1,0 +1,81 @@
+"""Host-side multi-rank logic: k-point pool and band-group partitions (the reference's
+formulas) and the scalar reductions that follow the eigensolve, over a world_size-2 gloo
+process group on CPU."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+from dftfe_gb300 import pools
+
+
+@pytest.mark.parametrize("n,P,expect", [
+    (8, 2, [(0, 5), (5, 8)]),
+    (4, 3, [(0, 2), (2, 4), (-1, -1)]),
+    (5, 3, [(0, 2), (2, 4), (4, 5)]),
+    (3, 3, [(0, 2), (2, 3), (-1, -1)]),
+    (1, 4, [(0, 1), (-1, -1), (-1, -1), (-1, -1)]),
+    (7, 1, [(0, 7)]),
+])
+def test_kpoint_pool_ranges(n, P, expect):
+    got = pools.kpoint_pool_ranges(n, P)
+    assert got == expect
+    covered = [i for lo, hi in got if lo >= 0 for i in range(lo, hi)]
+    assert covered == list(range(n))
+
+
+def test_band_group_ranges():
+    assert pools.band_group_ranges(10, 3) == [(0, 3), (3, 6), (6, 10)]
+    assert pools.band_group_ranges(8, 1) == [(0, 8)]
+    with pytest.raises(ValueError):
+        pools.band_group_ranges(2, 3)
+
+
+def test_single_process_reductions_are_identity():
+    assert pools.max_over_ranks(2.5) == 2.5
+    assert pools.sum_over_ranks(-1.0) == -1.0
+    assert pools.max_highest_occupied_residual([np.array([0.1, 0.3]), np.array([0.2, 0.05])], 1) == 0.3
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, n_k, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        lo, hi = pools.kpoint_pool_ranges(n_k, world)[rank]
+        mine = range(lo, hi) if lo >= 0 else range(0)
+        # residual norms of the highest occupied state: k-point k has 0.01 * (k + 1)
+        res = [np.array([0.0, 0.01 * (k + 1)]) for k in mine]
+        r = pools.max_highest_occupied_residual(res, 1)
+        s = pools.sum_over_ranks(float(len(mine)))
+        t = pools.max_over_ranks(10.0 + rank)
+        out.put((rank, r, s, t))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("n_k", [5, 1])
+def test_pool_reductions_over_two_gloo_ranks(n_k):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, n_k, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, r, s, t in res:
+        assert abs(r - 0.01 * n_k) < 1e-15     # the last k-point's residual, on every rank
+        assert s == n_k                        # every k-point counted once
+        assert t == 11.0
