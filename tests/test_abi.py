@@ -46,3 +46,23 @@ def test_host_only_entry_points(lib):
     # null handles are rejected with a status, not a crash
     assert l.chefsi_operator_create(None, None) == _lib.CHEFSI_ERR_INVALID
     assert b"null" in l.chefsi_last_error()
+
+
+@pytest.mark.parametrize("compiler,flags", [("gcc", ["-std=c99", "-x", "c"]),
+                                            ("g++", ["-std=c++17", "-x", "c++"])])
+def test_header_compiles_and_links_from_c_and_cpp(lib, tmp_path, compiler, flags):
+    """include/chefsi.h from a C99 and a C++17 consumer (tests/abi/consumer.c): compiled with
+    -Wall -Werror, linked against the library, and run for its host-side calls."""
+    import shutil
+    import subprocess
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not installed")
+    libdir = os.path.dirname(lib._name)
+    exe = tmp_path / f"consumer_{compiler}"
+    cmd = [compiler, *flags, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "abi", "consumer.c"), "-x", "none", "-o", str(exe),
+           "-L", libdir, "-lchefsi_gb300", f"-Wl,-rpath,{libdir}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    ver, m, rejected, _ = out.strip().split("|")
+    assert "sm_103a" in ver and m == "24" and rejected == "1"
