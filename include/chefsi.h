@@ -213,7 +213,10 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
 
 /* Rayleigh-Ritz in the generalised form; eigenvalues to host eig_host (N), X rotated in
    place to the Ritz vectors. If HX_out is non-null it receives A X_rot (FP64, [M][N]); if
-   W_out is non-null it receives the N x N coefficient matrix W = L^{-T} Q (X_rot = X W). */
+   W_out is non-null it receives the N x N coefficient matrix W = L^{-T} Q (X_rot = X W).
+   precision MIXED takes the Gram and rotation products to the tensor cores and keeps the H X
+   that feeds X^T H X in FP64 (the solver's rr_precision default); a solver created with
+   rr_precision = CHEFSI_PREC_FP32_TC uses the three-term tensor-core H X instead. */
 int chefsi_rayleigh_ritz(chefsi_operator op, void* X, int64_t ld, int32_t N, double* eig_host,
                          double* HX_out, double* W_out, int32_t precision, void* stream);
 
