@@ -407,9 +407,26 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
 
     def solve(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, eigenValues=None,
               residualNorms=None, computeResidual: bool = True, useMixedPrec: bool = False,
-              isFirstScf: bool = False):
-        """One CheFSI iteration on X [n_dofs, N] in place; returns (eigenValues, residualNorms)."""
+              isFirstScf: bool = False, eigenVectorsRotFracDensity: torch.Tensor | None = None):
+        """One CheFSI iteration on X [n_dofs, N] in place; returns (eigenValues, residualNorms).
+
+        As the reference's solve, an eigenValues array shorter than N asks for the
+        spectrum-split Rayleigh-Ritz step: its N - len(eigenValues) lowest states are the core
+        states, eigenVectorsRotFracDensity [n_dofs, len(eigenValues)] receives the fractional
+        Ritz vectors, and eigenValues / residualNorms are filled for those."""
         N = X.shape[1]
+        if eigenValues is not None and len(eigenValues) < N:
+            nfr = len(eigenValues)
+            if eigenVectorsRotFracDensity is None:
+                raise ValueError("a spectrum-split solve needs eigenVectorsRotFracDensity")
+            ev, rn, _ = self.solveSpectrumSplit(operatorMatrix, X, N - nfr,
+                                                eigenVectorsRotFracDensity, computeResidual,
+                                                useMixedPrec, isFirstScf)
+            eigenValues[:] = ev
+            if residualNorms is None:
+                return eigenValues, rn
+            residualNorms[:nfr] = rn
+            return eigenValues, residualNorms
         ev = np.zeros(N) if eigenValues is None else eigenValues
         rn = np.zeros(N) if residualNorms is None else residualNorms
         h = self._handle(useMixedPrec)
@@ -432,6 +449,25 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
             h, operatorMatrix.handle, _ptr(X), N, int(Noc), _ptr(XFrac), _np_ptr(ev), _np_ptr(rn),
             int(computeResidual), int(isFirstScf), _stream()))
         return ev, rn, XFrac
+
+    def densityMatrixEigenBasisFirstOrderResponse(self, operatorMatrix: KohnShamOperator,
+                                                  eigenVectors: torch.Tensor, eigenValues,
+                                                  fermiEnergy: float, TVal: float,
+                                                  useMixedPrec: bool = False) -> np.ndarray:
+        """The solver member of the reference
+        (chebyshevOrthogonalizedSubspaceIterationSolverDevice.cc:1083-1189): eigenVectors in the
+        FE basis are scaled by M^{1/2} into the Loewdin basis, the response is applied there
+        (operatorMatrix is the first-order operator H'), and the result is scaled back by
+        M^{-1/2}. Returns densityMatDerFermiEnergy."""
+        sq = operatorMatrix.getSqrtMassVec().reshape(-1, 1)
+        eigenVectors.mul_(sq)
+        try:
+            dmu = densityMatrixEigenBasisFirstOrderResponse(
+                operatorMatrix, eigenVectors, eigenValues, fermiEnergy, TVal,
+                precision=self.params.mixed_precision if useMixedPrec else "fp64")
+        finally:
+            eigenVectors.mul_(operatorMatrix.getInvSqrtMassVec().reshape(-1, 1))
+        return dmu
 
     def solveNoRR(self, operatorMatrix: KohnShamOperator, X: torch.Tensor, numberPasses: int = 1,
                   useMixedPrec: bool = False, isFirstScf: bool = False):
