@@ -72,6 +72,7 @@ class Params(ctypes.Structure):
         ("lanczos_steps", ctypes.c_int32), ("reproducible", ctypes.c_int32),
         ("first_scf_degree_scale", ctypes.c_double), ("keep_hx", ctypes.c_int32),
         ("rr_precision", ctypes.c_int32), ("ss_frac_reduced", ctypes.c_int32),
+        ("rr_block", ctypes.c_int32), ("rr_slab_rows", ctypes.c_int32),
     ]
 
 

@@ -361,6 +361,10 @@ class SolverParams:
     # spectrum split in mixed mode: the block of X^T H X coupling the fractional states from
     # an FP64 H X (False, useMixedPrecXTHXSpectrumSplit's map) or from the rr_precision H X
     spectrum_split_frac_reduced: bool = False
+    # memory-bounded Rayleigh-Ritz: column block (0 automatic, > 0 forced, < 0 never) and
+    # dofs per row slab (0 automatic)
+    rr_block: int = 0
+    rr_slab_rows: int = 0
 
 
 class ChebyshevOrthogonalizedSubspaceIterationSolver:
@@ -385,6 +389,8 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
             p.keep_hx = int(self.params.keep_hx)
             p.rr_precision = _prec(self.params.rr_precision)
             p.ss_frac_reduced = int(self.params.spectrum_split_frac_reduced)
+            p.rr_block = int(self.params.rr_block)
+            p.rr_slab_rows = int(self.params.rr_slab_rows)
             h = ctypes.c_void_p()
             check(self._lib.chefsi_solver_create(ctypes.byref(p), ctypes.byref(h)))
             self._h[key] = h

@@ -445,6 +445,171 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
   return CHEFSI_OK;
 }
 
+// Rayleigh-Ritz of rayleigh_ritz_real with its workspaces bounded by a column block of rr_block
+// vectors and a row slab of dofs, for blocks whose full-size workspaces do not fit the GPU (4096
+// vectors over 4.1M dofs: 134 GB for X alone). The reference forms X^T H X the same way, one
+// wfcBlockSize column block at a time (XtHX, kohnShamDFTOperatorDevice.cc:4003-4157):
+//   S = X^T X: the tensor-core Gram accumulated over row slabs (each slab split with its own
+//     column exponents) or the FP64 / FP32 Gram directly;
+//   Hp[j0:, j0:j0+b] = X[:, j0:]^T H X[:, j0:j0+b] per column block, H X of one block at a time;
+//   X <- X W by row slabs (in place; the rotation reads the slab's split);
+//   residual norms from a fresh H X of each rotated block (no full-size H X is kept).
+int rayleigh_ritz_real_blocked(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld,
+                               int N, int prec, double* res, cudaStream_t st) {
+  const int64_t M = op->n_dofs;
+  const bool tcd = prec == CHEFSI_PREC_MIXED && dense_tc_available();
+  const int blk = std::max(1, std::min(s->p.rr_block > 0 ? s->p.rr_block : 256, N));
+  int64_t ms = s->p.rr_slab_rows > 0 ? s->p.rr_slab_rows
+                                     : std::max<int64_t>(64, (int64_t)(1ll << 30) / std::max(1, N));
+  ms = std::min<int64_t>(M, std::max<int64_t>(64, (ms + 63) / 64 * 64));
+  double* S = s->S.ensure((size_t)N * N);
+  double* Hp = s->Hp.ensure((size_t)N * N);
+  double* T1 = s->T1.ensure((size_t)N * N);
+  double* Z = s->Z.ensure((size_t)N * N);
+  double* W = s->W.ensure((size_t)N * N);
+  double* w = s->evals.ensure(N);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[1], st));
+  CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+  if (tcd) {
+    for (int64_t r0 = 0; r0 < M; r0 += ms) {
+      const int64_t mr = std::min(ms, M - r0);
+      tc_exponents<double>(X + r0 * ld, ld, mr, N, s->tx, st);
+      tc_split_transposed<double>(X + r0 * ld, ld, mr, N, s->tx, st);
+      tc_gram(s->tx, nullptr, S, N, true, s->tcw, st);
+    }
+  } else {
+    gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
+  }
+  symmetrize_lower(S, N, st);
+  if (fault_injected("not_spd")) {
+    k_negate_diag0<<<1, 1, 0, st>>>(S);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower(S, N, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+    return rc;
+  }
+  trtri_lower(S, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
+  const int rrp = s->p.rr_precision;
+  const bool tc3 = is_mixed(prec) && rrp == CHEFSI_PREC_FP32_TC && tc_split_usable(op, blk);
+  const bool tc2 = is_mixed(prec) && rrp == CHEFSI_PREC_MIXED && tc_split_usable(op, blk);
+  const bool hx32 = is_mixed(prec) && (rrp == CHEFSI_PREC_FP32 || rrp == CHEFSI_PREC_FP32_TC || tc2);
+  float* x32 = hx32 ? s->Xb32.ensure((size_t)M * blk) : nullptr;
+  float* y32 = hx32 ? s->Yb32.ensure((size_t)M * blk) : nullptr;
+  double* HXb = s->HX.ensure((size_t)M * blk);
+  // H X of columns [j0, j0 + b) into y32 (reduced precision) or HXb (FP64), leading dim b;
+  // with to_f64 the reduced result is also widened into HXb
+  auto hx_block = [&](int j0, int b, bool to_f64) {
+    if (hx32) {
+      double scale = 1.0;
+      if (tc2 || tc3) {
+        double* sc = s->scal.ensure(1);
+        absmax_block_f64(X + j0, ld, M, b, sc, st);
+        double amax = 0.0;
+        CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CHEFSI_CUDA(cudaStreamSynchronize(st));
+        if (amax > 0.0 && std::isfinite(amax))
+          scale = std::ldexp(1.0, (tc3 ? 14 : 8) - (int)std::ceil(std::log2(amax)));
+      }
+      copy_block<double, float>(X + j0, ld, x32, b, M, b, scale, st);
+      bool done = false;
+      if (tc3)
+        done = hx_tc3(op, x32, b, y32, b, b, 1.0 / scale, false, st);
+      else if (tc2)
+        done = hx_tc(op, x32, b, y32, b, b, 1.0 / scale, false, st);
+      if (!done) hx_f32(op, x32, b, y32, b, b, 1.0 / scale, false, st);
+      if (to_f64) copy_block<float, double>(y32, b, HXb, b, M, b, 1.0, st);
+    } else {
+      hx_f64(op, X + j0, ld, HXb, b, b, 1.0, false, st);
+    }
+  };
+  CHEFSI_CUDA(cudaMemsetAsync(Hp, 0, sizeof(double) * N * N, st));
+  for (int j0 = 0; j0 < N; j0 += blk) {
+    const int b = std::min(blk, N - j0);
+    const int nr = N - j0;
+    hx_block(j0, b, !tcd);
+    double* C = Hp + (int64_t)j0 * N + j0;
+    if (tcd) {
+      for (int64_t r0 = 0; r0 < M; r0 += ms) {
+        const int64_t mr = std::min(ms, M - r0);
+        tc_exponents<double>(X + r0 * ld + j0, ld, mr, nr, s->tx, st);
+        tc_split_transposed<double>(X + r0 * ld + j0, ld, mr, nr, s->tx, st);
+        if (hx32) {
+          tc_exponents<float>(y32 + r0 * b, b, mr, b, s->th, st);
+          tc_split_transposed<float>(y32 + r0 * b, b, mr, b, s->th, st);
+        } else {
+          tc_exponents<double>(HXb + r0 * b, b, mr, b, s->th, st);
+          tc_split_transposed<double>(HXb + r0 * b, b, mr, b, s->th, st);
+        }
+        tc_gram(s->tx, &s->th, C, N, false, s->tcw, st);
+      }
+    } else {
+      gram_f64(X + j0, ld, HXb, b, M, nr, b, C, N, prec, false, st);
+    }
+  }
+  symmetrize_lower(Hp, N, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[3], st));
+  gemm_f64('N', 'N', N, N, N, 1.0, S, N, Hp, N, 0.0, T1, N, CHEFSI_PREC_FP64, st);
+  gemm_f64('N', 'T', N, N, N, 1.0, T1, N, S, N, 0.0, Hp, N, CHEFSI_PREC_FP64, st);
+  symmetrize_lower(Hp, N, st);
+  rc = syevd(Hp, N, w, Z, st);
+  if (rc != CHEFSI_OK) return rc;
+  gemm_f64('T', 'N', N, N, N, 1.0, S, N, Z, N, 0.0, W, N, CHEFSI_PREC_FP64, st);
+  CHEFSI_CUDA(cudaEventRecord(s->ev[4], st));
+  if (tcd) {
+    for (int64_t r0 = 0; r0 < M; r0 += ms) {
+      const int64_t mr = std::min(ms, M - r0);
+      tc_exponents<double>(X + r0 * ld, ld, mr, N, s->tx, st);
+      tc_split_rows<double>(X + r0 * ld, ld, mr, N, s->tx, st);
+      tc_rotate(s->tx, W, N, N, X + r0 * ld, ld, s->tcw, st);
+    }
+  } else {
+    rotate_rows(s, X, ld, M, N, W, prec, st);
+  }
+  rc = tc_dense_check_error(s->tcw, st);
+  if (rc != CHEFSI_OK) {
+    set_last_error("tensor-core Rayleigh-Ritz products: a bounded device wait expired");
+    return rc;
+  }
+  CHEFSI_CUDA(cudaEventRecord(s->ev[5], st));
+  if (res) {
+    for (int j0 = 0; j0 < N; j0 += blk) {
+      const int b = std::min(blk, N - j0);
+      hx_block(j0, b, true);
+      residual_norms_f64(X + j0, ld, HXb, b, M, b, w + j0, res + j0, st);
+    }
+  }
+  if (hx32) {
+    const int tc = tc_check_error(op, st);
+    if (tc != CHEFSI_OK) {
+      set_last_error("tensor-core HX: a bounded device wait expired");
+      return tc;
+    }
+  }
+  return CHEFSI_OK;
+}
+
+// Whether a real Rayleigh-Ritz step of N vectors takes the blocked form: forced by rr_block > 0,
+// never with rr_block < 0, otherwise when the full-size workspaces it still has to allocate
+// (about 30 bytes per dof and vector in the mixed mode, 8 in FP64) exceed 90% of the free
+// device memory.
+bool rr_blocked(chefsi_solver_s* s, chefsi_operator_s* op, int N, int prec) {
+  if (s->p.rr_block > 0) return true;
+  if (s->p.rr_block < 0) return false;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const double mn = (double)op->n_dofs * N;
+  const double need = (is_mixed(prec) ? 30.0 : 8.0) * mn;
+  const double held = 8.0 * s->HX.n + 4.0 * (double)(s->Xb32.n + s->Yb32.n) +
+                      2.0 * (double)(s->tx.hi.n + s->tx.lo.n + s->th.hi.n + s->th.lo.n);
+  return need > held + 0.9 * (double)fr;
+}
+
 // Spectrum-split Rayleigh-Ritz (rayleighRitzGEPSpectrumSplitDirect,
 // src/linAlg/rayleighRitzDevice.cc:822-1455) for a real operator:
 //   S = X^T X = L L^T;  X <- X L^{-T} (Cholesky-GS, X stays in this orthonormal basis);
@@ -1040,6 +1205,8 @@ chefsi_params default_params() {
   p.keep_hx = 1;
   p.rr_precision = CHEFSI_PREC_FP64;
   p.ss_frac_reduced = 0;
+  p.rr_block = 0;
+  p.rr_slab_rows = 0;
   return p;
 }
 
@@ -1625,6 +1792,10 @@ static int solve_after_filter(chefsi_solver_s* s, chefsi_operator_s* op, void* X
     if (rc != CHEFSI_OK) return rc;
     if (compute_residual)
       residual_norms_c64((const cplx*)X, N, (const cplx*)s->HX.ptr, N, M, N, s->evals.ptr, res, st);
+  } else if (rr_blocked(s, op, N, prec)) {
+    int rc = rayleigh_ritz_real_blocked(s, op, (double*)X, N, N, prec,
+                                        compute_residual ? res : nullptr, st);
+    if (rc != CHEFSI_OK) return rc;
   } else {
     int rc = rayleigh_ritz_real(s, op, (double*)X, N, N, prec, true, st);
     if (rc != CHEFSI_OK) return rc;

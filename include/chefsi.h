@@ -146,6 +146,12 @@ typedef struct {
                                    fractionally occupied states from an FP64 H X (the
                                    precision map of useMixedPrecXTHXSpectrumSplit); 1 keeps
                                    the rr_precision H X there too */
+  int32_t rr_block;             /* real Rayleigh-Ritz step in column blocks (X^T H X one block
+                                   of H X at a time, Gram and rotation by row slabs, no
+                                   full-size H X): 0 (default) when the full-size workspaces
+                                   would not fit the free device memory, > 0 always with
+                                   blocks of that many vectors, < 0 never */
+  int32_t rr_slab_rows;         /* dofs per row slab of the blocked step (0: about 2^30 / N) */
 } chefsi_params;
 
 const char* chefsi_last_error(void);
