@@ -39,7 +39,8 @@ EXPORTS = [
     "chefsi_solver_timings", "chefsi_solver_set_profiling", "chefsi_solver_hx_stats",
     "chefsi_solve", "chefsi_solve_spectrum_split", "chefsi_solve_batched", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
     "chefsi_axpby", "chefsi_convert_block", "chefsi_density", "chefsi_assemble_cell_hamiltonians",
-    "chefsi_assemble_cell_hamiltonians_bloch", "chefsi_operator_update_cell_matrices",
+    "chefsi_assemble_cell_hamiltonians_bloch", "chefsi_assemble_cell_hamiltonians_gga",
+    "chefsi_operator_update_cell_matrices",
     "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract",
 ]
 
@@ -116,6 +117,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_convert_block": ([i32, vp, i64, i32, vp, i64, i64, i32, f64, vp], ctypes.c_int),
         "chefsi_density": ([vp, vp, i64, i32, vp, i32, vp, vp, vp, i32, i32, vp], ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians": ([i32, i32, i32, vp, vp, vp, vp, vp], ctypes.c_int),
+        "chefsi_assemble_cell_hamiltonians_gga": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp],
+                                                  ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians_bloch": ([i32, i32, i32, vp, vp, vp, vp, vp, i32, vp, vp,
                                                      vp], ctypes.c_int),
         "chefsi_operator_update_cell_matrices": ([vp, vp, vp], ctypes.c_int),

@@ -306,6 +306,23 @@ def assemble_cell_hamiltonians(shape: torch.Tensor, stiffness: torch.Tensor,
     return out
 
 
+def assemble_cell_hamiltonians_gga(shape: torch.Tensor, shape_grad: torch.Tensor,
+                                   stiffness: torch.Tensor, v_jxw: torch.Tensor,
+                                   gga_jxw: torch.Tensor) -> torch.Tensor:
+    """GGA cell Hamiltonians [n_cells, n_e, n_e] on the GPU (hamMatrixKernelGGAMemOpt, real):
+    gga_jxw is derExcWithSigmaTimesGradRhoJxW [n_cells, n_q, 3]."""
+    nc, nq = v_jxw.shape
+    ne = stiffness.shape[0]
+    if tuple(gga_jxw.shape) != (nc, nq, 3):
+        raise ValueError("gga_jxw must be [n_cells, n_q, 3]")
+    g = gga_jxw.contiguous()
+    out = torch.empty((nc, ne, ne), dtype=torch.float64, device=v_jxw.device)
+    check(_lib.load().chefsi_assemble_cell_hamiltonians_gga(
+        nc, ne, nq, _ptr(shape), _ptr(shape_grad), _ptr(stiffness), _ptr(v_jxw), _ptr(g),
+        _ptr(out), _stream()))
+    return out
+
+
 def assemble_cell_hamiltonians_bloch(shape: torch.Tensor, shape_grad: torch.Tensor,
                                      stiffness: torch.Tensor, v_jxw: torch.Tensor,
                                      jxw: torch.Tensor, kpoints) -> torch.Tensor:

@@ -125,6 +125,80 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// GGA cell Hamiltonians, real (the formula of hamMatrixKernelGGAMemOpt,
+// src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:283-456):
+//   out[c][I][J] = 0.5 K[I][J] + sum_q ( v[c][q] N_qI N_qJ
+//                  + 2 sum_d g[c][q][d] (dN_d[q][I] N_qJ + N_qI dN_d[q][J]) )
+// (g = derExcWithSigmaTimesGradRhoJxW). Folded into two operand families per quadrature point:
+// A0_I = v N_I + 2 sum_d g_d dN_dI against N_J, and A_d,I = 2 g_d N_I against dN_dJ.
+__global__ void __launch_bounds__(256)
+    k_assemble_gga(int n_cells, int n_e, int n_q, const double* __restrict__ N,
+                   const double* __restrict__ dN, const double* __restrict__ K,
+                   const double* __restrict__ v, const double* __restrict__ g,
+                   double* __restrict__ out, int nt) {
+  __shared__ double A[4][16][T + 1];
+  __shared__ double Bt[4][16][T + 1];
+  const int64_t blk = blockIdx.x;
+  const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
+  const int c = (int)(blk / ((int64_t)nt * nt));
+  const int i0 = ti * T, j0 = tj * T;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 per thread
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  const double* vc = v + (int64_t)c * n_q;
+  const double* gc = g + (int64_t)c * n_q * 3;
+  for (int q0 = 0; q0 < n_q; q0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * T; idx += 256) {
+      const int qq = idx / T, k = idx % T;
+      const int q = q0 + qq;
+      const bool okq = q < n_q;
+      const bool oki = okq && i0 + k < n_e, okj = okq && j0 + k < n_e;
+      const double g0 = okq ? gc[3 * q] : 0.0, g1 = okq ? gc[3 * q + 1] : 0.0,
+                   g2 = okq ? gc[3 * q + 2] : 0.0;
+      if (oki) {
+        const int64_t iI = (int64_t)q * n_e + i0 + k;
+        const int64_t qn = (int64_t)n_q * n_e;
+        const double ni = N[iI];
+        A[0][qq][k] = ni * vc[q] + 2.0 * (g0 * dN[iI] + g1 * dN[qn + iI] + g2 * dN[2 * qn + iI]);
+        A[1][qq][k] = 2.0 * g0 * ni;
+        A[2][qq][k] = 2.0 * g1 * ni;
+        A[3][qq][k] = 2.0 * g2 * ni;
+      } else {
+        A[0][qq][k] = A[1][qq][k] = A[2][qq][k] = A[3][qq][k] = 0.0;
+      }
+      if (okj) {
+        const int64_t iJ = (int64_t)q * n_e + j0 + k;
+        const int64_t qn = (int64_t)n_q * n_e;
+        Bt[0][qq][k] = N[iJ];
+        Bt[1][qq][k] = dN[iJ];
+        Bt[2][qq][k] = dN[qn + iJ];
+        Bt[3][qq][k] = dN[2 * qn + iJ];
+      } else {
+        Bt[0][qq][k] = Bt[1][qq][k] = Bt[2][qq][k] = Bt[3][qq][k] = 0.0;
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int qq = 0; qq < 16; ++qq)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int ii = ty + 16 * r, jj = tx + 16 * s;
+          double t = acc[r][s];
+#pragma unroll
+          for (int f = 0; f < 4; ++f) t = fma(A[f][qq][ii], Bt[f][qq][jj], t);
+          acc[r][s] = t;
+        }
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int I = i0 + ty + 16 * r, J = j0 + tx + 16 * s;
+      if (I < n_e && J < n_e)
+        out[((int64_t)c * n_e + I) * n_e + J] = 0.5 * K[(int64_t)I * n_e + J] + acc[r][s];
+    }
+}
+
 // G[c][I][J] += alpha * sum_b d[gI] u[gI][b] d[gJ] w[gJ][b], g = map[c][.]
 __global__ void __launch_bounds__(256)
     k_cell_outer(const int* __restrict__ map, int n_e, const double* __restrict__ d,
@@ -207,6 +281,16 @@ void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const 
   CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
   k_assemble_bloch<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w, n_k, kpts,
                                                      reinterpret_cast<double2*>(out), nt);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void assemble_cells_gga(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                        const double* K, const double* v, const double* g, double* out,
+                        cudaStream_t st) {
+  const int nt = (n_e + T - 1) / T;
+  const int64_t blocks = (int64_t)n_cells * nt * nt;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
+  k_assemble_gga<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, g, out, nt);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -1627,6 +1627,19 @@ int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, i
   CHEFSI_API_END
 }
 
+int chefsi_assemble_cell_hamiltonians_gga(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                          const double* shape, const double* shape_grad,
+                                          const double* stiffness, const double* v_jxw,
+                                          const double* gga_jxw, double* out, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(shape && shape_grad && stiffness && v_jxw && gga_jxw && out && n_cells > 0 &&
+                     nodes_per_cell > 0 && n_q > 0,
+                 "bad argument");
+  assemble_cells_gga(n_cells, nodes_per_cell, n_q, shape, shape_grad, stiffness, v_jxw, gga_jxw,
+                     out, as_stream(stream));
+  CHEFSI_API_END
+}
+
 int chefsi_assemble_cell_hamiltonians_bloch(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
                                             const double* shape, const double* shape_grad,
                                             const double* stiffness, const double* v_jxw,

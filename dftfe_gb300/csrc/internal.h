@@ -252,6 +252,9 @@ void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaS
 // adjoint / assembly building blocks (adjoint.cu)
 void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
                     const double* v, double* out, cudaStream_t st);
+void assemble_cells_gga(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                        const double* K, const double* v, const double* g, double* out,
+                        cudaStream_t st);
 void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const double* dN,
                           const double* K, const double* v, const double* w, int n_k,
                           const double* kpts, double* out, cudaStream_t st);

@@ -285,6 +285,17 @@ int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, i
                                       const double* shape, const double* stiffness,
                                       const double* v_jxw, double* out, void* stream);
 
+/* GGA cell Hamiltonians, real (hamMatrixKernelGGAMemOpt,
+   src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:283-456):
+   out[c][I][J] = 0.5 stiffness[I][J] + sum_q ( v_jxw[c][q] N_qI N_qJ
+                  + 2 sum_d gga_jxw[c][q][d] (shape_grad[d][q][I] N_qJ + N_qI shape_grad[d][q][J]) )
+   with gga_jxw = derExcWithSigmaTimesGradRhoJxW [n_cells][n_q][3] and shape_grad
+   [3][n_q][n_e] the real-space shape-function gradients; device pointers. */
+int chefsi_assemble_cell_hamiltonians_gga(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
+                                          const double* shape, const double* shape_grad,
+                                          const double* stiffness, const double* v_jxw,
+                                          const double* gga_jxw, double* out, void* stream);
+
 /* Bloch cell Hamiltonians for n_k k-points (the k-point form of hamMatrixKernelLDA,
    src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:119-280), stored as the matrix
    applied to the cell vector (interleaved complex, the layout chefsi_operator_create takes):

@@ -173,6 +173,25 @@ def cell_hamiltonians_direct(K: np.ndarray, N: np.ndarray, vjxw: np.ndarray) -> 
     return H
 
 
+def cell_hamiltonians_gga_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, vjxw: np.ndarray,
+                                 gjxw: np.ndarray) -> np.ndarray:
+    """Real GGA cell matrices by the q-loop of hamMatrixKernelGGAMemOpt
+    (hamiltonianMatrixCalculatorFlattenedDevice.cc:283-456): per cell and quadrature point
+    vEffJxW N_I N_J + 2 sum_d derExcWithSigmaTimesGradRhoJxW_d (dN_dI N_J + dN_dJ N_I), plus
+    0.5 K. gjxw [n_cells][n_q][3]; returns [n_cells, n_e, n_e]."""
+    nc, nq = vjxw.shape
+    out = np.empty((nc,) + K.shape)
+    for c in range(nc):
+        val = np.zeros(K.shape)
+        for q in range(nq):
+            val += vjxw[c, q] * np.outer(N[q], N[q])
+            for d in range(3):
+                gd = np.outer(dN[d, q], N[q])
+                val += 2.0 * gjxw[c, q, d] * (gd + gd.T)
+        out[c] = 0.5 * K + val
+    return out
+
+
 def cell_hamiltonians_bloch_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, vjxw: np.ndarray,
                                    jxw: np.ndarray, kpoints: np.ndarray) -> np.ndarray:
     """Bloch cell matrices by the q-loop of the k-point hamMatrixKernelLDA

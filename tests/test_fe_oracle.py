@@ -248,3 +248,21 @@ def test_oracle_bloch_cell_matrices_match_fe_module():
     assert np.abs(H[0] - pr.cell_mats).max() < 1e-12 * np.abs(pr.cell_mats).max()
     real = fe.cell_hamiltonians(mesh, vjxw)
     assert np.abs(H[1] - real).max() < 1e-12 * np.abs(real).max()
+
+
+def test_oracle_gga_cell_matrices():
+    """The GGA q-loop against a matrix form of the same sums, its symmetry, and its LDA limit."""
+    from tests.helpers import shape_tables
+    pr = small_problem(n=2, L=4.0, p=2, wells=2)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    vjxw = pr.info["vjxw"]
+    g = np.random.default_rng(3).standard_normal((mesh.n_cells, len(w3), 3)) * w3[None, :, None]
+    K = mesh.stiffness_cell()
+    H = orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, g)
+    G = np.einsum('cqd,dqi,qj->cij', g, dN, N)
+    ref = 0.5 * K[None] + np.einsum('cq,qi,qj->cij', vjxw, N, N) + 2.0 * (G + G.transpose(0, 2, 1))
+    assert np.abs(H - ref).max() < 1e-12 * np.abs(ref).max()
+    assert np.abs(H - H.transpose(0, 2, 1)).max() < 1e-13 * np.abs(H).max()
+    lda = orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, np.zeros_like(g))
+    assert np.abs(lda - fe.cell_hamiltonians(mesh, vjxw)).max() < 1e-12 * np.abs(lda).max()
