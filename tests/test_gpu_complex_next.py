@@ -103,18 +103,3 @@ def test_bloch_cell_assembly_matches_oracle(C, p):
     assert rel(out, ref) < 1e-12
     assert rel(out[0], pr.cell_mats) < 1e-12
 
-
-@pytest.mark.parametrize("p", [2, 4])
-def test_gga_cell_assembly_matches_oracle(C, p):
-    """On-device real GGA cell matrices against the oracle's q-loop (p = 4: ragged tiles)."""
-    from tests.helpers import shape_tables
-    pr = small_problem(n=2, L=4.0, p=p, wells=2)
-    mesh = pr.mesh
-    N, dN, w3 = shape_tables(mesh)
-    vjxw = pr.info["vjxw"]
-    g = np.random.default_rng(p).standard_normal((mesh.n_cells, len(w3), 3)) * w3[None, :, None]
-    K_ = mesh.stiffness_cell()
-    ref = orc.cell_hamiltonians_gga_direct(K_, N, dN, vjxw, g)
-    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
-    out = C.assemble_cell_hamiltonians_gga(t(N), t(dN), t(K_), t(vjxw), t(g)).cpu().numpy()
-    assert rel(out, ref) < 1e-12

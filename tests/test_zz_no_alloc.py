@@ -6,7 +6,7 @@ synchronisation). It keeps its workspace in one file-scope device array, so it i
 to N <= 256. This test calls both entry points through the C ABI (ctypes on
 libchefsi_gb300.so) on two matrices in a row -- the second call finds the first call's
 leftovers in the shared array -- and requires the same eigenvalues (1e-12 relative) and the
-same eigenvectors up to sign (1e-10). This file is collected last on purpose.
+same eigenvectors up to sign (1e-10). This file is collected after the parity files on purpose.
 """
 import ctypes
 

@@ -1,0 +1,38 @@
+"""Real GGA cell Hamiltonians on the device (chefsi_assemble_cell_hamiltonians_gga) against the
+oracle's q-loop of the GGA cell-matrix formula. Tolerance 1e-12 relative (FP64 sums in another
+order). Collected after the other GPU files.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as orc
+from tests.helpers import small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def C(cuda):
+    from dftfe_gb300 import chefsi
+    return chefsi
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_gga_cell_assembly_matches_oracle(C, p):
+    """On-device real GGA cell matrices against the oracle's q-loop (p = 4: ragged tiles)."""
+    from tests.helpers import shape_tables
+    pr = small_problem(n=2, L=4.0, p=p, wells=2)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    vjxw = pr.info["vjxw"]
+    g = np.random.default_rng(p).standard_normal((mesh.n_cells, len(w3), 3)) * w3[None, :, None]
+    K_ = mesh.stiffness_cell()
+    ref = orc.cell_hamiltonians_gga_direct(K_, N, dN, vjxw, g)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    out = C.assemble_cell_hamiltonians_gga(t(N), t(dN), t(K_), t(vjxw), t(g)).cpu().numpy()
+    assert rel(out, ref) < 1e-12
