@@ -325,16 +325,26 @@ def assemble_cell_hamiltonians_gga(shape: torch.Tensor, shape_grad: torch.Tensor
 
 def assemble_cell_hamiltonians_bloch(shape: torch.Tensor, shape_grad: torch.Tensor,
                                      stiffness: torch.Tensor, v_jxw: torch.Tensor,
-                                     jxw: torch.Tensor, kpoints) -> torch.Tensor:
+                                     jxw: torch.Tensor, kpoints,
+                                     gga_jxw: torch.Tensor | None = None) -> torch.Tensor:
     """Bloch cell Hamiltonians [n_k, n_cells, n_e, n_e] (complex128) for every k-point, on the
-    GPU (the k-point form of hamMatrixKernelLDA; the matrix applied to the cell vector)."""
+    GPU (the k-point form of hamMatrixKernelLDA, or of hamMatrixKernelGGAMemOpt with gga_jxw
+    [n_cells, n_q, 3]; the matrix applied to the cell vector)."""
     nc, nq = v_jxw.shape
     ne = stiffness.shape[0]
     k = np.ascontiguousarray(np.asarray(kpoints, dtype=np.float64).reshape(-1, 3))
     out = torch.empty((k.shape[0], nc, ne, ne), dtype=torch.complex128, device=v_jxw.device)
-    check(_lib.load().chefsi_assemble_cell_hamiltonians_bloch(
-        nc, ne, nq, _ptr(shape), _ptr(shape_grad), _ptr(stiffness), _ptr(v_jxw), _ptr(jxw),
-        k.shape[0], _np_ptr(k), _ptr(out), _stream()))
+    if gga_jxw is None:
+        check(_lib.load().chefsi_assemble_cell_hamiltonians_bloch(
+            nc, ne, nq, _ptr(shape), _ptr(shape_grad), _ptr(stiffness), _ptr(v_jxw), _ptr(jxw),
+            k.shape[0], _np_ptr(k), _ptr(out), _stream()))
+        return out
+    if tuple(gga_jxw.shape) != (nc, nq, 3):
+        raise ValueError("gga_jxw must be [n_cells, n_q, 3]")
+    g = gga_jxw.contiguous()
+    check(_lib.load().chefsi_assemble_cell_hamiltonians_bloch_gga(
+        nc, ne, nq, _ptr(shape), _ptr(shape_grad), _ptr(stiffness), _ptr(v_jxw), _ptr(g),
+        _ptr(jxw), k.shape[0], _np_ptr(k), _ptr(out), _stream()))
     return out
 
 

@@ -62,16 +62,23 @@ __global__ void __launch_bounds__(256)
 //   Re out[k][c][I][J] = 0.5 K[I][J] + sum_q v[c][q] N_qI N_qJ + |k|^2/2 sum_q w[c][q] N_qI N_qJ
 //   Im out[k][c][I][J] = -sum_d k_d sum_q w[c][q] N_qI dN_d[q][J]
 // (w = JxW, dN_d the real-space shape-function gradients). The five cell sums are formed once
-// per cell tile and combined for every k-point in the epilogue.
+// per cell tile and combined for every k-point in the epilogue. GGA (the k-point form of
+// hamMatrixKernelGGAMemOpt, :458-655) adds to the real part the gradient terms
+// 2 sum_q sum_d g[c][q][d] (dN_d[q][I] N_qJ + N_qI dN_d[q][J]), g = derExcWithSigmaTimesGradRhoJxW,
+// folded as for the real GGA kernel: 2 sum_d g_d dN_dI into the potential operand and three
+// more operands 2 g_d N_I against the gradient operands already loaded.
+template <bool GGA>
 __global__ void __launch_bounds__(256)
     k_assemble_bloch(int n_cells, int n_e, int n_q, const double* __restrict__ N,
                      const double* __restrict__ dN, const double* __restrict__ K,
-                     const double* __restrict__ v, const double* __restrict__ w, int n_k,
-                     const double* __restrict__ kpts, double2* __restrict__ out, int nt) {
+                     const double* __restrict__ v, const double* __restrict__ w,
+                     const double* __restrict__ g, int n_k, const double* __restrict__ kpts,
+                     double2* __restrict__ out, int nt) {
   __shared__ double Av[16][T + 1];
   __shared__ double Aw[16][T + 1];
   __shared__ double Bn[16][T + 1];
   __shared__ double Bd[3][16][T + 1];
+  __shared__ double Ag[GGA ? 3 : 1][16][T + 1];
   const int64_t blk = blockIdx.x;
   const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
   const int c = (int)(blk / ((int64_t)nt * nt));
@@ -89,6 +96,16 @@ __global__ void __launch_bounds__(256)
       const double ni = oki ? N[(int64_t)q * n_e + i0 + k] : 0.0;
       Av[qq][k] = oki ? ni * vc[q] : 0.0;
       Aw[qq][k] = oki ? ni * wc[q] : 0.0;
+      if constexpr (GGA) {
+        if (oki) {
+          const double* gq = g + ((int64_t)c * n_q + q) * 3;
+          const int64_t iI = (int64_t)q * n_e + i0 + k, qn = (int64_t)n_q * n_e;
+          for (int d = 0; d < 3; ++d) Ag[d][qq][k] = 2.0 * gq[d] * ni;
+          Av[qq][k] += 2.0 * (gq[0] * dN[iI] + gq[1] * dN[qn + iI] + gq[2] * dN[2 * qn + iI]);
+        } else {
+          for (int d = 0; d < 3; ++d) Ag[d][qq][k] = 0.0;
+        }
+      }
       Bn[qq][k] = okj ? N[(int64_t)q * n_e + j0 + k] : 0.0;
       for (int d = 0; d < 3; ++d)
         Bd[d][qq][k] = okj ? dN[((int64_t)d * n_q + q) * n_e + j0 + k] : 0.0;
@@ -106,6 +123,10 @@ __global__ void __launch_bounds__(256)
           sm[r][s] = fma(aw, Bn[qq][jj], sm[r][s]);
 #pragma unroll
           for (int d = 0; d < 3; ++d) sg[d][r][s] = fma(aw, Bd[d][qq][jj], sg[d][r][s]);
+          if constexpr (GGA) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) sv[r][s] = fma(Ag[d][qq][ty + 16 * r], Bd[d][qq][jj], sv[r][s]);
+          }
         }
       }
     __syncthreads();
@@ -275,12 +296,18 @@ void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double
 
 void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const double* dN,
                           const double* K, const double* v, const double* w, int n_k,
-                          const double* kpts, double* out, cudaStream_t st) {
+                          const double* kpts, double* out, cudaStream_t st, const double* g) {
   const int nt = (n_e + T - 1) / T;
   const int64_t blocks = (int64_t)n_cells * nt * nt;
   CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
-  k_assemble_bloch<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w, n_k, kpts,
-                                                     reinterpret_cast<double2*>(out), nt);
+  if (g)
+    k_assemble_bloch<true><<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w, g,
+                                                           n_k, kpts,
+                                                           reinterpret_cast<double2*>(out), nt);
+  else
+    k_assemble_bloch<false><<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w,
+                                                            nullptr, n_k, kpts,
+                                                            reinterpret_cast<double2*>(out), nt);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -1659,6 +1659,27 @@ int chefsi_assemble_cell_hamiltonians_bloch(int32_t n_cells, int32_t nodes_per_c
   CHEFSI_API_END
 }
 
+int chefsi_assemble_cell_hamiltonians_bloch_gga(int32_t n_cells, int32_t nodes_per_cell,
+                                                int32_t n_q, const double* shape,
+                                                const double* shape_grad, const double* stiffness,
+                                                const double* v_jxw, const double* gga_jxw,
+                                                const double* jxw, int32_t n_k,
+                                                const double* kpoints_host, void* out,
+                                                void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(shape && shape_grad && stiffness && v_jxw && gga_jxw && jxw && kpoints_host &&
+                     out && n_cells > 0 && nodes_per_cell > 0 && n_q > 0 && n_k > 0,
+                 "bad argument");
+  cudaStream_t st = as_stream(stream);
+  DeviceBuffer<double> kd((size_t)3 * n_k);
+  CHEFSI_CUDA(cudaMemcpyAsync(kd.ptr, kpoints_host, sizeof(double) * 3 * n_k,
+                              cudaMemcpyHostToDevice, st));
+  assemble_cells_bloch(n_cells, nodes_per_cell, n_q, shape, shape_grad, stiffness, v_jxw, jxw, n_k,
+                       kd.ptr, (double*)out, st, gga_jxw);
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  CHEFSI_API_END
+}
+
 int chefsi_operator_update_cell_matrices(chefsi_operator op, const double* cell_matrices,
                                          void* stream) {
   CHEFSI_API_BEGIN

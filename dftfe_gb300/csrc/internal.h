@@ -255,9 +255,11 @@ void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double
 void assemble_cells_gga(int n_cells, int n_e, int n_q, const double* N, const double* dN,
                         const double* K, const double* v, const double* g, double* out,
                         cudaStream_t st);
+// g (nullable): derExcWithSigmaTimesGradRhoJxW [n_cells][n_q][3] for the GGA terms
 void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const double* dN,
                           const double* K, const double* v, const double* w, int n_k,
-                          const double* kpts, double* out, cudaStream_t st);
+                          const double* kpts, double* out, cudaStream_t st,
+                          const double* g = nullptr);
 // G_c += alpha * sum_b weights[b] (D u_b)_c (D w_b)_c^T (weights null: 1), D = M^{-1/2}
 void cell_outer(chefsi_operator_s* op, const double* u, const double* w, int64_t ld, int B,
                 double alpha, double* G, cudaStream_t st, const double* weights = nullptr);

@@ -310,6 +310,18 @@ int chefsi_assemble_cell_hamiltonians_bloch(int32_t n_cells, int32_t nodes_per_c
                                             const double* jxw, int32_t n_k,
                                             const double* kpoints_host, void* out, void* stream);
 
+/* The GGA form of chefsi_assemble_cell_hamiltonians_bloch (hamMatrixKernelGGAMemOpt, complex,
+   src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:458-655): the real part also
+   carries 2 sum_q sum_d gga_jxw[c][q][d] (shape_grad[d][q][I] N_qJ + N_qI shape_grad[d][q][J]),
+   gga_jxw [n_cells][n_q][3] on the device. */
+int chefsi_assemble_cell_hamiltonians_bloch_gga(int32_t n_cells, int32_t nodes_per_cell,
+                                                int32_t n_q, const double* shape,
+                                                const double* shape_grad, const double* stiffness,
+                                                const double* v_jxw, const double* gga_jxw,
+                                                const double* jxw, int32_t n_k,
+                                                const double* kpoints_host, void* out,
+                                                void* stream);
+
 /* Replace the operator's cell matrices with new unscaled ones (device pointer), as
    computeHamiltonianMatricesAllkpt does each SCF step; derived copies are refreshed. */
 int chefsi_operator_update_cell_matrices(chefsi_operator op, const double* cell_matrices,

@@ -193,12 +193,15 @@ def cell_hamiltonians_gga_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, v
 
 
 def cell_hamiltonians_bloch_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, vjxw: np.ndarray,
-                                   jxw: np.ndarray, kpoints: np.ndarray) -> np.ndarray:
+                                   jxw: np.ndarray, kpoints: np.ndarray,
+                                   gjxw: np.ndarray | None = None) -> np.ndarray:
     """Bloch cell matrices by the q-loop of the k-point hamMatrixKernelLDA
     (hamiltonianMatrixCalculatorFlattenedDevice.cc:119-280): per cell the sums val, valRealKpt
     and valImagKpt[d] over the quadrature points, combined per k-point as
     0.5 K + val + |k|^2/2 valRealKpt + i k . valImagKpt, then transposed to the matrix applied to
-    the cell vector. Returns [n_k, n_cells, n_e, n_e] complex."""
+    the cell vector. Returns [n_k, n_cells, n_e, n_e] complex. With gjxw [n_cells][n_q][3]
+    (derExcWithSigmaTimesGradRhoJxW) val also carries the GGA terms of hamMatrixKernelGGAMemOpt
+    (:458-655), 2 sum_d g_d (dN_dI N_J + dN_dJ N_I)."""
     nc, nq = vjxw.shape
     ne = K.shape[0]
     kp = np.asarray(kpoints, dtype=np.float64).reshape(-1, 3)
@@ -213,6 +216,9 @@ def cell_hamiltonians_bloch_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray,
             val_m += jxw[c, q] * nn
             for d in range(3):
                 val_g[d] -= jxw[c, q] * np.outer(dN[d, q], N[q])   # [I][J]: dN_I N_J
+                if gjxw is not None:
+                    gd = np.outer(dN[d, q], N[q])
+                    val += 2.0 * gjxw[c, q, d] * (gd + gd.T)
         for i, k in enumerate(kp):
             ref = (0.5 * K + val + 0.5 * float(k @ k) * val_m) + 1j * np.tensordot(k, val_g, 1)
             out[i, c] = ref.T

@@ -266,3 +266,21 @@ def test_oracle_gga_cell_matrices():
     assert np.abs(H - H.transpose(0, 2, 1)).max() < 1e-13 * np.abs(H).max()
     lda = orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, np.zeros_like(g))
     assert np.abs(lda - fe.cell_hamiltonians(mesh, vjxw)).max() < 1e-12 * np.abs(lda).max()
+
+
+def test_oracle_bloch_gga_is_bloch_lda_plus_the_real_gga_terms():
+    from tests.helpers import shape_tables
+    k = [0.2, -0.1, 0.3]
+    pr = small_problem(n=2, L=4.0, p=2, wells=2, kpoint=k)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    jxw = np.broadcast_to(w3, (mesh.n_cells, len(w3))).copy()
+    vjxw = pr.info["vjxw"]
+    g = np.random.default_rng(4).standard_normal((mesh.n_cells, len(w3), 3)) * w3[None, :, None]
+    K = mesh.stiffness_cell()
+    kp = np.array([k])
+    lda = orc.cell_hamiltonians_bloch_direct(K, N, dN, vjxw, jxw, kp)[0]
+    gga = orc.cell_hamiltonians_bloch_direct(K, N, dN, vjxw, jxw, kp, g)[0]
+    real_term = orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, g) - \
+        orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, np.zeros_like(g))
+    assert np.abs(gga - lda - real_term).max() < 1e-12 * np.abs(gga).max()

@@ -36,3 +36,26 @@ def test_gga_cell_assembly_matches_oracle(C, p):
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
     out = C.assemble_cell_hamiltonians_gga(t(N), t(dN), t(K_), t(vjxw), t(g)).cpu().numpy()
     assert rel(out, ref) < 1e-12
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_bloch_gga_cell_assembly_matches_oracle(C, p):
+    """On-device Bloch GGA cell matrices for two k-points against the oracle's q-loop, and the
+    GGA-free launch of the same entry family unchanged."""
+    from tests.helpers import shape_tables
+    K = [0.2, -0.1, 0.3]
+    pr = small_problem(n=2, L=4.0, p=p, wells=2, kpoint=K)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    jxw = np.broadcast_to(w3, (mesh.n_cells, len(w3))).copy()
+    vjxw = pr.info["vjxw"]
+    g = np.random.default_rng(p + 10).standard_normal((mesh.n_cells, len(w3), 3)) * w3[None, :, None]
+    kp = np.array([K, [0.5, 0.25, -0.4]])
+    K_ = mesh.stiffness_cell()
+    ref = orc.cell_hamiltonians_bloch_direct(K_, N, dN, vjxw, jxw, kp, g)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    out = C.assemble_cell_hamiltonians_bloch(t(N), t(dN), t(K_), t(vjxw), t(jxw), kp,
+                                             gga_jxw=t(g)).cpu().numpy()
+    assert rel(out, ref) < 1e-12
+    lda = C.assemble_cell_hamiltonians_bloch(t(N), t(dN), t(K_), t(vjxw), t(jxw), kp[:1])
+    assert rel(lda.cpu().numpy()[0], pr.cell_mats) < 1e-12
