@@ -7,11 +7,16 @@ Names and argument meaning follow the reference:
   ``getSqrtMassVec`` / ``getInvSqrtMassVec`` (:68-72);
 * ``ChebyshevOrthogonalizedSubspaceIterationSolver`` --
   ``chebyshevOrthogonalizedSubspaceIterationSolverDevice``
-  (include/chebyshevOrthogonalizedSubspaceIterationSolverDevice.h:37-166): ``solve``,
-  ``solveNoRR``, ``reinitSpectrumBounds``;
+  (include/chebyshevOrthogonalizedSubspaceIterationSolverDevice.h:37-166): ``solve`` (with
+  the spectrum-split branch), ``solveNoRR``, ``densityMatrixEigenBasisFirstOrderResponse``,
+  ``reinitSpectrumBounds``;
 * ``lanczosLowerUpperBoundEigenSpectrum``, ``chebyshevFilter``, ``fillOverlapMatrix``,
-  ``rayleighRitzGEP``, ``pseudoGramSchmidtOrthogonalization``, ``computeEigenResidualNorm``
-  -- the linearAlgebraOperationsDevice functions of the same names.
+  ``rayleighRitzGEP``, ``rayleighRitzGEPSpectrumSplitDirect``,
+  ``densityMatrixEigenBasisFirstOrderResponse``, ``pseudoGramSchmidtOrthogonalization``,
+  ``computeEigenResidualNorm`` -- the linearAlgebraOperationsDevice functions of the same
+  names; ``copyValueType1ArrToValueType2Arr`` (deviceKernelsGeneric);
+* ``density`` (densityCalculator), the cell-matrix assembly functions
+  (hamiltonianMatrixCalculatorFlattenedDevice), ``solve_batched`` (the k-point loop).
 
 Vectors are torch CUDA tensors in DFT-FE's flattened layout [n_dofs, n_vectors]
 (vector index fastest). Every call goes through libchefsi_gb300.so; there is no CPU path.
