@@ -191,7 +191,9 @@ def run_ours(args):
     N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
     op = chefsi.KohnShamOperator.from_problem(pr)
     lo, blow, up = first_bounds(chefsi, op, N)
-    params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=N, wfcBlockSize=N,
+    # the large workload (4096 vectors) is filtered in blocks of 256, the others in one block
+    blk = 256 if args.workload == "large" else N
+    params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=blk, wfcBlockSize=blk,
                                  mixed_precision="mixed", rr_precision=args.rr_precision)
     solver = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params)
     solver.reinitSpectrumBounds(lo, blow, up)
