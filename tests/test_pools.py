@@ -79,3 +79,32 @@ def test_pool_reductions_over_two_gloo_ranks(n_k):
         assert abs(r - 0.01 * n_k) < 1e-15     # the last k-point's residual, on every rank
         assert s == n_k                        # every k-point counted once
         assert t == 11.0
+
+
+def test_partitions_cover_every_index_once():
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.given(st.integers(0, 500), st.integers(1, 64))
+    @hyp.settings(max_examples=300, deadline=None)
+    def kpoints(n, P):
+        got = pools.kpoint_pool_ranges(n, P)
+        assert len(got) == P
+        covered = [i for lo, hi in got if lo >= 0 for i in range(lo, hi)]
+        assert covered == list(range(n))
+        # non-empty pools come first, each a contiguous block of at most n // P + 1
+        sizes = [hi - lo for lo, hi in got if lo >= 0]
+        assert all(0 < s <= n // P + 1 for s in sizes)
+
+    @hyp.given(st.integers(1, 500), st.integers(1, 64))
+    @hyp.settings(max_examples=300, deadline=None)
+    def bands(n, G):
+        if n // G == 0:
+            with pytest.raises(ValueError):
+                pools.band_group_ranges(n, G)
+            return
+        got = pools.band_group_ranges(n, G)
+        assert [i for lo, hi in got for i in range(lo, hi)] == list(range(n))
+
+    kpoints()
+    bands()
