@@ -66,3 +66,20 @@ def test_header_compiles_and_links_from_c_and_cpp(lib, tmp_path, compiler, flags
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     ver, m, rejected, _ = out.strip().split("|")
     assert "sm_103a" in ver and m == "24" and rejected == "1"
+
+
+def test_cpp_host_layer_compiles_links_and_runs(lib, tmp_path):
+    """include/chefsi.hpp (the C++ host layer shaped like DFT-FE's operator and solver classes)
+    from a C++17 consumer: -Wall -Wextra -Werror, linked against the library, host logic run."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not installed")
+    libdir = os.path.dirname(lib._name)
+    exe = tmp_path / "consumer_cpp"
+    cmd = ["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "abi", "consumer.cpp"), "-o", str(exe),
+           "-L", libdir, "-lchefsi_gb300", f"-Wl,-rpath,{libdir}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    assert "empty operator" in out and "failures=0" in out
