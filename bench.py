@@ -114,63 +114,218 @@ def first_bounds(chefsi, op, n_wfc):
     return lo, min(blow, lo + 0.5 * (up - lo)), up
 
 
-def cpu_sample(pr, m, N, max_seconds=25.0):
-    """Time the CPU oracle's HX on a bounded block of vectors and extrapolate one CheFSI
-    iteration: (m + 2) HX over all N vectors + the dense RR products (numpy BLAS, timed on
-    an (M x n_s) sample and scaled by (N/n_s)^2)."""
-    from oracle import oracle as orc
-    op = orc.OracleOperator(pr.cell_map, pr.cell_mats, pr.inv_sqrt_mass, pr.n_dofs,
-                            projectors=pr.nonlocal_)
-    threads = orc.lib().oracle_num_threads()
-    rng = np.random.default_rng(0)
-    B = 8
-    X = rng.uniform(-1, 1, (pr.n_dofs, B))
-    op.HX(X)  # warm
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
-        op.HX(X)
-        reps += 1
-        if time.perf_counter() - t0 > max_seconds * 0.6 or reps >= 3:
-            break
-    t_hx = (time.perf_counter() - t0) / reps
-    ns = min(N, 128)
-    Xs = rng.standard_normal((pr.n_dofs, ns))
-    t0 = time.perf_counter()
-    S = Xs.T @ Xs
-    _ = Xs @ S
-    t_gemm = (time.perf_counter() - t0) / 2.0   # one (M x ns x ns) product
-    t_iter = (m + 2) * t_hx * (N / B) + 4 * t_gemm * (N / ns) ** 2
-    return {"value": t_iter, "unit": "s/iter", "cores": threads, "kind": "port",
-            "sample": f"oracle HX on {B} of {N} vectors x{reps} ({t_hx:.2f} s each) and a "
-                      f"{pr.n_dofs}x{ns}x{ns} numpy GEMM; iteration = (m+2) HX x N/{B} + "
-                      f"4 GEMM x (N/{ns})^2"}
+CPU_SAMPLE_VECTORS = 8
+
+
+class OracleIterations:
+    """Real CheFSI iterations of the CPU oracle (the FP64 restatement of the reference's CPU
+    solve: filter, RR-GEP, residual norms, bounds update) on a bounded sample of the workload:
+    the workload's operator (same mesh, cell matrices and projectors) with n_s of its N
+    vectors. The first-call bounds use the workload's N, so the filter polynomial is the one
+    the full problem would get."""
+
+    def __init__(self, pr, m, n_s=CPU_SAMPLE_VECTORS):
+        from oracle import oracle as orc
+        self.orc = orc
+        self.pr, self.m, self.n_s = pr, m, min(n_s, pr.n_wfc)
+        self.op = orc.OracleOperator(pr.cell_map, pr.cell_mats, pr.inv_sqrt_mass, pr.n_dofs,
+                                     projectors=pr.nonlocal_)
+        self.threads = orc.lib().oracle_num_threads()
+        v0 = np.random.default_rng(0).uniform(0.0, 1.0, pr.n_dofs)
+        lo, up = orc.lanczos_bounds(self.op, v0, 20)
+        blow = lo + (up - lo) / pr.n_dofs * pr.n_wfc * 200.0
+        self.state = orc.SolverState(a0=lo, b_low=min(blow, lo + 0.5 * (up - lo)), b_up=up)
+        self.X = np.ascontiguousarray(pr.initial_vectors(self.n_s))
+        self.steps = []
+
+    def step(self):
+        t0 = time.perf_counter()
+        ev, res, self.X = self.orc.solve(self.op, self.X, self.state, m=self.m)
+        dt = time.perf_counter() - t0
+        self.steps.append(dt)
+        return dt
+
+    def extrapolated(self, t_step):
+        """Scale a sample iteration to all N vectors: the filter and the HX are linear in N;
+        the dense Rayleigh-Ritz products (X^T X, X^T H X, X W: 3 x 2 M N^2 flops) are timed as
+        one numpy (M x 128 x 128) product and scaled by (N/128)^2 (labelled as an estimate)."""
+        pr, N = self.pr, self.pr.n_wfc
+        ns = min(N, 128)
+        Xs = np.random.default_rng(1).standard_normal((pr.n_dofs, ns))
+        t0 = time.perf_counter()
+        S = Xs.T @ Xs
+        _ = Xs @ S
+        t_gemm = (time.perf_counter() - t0) / 2.0
+        return {"value": t_step * N / self.n_s + 3 * t_gemm * (N / ns) ** 2, "unit": "s/iter",
+                "kind": "extrapolated",
+                "how": f"sample iteration x N/{self.n_s} + 3 dense (M x N x N) products from a "
+                       f"timed {pr.n_dofs}x{ns}x{ns} numpy GEMM x (N/{ns})^2"}
+
+    def describe(self):
+        return (f"real oracle CheFSI iterations (Chebyshev filter degree {self.m}, RR-GEP, "
+                f"residual norms, bounds update) on the workload's operator "
+                f"({self.pr.n_dofs} dofs) with {self.n_s} of its {self.pr.n_wfc} vectors")
+
+
+def cpu_baseline_line(pr, m):
+    """cpu_baseline of the bench line: two real oracle iterations on the bounded sample (the
+    second timed), and the labelled extrapolation to the full workload."""
+    it = OracleIterations(pr, m)
+    it.step()
+    t = it.step()
+    return {"value": t, "unit": "s/iter", "cores": it.threads, "kind": "port",
+            "sample": it.describe(), "n_wfc_sample": it.n_s, "steps_run": 2,
+            "extrapolated_full_n": it.extrapolated(t)}
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU CheFSI (the oracle port of it; the reference
+    itself cannot be built here) timed on the machine's host cores. Every step is one real
+    iteration on the bounded sample; nothing in `value` is scaled."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     pr = build_workload(args.workload, args.seed)
     m = pr.cheb_degree
-    N = pr.n_wfc
-    vals = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        base = cpu_sample(pr, m, N, max_seconds=20.0 if i < args.warmup else 25.0)
-        if i >= args.warmup:
-            vals.append(base["value"])
-    v = float(np.median(vals))
+    it = OracleIterations(pr, m)
+    for _ in range(args.warmup):
+        it.step()
+    t0 = time.perf_counter()
+    vals = [it.step() for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
+    v = float(np.mean(vals))
     line = {"metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "n_dofs": pr.n_dofs, "n_wfc": N,
-                       "cheb_degree": m},
-            "cpu_baseline": dict(base, value=v),
+            "config": {"workload": args.workload, "n_dofs": pr.n_dofs, "n_wfc": pr.n_wfc,
+                       "n_wfc_sample": it.n_s, "cheb_degree": m},
+            "steps_run": args.warmup + args.steps, "timed_wall_s": wall,
+            "cpu_baseline": {"value": v, "unit": "s/iter", "cores": it.threads, "kind": "port",
+                             "sample": it.describe()},
+            "extrapolated_full_n": it.extrapolated(v),
             "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def e2e_pipeline(step, X, n_steps):
+    """The iteration end to end through the public API with host buffers: every step copies
+    its input block from pinned host memory to the device, runs chefsi_solve (through the
+    Python mirror) and copies the rotated block back to pinned host memory. Two device
+    buffers and two copy streams pipeline the copies: the upload of step i+1 and the download
+    of step i-1 run on the copy engines while step i solves. Also measured: each copy alone
+    (the host link's rates)."""
+    import torch
+    M, N = X.shape
+    host_in = torch.empty((M, N), dtype=torch.float64, pin_memory=True)
+    host_in.copy_(X)
+    host_out = torch.empty((M, N), dtype=torch.float64, pin_memory=True)
+    bufs = [torch.empty_like(X), torch.empty_like(X)]
+    comp = torch.cuda.current_stream()
+    up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    # the copies alone
+    a, b, c = ev(), ev(), ev()
+    torch.cuda.synchronize()
+    a.record(comp)
+    bufs[0].copy_(host_in, non_blocking=True)
+    b.record(comp)
+    host_out.copy_(bufs[0], non_blocking=True)
+    c.record(comp)
+    torch.cuda.synchronize()
+    h2d_ms, d2h_ms = a.elapsed_time(b), b.elapsed_time(c)
+    uploaded = [ev() for _ in range(n_steps)]
+    solved = [ev() for _ in range(n_steps)]
+    downloaded = [None, None]
+    torch.cuda.synchronize()
+    t0, t1 = ev(), ev()
+    t0.record(comp)
+    up_s.wait_stream(comp)
+    with torch.cuda.stream(up_s):
+        bufs[0].copy_(host_in, non_blocking=True)
+        uploaded[0].record(up_s)
+    for i in range(n_steps):
+        if i + 1 < n_steps:
+            nb = (i + 1) % 2
+            if downloaded[nb] is not None:
+                up_s.wait_event(downloaded[nb])
+            with torch.cuda.stream(up_s):
+                bufs[nb].copy_(host_in, non_blocking=True)
+                uploaded[i + 1].record(up_s)
+        comp.wait_event(uploaded[i])
+        step(bufs[i % 2])
+        solved[i].record(comp)
+        down_s.wait_event(solved[i])
+        with torch.cuda.stream(down_s):
+            host_out.copy_(bufs[i % 2], non_blocking=True)
+            d = ev()
+            d.record(down_s)
+        downloaded[i % 2] = d
+    comp.wait_stream(down_s)
+    t1.record(comp)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / n_steps
+    return {"value": e2e_ms / 1e3, "unit": "s/iter", "h2d_bytes_per_step": M * N * 8,
+            "d2h_bytes_per_step": M * N * 8 + 2 * N * 8, "steps": n_steps,
+            "pipeline": "2 device buffers; upload of step i+1 and download of step i-1 overlap "
+                        "the solve of step i (copy streams)",
+            "h2d_ms_alone": h2d_ms, "d2h_ms_alone": d2h_ms,
+            "h2d_gbs": M * N * 8 / (h2d_ms * 1e-3) / 1e9, "d2h_gbs": M * N * 8 / (d2h_ms * 1e-3) / 1e9}
+
+
+def fp64_leg(pr, op, X, solver, params, up):
+    """The FP64 leg of the headline: from the bench's current block and bounds, one CheFSI
+    iteration of the project's FP64 GPU path and one mixed iteration, each timed with CUDA
+    events (not estimated); the mixed Ritz values against the FP64 ones (occupied and all),
+    the largest principal angle between the occupied Ritz subspaces and the largest occupied
+    residual norms."""
+    import torch
+    from dftfe_gb300 import chefsi
+    N, nocc = pr.n_wfc, pr.n_occupied
+    a0, bl, bu, _ = solver_bounds(solver)
+    out, occ = {}, {}
+    torch.cuda.empty_cache()
+    for mode in ("fp64", "mixed"):
+        # the FP64 iteration on a solver of its own (freed after it), the mixed one on the
+        # bench's solver (its workspaces exist already)
+        sv = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params) if mode == "fp64" else solver
+        sv.reinitSpectrumBounds(a0, bl, bu)
+        Xc = X.clone()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        e, r = sv.solve(op, Xc, useMixedPrec=(mode == "mixed"))
+        e1.record()
+        torch.cuda.synchronize()
+        out[mode] = (e.copy(), r.copy(), e0.elapsed_time(e1) / 1e3, sv.timings(mode == "mixed"))
+        occ[mode] = Xc[:, :nocc].contiguous()
+        del Xc, sv
+        torch.cuda.empty_cache()
+    s = torch.linalg.svdvals(occ["fp64"].T @ occ["mixed"]).cpu().numpy()
+    angle = float(np.arccos(np.clip(s.min(), -1.0, 1.0)))
+    del occ
+    d = np.abs(out["mixed"][0] - out["fp64"][0])
+    return {"fp64_s_per_iter": out["fp64"][2], "mixed_s_per_iter_same_block": out["mixed"][2],
+            "speedup_mixed_vs_fp64": out["fp64"][2] / out["mixed"][2],
+            "ritz_err_vs_fp64_Ha": {"occupied": float(d[:nocc].max()), "all": float(d.max()),
+                                    "occupied_states": nocc},
+            "subspace_angle_rad": angle,
+            "res_occ_max": {"mixed": float(out["mixed"][1][:nocc].max()),
+                            "fp64": float(out["fp64"][1][:nocc].max())},
+            "fp64_phases_ms": out["fp64"][3],
+            "fp64_leg": "one FP64 and one mixed CheFSI iteration from the bench's final block and "
+                        "bounds (CUDA events); Ritz errors against the FP64 iteration"}
+
+
+def solver_bounds(solver):
+    import ctypes
+    from dftfe_gb300 import _lib
+    lib = _lib.load()
+    a0, bl, bu, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+    _lib.check(lib.chefsi_solver_get_bounds(solver._handle(True), ctypes.byref(a0), ctypes.byref(bl),
+                                            ctypes.byref(bu), ctypes.byref(d)))
+    return a0.value, bl.value, bu.value, d.value
 
 
 def run_ours(args):
@@ -236,22 +391,8 @@ def run_ours(args):
         t_ms = pools.max_over_ranks(t_ms)
     phases = solver.timings(True)
 
-    # end to end through the public API with host buffers: H2D of X, solve, D2H of X and
-    # of the eigenvalues / residual norms
-    host = torch.empty((M, N), dtype=torch.float64, pin_memory=True)
-    host.copy_(X)
-    Xd = torch.empty_like(X)
-    e2e_steps = max(1, min(args.steps, 2))
-    torch.cuda.synchronize()
-    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s2.record()
-    for _ in range(e2e_steps):
-        Xd.copy_(host, non_blocking=True)
-        ev, res = step(Xd)
-        host.copy_(Xd, non_blocking=True)
-    e2.record()
-    torch.cuda.synchronize()
-    e2e_ms = s2.elapsed_time(e2) / e2e_steps
+    e2e = e2e_pipeline(step, X, max(2, min(args.steps, 4)))
+    torch.cuda.empty_cache()
 
     hx_flops, hx_bytes = hx_algorithmic(pr, N)
     hbm, bf16, src = peaks()
@@ -279,15 +420,14 @@ def run_ours(args):
                                       "(profiles/cell_hx_tc_mixed_traffic.md)",
                      "kernel": "cell_hx_tc_kernel (+ nonlocal, filter HX)",
                      "algorithmic_bytes_per_launch": hx_bytes},
-        "e2e": {"value": e2e_ms / 1e3, "unit": "s/iter", "h2d_bytes_per_step": M * N * 8,
-                "d2h_bytes_per_step": M * N * 8 + 2 * N * 8},
+        "e2e": e2e,
         "clocks": clk.summary(),
     }
     line["gpu_launches"] = int(launches)
-    if args.fp64_compare:
-        line["fp64"] = fp64_compare(pr, op, lo, blow, up, m, N, dev)
+    if not args.no_fp64_leg and world == 1:
+        line.update(fp64_leg(pr, op, X, solver, params, up))
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_sample(pr, m, N)
+        line["cpu_baseline"] = cpu_baseline_line(pr, m)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -628,24 +768,6 @@ def run_adjoint_check(args):
     return 0
 
 
-def fp64_compare(pr, op, lo, blow, up, m, N, dev):
-    """One FP64 HX over all N vectors, timed, and the FP64 iteration estimate."""
-    import torch
-    from dftfe_gb300 import chefsi
-    X = torch.rand((pr.n_dofs, N), device=dev, dtype=torch.float64)
-    Y = torch.empty_like(X)
-    op.HX(X[:, :64].contiguous(), Y[:, :64].contiguous())
-    torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record()
-    op.HX(X, Y)
-    e.record()
-    torch.cuda.synchronize()
-    hx64 = s.elapsed_time(e)
-    return {"hx_fp64_ms": hx64, "iter_fp64_ms_est": (m + 2) * hx64,
-            "note": "FP64 iteration estimated as (m+2) FP64 HX; dense FP64 steps excluded"}
-
-
 def run_bloch(args):
     """Batched Bloch workload: 32 independent complex Hamiltonians (6^3..14^3 cells at FE
     degree 4, 64..512 wavefunctions, 4..16 wells, k uniform in the first Brillouin zone).
@@ -737,7 +859,8 @@ def main():
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
-    ap.add_argument("--fp64-compare", action="store_true")
+    ap.add_argument("--no-fp64-leg", action="store_true",
+                    help="skip the FP64 iteration and the Ritz-error comparison after the timed steps")
     ap.add_argument("--density-check", action="store_true",
                     help="time chefsi_density on the workload and check 16 cells against a direct sum")
     ap.add_argument("--spectrum-split-check", action="store_true",

@@ -9,14 +9,16 @@
 // file-scope device array instead, sized for N <= kNoAllocMaxN.
 //
 // The array's name is a host-side stand-in in host code, so its device address is looked up
-// once per device with cudaGetSymbolAddress (the first call on a device does this), and that
-// address is what the kernels receive. Every call shares the array and it keeps the previous
-// call's contents; everything that must start at zero is cleared on each call. Calls that
-// overlap on the GPU (different streams, or different threads on one device) race on the
-// array and must be serialised by the caller.
+// with cudaGetSymbolAddress on the current device, and that address is what the kernels
+// receive. The CUDA runtime loads this library's device code lazily: the first look-up on a
+// device loads the module and places the array in device memory there (about 3.3 MB, kept
+// until the process exits), so a caller whose pool allocator takes the device memory makes
+// one warm-up call first. The look-up is repeated on every call (it is a host-side query once
+// the module is loaded), so the address stays right after a cudaDeviceReset. Every call shares
+// the array and it keeps the previous call's contents; everything that must start at zero is
+// cleared on each call. Calls that overlap on the GPU (different streams, or different
+// threads on one device) race on the array and must be serialised by the caller.
 #include "internal.h"
-
-#include <mutex>
 
 namespace chefsi {
 
@@ -38,27 +40,17 @@ constexpr size_t kScratchDoubles = kOffTol + 32;
 
 static __device__ __align__(256) double g_syevd_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
-
-// device address of g_syevd_scratch on the current device (looked up on first use)
+// device address of g_syevd_scratch on the current device (the first look-up on a device
+// loads the module there)
 double* scratch_on_current_device() {
-  int dev = 0;
-  CHEFSI_CUDA(cudaGetDevice(&dev));
-  CHEFSI_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_syevd_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      cudaGetLastError();
-      throw Error(CHEFSI_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") +
-                                       cudaGetErrorString(e));
-    }
-    g_scratch_ptr[dev] = static_cast<double*>(p);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_syevd_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    cudaGetLastError();
+    throw Error(CHEFSI_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") +
+                                     cudaGetErrorString(e));
   }
-  return g_scratch_ptr[dev];
+  return static_cast<double*>(p);
 }
 
 // cluster tolerance 1e-5 * max_j (|d_j| + |e_{j-1}| + |e_j|), computed on the device

@@ -110,7 +110,10 @@ typedef struct {
   const double* inv_sqrt_mass;  /* [n_dofs] M^{-1/2} */
   /* constraints: slave rows in CSR form over master dofs (0 rows = none). When present the
      operator runs DFT-FE's sequence (scale, distribute, cell products, adjoint distribute,
-     scale); otherwise the mass scaling is folded into the cell matrices. */
+     scale); otherwise the mass scaling is folded into the cell matrices. The inhomogeneities
+     g_s of the reference's distribute (utils/constraintMatrixInfoDevice.cc:62-63) are taken
+     as zero: x_s = sum_m w_sm x_m, which is the reference's case for wavefunctions (their
+     constraints are homogeneous; only the electrostatics carries nonzero g_s). */
   int32_t n_constrained;
   const int32_t* constrained_ids; /* [n_constrained] */
   const int32_t* constraint_ptr;  /* [n_constrained+1] */
@@ -206,11 +209,14 @@ int chefsi_heevd(int32_t N, double* A, double* w, double* Z, void* stream);
    For callers that cannot allocate device memory during a solve -- an application whose
    pool allocator owns the GPU's memory, or one that cannot take the device-wide
    synchronisation of cudaFree. The workspace is a file-scope device array sized for
-   N <= 256 (about 3.3 MB, held by every device that loads the library until the process
-   exits); larger N returns CHEFSI_ERR_INVALID. The first call on each device looks up the
-   array's device address (cudaGetSymbolAddress): make that first call before any stream
-   capture. All calls share the array, so calls that overlap on the GPU race; serialise them.
-   Same arguments and results as chefsi_syevd. */
+   N <= 256 (about 3.3 MB per device); larger N returns CHEFSI_ERR_INVALID. The CUDA runtime
+   loads the library's device code lazily, so the array is placed in device memory when the
+   first call on a device looks up its address (cudaGetSymbolAddress): make one warm-up call
+   (any N <= 256) on each device before the caller's pool reserves the device memory, and
+   before any stream capture. From then on the array stays allocated on that device until the
+   process exits, and later calls allocate nothing. Every call synchronises its stream (it
+   reads the cluster tolerance back to the host). All calls share the array, so calls that
+   overlap on the GPU race; serialise them. Same arguments and results as chefsi_syevd. */
 int chefsi_syevd_noalloc(int32_t N, double* A, double* w, double* Z, void* stream);
 
 /* Cholesky-Gram-Schmidt: S = X^H X, S = L L^H, X <- X L^{-H}. */

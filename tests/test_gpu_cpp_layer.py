@@ -1,0 +1,128 @@
+"""The DFT-FE-facing C++ layer (include/chefsi.hpp) on the GPU, from a C++ process.
+
+tests/abi/solve_gpu.cpp is compiled with g++ against chefsi.hpp and linked with the library
+and the CUDA runtime; it builds the operator from the seeded problem's arrays, allocates X with
+cudaMalloc and runs solve() the way kohnShamEigenSpaceCompute does: a first filtering call
+(Lanczos bounds, the first-call bLow), three more full Rayleigh-Ritz solves, then two solves
+that ask for N - Noc eigenvalues (the spectrum-split branch). It writes the bounds each solve
+used and the Ritz values and residual norms it returned. The oracle repeats the same
+iterations on the CPU with those bounds (full: oracle.solve; split: the oracle's filter and
+spectrum-split Rayleigh-Ritz).
+
+Tolerances: FP64 every Ritz value and residual norm within 1e-8; mixed the occupied Ritz values
+of the full solves within 1e-6 Ha and the fractional Ritz values within 1e-4 Ha.
+"""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from tests.helpers import oracle_op, small_problem
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+N_FULL, N_SPLIT, DEGREE = 4, 2, 10
+
+
+def cuda_home():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "include", "cuda_runtime.h")):
+            return c
+    pytest.skip("CUDA toolkit headers not found")
+
+
+@pytest.fixture(scope="module")
+def exe(cuda, tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not installed")
+    from dftfe_gb300 import build
+    libdir = os.path.dirname(build.build())
+    ch = cuda_home()
+    out = tmp_path_factory.mktemp("cpp") / "solve_gpu"
+    cudalib = [os.path.join(ch, d) for d in ("lib64", "lib") if os.path.isdir(os.path.join(ch, d))]
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ch, "include"),
+           os.path.join(ROOT, "tests", "abi", "solve_gpu.cpp"), "-o", str(out),
+           "-L", libdir, "-lchefsi_gb300", f"-Wl,-rpath,{libdir}"]
+    for d in cudalib:
+        cmd += ["-L", d, f"-Wl,-rpath,{d}"]
+    cmd += ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(out)
+
+
+def write_inputs(pr, d, n_core):
+    nl = pr.nonlocal_
+    np.ascontiguousarray(pr.cell_map, np.int32).tofile(d / "cell_map.bin")
+    np.ascontiguousarray(pr.cell_mats, np.float64).tofile(d / "cell_mats.bin")
+    np.ascontiguousarray(pr.sqrt_mass, np.float64).tofile(d / "sqrt_mass.bin")
+    np.ascontiguousarray(pr.inv_sqrt_mass, np.float64).tofile(d / "inv_sqrt_mass.bin")
+    np.ascontiguousarray(nl.ptr, np.int32).tofile(d / "atom_ptr.bin")
+    np.ascontiguousarray(nl.dofs, np.int32).tofile(d / "atom_dofs.bin")
+    np.ascontiguousarray(nl.values, np.float64).tofile(d / "atom_proj.bin")
+    np.ascontiguousarray(nl.couplings, np.float64).tofile(d / "couplings.bin")
+    np.ascontiguousarray(pr.initial_vectors(), np.float64).tofile(d / "X0.bin")
+    nc, ne = pr.cell_map.shape
+    (d / "meta.txt").write_text(
+        f"{pr.n_dofs} {nc} {ne} {nl.n_atoms} {nl.n_proj} {len(nl.dofs)} {pr.n_wfc} {N_FULL} "
+        f"{N_SPLIT} {n_core} {DEGREE}\n")
+
+
+def read_outputs(d):
+    rows = []
+    for line in (d / "out.txt").read_text().split("\n"):
+        if not line.strip():
+            continue
+        t = line.split()
+        n = int(t[4])
+        v = np.array([float(x) for x in t[5:]])
+        rows.append(((float(t[1]), float(t[2]), float(t[3])), v[:n], v[n:2 * n]))
+    return rows
+
+
+def oracle_replay(pr, rows, n_core):
+    """The same solves on the oracle, each with the bounds the C++ run used."""
+    ora = oracle_op(pr)
+    X = pr.initial_vectors()
+    out = []
+    for k, ((a0, bl, bu), _, _) in enumerate(rows):
+        if k < N_FULL:
+            ev, res, X = orc.solve(ora, X, orc.SolverState(a0, bl, bu), m=DEGREE)
+        else:
+            Xf = ora.chebyshev_filter(X, DEGREE, bl, bu, a0)
+            ev, X, XF, HXF = orc.rayleigh_ritz_spectrum_split(ora, Xf, n_core)
+            res = np.sqrt(((HXF - XF * ev[None, :]) ** 2).sum(0))
+        out.append((ev, res))
+    return out
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_cpp_layer_solve_matches_oracle(exe, tmp_path, mixed):
+    pr = small_problem(n=3, L=6.0, p=2, wells=3, nwfc=16, seed=11, projectors=True)
+    n_core = 8
+    write_inputs(pr, tmp_path, n_core)
+    r = subprocess.run([exe, str(tmp_path), "1" if mixed else "0"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = read_outputs(tmp_path)
+    assert len(rows) == N_FULL + N_SPLIT
+    # the first call derived its bounds itself (Lanczos): a0 = floor(lambda_min), the
+    # first-call bLow formula, and b an integer
+    (a0, bl, bu), _, _ = rows[0]
+    assert a0 == np.floor(a0) and bu == np.floor(bu) and bu > bl > a0
+    ref = oracle_replay(pr, rows, n_core)
+    nocc = pr.n_occupied
+    for k, ((_, ev, res), (ev_o, res_o)) in enumerate(zip(rows, ref)):
+        assert len(ev) == len(ev_o) == (pr.n_wfc if k < N_FULL else pr.n_wfc - n_core)
+        if not mixed:
+            assert np.abs(ev - ev_o).max() < 1e-8, (k, ev - ev_o)
+            assert np.abs(res - res_o).max() < 1e-8, (k, res - res_o)
+        elif k < N_FULL:
+            assert np.abs(ev[:nocc] - ev_o[:nocc]).max() < 1e-6, (k, ev - ev_o)
+        else:
+            assert np.abs(ev - ev_o).max() < 1e-4, (k, ev - ev_o)

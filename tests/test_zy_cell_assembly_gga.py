@@ -1,6 +1,6 @@
 """Real GGA cell Hamiltonians on the device (chefsi_assemble_cell_hamiltonians_gga) against the
 oracle's q-loop of the GGA cell-matrix formula. Tolerance 1e-12 relative (FP64 sums in another
-order). Collected after the other GPU files.
+order). Collected after the other GPU files and before the allocation-free entry point's file.
 """
 import numpy as np
 import pytest

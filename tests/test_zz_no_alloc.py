@@ -6,7 +6,8 @@ synchronisation). It keeps its workspace in one file-scope device array, so it i
 to N <= 256. This test calls both entry points through the C ABI (ctypes on
 libchefsi_gb300.so) on two matrices in a row -- the second call finds the first call's
 leftovers in the shared array -- and requires the same eigenvalues (1e-12 relative) and the
-same eigenvectors up to sign (1e-10). This file is collected after the parity files on purpose.
+same eigenvectors up to sign (1e-10); after a warm-up call, a call must leave the device's free
+memory unchanged. This file is collected after every other test file on purpose.
 """
 import ctypes
 
@@ -55,6 +56,29 @@ def test_syevd_noalloc_matches_syevd(cuda):
         assert np.abs(P1[:, ok] - P0[:, ok]).max() < 1e-10
         assert np.abs(Z1.T @ Z1 - np.eye(n)).max() < 1e-10
         assert np.abs(A @ Z1 - Z1 * w1).max() < 1e-10 * max(1.0, np.abs(w1).max())
+
+
+def test_syevd_noalloc_allocates_nothing_after_warmup(cuda):
+    """After one warm-up call on the device (which places the array in device memory: the
+    runtime loads device code lazily), a call leaves the device's free memory unchanged; the
+    operands are created before the measurement."""
+    from dftfe_gb300 import _lib
+    lib = _lib.load()
+    n = 128
+    A = _sym(n, 3)
+    _call(lib.chefsi_syevd_noalloc, A)  # warm-up
+    a = torch.from_numpy(A).cuda().contiguous()
+    w = torch.empty(n, dtype=torch.float64, device="cuda")
+    Z = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = lib.chefsi_syevd_noalloc(n, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                                  ctypes.c_void_p(Z.data_ptr()), stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == 0, lib.chefsi_last_error()
+    assert free1 == free0
 
 
 def test_syevd_noalloc_rejects_oversize(cuda):
