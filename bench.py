@@ -302,8 +302,10 @@ def fp64_leg(pr, op, X, solver, params, up):
         occ[mode] = Xc[:, :nocc].contiguous()
         del Xc, sv
         torch.cuda.empty_cache()
-    s = torch.linalg.svdvals(occ["fp64"].T @ occ["mixed"]).cpu().numpy()
-    angle = float(np.arccos(np.clip(s.min(), -1.0, 1.0)))
+    # largest principal angle: arcsin of || Qm - Qf (Qf^T Qm) ||_2 (accurate for small angles)
+    Qf, Qm = occ["fp64"], occ["mixed"]
+    r = Qm - Qf @ (Qf.T @ Qm)
+    angle = float(np.arcsin(min(1.0, float(torch.linalg.matrix_norm(r, ord=2)))))
     del occ
     d = np.abs(out["mixed"][0] - out["fp64"][0])
     return {"fp64_s_per_iter": out["fp64"][2], "mixed_s_per_iter_same_block": out["mixed"][2],

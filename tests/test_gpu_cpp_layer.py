@@ -10,7 +10,10 @@ iterations on the CPU with those bounds (full: oracle.solve; split: the oracle's
 spectrum-split Rayleigh-Ritz).
 
 Tolerances: FP64 every Ritz value and residual norm within 1e-8; mixed the occupied Ritz values
-of the full solves within 1e-6 Ha and the fractional Ritz values within 1e-4 Ha.
+of the full solves within 1e-5 Ha and the fractional Ritz values within 1e-4 Ha. After a few
+degree-10 iterations these states are far from converged (residual norms 0.2 to 3), so the
+mixed rounding reaches the Ritz values at first order through the residual: the 1e-6 Ha bar of
+converged states is checked at the 64,000-dof workload (tests/test_zx_config0_parity.py).
 """
 import os
 import shutil
@@ -103,7 +106,8 @@ def oracle_replay(pr, rows, n_core):
 
 @pytest.mark.parametrize("mixed", [False, True])
 def test_cpp_layer_solve_matches_oracle(exe, tmp_path, mixed):
-    pr = small_problem(n=3, L=6.0, p=2, wells=3, nwfc=16, seed=11, projectors=True)
+    # 4,096 dofs: the first-call bLow = a0 + (b - a0) N / M 200 stays below b (N / M < 1/200)
+    pr = small_problem(n=4, L=8.0, p=4, wells=3, nwfc=16, seed=11, projectors=True)
     n_core = 8
     write_inputs(pr, tmp_path, n_core)
     r = subprocess.run([exe, str(tmp_path), "1" if mixed else "0"], capture_output=True, text=True,
@@ -123,6 +127,6 @@ def test_cpp_layer_solve_matches_oracle(exe, tmp_path, mixed):
             assert np.abs(ev - ev_o).max() < 1e-8, (k, ev - ev_o)
             assert np.abs(res - res_o).max() < 1e-8, (k, res - res_o)
         elif k < N_FULL:
-            assert np.abs(ev[:nocc] - ev_o[:nocc]).max() < 1e-6, (k, ev - ev_o)
+            assert np.abs(ev[:nocc] - ev_o[:nocc]).max() < 1e-5, (k, ev - ev_o)
         else:
             assert np.abs(ev - ev_o).max() < 1e-4, (k, ev - ev_o)

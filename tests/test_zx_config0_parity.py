@@ -60,9 +60,12 @@ def gpu_run(pr, bounds, mixed):
 
 
 def occupied_angle(Xa, Xb, nocc):
-    """Largest principal angle between the spans of the first nocc columns (orthonormal)."""
-    s = np.linalg.svd(Xa[:, :nocc].T @ Xb[:, :nocc], compute_uv=False)
-    return float(np.arccos(np.clip(s.min(), -1.0, 1.0)))
+    """Largest principal angle between the spans of the first nocc columns (orthonormal
+    bases): arcsin of the spectral norm of Qb - Qa (Qa^T Qb), which stays accurate for small
+    angles (the arccos of the smallest singular value of Qa^T Qb bottoms out near 5e-8)."""
+    Qa, Qb = Xa[:, :nocc], Xb[:, :nocc]
+    r = Qb - Qa @ (Qa.T @ Qb)
+    return float(np.arcsin(min(1.0, np.linalg.norm(r, 2))))
 
 
 def test_config0_fp64_matches_oracle(cuda, ref):
