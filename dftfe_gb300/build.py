@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libchefsi_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["operator.cu", "dense.cu", "dense_tc.cu", "dense_c.cu", "api.cu", "tc.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["operator.cu", "dense.cu", "dense_tc.cu", "dense_c.cu", "api.cu", "tc.cu", "fused.cu", "noalloc.cu", "adjoint.cu"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
 

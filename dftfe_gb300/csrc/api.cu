@@ -38,6 +38,7 @@ struct chefsi_solver_s {
   DeviceBuffer<float> Xb32, Yb32;
   TcOperand tx, th;      // FP16 splits of X and HX for the tensor-core RR products
   DeviceBuffer<__half> xs_hi, xs_lo;  // FP16 split of the filter's HX input
+  FusedWork fzw;                      // the fused filter's split buffers and accumulators
   TcDenseWork tcw;
   double times[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[8] = {};
@@ -146,6 +147,11 @@ void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double
 // split once.
 void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
                     int B, int m, double a, double b, double a0, cudaStream_t st) {
+  if (s->p.fused_recurrence >= 0 && fused_plan_usable(op)) {
+    // one launch per degree finishes the recurrence and applies the nonlocal term
+    cheb_filter_fused(op, s->fzw, X, M, B, m, a, b, a0, [&] { s->hx_mark(st); }, st);
+    return;
+  }
   __half* hi = s->xs_hi.ensure((size_t)M * B);
   __half* lo = s->xs_lo.ensure((size_t)M * B);
   const double e = (b - a) / 2.0, c = (b + a) / 2.0;
@@ -1207,6 +1213,7 @@ chefsi_params default_params() {
   p.ss_frac_reduced = 0;
   p.rr_block = 0;
   p.rr_slab_rows = 0;
+  p.fused_recurrence = 0;
   return p;
 }
 

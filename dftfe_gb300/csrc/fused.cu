@@ -1,0 +1,454 @@
+// The fused Chebyshev filter on tensor cores: one persistent launch per degree finishes the
+// three-term recurrence inside the HX kernel's epilogue, and the nonlocal apply rides in the
+// same launch as extra K columns of the cell matrices.
+//
+// DFT-FE's filter (linearAlgebraOperationsDevice::chebyshevFilter,
+// src/linAlg/linearAlgebraOperationsDevice.cc:531-727) runs per degree an HX (gather,
+// cell GEMMs, scatter; the nonlocal term by a projection, a cross-cell reduction and an apply)
+// and combinedDeviceKernel (:37-104), an axpby pass over the whole block. Here, per degree j:
+//   1. W = C^T x_{j-1} over the projector rows (nl projection from the split rows), written
+//      as split rows n_dofs + a P + i of the same buffer, scaled by 2^t;
+//   2. one launch of cell_hx_tc_kernel<FUSED> computes, for every dof row,
+//        x_j = a_j (A x_{j-1} + C V W) + c_j x_{j-1} + b_j x_{j-2}
+//      and writes its FP16 hi + lo split: the vectors live only as split rows, so the next
+//      degree's gather reads them directly and no separate recurrence pass exists.
+// Rows of one cell entry are finished by that unit; rows shared by several cell entries go
+// through FP32 accumulators pre-set to c_j x_{j-1} + b_j x_{j-2} by the unit that finished
+// them in the previous degree (see TcFused in tc.cu).
+#include "internal.h"
+#include "tc_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace chefsi {
+
+namespace {
+
+constexpr int kNlChunkRows = 256;  // rows per projection chunk (the operator's chunk table)
+
+// acc[s][v] = c (hi + lo)[dof_s][v] for the shared rows (float4 units)
+__global__ void k_fz_acc_init(const __half* __restrict__ hi, const __half* __restrict__ lo,
+                              const int* __restrict__ shared_dof, int64_t n_shared, int B, float c,
+                              float* __restrict__ acc) {
+  const int q = B / 4;
+  const int64_t n = n_shared * q;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t / q;
+    const int v = (int)(t - s * q) * 4;
+    const int64_t o = (int64_t)shared_dof[s] * B + v;
+    const __half2* h = reinterpret_cast<const __half2*>(hi + o);
+    const __half2* l = reinterpret_cast<const __half2*>(lo + o);
+    const float2 h0 = __half22float2(h[0]), h1 = __half22float2(h[1]);
+    const float2 l0 = __half22float2(l[0]), l1 = __half22float2(l[1]);
+    *reinterpret_cast<float4*>(acc + s * B + v) =
+        make_float4(c * (h0.x + l0.x), c * (h0.y + l0.y), c * (h1.x + l1.x), c * (h1.y + l1.y));
+  }
+}
+
+// (hi, lo) = split(scale * W) over n entries (float4 units): the W rows of the split buffer
+__global__ void k_fz_w_split(const float* __restrict__ W, int64_t n, float scale,
+                             __half* __restrict__ hi, __half* __restrict__ lo) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float4 w = reinterpret_cast<const float4*>(W)[t];
+    const float v[4] = {scale * w.x, scale * w.y, scale * w.z, scale * w.w};
+    __half h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      h[i] = __float2half_rn(v[i]);
+      l[i] = __float2half_rn(v[i] - __half2float(h[i]));
+    }
+    reinterpret_cast<__half2*>(hi)[2 * t] = __halves2half2(h[0], h[1]);
+    reinterpret_cast<__half2*>(hi)[2 * t + 1] = __halves2half2(h[2], h[3]);
+    reinterpret_cast<__half2*>(lo)[2 * t] = __halves2half2(l[0], l[1]);
+    reinterpret_cast<__half2*>(lo)[2 * t + 1] = __halves2half2(l[2], l[3]);
+  }
+}
+
+// x = hi + lo over n entries (float4 units)
+__global__ void k_fz_join(const __half* __restrict__ hi, const __half* __restrict__ lo, int64_t n,
+                          float* __restrict__ x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const __half2* h = reinterpret_cast<const __half2*>(hi) + 2 * t;
+    const __half2* l = reinterpret_cast<const __half2*>(lo) + 2 * t;
+    const float2 h0 = __half22float2(h[0]), h1 = __half22float2(h[1]);
+    const float2 l0 = __half22float2(l[0]), l1 = __half22float2(l[1]);
+    reinterpret_cast<float4*>(x)[t] = make_float4(h0.x + l0.x, h0.y + l0.y, h1.x + l1.x, h1.y + l1.y);
+  }
+}
+
+// the projector columns of the extended tiles: entry idx[k] of the tile array receives the split
+// of val[k] (already scaled)
+__global__ void k_fz_scatter(const int64_t* __restrict__ idx, const double* __restrict__ val,
+                             int64_t n, __half* __restrict__ hi, __half* __restrict__ lo) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = val[t];
+    const __half h = __double2half(v);
+    hi[idx[t]] = h;
+    lo[idx[t]] = __double2half(v - (double)__half2float(h));
+  }
+}
+
+// W[a][i][b] += sum over one chunk of atom a's rows of C[r][i] x[dof_r][b], x given by its FP16
+// split rows: one CTA per (row chunk, 128 vectors); 8 warps over interleaved rows, U gathered
+// rows in flight per lane (4 vectors each: 8-byte hi and lo pieces), partial sums reduced in
+// shared memory and added with one float4 atomic per (projector, lane). PP >= P.
+template <int PP, int U>
+__global__ void __launch_bounds__(256, PP <= 8 ? 4 : 2)
+    k_nl_project_split(const int* __restrict__ chunk_atom, const int* __restrict__ chunk_row0,
+                       const int* __restrict__ atom_ptr, const int* __restrict__ dofs,
+                       const float* __restrict__ C, int P, const __half* __restrict__ xh,
+                       const __half* __restrict__ xl, int64_t ld, float* __restrict__ W, int B) {
+  extern __shared__ float4 red_dyn[];  // [8][P][32]
+  __shared__ float Cs[kNlChunkRows * PP];
+  __shared__ int Ds[kNlChunkRows];
+  const int ch = blockIdx.x;
+  const int a = chunk_atom[ch];
+  const int r0 = chunk_row0[ch];
+  const int nr = min(r0 + kNlChunkRows, atom_ptr[a + 1]) - r0;
+  for (int i = threadIdx.x; i < nr * P; i += blockDim.x) Cs[i] = C[(size_t)r0 * P + i];
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) Ds[i] = dofs[r0 + i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.y * 128 + lane * 4;
+  float4 acc[PP];
+#pragma unroll
+  for (int j = 0; j < PP; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto load4 = [&](int r) {
+    const int64_t o = (int64_t)Ds[r] * ld + b;
+    const uint2 hu = __ldg(reinterpret_cast<const uint2*>(xh + o));
+    const uint2 lu = __ldg(reinterpret_cast<const uint2*>(xl + o));
+    const float2 h0 = __half22float2(*reinterpret_cast<const __half2*>(&hu.x));
+    const float2 h1 = __half22float2(*reinterpret_cast<const __half2*>(&hu.y));
+    const float2 l0 = __half22float2(*reinterpret_cast<const __half2*>(&lu.x));
+    const float2 l1 = __half22float2(*reinterpret_cast<const __half2*>(&lu.y));
+    return make_float4(h0.x + l0.x, h0.y + l0.y, h1.x + l1.x, h1.y + l1.y);
+  };
+  if (b < B) {
+    int r = warp;
+    for (; r + 8 * (U - 1) < nr; r += 8 * U) {
+      float4 xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = load4(r + 8 * u);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < PP; ++j) {
+          if (j >= P) break;
+          const float cv = Cs[(r + 8 * u) * P + j];
+          acc[j].x = fmaf(cv, xv[u].x, acc[j].x);
+          acc[j].y = fmaf(cv, xv[u].y, acc[j].y);
+          acc[j].z = fmaf(cv, xv[u].z, acc[j].z);
+          acc[j].w = fmaf(cv, xv[u].w, acc[j].w);
+        }
+    }
+    for (; r < nr; r += 8) {
+      const float4 xv = load4(r);
+#pragma unroll
+      for (int j = 0; j < PP; ++j) {
+        if (j >= P) break;
+        const float cv = Cs[r * P + j];
+        acc[j].x = fmaf(cv, xv.x, acc[j].x);
+        acc[j].y = fmaf(cv, xv.y, acc[j].y);
+        acc[j].z = fmaf(cv, xv.z, acc[j].z);
+        acc[j].w = fmaf(cv, xv.w, acc[j].w);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PP; ++j)
+    if (j < P) red_dyn[(warp * P + j) * 32 + lane] = acc[j];
+  __syncthreads();
+  for (int t = threadIdx.x; t < P * 32; t += blockDim.x) {
+    const int j = t >> 5, l = t & 31;
+    float4 sum = red_dyn[j * 32 + l];
+    for (int w2 = 1; w2 < 8; ++w2) {
+      const float4 v = red_dyn[(w2 * P + j) * 32 + l];
+      sum.x += v.x, sum.y += v.y, sum.z += v.z, sum.w += v.w;
+    }
+    const int bb = blockIdx.y * 128 + l * 4;
+    if (bb < B) atomicAdd(reinterpret_cast<float4*>(&W[((size_t)a * P + j) * B + bb]), sum);
+  }
+}
+
+template <int PP, int U>
+void launch_project_split(chefsi_operator_s* op, const __half* xh, const __half* xl, int B,
+                          float* W, cudaStream_t st) {
+  dim3 grid(op->nl_n_chunks, (B + 127) / 128);
+  const size_t red = sizeof(float4) * 8 * op->n_proj * 32;
+  CHEFSI_CUDA(cudaFuncSetAttribute(k_nl_project_split<PP, U>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(float4) * 8 * PP * 32)));
+  k_nl_project_split<PP, U><<<grid, 256, red, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
+                                                    op->nl_ptr.ptr, op->nl_dofs.ptr,
+                                                    op->nl_vals32.ptr, op->n_proj, xh, xl, B, W, B);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+template <typename T>
+std::vector<T> to_host(const DeviceBuffer<T>& b, size_t n) {
+  std::vector<T> h(n);
+  if (n) CHEFSI_CUDA(cudaMemcpy(h.data(), b.ptr, n * sizeof(T), cudaMemcpyDeviceToHost));
+  return h;
+}
+template <typename T>
+void to_device(DeviceBuffer<T>& b, const std::vector<T>& h) {
+  b.reset(h.size());
+  if (!h.empty())
+    CHEFSI_CUDA(cudaMemcpy(b.ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+bool fused_plan_usable(chefsi_operator_s* op) {
+  return tc_usable(op) && !op->is_complex && op->folded && op->n_proj <= 16;
+}
+
+void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
+  FusedPlan& fp = op->fz;
+  if (fp.ready) return;
+  CHEFSI_REQUIRE(fused_plan_usable(op), "fused filter step: operator not supported");
+  const int nc = op->n_cells, ne = op->n_e;
+  const int64_t M = op->n_dofs;
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  const std::vector<int> map = to_host(op->map, (size_t)nc * ne);
+  // cell entries per dof (CSR) and the shared-row numbering
+  std::vector<int64_t> eptr(M + 1, 0);
+  for (int v : map) ++eptr[v + 1];
+  for (int64_t d = 0; d < M; ++d) eptr[d + 1] += eptr[d];
+  std::vector<int> ent(eptr[M]);
+  {
+    std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
+    for (int64_t k = 0; k < (int64_t)map.size(); ++k) ent[fill[map[k]]++] = (int)k;  // c * ne + I
+  }
+  std::vector<int> sidx(M, -1), shared_dof;
+  std::vector<unsigned char> ncontrib;
+  for (int64_t d = 0; d < M; ++d) {
+    const int64_t cnt = eptr[d + 1] - eptr[d];
+    CHEFSI_REQUIRE(cnt <= 255, "fused filter step: a dof with more than 255 cell entries");
+    if (cnt > 1) {
+      sidx[d] = (int)shared_dof.size();
+      shared_dof.push_back((int)d);
+      ncontrib.push_back((unsigned char)cnt);
+    }
+  }
+  std::vector<int> rowinfo((size_t)nc * ne * 2);
+  for (size_t k = 0; k < map.size(); ++k) {
+    rowinfo[2 * k] = map[k];
+    rowinfo[2 * k + 1] = sidx[map[k]];
+  }
+  // projector (atom, dof) pairs -> cell entries, atoms -> per-cell slots
+  const int P = op->n_atoms ? op->n_proj : 0;
+  std::vector<std::vector<int>> slots(nc);
+  auto slot_of = [&](int c, int a) {
+    const auto& v = slots[c];
+    for (size_t i = 0; i < v.size(); ++i)
+      if (v[i] == a) return (int)i;
+    return -1;
+  };
+  std::vector<int> nptr, ndofs;
+  std::vector<double> C, V;
+  if (P) {
+    nptr = to_host(op->nl_ptr, (size_t)op->n_atoms + 1);
+    ndofs = to_host(op->nl_dofs, (size_t)op->nl_nnz);
+    C = to_host(op->nl_vals64, (size_t)op->nl_nnz * P);
+    V = to_host(op->couplings, (size_t)op->n_atoms * P);
+    // rows owned by one cell entry fix their cell; the others join a cell of theirs that has
+    // the atom already, else the one with the fewest atoms
+    for (int a = 0; a < op->n_atoms; ++a)
+      for (int r = nptr[a]; r < nptr[a + 1]; ++r) {
+        const int d = ndofs[r];
+        if (eptr[d + 1] - eptr[d] != 1) continue;
+        const int c = ent[eptr[d]] / ne;
+        if (slot_of(c, a) < 0) slots[c].push_back(a);
+      }
+    for (int a = 0; a < op->n_atoms; ++a)
+      for (int r = nptr[a]; r < nptr[a + 1]; ++r) {
+        const int d = ndofs[r];
+        bool have = false;
+        int best = -1;
+        for (int64_t k = eptr[d]; k < eptr[d + 1]; ++k) {
+          const int c = ent[k] / ne;
+          if (slot_of(c, a) >= 0) {
+            have = true;
+            break;
+          }
+          if (best < 0 || slots[c].size() < slots[best].size()) best = c;
+        }
+        if (!have) slots[best].push_back(a);
+      }
+  }
+  int max_slots = 0;
+  for (const auto& v : slots) max_slots = std::max(max_slots, (int)v.size());
+  const int kstride = (ne + P * max_slots + 31) / 32 * 32;
+  const int nkb = kstride / 32;
+  std::vector<int> mapk((size_t)nc * kstride, -1);
+  for (int c = 0; c < nc; ++c) {
+    for (int I = 0; I < ne; ++I) mapk[(size_t)c * kstride + I] = map[(size_t)c * ne + I];
+    for (size_t sl = 0; sl < slots[c].size(); ++sl)
+      for (int j = 0; j < P; ++j)
+        mapk[(size_t)c * kstride + ne + sl * P + j] = (int)(M + (int64_t)slots[c][sl] * P + j);
+  }
+  CHEFSI_REQUIRE(M + (int64_t)op->n_atoms * P < (1ll << 31),
+                 "fused filter step: too many rows for 32-bit map entries");
+  // scales: 2^t W with max |x| <= 2^9 stays below 2^15; the tiles hold 2^s A and 2^(s-t) C V
+  double wscale = 1.0, ext_max = 0.0;
+  if (P) {
+    double n1max = 0.0;
+    for (int a = 0; a < op->n_atoms; ++a)
+      for (int j = 0; j < P; ++j) {
+        double n1 = 0.0;
+        for (int r = nptr[a]; r < nptr[a + 1]; ++r) n1 += std::fabs(C[(size_t)r * P + j]);
+        n1max = std::max(n1max, n1);
+      }
+    if (n1max > 0.0 && std::isfinite(n1max)) wscale = std::ldexp(1.0, (int)std::floor(6.0 - std::log2(n1max)));
+    for (int a = 0; a < op->n_atoms; ++a)
+      for (int r = nptr[a]; r < nptr[a + 1]; ++r)
+        for (int j = 0; j < P; ++j)
+          ext_max = std::max(ext_max, std::fabs(C[(size_t)r * P + j] * V[(size_t)a * P + j]) / wscale);
+  }
+  DeviceBuffer<double> amax(1);
+  absmax_block_f64(op->mats64.ptr, ne, (int64_t)nc * ne, ne, amax.ptr, st);
+  double am = 0.0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&am, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  am = std::max(am, ext_max);
+  const int e = (am > 0 && std::isfinite(am)) ? 14 - (int)std::floor(std::log2(am)) : 0;
+  const double scale = std::ldexp(1.0, e);
+  int n_half = 0, n_halves = 0;
+  tc_row_split(ne, &n_half, &n_halves);
+  const size_t ntile = (size_t)nc * n_halves * nkb * n_half * 32;
+  fp.hi.reset(ntile);
+  fp.lo.reset(ntile);
+  split_mats_ext(op, nkb, scale, fp.hi.ptr, fp.lo.ptr, st);
+  if (P) {
+    std::vector<int64_t> idx;
+    std::vector<double> val;
+    idx.reserve((size_t)op->nl_nnz * P);
+    val.reserve((size_t)op->nl_nnz * P);
+    for (int a = 0; a < op->n_atoms; ++a)
+      for (int r = nptr[a]; r < nptr[a + 1]; ++r) {
+        const int d = ndofs[r];
+        int entry = -1, sl = -1;
+        for (int64_t k = eptr[d]; k < eptr[d + 1] && entry < 0; ++k) {
+          const int s2 = slot_of(ent[k] / ne, a);
+          if (s2 >= 0) entry = ent[k], sl = s2;
+        }
+        CHEFSI_REQUIRE(entry >= 0, "fused filter step: projector row without a cell");
+        const int c = entry / ne, I = entry % ne;
+        const int half = I / n_half, ri = I % n_half;
+        for (int j = 0; j < P; ++j) {
+          const int J = ne + sl * P + j;
+          const int64_t tix = ((int64_t)c * n_halves + half) * nkb + J / 32;
+          idx.push_back(tix * n_half * 32 + tcx::sw64_offset((uint32_t)ri, 2u * (uint32_t)(J % 32)) / 2);
+          val.push_back(scale / wscale * C[(size_t)r * P + j] * V[(size_t)a * P + j]);
+        }
+      }
+    DeviceBuffer<int64_t> didx;
+    DeviceBuffer<double> dval;
+    to_device(didx, idx);
+    to_device(dval, val);
+    k_fz_scatter<<<grid_for((int64_t)idx.size(), 256), 256, 0, st>>>(didx.ptr, dval.ptr,
+                                                                     (int64_t)idx.size(), fp.hi.ptr,
+                                                                     fp.lo.ptr);
+    CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+  }
+  to_device(fp.mapk, mapk);
+  to_device(fp.rowinfo, rowinfo);
+  to_device(fp.ncontrib, ncontrib);
+  to_device(fp.shared_dof, shared_dof);
+  fp.nkb = nkb;
+  fp.kstride = kstride;
+  fp.max_slots = max_slots;
+  fp.n_shared = (int64_t)shared_dof.size();
+  fp.rows = M + (int64_t)op->n_atoms * P;
+  fp.scale = (float)scale;
+  fp.wscale = (float)wscale;
+  fp.ready = true;
+}
+
+// The filter of one block: X [M][B] FP32 in (scaled so that max |x| ~ 2^8), p_m(A) X out.
+// Coefficients of the sigma-scaled recurrence (linearAlgebraOperationsDevice.cc:531-727):
+//   x_1 = alpha1 (A - c) x_0, alpha1 = sigma1 / e;
+//   x_j = alpha1_j (A - c) x_{j-1} + alpha2_j x_{j-2}, sigma2 = 1 / (gamma - sigma),
+//   alpha1_j = 2 sigma2 / e, alpha2_j = -sigma sigma2.
+void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M, int B, int m,
+                       double a, double b, double a0, const std::function<void()>& mark,
+                       cudaStream_t st) {
+  prepare_fused_plan(op, st);
+  const FusedPlan& fp = op->fz;
+  const int n_chunks = (B + 127) / 128;
+  const size_t nrows = (size_t)fp.rows * B;
+  __half* h[2] = {w.hi[0].ensure(nrows), w.hi[1].ensure(nrows)};
+  __half* l[2] = {w.lo[0].ensure(nrows), w.lo[1].ensure(nrows)};
+  float* acc = w.acc.ensure(std::max<size_t>(1, (size_t)fp.n_shared * B));
+  unsigned* counter = w.counter.ensure(std::max<size_t>(1, (size_t)fp.n_shared * n_chunks));
+  float* W = op->n_atoms ? w.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
+  CHEFSI_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * (size_t)fp.n_shared * n_chunks, st));
+  // coefficients a_j, c_j, b_j for j = 1..m
+  std::vector<double> ca(m + 2, 0.0), cc(m + 2, 0.0), cb(m + 2, 0.0);
+  {
+    const double e = (b - a) / 2.0, c = (b + a) / 2.0;
+    double sigma = e / (a0 - c);
+    const double sigma1 = sigma, gamma = 2.0 / sigma1;
+    ca[1] = sigma1 / e;
+    cc[1] = -c * ca[1];
+    for (int j = 2; j <= m; ++j) {
+      const double sigma2 = 1.0 / (gamma - sigma);
+      ca[j] = 2.0 * sigma2 / e;
+      cc[j] = -c * ca[j];
+      cb[j] = -(sigma * sigma2);
+      sigma = sigma2;
+    }
+  }
+  split_rows_f32(X, B, M, B, h[0], l[0], st);
+  if (fp.n_shared) {
+    k_fz_acc_init<<<grid_for(fp.n_shared * (B / 4), 256), 256, 0, st>>>(
+        h[0], l[0], fp.shared_dof.ptr, fp.n_shared, B, (float)cc[1], acc);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  for (int j = 1; j <= m; ++j) {
+    const int in = (j - 1) & 1, out = j & 1;
+    mark();
+    if (op->n_atoms) {
+      const size_t nw = (size_t)op->n_atoms * op->n_proj * B;
+      CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * nw, st));
+      if (op->n_proj <= 4)
+        launch_project_split<4, 8>(op, h[in], l[in], B, W, st);
+      else if (op->n_proj <= 8)
+        launch_project_split<8, 4>(op, h[in], l[in], B, W, st);
+      else
+        launch_project_split<16, 4>(op, h[in], l[in], B, W, st);
+      k_fz_w_split<<<grid_for((int64_t)nw / 4, 256), 256, 0, st>>>(W, (int64_t)nw, fp.wscale,
+                                                                   h[in] + M * B, l[in] + M * B);
+      CHEFSI_CHECK_LAUNCH();
+    }
+    TcFusedLaunch f{};
+    f.op = op;
+    f.xhi = h[in];
+    f.xlo = l[in];
+    f.ohi = h[out];
+    f.olo = l[out];
+    f.acc = acc;
+    f.counter = counter;
+    f.B = B;
+    f.a = ca[j];
+    f.c = cc[j];
+    f.b = cb[j];
+    f.has_next = j < m;
+    f.cn = cc[j + 1];
+    f.bn = cb[j + 1];
+    hx_tc_fused_launch(f, st);
+    mark();
+  }
+  k_fz_join<<<grid_for(M * B / 4, 256), 256, 0, st>>>(h[m & 1], l[m & 1], M * B, X);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+}  // namespace chefsi

@@ -3,6 +3,7 @@
 
 #include "common.cuh"
 
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -34,6 +35,30 @@ struct TensorCellMats {
   bool lo3_ready = false;
 };
 
+// Tables of the fused filter step (tc.cu, fused.cu), built once per operator on first use:
+// * rows: every cell entry (cell, node) is "single" when its dof has no other cell entry (its
+//   row is finished by one unit) or "shared" (an FP32 accumulator row and arrival counters);
+// * the nonlocal term as extra K columns of the cell matrices: each (atom, dof) pair of the
+//   projectors is given to one cell entry of its dof (greedily, so that few cells take more
+//   than one atom), a cell's atoms occupy n_proj K columns each after its n_e nodes, holding
+//   2^-t C V for the entry's dof; the K side gathers those columns from rows n_dofs + a P + j
+//   of the split buffer, where 2^t W = 2^t C^T x sits. Cells with fewer atoms get zero columns.
+struct FusedPlan {
+  bool ready = false;
+  int nkb = 0;            // K-blocks of 32 (nodes and projector columns)
+  int kstride = 0;        // = 32 nkb
+  int max_slots = 0;      // most atoms any cell takes
+  int64_t n_shared = 0;
+  int64_t rows = 0;       // split-buffer rows: n_dofs + n_atoms n_proj
+  float scale = 1.f;      // 2^s of the tiles
+  float wscale = 1.f;     // 2^t of the W rows
+  DeviceBuffer<int> mapk;         // [n_cells][kstride]
+  DeviceBuffer<int> rowinfo;      // [n_cells][n_e] x {dof, shared index or -1}
+  DeviceBuffer<unsigned char> ncontrib;  // [n_shared]
+  DeviceBuffer<int> shared_dof;   // [n_shared]
+  DeviceBuffer<__half> hi, lo;    // extended cell-matrix tiles [n_cells][halves][nkb][n_half x 32]
+};
+
 }  // namespace chefsi
 
 struct chefsi_operator_s {
@@ -47,6 +72,7 @@ struct chefsi_operator_s {
   chefsi::DeviceBuffer<double> mats64;    // [n_cells][n_e][n_e] (x2 for complex)
   chefsi::DeviceBuffer<float> mats32;     // FP32 copy (real only)
   chefsi::TensorCellMats tc;              // FP16 split copy for the tensor-core filter HX
+  chefsi::FusedPlan fz;                   // tables of the fused filter step
   chefsi::DeviceBuffer<double> sqrt_mass, inv_sqrt_mass;
 
   // constraints
@@ -146,6 +172,43 @@ void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, doubl
 void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
                     cudaStream_t st);
 void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st);
+// one fused filter step (tc.cu): x_j from the split rows of x_{j-1} (xhi/xlo, rows n_dofs +
+// n_atoms n_proj: the last ones hold 2^t W) and x_{j-2} (ohi/olo on entry, single rows);
+// x_j = a A x_{j-1} + c x_{j-1} + b x_{j-2} into ohi/olo; shared rows through acc / counter,
+// whose accumulators are left pre-set to cn x_j + bn x_{j-1} when has_next
+struct TcFusedLaunch {
+  chefsi_operator_s* op;
+  const __half* xhi;
+  const __half* xlo;
+  __half* ohi;
+  __half* olo;
+  float* acc;
+  unsigned* counter;
+  int B;
+  double a, c, b, cn, bn;
+  int has_next;
+};
+void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st);
+// row halves of the tensor-core tiles for n_e nodes (n_half rows each)
+void tc_row_split(int n_e, int* n_half, int* n_halves);
+// (cell, half, K-block) tiles of 2^s A_e over nkb K-blocks (columns past n_e zero)
+void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __half* lo,
+                    cudaStream_t st);
+// workspaces of the fused filter (grow-only): two split buffers (x_{j-1}; x_{j-2} -> x_j), the
+// shared rows' accumulators and arrival counters, the projector coefficients W
+struct FusedWork {
+  DeviceBuffer<__half> hi[2], lo[2];
+  DeviceBuffer<float> acc, W;
+  DeviceBuffer<unsigned> counter;
+};
+// the Chebyshev filter of one FP32 block X [M][B] (max |x| ~ 2^8) with the fused steps; mark()
+// is called before and after every degree (profiling events)
+void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M, int B, int m,
+                       double a, double b, double a0, const std::function<void()>& mark,
+                       cudaStream_t st);
+// the tables of the fused step (fused.cu); false if the operator does not take the fused path
+bool fused_plan_usable(chefsi_operator_s* op);
+void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st);
 // device error flag of the tensor-core kernel (CHEFSI_OK or CHEFSI_ERR_TIMEOUT); clears it
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st);
 // nonlocal term y += scalar * C V C^T x for FP32 vectors (used by the tensor-core path)

@@ -84,6 +84,27 @@ struct TcProblem {
 };
 constexpr int kMaxGroup = 32;
 
+// The fused filter step (one problem): the epilogue finishes the three-term recurrence
+//   x_j = out_scale D + cj x_{j-1} + bj x_{j-2}
+// instead of scatter-adding D. Rows that one cell entry owns alone ("single" rows) are written
+// at once as the FP16 split of x_j (x_{j-1} from the input split rows, x_{j-2} from the output
+// rows, which still hold it); rows shared by several cell entries are reduced into FP32
+// accumulators (pre-set to cj x_{j-1} + bj x_{j-2}), and the unit that brings the last
+// contribution of a row (per 128-vector chunk, counted with acquire-release atomics) writes
+// its split and pre-sets the accumulator for the next step: cn x_j + bn x_{j-1}.
+struct TcFused {
+  const int* mapk;                 // [n_cells][kstride] split row feeding K index J (-1: zero)
+  int kstride;
+  int has_next;
+  const int2* rowinfo;             // [n_cells][n_e] {dof, shared index or -1}
+  __half* ohi;                     // output split rows (x_j); single rows hold x_{j-2} on entry
+  __half* olo;
+  float* acc;                      // [n_shared][B] accumulators of the shared rows
+  unsigned* counter;               // [n_shared][n_chunks] arrivals
+  const unsigned char* ncontrib;   // [n_shared] cell entries per shared row
+  float cj, bj, cn, bn;
+};
+
 struct TcArgs {
   TcProblem prob[kMaxGroup];
   int n_probs;
@@ -99,6 +120,7 @@ struct TcArgs {
   int xstages;     // X ring depth
   int lookahead;   // K-blocks of X copies in flight per producer thread
   int* err;
+  TcFused fz;      // FUSED launches only
 };
 static_assert(sizeof(TcArgs) <= 4096, "kernel parameters above 4 KB");
 
@@ -113,9 +135,12 @@ struct Layout {
   int aoff;     // start of the matrix ring
   int bars;     // barrier block
   int offs;     // epilogue row offsets: 2 x 256 int64 (one table per accumulator)
+  int queue;    // fused step: two queues of finished shared rows (count + 256 entries each)
   int total;
 };
-__host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages, int ns) {
+constexpr int kQueueStride = 264;  // ints per queue (count, 256 entries, padding)
+__host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages, int ns,
+                                              bool fused = false) {
   Layout L;
   L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
   L.xstage = ns * kXTile;
@@ -123,7 +148,8 @@ __host__ __device__ inline Layout make_layout(int n_half, int stages, int xstage
   L.aoff = xstages * L.xstage;
   L.bars = L.aoff + stages * L.astage;
   L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 8);
-  L.total = L.offs + 2 * 256 * 8;
+  L.queue = L.offs + 2 * 256 * 8;
+  L.total = L.queue + (fused ? 2 * kQueueStride * 4 : 0);
   return L;
 }
 
@@ -159,6 +185,34 @@ __device__ __forceinline__ bool epilogue_sync_and(bool v) {
       : "r"((uint32_t)v), "n"(kEpiWarps * 32)
       : "memory");
   return r != 0;
+}
+
+// named barrier 2 among the epilogue threads
+__device__ __forceinline__ void epilogue_sync() {
+  asm volatile("bar.sync 2, %0;" ::"n"(kEpiWarps * 32) : "memory");
+}
+// arrival on a shared row's counter: release of this CTA's reductions (ordered before by the
+// epilogue barrier) and acquire of the other contributors' ones
+__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v)
+               : "memory");
+  return old;
+}
+// 16-byte load at L2 (the reductions of other SMs live there; never an L1 copy)
+__device__ __forceinline__ float4 ld_cg_f4(const float* p) {
+  float4 v;
+  asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p)
+               : "memory");
+  return v;
+}
+
+// FP32 -> FP16 hi + lo (22 significant bits; the vectors are pre-scaled into FP16's range)
+__device__ __forceinline__ void split_f32(float a, __half& h, __half& l) {
+  h = __float2half_rn(a);
+  l = __float2half_rn(a - __half2float(h));
 }
 
 struct Unit {
@@ -212,14 +266,17 @@ constexpr int kChunkCols = 96;
 //       cells, rows = quadrature points in parts of n_half), so D[v][q] = psi_v(x_q) for the
 //       gathered vectors; the epilogue adds occ_v D[v][q]^2 over the vectors into rho[c][q]
 //       (warp butterfly reduction, one FP32 atomic per quadrature point and warp).
-template <int NS, bool KCHUNK, bool DENS = false>
+// FUSED: the fused filter step (see TcFused): the K side gathers through the extended map
+//        (the cell's nodes, then its projector coefficients W), the epilogue finishes the
+//        recurrence.
+template <int NS, bool KCHUNK, bool DENS = false, bool FUSED = false>
 __global__ void __launch_bounds__(kThreads3, 1)
     cell_hx_tc_kernel(TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int S = args.stages, SX = args.xstages;
-  const Layout L = make_layout(args.n_half, S, SX, NS);
+  const Layout L = make_layout(args.n_half, S, SX, NS, FUSED);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] cell-matrix tile bytes landed
   uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
@@ -411,11 +468,12 @@ __global__ void __launch_bounds__(kThreads3, 1)
     auto load_next = [&]() {
       nxt.valid = c_it < my_units;
       if (nxt.valid) {
-        const int* mrow = args.prob[c_w.p].map + (int64_t)c_w.cell * args.n_e;
+        const int kst = FUSED ? args.fz.kstride : args.n_e;
+        const int* mrow = (FUSED ? args.fz.mapk : args.prob[c_w.p].map) + (int64_t)c_w.cell * kst;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int J = c_kb * kKB + j * 8 + rsub;
-          nxt.rows[j] = J < args.n_e ? __ldg(mrow + J) : -1;
+          nxt.rows[j] = J < kst ? __ldg(mrow + J) : -1;
         }
         nxt.vb = c_w.chunk * kVec + cc * 8;
         nxt.p = c_w.p;
@@ -524,6 +582,118 @@ __global__ void __launch_bounds__(kThreads3, 1)
                 const int64_t o = offs[c_beg + 16 * gi + i];
                 if (o >= 0) atomicAdd(dstb + o, osc * sum[16 * gi + i]);
               }
+            }
+          }
+        }
+      }
+    } else if (FUSED) {
+      // ---- the fused filter step: finish the recurrence in the epilogue
+      const TcFused& fz = args.fz;
+      const TcProblem& pr = args.prob[0];
+      const int e = threadIdx.x - 192;          // epilogue thread 0..255
+      const int ew = warp - 6;                  // epilogue warp 0..7
+      int* queues = reinterpret_cast<int*>(smem + L.queue);
+      if (e < 2) queues[e * kQueueStride] = 0;  // ordered by the first unit's barrier
+      const int64_t ld = pr.ldx;                // split rows, accumulators: ld = B
+      for (int64_t it = 0; it < my_units; ++it) {
+        const int buf = (int)(it & 1);
+        const uint32_t ph = (uint32_t)((it >> 1) & 1);
+        const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
+        fence_after();
+        const Unit w = unit_at(it, first, step, args);
+        const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
+        // the unit's rows: {dof, shared index or -1}, staged once
+        int2* rinfo = reinterpret_cast<int2*>(smem + L.offs) + buf * 256;
+        if (okw)
+          for (int I = e; I < args.n_half; I += kEpiWarps * 32)
+            rinfo[I] = I < nrows ? __ldg(fz.rowinfo + (int64_t)w.cell * args.n_e +
+                                         w.half * args.n_half + I)
+                                 : make_int2(-1, -1);
+        if (!epilogue_sync_and(okw)) break;
+        const int gb = w.chunk * kVec + q * 32 + lane;
+        const bool vok = gb < pr.B;
+        const float osc = pr.out_scale;
+        const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
+        for (int c0 = c_beg; c0 < c_end; c0 += 16) {
+          float vals[16];
+          tmem_ld16(tq + c0, vals);
+          if (vok) {
+            float xm1[16], xm2[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int2 r = rinfo[c0 + i];
+              xm1[i] = 0.f;
+              xm2[i] = 0.f;
+              if (r.x >= 0 && r.y < 0) {
+                const int64_t o = (int64_t)r.x * ld + gb;
+                xm1[i] = __half2float(__ldg(pr.xhi + o)) + __half2float(__ldg(pr.xlo + o));
+                if (fz.bj != 0.f) xm2[i] = __half2float(fz.ohi[o]) + __half2float(fz.olo[o]);
+              }
+            }
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int2 r = rinfo[c0 + i];
+              if (r.x < 0) continue;
+              const float v = osc * vals[i];
+              if (r.y < 0) {
+                const float x = fmaf(fz.bj, xm2[i], fmaf(fz.cj, xm1[i], v));
+                const int64_t o = (int64_t)r.x * ld + gb;
+                __half h, l;
+                split_f32(x, h, l);
+                fz.ohi[o] = h;
+                fz.olo[o] = l;
+              } else {
+                atomicAdd(fz.acc + (int64_t)r.y * ld + gb, v);
+              }
+            }
+          }
+        }
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
+        // arrivals: every epilogue thread's reductions of the unit are issued (barrier), then
+        // one acquire-release increment per shared row and chunk; the unit that brings a
+        // row's last contribution queues the row
+        epilogue_sync();
+        int* qb = queues + buf * kQueueStride;
+        for (int I = e; I < nrows; I += kEpiWarps * 32) {
+          const int2 r = rinfo[I];
+          if (r.y >= 0) {
+            const unsigned old = atom_add_acq_rel_gpu(fz.counter + (int64_t)r.y * pr.n_chunks + w.chunk, 1u);
+            if ((old + 1u) % (unsigned)__ldg(fz.ncontrib + r.y) == 0u) qb[1 + atomicAdd(qb, 1)] = I;
+          }
+        }
+        epilogue_sync();
+        if (e == 0) queues[(buf ^ 1) * kQueueStride] = 0;  // last read in the previous unit
+        const int nq = qb[0];
+        const int v0 = w.chunk * kVec + lane * 4;
+        for (int k = ew; k < nq; k += kEpiWarps) {
+          const int2 r = rinfo[qb[1 + k]];
+          if (v0 < pr.B) {
+            const float4 a = ld_cg_f4(fz.acc + (int64_t)r.y * ld + v0);
+            const int64_t o = (int64_t)r.x * ld + v0;
+            __half h[4], l[4];
+            split_f32(a.x, h[0], l[0]);
+            split_f32(a.y, h[1], l[1]);
+            split_f32(a.z, h[2], l[2]);
+            split_f32(a.w, h[3], l[3]);
+            __half2* oh = reinterpret_cast<__half2*>(fz.ohi + o);
+            __half2* ol = reinterpret_cast<__half2*>(fz.olo + o);
+            oh[0] = __halves2half2(h[0], h[1]);
+            oh[1] = __halves2half2(h[2], h[3]);
+            ol[0] = __halves2half2(l[0], l[1]);
+            ol[1] = __halves2half2(l[2], l[3]);
+            if (fz.has_next) {
+              const __half2* ih = reinterpret_cast<const __half2*>(pr.xhi + o);
+              const __half2* il = reinterpret_cast<const __half2*>(pr.xlo + o);
+              const float2 h01 = __half22float2(__ldg(ih)), h23 = __half22float2(__ldg(ih + 1));
+              const float2 l01 = __half22float2(__ldg(il)), l23 = __half22float2(__ldg(il + 1));
+              float4 nx;
+              nx.x = fmaf(fz.bn, h01.x + l01.x, fz.cn * a.x);
+              nx.y = fmaf(fz.bn, h01.y + l01.y, fz.cn * a.y);
+              nx.z = fmaf(fz.bn, h23.x + l23.x, fz.cn * a.z);
+              nx.w = fmaf(fz.bn, h23.y + l23.y, fz.cn * a.w);
+              *reinterpret_cast<float4*>(fz.acc + (int64_t)r.y * ld + v0) = nx;
             }
           }
         }
@@ -651,6 +821,24 @@ __global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n
   }
 }
 
+// the fused step's tiles: (cell, half, K-block) tiles over nkb K-blocks; nodes J < n_e from the
+// cell matrices, the projector columns (J >= n_e) left zero here and scattered afterwards
+__global__ void k_split_mats_ext(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
+                                 int n_halves, int nkb, double scale, __half* __restrict__ hi,
+                                 __half* __restrict__ lo) {
+  const int64_t n = (int64_t)n_cells * n_halves * nkb * n_half * 32;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int c, I, J;
+    tile_entry(t, n_half, n_halves, nkb, c, I, J);
+    double v = 0.0;
+    if (I < n_e && J < n_e) v = scale * mats[((int64_t)c * n_e + I) * n_e + J];
+    const __half h = __double2half(v);
+    hi[t] = h;
+    lo[t] = __double2half(v - (double)__half2float(h));
+  }
+}
+
 // third term of the three-term split of the cell matrices: lo3 = fp16(v - hi - lo) with
 // v = 2^s A_e, hi = fp16(v), lo = fp16(v - hi) (the two-term arrays), in the same tile layout
 __global__ void k_split_mats_lo3(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
@@ -667,12 +855,6 @@ __global__ void k_split_mats_lo3(const double* __restrict__ mats, int n_cells, i
     const double l = (double)__half2float(__double2half(v - h));
     lo3[t] = __double2half(v - h - l);
   }
-}
-
-// FP32 -> FP16 hi + lo (22 significant bits; the vectors are pre-scaled into FP16's range)
-__device__ __forceinline__ void split_f32(float a, __half& h, __half& l) {
-  h = __float2half_rn(a);
-  l = __float2half_rn(a - __half2float(h));
 }
 
 // FP32 -> FP16 hi + lo + lo3, exact: x - hi and (x - hi) - lo are exact in FP32 and the last
@@ -798,7 +980,7 @@ struct TcPlan {
   int npad, n_half, n_halves, buf_stride, tmem_cols, stages, xstages, smem;
 };
 
-TcPlan plan_for(int n_e, int ns) {
+TcPlan plan_for(int n_e, int ns, bool fused = false) {
   TcPlan p{};
   p.npad = (n_e + 31) / 32 * 32;
   if (p.npad <= 256) {
@@ -815,7 +997,7 @@ TcPlan plan_for(int n_e, int ns) {
   const int budget = 220 * 1024;
   p.stages = 3;
   p.xstages = 8;
-  auto total = [&] { return make_layout(p.n_half, p.stages, p.xstages, ns).total + 1024; };
+  auto total = [&] { return make_layout(p.n_half, p.stages, p.xstages, ns, fused).total + 1024; };
   while (p.xstages > 3 && total() > budget) --p.xstages;
   if (total() > budget) p.stages = 2;
   p.smem = total();
@@ -949,6 +1131,87 @@ void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipelin
   auto kernel = ns == 3 ? cell_hx_tc_kernel<3, true> : cell_hx_tc_kernel<2, false>;
   CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   const int64_t grid = std::min<int64_t>(device_sms(), pairs);
+  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void tc_row_split(int n_e, int* n_half, int* n_halves) {
+  const TcPlan p = plan_for(n_e, 2, true);
+  *n_half = p.n_half;
+  *n_halves = p.n_halves;
+}
+
+void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __half* lo,
+                    cudaStream_t st) {
+  const TcPlan p = plan_for(op->n_e, 2, true);
+  const int64_t n = (int64_t)op->n_cells * p.n_halves * nkb * p.n_half * 32;
+  k_split_mats_ext<<<grid_for(n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, op->n_e, p.n_half,
+                                                     p.n_halves, nkb, scale, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
+  chefsi_operator_s* op = f.op;
+  const FusedPlan& fp = op->fz;
+  CHEFSI_REQUIRE(fp.ready, "fused filter step: tables not prepared");
+  const int n_e = op->n_e;
+  const TcPlan p = plan_for(n_e, 2, true);
+  CHEFSI_REQUIRE(f.B % 8 == 0 && (reinterpret_cast<uintptr_t>(f.xhi) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(f.xlo) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(f.ohi) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(f.olo) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(f.acc) & 15) == 0,
+                 "fused filter step: 16-byte aligned rows, B a multiple of 8");
+  TcArgs a{};
+  a.n_probs = 1;
+  a.n_e = n_e;
+  a.n_rows = n_e;
+  a.nkb = fp.nkb;
+  a.n_half = p.n_half;
+  a.n_halves = p.n_halves;
+  a.buf_stride = p.buf_stride;
+  a.tmem_cols = p.tmem_cols;
+  a.stages = p.stages;
+  a.xstages = p.xstages;
+  a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
+  if (!op->tc_err.ptr) {
+    op->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  }
+  a.err = op->tc_err.ptr;
+  TcProblem& pr = a.prob[0];
+  pr.xhi = f.xhi;
+  pr.xlo = f.xlo;
+  pr.xlo3 = f.xlo;
+  pr.dst = nullptr;
+  pr.map = op->map.ptr;
+  pr.ahi = fp.hi.ptr;
+  pr.alo = fp.lo.ptr;
+  pr.alo3 = fp.lo.ptr;
+  pr.ldx = f.B;
+  pr.ldd = f.B;
+  pr.B = f.B;
+  pr.n_chunks = (f.B + kVec - 1) / kVec;
+  pr.out_scale = (float)(f.a / fp.scale);
+  pr.pair_begin = 0;
+  a.n_pairs = (int64_t)op->n_cells * pr.n_chunks;
+  TcFused& z = a.fz;
+  z.mapk = fp.mapk.ptr;
+  z.kstride = fp.kstride;
+  z.has_next = f.has_next;
+  z.rowinfo = reinterpret_cast<const int2*>(fp.rowinfo.ptr);
+  z.ohi = f.ohi;
+  z.olo = f.olo;
+  z.acc = f.acc;
+  z.counter = f.counter;
+  z.ncontrib = fp.ncontrib.ptr;
+  z.cj = (float)f.c;
+  z.bj = (float)f.b;
+  z.cn = (float)f.cn;
+  z.bn = (float)f.bn;
+  auto kernel = cell_hx_tc_kernel<2, false, false, true>;
+  CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
   kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
   CHEFSI_CHECK_LAUNCH();
 }
