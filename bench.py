@@ -85,19 +85,22 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one cell_hx_tc_kernel launch (ncu capture of
-# `bench.py --workload mixed --hx-only`, summarised in profiles/cell_hx_tc_mixed_traffic.md)
-TC_TRAFFIC_BYTES = {"mixed": 20.33e9 + 8.20e9}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the filter's tensor-core kernel
+# (ncu captures summarised in profiles/): the separate-pass HX kernel on the full workload, and
+# the fused step's kernel (None until captured)
+TC_TRAFFIC_BYTES = {("mixed", False): 20.33e9 + 8.20e9}
 
 
-def hx_algorithmic(pr, B, s_h=4, s_x=4):
+def hx_algorithmic(pr, B, s_h=4, s_x=4, fused=False):
     """Bytes and flops of one filter HX over B vectors (reference formulation):
-    flops = 2 n_c n_e^2 B + 4 n_nlc-rows P B; bytes = s_H n_c n_e^2 + 2 s_X M B + 4 n_c n_e."""
+    flops = 2 n_c n_e^2 B + 4 n_nlc-rows P B; bytes = s_H n_c n_e^2 + 2 s_X M B + 4 n_c n_e.
+    A fused filter step (the recurrence finished in the same launch) also reads x_{k-2}:
+    + s_X M B."""
     nc, ne = pr.mesh.n_cells, pr.mesh.nodes_per_cell
     nl_rows = 0 if pr.nonlocal_ is None else int(pr.nonlocal_.ptr[-1])
     P = 0 if pr.nonlocal_ is None else pr.nonlocal_.n_proj
     flops = 2.0 * nc * ne * ne * B + 4.0 * nl_rows * P * B
-    bytes_ = s_h * nc * ne * ne + 2.0 * s_x * pr.n_dofs * B + 4.0 * nc * ne
+    bytes_ = s_h * nc * ne * ne + (3.0 if fused else 2.0) * s_x * pr.n_dofs * B + 4.0 * nc * ne
     return flops, bytes_
 
 
@@ -350,8 +353,10 @@ def run_ours(args):
     lo, blow, up = first_bounds(chefsi, op, N)
     # the large workload (4096 vectors) is filtered in blocks of 256, the others in one block
     blk = 256 if args.workload == "large" else N
+    fused = not args.no_fused
     params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=blk, wfcBlockSize=blk,
-                                 mixed_precision="mixed", rr_precision=args.rr_precision)
+                                 mixed_precision="mixed", rr_precision=args.rr_precision,
+                                 fused_recurrence=fused)
     solver = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params)
     solver.reinitSpectrumBounds(lo, blow, up)
     solver.set_profiling(True, mixed=True)
@@ -396,7 +401,9 @@ def run_ours(args):
     e2e = e2e_pipeline(step, X, max(2, min(args.steps, 4)))
     torch.cuda.empty_cache()
 
-    hx_flops, hx_bytes = hx_algorithmic(pr, N)
+    hx_flops, hx_bytes = hx_algorithmic(pr, blk, fused=fused)
+    hx_flops *= N / blk
+    hx_bytes *= N / blk
     hbm, bf16, src = peaks()
     avg_hx_ms = hx_ms / max(hx_n, 1)
     achieved = hx_bytes / (avg_hx_ms * 1e-3) / 1e9
@@ -409,6 +416,7 @@ def run_ours(args):
                    "fe_degree": pr.mesh.p, "n_wfc": N, "cheb_degree": m, "wells": 64,
                    "projectors_per_well": 8, "precision": "mixed",
                    "rr_hx_precision": args.rr_precision, "l2": "inputs > L2 (X is 14 GB)",
+                   "filter": "fused recurrence" if fused else "separate recurrence pass",
                    "parallelism": f"replicas{world}"},
         "hx_gflops": hx_flops / (avg_hx_ms * 1e-3) / 1e9,
         "hx_ms": avg_hx_ms, "hx_launches_timed": hx_n,
@@ -417,10 +425,13 @@ def run_ours(args):
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
-                     "traffic": TC_TRAFFIC_BYTES.get(args.workload), "peak_source": src,
-                     "traffic_scope": "cell_hx_tc_kernel launch alone, dram read + write, ncu "
-                                      "(profiles/cell_hx_tc_mixed_traffic.md)",
-                     "kernel": "cell_hx_tc_kernel (+ nonlocal, filter HX)",
+                     "traffic": TC_TRAFFIC_BYTES.get((args.workload, fused)), "peak_source": src,
+                     "traffic_scope": "the filter step's tensor-core kernel launch alone, dram "
+                                      "read + write, ncu (profiles/)",
+                     "kernel": ("cell_hx_tc_kernel<FUSED> + nonlocal projection: one filter step "
+                                "(HX, nonlocal, recurrence)") if fused else
+                               "cell_hx_tc_kernel + nonlocal kernels (filter HX; recurrence pass "
+                               "not included)",
                      "algorithmic_bytes_per_launch": hx_bytes},
         "e2e": e2e,
         "clocks": clk.summary(),
@@ -861,6 +872,8 @@ def main():
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
+    ap.add_argument("--no-fused", action="store_true",
+                    help="filter with the separate recurrence pass and nonlocal kernels")
     ap.add_argument("--no-fp64-leg", action="store_true",
                     help="skip the FP64 iteration and the Ritz-error comparison after the timed steps")
     ap.add_argument("--density-check", action="store_true",

@@ -12,9 +12,9 @@
 //        x_j = a_j (A x_{j-1} + C V W) + c_j x_{j-1} + b_j x_{j-2}
 //      and writes its FP16 hi + lo split: the vectors live only as split rows, so the next
 //      degree's gather reads them directly and no separate recurrence pass exists.
-// Rows of one cell entry are finished by that unit; rows shared by several cell entries go
-// through FP32 accumulators pre-set to c_j x_{j-1} + b_j x_{j-2} by the unit that finished
-// them in the previous degree (see TcFused in tc.cu).
+// Every row is reduced into an FP32 accumulator pre-set to c_j x_{j-1} + b_j x_{j-2}; the unit
+// that brings a row's last contribution (counted per row and 128-vector chunk) finishes it and
+// pre-sets the accumulator for the next degree (see TcFused in tc.cu).
 #include "internal.h"
 #include "tc_common.cuh"
 
@@ -28,22 +28,16 @@ namespace {
 
 constexpr int kNlChunkRows = 256;  // rows per projection chunk (the operator's chunk table)
 
-// acc[s][v] = c (hi + lo)[dof_s][v] for the shared rows (float4 units)
+// acc = c (hi + lo) over n entries (float4 units): the accumulators of the first degree
 __global__ void k_fz_acc_init(const __half* __restrict__ hi, const __half* __restrict__ lo,
-                              const int* __restrict__ shared_dof, int64_t n_shared, int B, float c,
-                              float* __restrict__ acc) {
-  const int q = B / 4;
-  const int64_t n = n_shared * q;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+                              int64_t n, float c, float* __restrict__ acc) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t s = t / q;
-    const int v = (int)(t - s * q) * 4;
-    const int64_t o = (int64_t)shared_dof[s] * B + v;
-    const __half2* h = reinterpret_cast<const __half2*>(hi + o);
-    const __half2* l = reinterpret_cast<const __half2*>(lo + o);
+    const __half2* h = reinterpret_cast<const __half2*>(hi) + 2 * t;
+    const __half2* l = reinterpret_cast<const __half2*>(lo) + 2 * t;
     const float2 h0 = __half22float2(h[0]), h1 = __half22float2(h[1]);
     const float2 l0 = __half22float2(l[0]), l1 = __half22float2(l[1]);
-    *reinterpret_cast<float4*>(acc + s * B + v) =
+    reinterpret_cast<float4*>(acc)[t] =
         make_float4(c * (h0.x + l0.x), c * (h0.y + l0.y), c * (h1.x + l1.x), c * (h1.y + l1.y));
   }
 }
@@ -226,14 +220,14 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
     std::vector<int64_t> fill(eptr.begin(), eptr.end() - 1);
     for (int64_t k = 0; k < (int64_t)map.size(); ++k) ent[fill[map[k]]++] = (int)k;  // c * ne + I
   }
-  std::vector<int> sidx(M, -1), shared_dof;
+  std::vector<int> sidx(M, -1);
   std::vector<unsigned char> ncontrib;
+  int64_t n_shared = 0;
   for (int64_t d = 0; d < M; ++d) {
     const int64_t cnt = eptr[d + 1] - eptr[d];
     CHEFSI_REQUIRE(cnt <= 255, "fused filter step: a dof with more than 255 cell entries");
     if (cnt > 1) {
-      sidx[d] = (int)shared_dof.size();
-      shared_dof.push_back((int)d);
+      sidx[d] = (int)n_shared++;
       ncontrib.push_back((unsigned char)cnt);
     }
   }
@@ -362,11 +356,10 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   to_device(fp.mapk, mapk);
   to_device(fp.rowinfo, rowinfo);
   to_device(fp.ncontrib, ncontrib);
-  to_device(fp.shared_dof, shared_dof);
   fp.nkb = nkb;
   fp.kstride = kstride;
   fp.max_slots = max_slots;
-  fp.n_shared = (int64_t)shared_dof.size();
+  fp.n_shared = n_shared;
   fp.rows = M + (int64_t)op->n_atoms * P;
   fp.scale = (float)scale;
   fp.wscale = (float)wscale;
@@ -387,7 +380,7 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
   const size_t nrows = (size_t)fp.rows * B;
   __half* h[2] = {w.hi[0].ensure(nrows), w.hi[1].ensure(nrows)};
   __half* l[2] = {w.lo[0].ensure(nrows), w.lo[1].ensure(nrows)};
-  float* acc = w.acc.ensure(std::max<size_t>(1, (size_t)fp.n_shared * B));
+  float* acc = w.acc.ensure((size_t)M * B);
   unsigned* counter = w.counter.ensure(std::max<size_t>(1, (size_t)fp.n_shared * n_chunks));
   float* W = op->n_atoms ? w.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
   CHEFSI_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * (size_t)fp.n_shared * n_chunks, st));
@@ -408,11 +401,8 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
     }
   }
   split_rows_f32(X, B, M, B, h[0], l[0], st);
-  if (fp.n_shared) {
-    k_fz_acc_init<<<grid_for(fp.n_shared * (B / 4), 256), 256, 0, st>>>(
-        h[0], l[0], fp.shared_dof.ptr, fp.n_shared, B, (float)cc[1], acc);
-    CHEFSI_CHECK_LAUNCH();
-  }
+  k_fz_acc_init<<<grid_for(M * B / 4, 256), 256, 0, st>>>(h[0], l[0], M * B, (float)cc[1], acc);
+  CHEFSI_CHECK_LAUNCH();
   for (int j = 1; j <= m; ++j) {
     const int in = (j - 1) & 1, out = j & 1;
     mark();

@@ -37,7 +37,8 @@ struct TensorCellMats {
 
 // Tables of the fused filter step (tc.cu, fused.cu), built once per operator on first use:
 // * rows: every cell entry (cell, node) is "single" when its dof has no other cell entry (its
-//   row is finished by one unit) or "shared" (an FP32 accumulator row and arrival counters);
+//   row is finished by the one unit that reduces into it) or "shared" (arrival counters per
+//   128-vector chunk decide which unit finishes it);
 // * the nonlocal term as extra K columns of the cell matrices: each (atom, dof) pair of the
 //   projectors is given to one cell entry of its dof (greedily, so that few cells take more
 //   than one atom), a cell's atoms occupy n_proj K columns each after its n_e nodes, holding
@@ -55,7 +56,6 @@ struct FusedPlan {
   DeviceBuffer<int> mapk;         // [n_cells][kstride]
   DeviceBuffer<int> rowinfo;      // [n_cells][n_e] x {dof, shared index or -1}
   DeviceBuffer<unsigned char> ncontrib;  // [n_shared]
-  DeviceBuffer<int> shared_dof;   // [n_shared]
   DeviceBuffer<__half> hi, lo;    // extended cell-matrix tiles [n_cells][halves][nkb][n_half x 32]
 };
 
@@ -194,8 +194,8 @@ void tc_row_split(int n_e, int* n_half, int* n_halves);
 // (cell, half, K-block) tiles of 2^s A_e over nkb K-blocks (columns past n_e zero)
 void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __half* lo,
                     cudaStream_t st);
-// workspaces of the fused filter (grow-only): two split buffers (x_{j-1}; x_{j-2} -> x_j), the
-// shared rows' accumulators and arrival counters, the projector coefficients W
+// workspaces of the fused filter (grow-only): two split buffers (x_{j-1}; x_j), the rows' FP32
+// accumulators [n_dofs][B], the shared rows' arrival counters, the projector coefficients W
 struct FusedWork {
   DeviceBuffer<__half> hi[2], lo[2];
   DeviceBuffer<float> acc, W;

@@ -86,20 +86,20 @@ constexpr int kMaxGroup = 32;
 
 // The fused filter step (one problem): the epilogue finishes the three-term recurrence
 //   x_j = out_scale D + cj x_{j-1} + bj x_{j-2}
-// instead of scatter-adding D. Rows that one cell entry owns alone ("single" rows) are written
-// at once as the FP16 split of x_j (x_{j-1} from the input split rows, x_{j-2} from the output
-// rows, which still hold it); rows shared by several cell entries are reduced into FP32
-// accumulators (pre-set to cj x_{j-1} + bj x_{j-2}), and the unit that brings the last
-// contribution of a row (per 128-vector chunk, counted with acquire-release atomics) writes
-// its split and pre-sets the accumulator for the next step: cn x_j + bn x_{j-1}.
+// instead of only scatter-adding D. Every row's FP32 accumulator is pre-set to
+// cj x_{j-1} + bj x_{j-2} (by the previous degree); the drain warps reduce D into it. Once the
+// unit's reductions are performed, the finalizer warps count the unit's arrival on each shared
+// row (acquire-release atomics per row and 128-vector chunk); the unit that brings a row's last
+// contribution (always, for rows of one cell entry) writes the row's FP16 split of x_j and
+// pre-sets its accumulator for the next degree: cn x_j + bn x_{j-1}.
 struct TcFused {
   const int* mapk;                 // [n_cells][kstride] split row feeding K index J (-1: zero)
   int kstride;
   int has_next;
   const int2* rowinfo;             // [n_cells][n_e] {dof, shared index or -1}
-  __half* ohi;                     // output split rows (x_j); single rows hold x_{j-2} on entry
+  __half* ohi;                     // output split rows (x_j)
   __half* olo;
-  float* acc;                      // [n_shared][B] accumulators of the shared rows
+  float* acc;                      // [n_dofs][B] accumulators
   unsigned* counter;               // [n_shared][n_chunks] arrivals
   const unsigned char* ncontrib;   // [n_shared] cell entries per shared row
   float cj, bj, cn, bn;
@@ -147,7 +147,7 @@ __host__ __device__ inline Layout make_layout(int n_half, int stages, int xstage
   L.astage = ns * L.a_tile;
   L.aoff = xstages * L.xstage;
   L.bars = L.aoff + stages * L.astage;
-  L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 8);
+  L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 12);
   L.queue = L.offs + 2 * 256 * 8;
   L.total = L.queue + (fused ? 2 * kQueueStride * 4 : 0);
   return L;
@@ -252,6 +252,23 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
 //                 instruction; row offsets staged in shared memory once per unit),
 //                 overlapped with the MMAs of the next unit
 constexpr int kThreads3 = 192 + 32 * kEpiWarps;
+// the fused step adds a warpgroup of finalizer warps (the recurrence of finished rows)
+constexpr int kFinWarps = 8;
+constexpr int kThreadsFused = kThreads3 + 32 * kFinWarps;
+// named barrier 3 among the finalizer warps, with an AND-reduction of v
+__device__ __forceinline__ bool fin_sync_and(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 3, %2, pi;\n"
+      " selp.u32 %0, 1, 0, po;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kFinWarps * 32)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void fin_sync() {
+  asm volatile("bar.sync 3, %0;" ::"n"(kFinWarps * 32) : "memory");
+}
 
 // NS = 2: the filter's split (hi + lo, 22 bits), products Xhi Ahi + Xhi Alo + Xlo Ahi.
 // NS = 3: hi + lo + lo3 (33 bits: an FP32 vector exactly, the cell matrix to 2^-33), products
@@ -270,7 +287,7 @@ constexpr int kChunkCols = 96;
 //        (the cell's nodes, then its projector coefficients W), the epilogue finishes the
 //        recurrence.
 template <int NS, bool KCHUNK, bool DENS = false, bool FUSED = false>
-__global__ void __launch_bounds__(kThreads3, 1)
+__global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     cell_hx_tc_kernel(TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -287,6 +304,8 @@ __global__ void __launch_bounds__(kThreads3, 1)
   uint64_t* mma_done = acc_full + 4;                // final MMA completion
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(acc_full + 6);
+  uint64_t* rows_ready = acc_full + 7;    // [2] fused: a unit's reductions are performed
+  uint64_t* rows_empty = acc_full + 9;    // [2] fused: the finalizers are done with the slot
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t first = blockIdx.x;
@@ -311,6 +330,12 @@ __global__ void __launch_bounds__(kThreads3, 1)
       mbar_init(&acc_empty[b], kEpiWarps);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
+    if (FUSED) {
+      for (int b = 0; b < 2; ++b) {
+        mbar_init(&rows_ready[b], 1);
+        mbar_init(&rows_empty[b], kFinWarps);
+      }
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -523,6 +548,88 @@ __global__ void __launch_bounds__(kThreads3, 1)
       if (++s_arr == SX) s_arr = 0;
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
+  } else if (FUSED && warp >= 6 + kEpiWarps) {
+    // ---------------- fused step: finalizer warps, one unit behind the drain. For each unit:
+    // arrivals on the shared rows (acquire-release; the unit that brings a row's last
+    // contribution finishes it), then for every finished row (single rows always) and the
+    // unit's 128-vector chunk, a warp at a time with 16-byte accesses:
+    //   x_j = acc;  split(x_j) -> output rows;  acc <- cn x_j + bn x_{j-1}  (next degree)
+    const TcFused& fz = args.fz;
+    const TcProblem& pr = args.prob[0];
+    const int f = threadIdx.x - (192 + 32 * kEpiWarps);   // finalizer thread 0..255
+    const int fw = f >> 5;
+    int* lists = reinterpret_cast<int*>(smem + L.queue);
+    const int64_t ld = pr.ldx;
+    constexpr int kBatch = 4;
+    for (int64_t it = 0; it < my_units; ++it) {
+      const int slot = (int)(it & 1);
+      const uint32_t ph = (uint32_t)((it >> 1) & 1);
+      const bool okw = __all_sync(0xffffffffu, mbar_wait(&rows_ready[slot], ph, args.err, abort_flag));
+      int* list = lists + slot * kQueueStride;
+      if (f == 0) list[0] = 0;
+      if (!fin_sync_and(okw)) break;
+      const Unit w = unit_at(it, first, step, args);
+      const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
+      const int2* rinfo = reinterpret_cast<const int2*>(smem + L.offs) + slot * 256;
+      for (int I = f; I < nrows; I += 32 * kFinWarps) {
+        const int2 r = rinfo[I];
+        bool last = r.y < 0;
+        if (!last) {
+          const unsigned old = atom_add_acq_rel_gpu(fz.counter + (int64_t)r.y * pr.n_chunks + w.chunk, 1u);
+          last = (old + 1u) % (unsigned)__ldg(fz.ncontrib + r.y) == 0u;
+        }
+        if (last) list[1 + atomicAdd(list, 1)] = I;
+      }
+      fin_sync();
+      const int n = list[0];
+      const int v0 = w.chunk * kVec + lane * 4;
+      if (v0 < pr.B) {
+        for (int k0 = fw; k0 < n; k0 += kFinWarps * kBatch) {
+          float4 a[kBatch];
+          uint2 xh[kBatch], xl[kBatch];
+          int64_t o[kBatch];
+#pragma unroll
+          for (int b = 0; b < kBatch; ++b) {
+            const int k = k0 + b * kFinWarps;
+            o[b] = k < n ? (int64_t)rinfo[list[1 + k]].x * ld + v0 : -1;
+            if (o[b] >= 0) {
+              a[b] = ld_cg_f4(fz.acc + o[b]);
+              if (fz.has_next) {
+                xh[b] = __ldg(reinterpret_cast<const uint2*>(pr.xhi + o[b]));
+                xl[b] = __ldg(reinterpret_cast<const uint2*>(pr.xlo + o[b]));
+              }
+            }
+          }
+#pragma unroll
+          for (int b = 0; b < kBatch; ++b) {
+            if (o[b] < 0) continue;
+            __half h[4], l[4];
+            split_f32(a[b].x, h[0], l[0]);
+            split_f32(a[b].y, h[1], l[1]);
+            split_f32(a[b].z, h[2], l[2]);
+            split_f32(a[b].w, h[3], l[3]);
+            __half2 hh[2] = {__halves2half2(h[0], h[1]), __halves2half2(h[2], h[3])};
+            __half2 ll[2] = {__halves2half2(l[0], l[1]), __halves2half2(l[2], l[3])};
+            *reinterpret_cast<uint2*>(fz.ohi + o[b]) = *reinterpret_cast<uint2*>(hh);
+            *reinterpret_cast<uint2*>(fz.olo + o[b]) = *reinterpret_cast<uint2*>(ll);
+            if (fz.has_next) {
+              const float2 h01 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].x));
+              const float2 h23 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].y));
+              const float2 l01 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].x));
+              const float2 l23 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].y));
+              float4 nx;
+              nx.x = fmaf(fz.bn, h01.x + l01.x, fz.cn * a[b].x);
+              nx.y = fmaf(fz.bn, h01.y + l01.y, fz.cn * a[b].y);
+              nx.z = fmaf(fz.bn, h23.x + l23.x, fz.cn * a[b].z);
+              nx.w = fmaf(fz.bn, h23.y + l23.y, fz.cn * a[b].w);
+              *reinterpret_cast<float4*>(fz.acc + o[b]) = nx;
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&rows_empty[slot]);
+    }
   } else {
     // ---------------- epilogue warps 6..6 + kEpiWarps - 1
     const int q = warp & 3;                  // tensor-memory lane quarter of this warp
@@ -587,116 +694,60 @@ __global__ void __launch_bounds__(kThreads3, 1)
         }
       }
     } else if (FUSED) {
-      // ---- the fused filter step: finish the recurrence in the epilogue
-      const TcFused& fz = args.fz;
+      // ---- the fused step's drain: every row of the unit is reduced into its FP32 accumulator
+      // (pre-set to c x_{j-1} + b x_{j-2}); at the start of the next unit the warps fence
+      // their reductions (gpu scope) and hand the unit to the finalizer warps
       const TcProblem& pr = args.prob[0];
-      const int e = threadIdx.x - 192;          // epilogue thread 0..255
-      const int ew = warp - 6;                  // epilogue warp 0..7
-      int* queues = reinterpret_cast<int*>(smem + L.queue);
-      if (e < 2) queues[e * kQueueStride] = 0;  // ordered by the first unit's barrier
-      const int64_t ld = pr.ldx;                // split rows, accumulators: ld = B
-      for (int64_t it = 0; it < my_units; ++it) {
+      const int e = threadIdx.x - 192;          // drain thread 0..255
+      bool ok = true;
+      int64_t it = 0;
+      for (; it < my_units; ++it) {
         const int buf = (int)(it & 1);
         const uint32_t ph = (uint32_t)((it >> 1) & 1);
-        const bool okw = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], ph, args.err, abort_flag));
+        bool okw = mbar_wait(&acc_full[buf], ph, args.err, abort_flag);
+        // the slot's row table was last read by the finalizers for unit it - 2
+        okw = okw && mbar_wait(&rows_empty[buf], ph ^ 1, args.err, abort_flag);
+        okw = __all_sync(0xffffffffu, okw);
         fence_after();
         const Unit w = unit_at(it, first, step, args);
         const int nrows = min(args.n_half, args.n_e - w.half * args.n_half);
-        // the unit's rows: {dof, shared index or -1}, staged once
         int2* rinfo = reinterpret_cast<int2*>(smem + L.offs) + buf * 256;
         if (okw)
           for (int I = e; I < args.n_half; I += kEpiWarps * 32)
-            rinfo[I] = I < nrows ? __ldg(fz.rowinfo + (int64_t)w.cell * args.n_e +
+            rinfo[I] = I < nrows ? __ldg(args.fz.rowinfo + (int64_t)w.cell * args.n_e +
                                          w.half * args.n_half + I)
                                  : make_int2(-1, -1);
-        if (!epilogue_sync_and(okw)) break;
+        // the previous unit's reductions are performed at gpu scope before it is handed over
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        if (!epilogue_sync_and(okw)) {
+          ok = false;
+          break;
+        }
+        if (it > 0 && e == 0) mbar_arrive(&rows_ready[(it - 1) & 1]);
         const int gb = w.chunk * kVec + q * 32 + lane;
         const bool vok = gb < pr.B;
+        float* accb = args.fz.acc + gb;
         const float osc = pr.out_scale;
         const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
         for (int c0 = c_beg; c0 < c_end; c0 += 16) {
           float vals[16];
           tmem_ld16(tq + c0, vals);
           if (vok) {
-            float xm1[16], xm2[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-              const int2 r = rinfo[c0 + i];
-              xm1[i] = 0.f;
-              xm2[i] = 0.f;
-              if (r.x >= 0 && r.y < 0) {
-                const int64_t o = (int64_t)r.x * ld + gb;
-                xm1[i] = __half2float(__ldg(pr.xhi + o)) + __half2float(__ldg(pr.xlo + o));
-                if (fz.bj != 0.f) xm2[i] = __half2float(fz.ohi[o]) + __half2float(fz.olo[o]);
-              }
-            }
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              const int2 r = rinfo[c0 + i];
-              if (r.x < 0) continue;
-              const float v = osc * vals[i];
-              if (r.y < 0) {
-                const float x = fmaf(fz.bj, xm2[i], fmaf(fz.cj, xm1[i], v));
-                const int64_t o = (int64_t)r.x * ld + gb;
-                __half h, l;
-                split_f32(x, h, l);
-                fz.ohi[o] = h;
-                fz.olo[o] = l;
-              } else {
-                atomicAdd(fz.acc + (int64_t)r.y * ld + gb, v);
-              }
+              const int d = rinfo[c0 + i].x;
+              if (d >= 0) atomicAdd(accb + (int64_t)d * pr.ldx, osc * vals[i]);
             }
           }
         }
         fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty[buf]);
-        // arrivals: every epilogue thread's reductions of the unit are issued (barrier), then
-        // one acquire-release increment per shared row and chunk; the unit that brings a
-        // row's last contribution queues the row
+      }
+      if (ok && it > 0) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         epilogue_sync();
-        int* qb = queues + buf * kQueueStride;
-        for (int I = e; I < nrows; I += kEpiWarps * 32) {
-          const int2 r = rinfo[I];
-          if (r.y >= 0) {
-            const unsigned old = atom_add_acq_rel_gpu(fz.counter + (int64_t)r.y * pr.n_chunks + w.chunk, 1u);
-            if ((old + 1u) % (unsigned)__ldg(fz.ncontrib + r.y) == 0u) qb[1 + atomicAdd(qb, 1)] = I;
-          }
-        }
-        epilogue_sync();
-        if (e == 0) queues[(buf ^ 1) * kQueueStride] = 0;  // last read in the previous unit
-        const int nq = qb[0];
-        const int v0 = w.chunk * kVec + lane * 4;
-        for (int k = ew; k < nq; k += kEpiWarps) {
-          const int2 r = rinfo[qb[1 + k]];
-          if (v0 < pr.B) {
-            const float4 a = ld_cg_f4(fz.acc + (int64_t)r.y * ld + v0);
-            const int64_t o = (int64_t)r.x * ld + v0;
-            __half h[4], l[4];
-            split_f32(a.x, h[0], l[0]);
-            split_f32(a.y, h[1], l[1]);
-            split_f32(a.z, h[2], l[2]);
-            split_f32(a.w, h[3], l[3]);
-            __half2* oh = reinterpret_cast<__half2*>(fz.ohi + o);
-            __half2* ol = reinterpret_cast<__half2*>(fz.olo + o);
-            oh[0] = __halves2half2(h[0], h[1]);
-            oh[1] = __halves2half2(h[2], h[3]);
-            ol[0] = __halves2half2(l[0], l[1]);
-            ol[1] = __halves2half2(l[2], l[3]);
-            if (fz.has_next) {
-              const __half2* ih = reinterpret_cast<const __half2*>(pr.xhi + o);
-              const __half2* il = reinterpret_cast<const __half2*>(pr.xlo + o);
-              const float2 h01 = __half22float2(__ldg(ih)), h23 = __half22float2(__ldg(ih + 1));
-              const float2 l01 = __half22float2(__ldg(il)), l23 = __half22float2(__ldg(il + 1));
-              float4 nx;
-              nx.x = fmaf(fz.bn, h01.x + l01.x, fz.cn * a.x);
-              nx.y = fmaf(fz.bn, h01.y + l01.y, fz.cn * a.y);
-              nx.z = fmaf(fz.bn, h23.x + l23.x, fz.cn * a.z);
-              nx.w = fmaf(fz.bn, h23.y + l23.y, fz.cn * a.w);
-              *reinterpret_cast<float4*>(fz.acc + (int64_t)r.y * ld + v0) = nx;
-            }
-          }
-        }
+        if (e == 0) mbar_arrive(&rows_ready[(it - 1) & 1]);
       }
     } else if (DENS) {
       for (int64_t it = 0; it < my_units; ++it) {
@@ -1212,7 +1263,7 @@ void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
   auto kernel = cell_hx_tc_kernel<2, false, false, true>;
   CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
-  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
+  kernel<<<(unsigned)grid, kThreadsFused, p.smem, st>>>(a);
   CHEFSI_CHECK_LAUNCH();
 }
 
