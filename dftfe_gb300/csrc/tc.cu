@@ -589,10 +589,7 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
       fin_sync();
       const int n = list[0];
       const int v0 = w.chunk * kVec + lane * 4;
-      // lanes past the block's last vector take part in the loop (it holds a __syncwarp) but
-      // touch no memory; the loop bounds are the same for the whole warp
-      const bool lok = v0 < pr.B;
-      {
+      if (v0 < pr.B) {
         for (int k0 = fw; k0 < n; k0 += kFinWarps * kBatch) {
           float4 a[kBatch];
           uint2 xh[kBatch], xl[kBatch];
@@ -605,7 +602,7 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
             o[b] = -1;
             src[b] = nullptr;
             shr[b] = false;
-            if (k < n && lok) {
+            if (k < n) {
               const int I = list[1 + k];
               const int2 r = rinfo[I];
               o[b] = (int64_t)r.x * ld + v0;
