@@ -1,21 +1,20 @@
 // The fused Chebyshev filter on tensor cores: one persistent launch per degree finishes the
-// three-term recurrence inside the HX kernel, and the nonlocal apply rides in the same launch
-// as extra K columns of the cell matrices.
+// three-term recurrence inside the HX kernel's epilogue, and the nonlocal apply rides in the
+// same launch as extra K columns of the cell matrices.
 //
 // DFT-FE's filter (linearAlgebraOperationsDevice::chebyshevFilter,
 // src/linAlg/linearAlgebraOperationsDevice.cc:531-727) runs per degree an HX (gather,
 // cell GEMMs, scatter; the nonlocal term by a projection, a cross-cell reduction and an apply)
-// and combinedDeviceKernel (:37-104), an axpby pass over the whole block. In the sigma form
-// x_j = a_j (A - c) x_{j-1} + b_j x_{j-2} with c the centre of the damped interval for every
-// degree, so c is folded into the tiles' diagonals once per filter call. Per degree j:
+// and combinedDeviceKernel (:37-104), an axpby pass over the whole block. Here, per degree j:
 //   1. W = C^T x_{j-1} over the projector rows (nl projection from the split rows), written
 //      as split rows n_dofs + a P + i of the same buffer, scaled by 2^t;
 //   2. one launch of cell_hx_tc_kernel<FUSED> computes, for every dof row,
-//        x_j = a_j ((A - c) x_{j-1} + C V W) + b_j x_{j-2}
-//      over the rows of x_{j-2} and writes its FP16 hi + lo split: the vectors live only as
-//      split rows, so the next degree's gather reads them directly and no recurrence pass
-//      exists. Rows of one cell entry pass through an L2-resident per-CTA scratch; rows shared
-//      by several entries through FP32 accumulators (see TcFused in tc.cu).
+//        x_j = a_j (A x_{j-1} + C V W) + c_j x_{j-1} + b_j x_{j-2}
+//      and writes its FP16 hi + lo split: the vectors live only as split rows, so the next
+//      degree's gather reads them directly and no separate recurrence pass exists.
+// Every row is reduced into an FP32 accumulator pre-set to c_j x_{j-1} + b_j x_{j-2}; the unit
+// that brings a row's last contribution (counted per row and 128-vector chunk) finishes it and
+// pre-sets the accumulator for the next degree (see TcFused in tc.cu).
 #include "internal.h"
 #include "tc_common.cuh"
 
@@ -29,30 +28,17 @@ namespace {
 
 constexpr int kNlChunkRows = 256;  // rows per projection chunk (the operator's chunk table)
 
-// the diagonal entries of the tiles: 2^s (A_II - c / n_entries) at diag_idx
-__global__ void k_fz_shift(const int64_t* __restrict__ idx, const double* __restrict__ dval,
-                           const int2* __restrict__ rowinfo, const unsigned char* __restrict__ ncontrib,
-                           int64_t n, double scale, double c, __half* __restrict__ hi,
-                           __half* __restrict__ lo) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+// acc = c (hi + lo) over n entries (float4 units): the accumulators of the first degree
+__global__ void k_fz_acc_init(const __half* __restrict__ hi, const __half* __restrict__ lo,
+                              int64_t n, float c, float* __restrict__ acc) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int sh = rowinfo[t].y;
-    const double ne = sh < 0 ? 1.0 : (double)ncontrib[sh];
-    const double v = scale * (dval[t] - c / ne);
-    const __half h = __double2half(v);
-    hi[idx[t]] = h;
-    lo[idx[t]] = __double2half(v - (double)__half2float(h));
-  }
-}
-
-// A_II of every cell entry (the folded cell matrices)
-__global__ void k_fz_diag(const double* __restrict__ mats, int64_t n_entries, int n_e,
-                          double* __restrict__ out) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_entries;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = t / n_e;
-    const int I = (int)(t - c * n_e);
-    out[t] = mats[(c * n_e + I) * n_e + I];
+    const __half2* h = reinterpret_cast<const __half2*>(hi) + 2 * t;
+    const __half2* l = reinterpret_cast<const __half2*>(lo) + 2 * t;
+    const float2 h0 = __half22float2(h[0]), h1 = __half22float2(h[1]);
+    const float2 l0 = __half22float2(l[0]), l1 = __half22float2(l[1]);
+    reinterpret_cast<float4*>(acc)[t] =
+        make_float4(c * (h0.x + l0.x), c * (h0.y + l0.y), c * (h1.x + l1.x), c * (h1.y + l1.y));
   }
 }
 
@@ -90,13 +76,12 @@ __global__ void k_fz_join(const __half* __restrict__ hi, const __half* __restric
 }
 
 // the projector columns of the extended tiles: entry idx[k] of the tile array receives the split
-// of scale * val[k]
+// of val[k] (already scaled)
 __global__ void k_fz_scatter(const int64_t* __restrict__ idx, const double* __restrict__ val,
-                             int64_t n, double scale, __half* __restrict__ hi,
-                             __half* __restrict__ lo) {
+                             int64_t n, __half* __restrict__ hi, __half* __restrict__ lo) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const double v = scale * val[t];
+    const double v = val[t];
     const __half h = __double2half(v);
     hi[idx[t]] = h;
     lo[idx[t]] = __double2half(v - (double)__half2float(h));
@@ -326,13 +311,18 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   double am = 0.0;
   CHEFSI_CUDA(cudaMemcpyAsync(&am, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
-  fp.amax = std::max(am, ext_max);
+  am = std::max(am, ext_max);
+  const int e = (am > 0 && std::isfinite(am)) ? 14 - (int)std::floor(std::log2(am)) : 0;
+  const double scale = std::ldexp(1.0, e);
   int n_half = 0, n_halves = 0;
   tc_row_split(ne, &n_half, &n_halves);
-  // tile elements of the projector columns and of the diagonal entries
-  std::vector<int64_t> idx;
-  std::vector<double> val;
+  const size_t ntile = (size_t)nc * n_halves * nkb * n_half * 32;
+  fp.hi.reset(ntile);
+  fp.lo.reset(ntile);
+  split_mats_ext(op, nkb, scale, fp.hi.ptr, fp.lo.ptr, st);
   if (P) {
+    std::vector<int64_t> idx;
+    std::vector<double> val;
     idx.reserve((size_t)op->nl_nnz * P);
     val.reserve((size_t)op->nl_nnz * P);
     for (int a = 0; a < op->n_atoms; ++a)
@@ -350,29 +340,17 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
           const int J = ne + sl * P + j;
           const int64_t tix = ((int64_t)c * n_halves + half) * nkb + J / 32;
           idx.push_back(tix * n_half * 32 + tcx::sw64_offset((uint32_t)ri, 2u * (uint32_t)(J % 32)) / 2);
-          val.push_back(C[(size_t)r * P + j] * V[(size_t)a * P + j] / wscale);
+          val.push_back(scale / wscale * C[(size_t)r * P + j] * V[(size_t)a * P + j]);
         }
       }
-  }
-  std::vector<int64_t> didx((size_t)nc * ne);
-  for (int c = 0; c < nc; ++c)
-    for (int I = 0; I < ne; ++I) {
-      const int half = I / n_half, ri = I % n_half;
-      const int64_t tix = ((int64_t)c * n_halves + half) * nkb + I / 32;
-      didx[(size_t)c * ne + I] =
-          tix * n_half * 32 + tcx::sw64_offset((uint32_t)ri, 2u * (uint32_t)(I % 32)) / 2;
-    }
-  to_device(fp.ext_idx, idx);
-  to_device(fp.ext_val, val);
-  to_device(fp.diag_idx, didx);
-  fp.diag_val.reset((size_t)nc * ne);
-  k_fz_diag<<<grid_for((int64_t)nc * ne, 256), 256, 0, st>>>(op->mats64.ptr, (int64_t)nc * ne, ne,
-                                                             fp.diag_val.ptr);
-  CHEFSI_CHECK_LAUNCH();
-  {
-    DeviceBuffer<double> dm(1);
-    absmax_block_f64(fp.diag_val.ptr, 1, (int64_t)nc * ne, 1, dm.ptr, st);
-    CHEFSI_CUDA(cudaMemcpyAsync(&fp.diag_max, dm.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    DeviceBuffer<int64_t> didx;
+    DeviceBuffer<double> dval;
+    to_device(didx, idx);
+    to_device(dval, val);
+    k_fz_scatter<<<grid_for((int64_t)idx.size(), 256), 256, 0, st>>>(didx.ptr, dval.ptr,
+                                                                     (int64_t)idx.size(), fp.hi.ptr,
+                                                                     fp.lo.ptr);
+    CHEFSI_CHECK_LAUNCH();
     CHEFSI_CUDA(cudaStreamSynchronize(st));
   }
   to_device(fp.mapk, mapk);
@@ -383,53 +361,9 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   fp.max_slots = max_slots;
   fp.n_shared = n_shared;
   fp.rows = M + (int64_t)op->n_atoms * P;
+  fp.scale = (float)scale;
   fp.wscale = (float)wscale;
-  fp.scale_exp = 1 << 30;  // no tiles yet
-  fp.shifted = false;
   fp.ready = true;
-}
-
-namespace {
-
-// the tiles at scale 2^e: the cell matrices, then the projector columns (diagonals unshifted)
-void build_fused_tiles(chefsi_operator_s* op, int e, cudaStream_t st) {
-  FusedPlan& fp = op->fz;
-  int n_half = 0, n_halves = 0;
-  tc_row_split(op->n_e, &n_half, &n_halves);
-  const size_t ntile = (size_t)op->n_cells * n_halves * fp.nkb * n_half * 32;
-  if (fp.hi.n != ntile) {
-    fp.hi.reset(ntile);
-    fp.lo.reset(ntile);
-  }
-  const double scale = std::ldexp(1.0, e);
-  split_mats_ext(op, fp.nkb, scale, fp.hi.ptr, fp.lo.ptr, st);
-  if (fp.ext_idx.n) {
-    k_fz_scatter<<<grid_for((int64_t)fp.ext_idx.n, 256), 256, 0, st>>>(
-        fp.ext_idx.ptr, fp.ext_val.ptr, (int64_t)fp.ext_idx.n, scale, fp.hi.ptr, fp.lo.ptr);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  fp.scale_exp = e;
-  fp.shifted = false;
-}
-
-}  // namespace
-
-// The shift c in the diagonal entries (2^s (A_II - c / n_entries)); the scale s is lowered (the
-// tiles rebuilt) when |A_II| + |c| would leave FP16's range at the current one.
-void fused_set_shift(chefsi_operator_s* op, double c, cudaStream_t st) {
-  FusedPlan& fp = op->fz;
-  const double big = std::max(fp.amax, fp.diag_max + std::fabs(c));
-  const int e = (big > 0 && std::isfinite(big)) ? 14 - (int)std::floor(std::log2(big)) : 0;
-  if (e < fp.scale_exp || fp.scale_exp == (1 << 30)) build_fused_tiles(op, e, st);
-  if (fp.shifted && fp.c_applied == c) return;
-  const int64_t n = (int64_t)op->n_cells * op->n_e;
-  k_fz_shift<<<grid_for(n, 256), 256, 0, st>>>(fp.diag_idx.ptr, fp.diag_val.ptr,
-                                               reinterpret_cast<const int2*>(fp.rowinfo.ptr),
-                                               fp.ncontrib.ptr, n, std::ldexp(1.0, fp.scale_exp), c,
-                                               fp.hi.ptr, fp.lo.ptr);
-  CHEFSI_CHECK_LAUNCH();
-  fp.c_applied = c;
-  fp.shifted = true;
 }
 
 // The filter of one block: X [M][B] FP32 in (scaled so that max |x| ~ 2^8), p_m(A) X out.
@@ -441,34 +375,34 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
                        double a, double b, double a0, const std::function<void()>& mark,
                        cudaStream_t st) {
   prepare_fused_plan(op, st);
-  const double e = (b - a) / 2.0, c = (b + a) / 2.0;
-  fused_set_shift(op, c, st);
   const FusedPlan& fp = op->fz;
   const int n_chunks = (B + 127) / 128;
   const size_t nrows = (size_t)fp.rows * B;
   __half* h[2] = {w.hi[0].ensure(nrows), w.hi[1].ensure(nrows)};
   __half* l[2] = {w.lo[0].ensure(nrows), w.lo[1].ensure(nrows)};
-  const size_t nacc = std::max<size_t>(1, (size_t)fp.n_shared * B);
-  float* acc = w.acc.ensure(nacc);
+  float* acc = w.acc.ensure((size_t)M * B);
   unsigned* counter = w.counter.ensure(std::max<size_t>(1, (size_t)fp.n_shared * n_chunks));
-  float* scratch = w.scratch.ensure((size_t)device_sms() * kScratchFloatsPerCta);
   float* W = op->n_atoms ? w.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
   CHEFSI_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * (size_t)fp.n_shared * n_chunks, st));
-  CHEFSI_CUDA(cudaMemsetAsync(acc, 0, sizeof(float) * nacc, st));   // the finalizers keep it zero
-  // coefficients: x_j = ca_j (A - c) x_{j-1} + cb_j x_{j-2}
-  std::vector<double> ca(m + 1, 0.0), cb(m + 1, 0.0);
+  // coefficients a_j, c_j, b_j for j = 1..m
+  std::vector<double> ca(m + 2, 0.0), cc(m + 2, 0.0), cb(m + 2, 0.0);
   {
+    const double e = (b - a) / 2.0, c = (b + a) / 2.0;
     double sigma = e / (a0 - c);
     const double sigma1 = sigma, gamma = 2.0 / sigma1;
     ca[1] = sigma1 / e;
+    cc[1] = -c * ca[1];
     for (int j = 2; j <= m; ++j) {
       const double sigma2 = 1.0 / (gamma - sigma);
       ca[j] = 2.0 * sigma2 / e;
+      cc[j] = -c * ca[j];
       cb[j] = -(sigma * sigma2);
       sigma = sigma2;
     }
   }
   split_rows_f32(X, B, M, B, h[0], l[0], st);
+  k_fz_acc_init<<<grid_for(M * B / 4, 256), 256, 0, st>>>(h[0], l[0], M * B, (float)cc[1], acc);
+  CHEFSI_CHECK_LAUNCH();
   for (int j = 1; j <= m; ++j) {
     const int in = (j - 1) & 1, out = j & 1;
     mark();
@@ -492,11 +426,14 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
     f.ohi = h[out];
     f.olo = l[out];
     f.acc = acc;
-    f.scratch = scratch;
     f.counter = counter;
     f.B = B;
     f.a = ca[j];
+    f.c = cc[j];
     f.b = cb[j];
+    f.has_next = j < m;
+    f.cn = cc[j + 1];
+    f.bn = cb[j + 1];
     hx_tc_fused_launch(f, st);
     mark();
   }

@@ -37,16 +37,13 @@ struct TensorCellMats {
 
 // Tables of the fused filter step (tc.cu, fused.cu), built once per operator on first use:
 // * rows: every cell entry (cell, node) is "single" when its dof has no other cell entry (its
-//   row is finished by the one unit that computes it) or "shared" (an FP32 accumulator row;
-//   arrival counters per 128-vector chunk decide which unit finishes it);
+//   row is finished by the one unit that reduces into it) or "shared" (arrival counters per
+//   128-vector chunk decide which unit finishes it);
 // * the nonlocal term as extra K columns of the cell matrices: each (atom, dof) pair of the
 //   projectors is given to one cell entry of its dof (greedily, so that few cells take more
 //   than one atom), a cell's atoms occupy n_proj K columns each after its n_e nodes, holding
 //   2^-t C V for the entry's dof; the K side gathers those columns from rows n_dofs + a P + j
-//   of the split buffer, where 2^t W = 2^t C^T x sits. Cells with fewer atoms get zero columns;
-// * the Chebyshev shift: the diagonal entry (I, I) of a cell's tile holds
-//   2^s (A_II - c / n_entries(dof I)), so the entries of a dof add up to A - c; patched in place
-//   when the filter's centre c changes.
+//   of the split buffer, where 2^t W = 2^t C^T x sits. Cells with fewer atoms get zero columns.
 struct FusedPlan {
   bool ready = false;
   int nkb = 0;            // K-blocks of 32 (nodes and projector columns)
@@ -54,20 +51,12 @@ struct FusedPlan {
   int max_slots = 0;      // most atoms any cell takes
   int64_t n_shared = 0;
   int64_t rows = 0;       // split-buffer rows: n_dofs + n_atoms n_proj
-  int scale_exp = 0;      // s: the tiles hold 2^s A
+  float scale = 1.f;      // 2^s of the tiles
   float wscale = 1.f;     // 2^t of the W rows
-  double amax = 0.0;      // max |A_e| and max 2^-t |C V| (the scale's base)
-  double diag_max = 0.0;  // max |A_II|
-  double c_applied = 0.0; // shift now in the diagonal entries
-  bool shifted = false;
   DeviceBuffer<int> mapk;         // [n_cells][kstride]
   DeviceBuffer<int> rowinfo;      // [n_cells][n_e] x {dof, shared index or -1}
   DeviceBuffer<unsigned char> ncontrib;  // [n_shared]
   DeviceBuffer<__half> hi, lo;    // extended cell-matrix tiles [n_cells][halves][nkb][n_half x 32]
-  DeviceBuffer<int64_t> diag_idx; // [n_cells][n_e] tile element of (I, I)
-  DeviceBuffer<double> diag_val;  // [n_cells][n_e] A_II
-  DeviceBuffer<int64_t> ext_idx;  // tile elements of the projector columns
-  DeviceBuffer<double> ext_val;   // their 2^-t C V values
 };
 
 }  // namespace chefsi
@@ -183,10 +172,10 @@ void axpby_split_f32(const float* x, float* y, int64_t M, int B, double a, doubl
 void nl_project_f32(chefsi_operator_s* op, const float* x, int64_t ldx, float* W, int B,
                     cudaStream_t st);
 void prepare_tensor_mats(chefsi_operator_s* op, cudaStream_t st);
-// one fused filter step (tc.cu): x_j = a (A - c) x_{j-1} + b x_{j-2} (the shift c is in the
-// plan's tiles) from the split rows of x_{j-1} (xhi/xlo, rows n_dofs + n_atoms n_proj: the last
-// ones hold 2^t W) into ohi/olo, which hold x_{j-2} on entry; shared rows through acc (zero on
-// entry and on exit) and counter; scratch: kScratchFloatsPerCta floats per CTA
+// one fused filter step (tc.cu): x_j from the split rows of x_{j-1} (xhi/xlo, rows n_dofs +
+// n_atoms n_proj: the last ones hold 2^t W) and x_{j-2} (ohi/olo on entry, single rows);
+// x_j = a A x_{j-1} + c x_{j-1} + b x_{j-2} into ohi/olo; shared rows through acc / counter,
+// whose accumulators are left pre-set to cn x_j + bn x_{j-1} when has_next
 struct TcFusedLaunch {
   chefsi_operator_s* op;
   const __half* xhi;
@@ -194,24 +183,22 @@ struct TcFusedLaunch {
   __half* ohi;
   __half* olo;
   float* acc;
-  float* scratch;
   unsigned* counter;
   int B;
-  double a, b;
+  double a, c, b, cn, bn;
+  int has_next;
 };
-constexpr int64_t kScratchFloatsPerCta = 2 * 256 * 128;
 void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st);
 // row halves of the tensor-core tiles for n_e nodes (n_half rows each)
 void tc_row_split(int n_e, int* n_half, int* n_halves);
 // (cell, half, K-block) tiles of 2^s A_e over nkb K-blocks (columns past n_e zero)
 void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __half* lo,
                     cudaStream_t st);
-// workspaces of the fused filter (grow-only): two split buffers (x_{j-1}; x_{j-2} -> x_j), the
-// shared rows' FP32 accumulators and arrival counters, the per-CTA scratch of the single rows,
-// the projector coefficients W
+// workspaces of the fused filter (grow-only): two split buffers (x_{j-1}; x_j), the rows' FP32
+// accumulators [n_dofs][B], the shared rows' arrival counters, the projector coefficients W
 struct FusedWork {
   DeviceBuffer<__half> hi[2], lo[2];
-  DeviceBuffer<float> acc, W, scratch;
+  DeviceBuffer<float> acc, W;
   DeviceBuffer<unsigned> counter;
 };
 // the Chebyshev filter of one FP32 block X [M][B] (max |x| ~ 2^8) with the fused steps; mark()
@@ -222,8 +209,6 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
 // the tables of the fused step (fused.cu); false if the operator does not take the fused path
 bool fused_plan_usable(chefsi_operator_s* op);
 void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st);
-// the filter's centre c in the fused tiles' diagonals (re-scaled tiles when needed)
-void fused_set_shift(chefsi_operator_s* op, double c, cudaStream_t st);
 // device error flag of the tensor-core kernel (CHEFSI_OK or CHEFSI_ERR_TIMEOUT); clears it
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st);
 // nonlocal term y += scalar * C V C^T x for FP32 vectors (used by the tensor-core path)

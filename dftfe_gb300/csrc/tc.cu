@@ -84,28 +84,27 @@ struct TcProblem {
 };
 constexpr int kMaxGroup = 32;
 
-// The fused filter step (one problem): with the shift folded into the tiles' diagonals the
-// recurrence is x_j = a_j (A - c) x_{j-1} + b_j x_{j-2}, and the MMA gives
-// D = 2^s (A - c) x_{j-1} (+ the projector columns). The drain warps write out_scale D of a row
-// that one cell entry owns ("single") to a per-CTA scratch that stays in L2, and reduce it into
-// a zero-started FP32 accumulator for a row shared by several entries. The finalizer warps, one
-// unit behind, count the unit's arrival on each shared row (acquire-release atomics per row and
-// 128-vector chunk); for every finished row (single rows always, shared rows when this unit
-// brought the last contribution) they read the value V, read x_{j-2} from the output rows,
-// write the FP16 split of x_j = V + b_j x_{j-2} over it, and then zero the shared row's
-// accumulator for the next degree or drop the single row's scratch lines from L2 unwritten.
+// The fused filter step (one problem): the epilogue finishes the three-term recurrence
+//   x_j = out_scale D + cj x_{j-1} + bj x_{j-2}
+// instead of only scatter-adding D. Every row's FP32 accumulator is pre-set to
+// cj x_{j-1} + bj x_{j-2} (by the previous degree); the drain warps reduce D into it. Once the
+// unit's reductions are performed, the finalizer warps count the unit's arrival on each shared
+// row (acquire-release atomics per row and 128-vector chunk); the unit that brings a row's last
+// contribution (always, for rows of one cell entry) writes the row's FP16 split of x_j and
+// pre-sets its accumulator for the next degree: cn x_j + bn x_{j-1}.
 struct TcFused {
   const int* mapk;                 // [n_cells][kstride] split row feeding K index J (-1: zero)
   int kstride;
+  int has_next;
   const int2* rowinfo;             // [n_cells][n_e] {dof, shared index or -1}
-  __half* ohi;                     // output split rows: x_{j-2} on entry, x_j on exit
+  __half* ohi;                     // output split rows (x_j)
   __half* olo;
-  float* acc;                      // [n_shared][B] accumulators of the shared rows
-  float* scratch;                  // [grid][2][256][128] single rows of the unit in flight
+  float* acc;                      // [n_dofs][B] accumulators
   unsigned* counter;               // [n_shared][n_chunks] arrivals
   const unsigned char* ncontrib;   // [n_shared] cell entries per shared row
-  float bj;
+  float cj, bj, cn, bn;
 };
+
 struct TcArgs {
   TcProblem prob[kMaxGroup];
   int n_probs;
@@ -199,10 +198,6 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned* p, unsigned v
   asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v)
                : "memory");
   return old;
-}
-// fire-and-forget FP32 reduction at L2 (no returned value)
-__device__ __forceinline__ void red_add_f32(float* p, float v) {
-  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
 }
 // 16-byte load at L2 (the reductions of other SMs live there; never an L1 copy)
 __device__ __forceinline__ float4 ld_cg_f4(const float* p) {
@@ -565,7 +560,6 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     const int fw = f >> 5;
     int* lists = reinterpret_cast<int*>(smem + L.queue);
     const int64_t ld = pr.ldx;
-    float* scr = fz.scratch + (int64_t)blockIdx.x * kScratchFloatsPerCta;
     constexpr int kBatch = 4;
     for (int64_t it = 0; it < my_units; ++it) {
       const int slot = (int)(it & 1);
@@ -594,61 +588,42 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
           float4 a[kBatch];
           uint2 xh[kBatch], xl[kBatch];
           int64_t o[kBatch];
-          float* src[kBatch];   // this lane's 4 values: a scratch row or an accumulator row
-          bool shr[kBatch];
 #pragma unroll
           for (int b = 0; b < kBatch; ++b) {
             const int k = k0 + b * kFinWarps;
-            o[b] = -1;
-            src[b] = nullptr;
-            shr[b] = false;
-            if (k < n) {
-              const int I = list[1 + k];
-              const int2 r = rinfo[I];
-              o[b] = (int64_t)r.x * ld + v0;
-              shr[b] = r.y >= 0;
-              src[b] = shr[b] ? fz.acc + (int64_t)r.y * ld + v0 : scr + (slot * 256 + I) * kVec + lane * 4;
-              a[b] = ld_cg_f4(src[b]);
-              if (fz.bj != 0.f) {
-                xh[b] = *reinterpret_cast<const uint2*>(fz.ohi + o[b]);
-                xl[b] = *reinterpret_cast<const uint2*>(fz.olo + o[b]);
+            o[b] = k < n ? (int64_t)rinfo[list[1 + k]].x * ld + v0 : -1;
+            if (o[b] >= 0) {
+              a[b] = ld_cg_f4(fz.acc + o[b]);
+              if (fz.has_next) {
+                xh[b] = __ldg(reinterpret_cast<const uint2*>(pr.xhi + o[b]));
+                xl[b] = __ldg(reinterpret_cast<const uint2*>(pr.xlo + o[b]));
               }
             }
           }
 #pragma unroll
           for (int b = 0; b < kBatch; ++b) {
             if (o[b] < 0) continue;
-            float4 x = a[b];
-            if (fz.bj != 0.f) {
-              const float2 h01 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].x));
-              const float2 h23 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].y));
-              const float2 l01 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].x));
-              const float2 l23 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].y));
-              x.x = fmaf(fz.bj, h01.x + l01.x, x.x);
-              x.y = fmaf(fz.bj, h01.y + l01.y, x.y);
-              x.z = fmaf(fz.bj, h23.x + l23.x, x.z);
-              x.w = fmaf(fz.bj, h23.y + l23.y, x.w);
-            }
             __half h[4], l[4];
-            split_f32(x.x, h[0], l[0]);
-            split_f32(x.y, h[1], l[1]);
-            split_f32(x.z, h[2], l[2]);
-            split_f32(x.w, h[3], l[3]);
+            split_f32(a[b].x, h[0], l[0]);
+            split_f32(a[b].y, h[1], l[1]);
+            split_f32(a[b].z, h[2], l[2]);
+            split_f32(a[b].w, h[3], l[3]);
             __half2 hh[2] = {__halves2half2(h[0], h[1]), __halves2half2(h[2], h[3])};
             __half2 ll[2] = {__halves2half2(l[0], l[1]), __halves2half2(l[2], l[3])};
             *reinterpret_cast<uint2*>(fz.ohi + o[b]) = *reinterpret_cast<uint2*>(hh);
             *reinterpret_cast<uint2*>(fz.olo + o[b]) = *reinterpret_cast<uint2*>(ll);
-          }
-          // shared rows: the accumulator restarts at zero; single rows: the scratch lines are
-          // dropped from L2 without a write-back (every lane of the warp has read them)
-          __syncwarp();
-#pragma unroll
-          for (int b = 0; b < kBatch; ++b) {
-            if (o[b] < 0) continue;
-            if (shr[b])
-              *reinterpret_cast<float4*>(src[b]) = make_float4(0.f, 0.f, 0.f, 0.f);
-            else if (lane < 4)  // the row's four 128-byte lines, one per lane
-              asm volatile("discard.global.L2 [%0], 128;" ::"l"(src[b] - lane * 4 + lane * 32) : "memory");
+            if (fz.has_next) {
+              const float2 h01 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].x));
+              const float2 h23 = __half22float2(*reinterpret_cast<const __half2*>(&xh[b].y));
+              const float2 l01 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].x));
+              const float2 l23 = __half22float2(*reinterpret_cast<const __half2*>(&xl[b].y));
+              float4 nx;
+              nx.x = fmaf(fz.bn, h01.x + l01.x, fz.cn * a[b].x);
+              nx.y = fmaf(fz.bn, h01.y + l01.y, fz.cn * a[b].y);
+              nx.z = fmaf(fz.bn, h23.x + l23.x, fz.cn * a[b].z);
+              nx.w = fmaf(fz.bn, h23.y + l23.y, fz.cn * a[b].w);
+              *reinterpret_cast<float4*>(fz.acc + o[b]) = nx;
+            }
           }
         }
       }
@@ -719,9 +694,9 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
         }
       }
     } else if (FUSED) {
-      // ---- the fused step's drain: single rows to the CTA's scratch, shared rows reduced into
-      // their accumulators; at the start of the next unit the warps fence these writes (gpu
-      // scope) and hand the unit to the finalizer warps
+      // ---- the fused step's drain: every row of the unit is reduced into its FP32 accumulator
+      // (pre-set to c x_{j-1} + b x_{j-2}); at the start of the next unit the warps fence
+      // their reductions (gpu scope) and hand the unit to the finalizer warps
       const TcProblem& pr = args.prob[0];
       const int e = threadIdx.x - 192;          // drain thread 0..255
       bool ok = true;
@@ -752,8 +727,6 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
         const int gb = w.chunk * kVec + q * 32 + lane;
         const bool vok = gb < pr.B;
         float* accb = args.fz.acc + gb;
-        float* scrb = args.fz.scratch + (int64_t)blockIdx.x * kScratchFloatsPerCta + buf * 256 * kVec +
-                      q * 32 + lane;
         const float osc = pr.out_scale;
         const uint32_t tq = tmem + buf * args.buf_stride + ((uint32_t)(q * 32) << 16);
         for (int c0 = c_beg; c0 < c_end; c0 += 16) {
@@ -762,11 +735,8 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
           if (vok) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-              const int2 r = rinfo[c0 + i];
-              if (r.y >= 0)
-                red_add_f32(accb + (int64_t)r.y * pr.ldx, osc * vals[i]);
-              else if (r.x >= 0)
-                scrb[(c0 + i) * kVec] = osc * vals[i];
+              const int d = rinfo[c0 + i].x;
+              if (d >= 0) atomicAdd(accb + (int64_t)d * pr.ldx, osc * vals[i]);
             }
           }
         }
@@ -1241,9 +1211,7 @@ void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
                      (reinterpret_cast<uintptr_t>(f.xlo) & 15) == 0 &&
                      (reinterpret_cast<uintptr_t>(f.ohi) & 15) == 0 &&
                      (reinterpret_cast<uintptr_t>(f.olo) & 15) == 0 &&
-                     (reinterpret_cast<uintptr_t>(f.acc) & 15) == 0 &&
-                     (reinterpret_cast<uintptr_t>(f.scratch) & 127) == 0 &&
-                     device_sms() <= 4096,
+                     (reinterpret_cast<uintptr_t>(f.acc) & 15) == 0,
                  "fused filter step: 16-byte aligned rows, B a multiple of 8");
   TcArgs a{};
   a.n_probs = 1;
@@ -1275,21 +1243,23 @@ void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
   pr.ldd = f.B;
   pr.B = f.B;
   pr.n_chunks = (f.B + kVec - 1) / kVec;
-  pr.out_scale = (float)std::ldexp(f.a, -fp.scale_exp);
+  pr.out_scale = (float)(f.a / fp.scale);
   pr.pair_begin = 0;
   a.n_pairs = (int64_t)op->n_cells * pr.n_chunks;
   TcFused& z = a.fz;
   z.mapk = fp.mapk.ptr;
   z.kstride = fp.kstride;
-
+  z.has_next = f.has_next;
   z.rowinfo = reinterpret_cast<const int2*>(fp.rowinfo.ptr);
   z.ohi = f.ohi;
   z.olo = f.olo;
   z.acc = f.acc;
   z.counter = f.counter;
   z.ncontrib = fp.ncontrib.ptr;
-  z.scratch = f.scratch;
+  z.cj = (float)f.c;
   z.bj = (float)f.b;
+  z.cn = (float)f.cn;
+  z.bn = (float)f.bn;
   auto kernel = cell_hx_tc_kernel<2, false, false, true>;
   CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
