@@ -353,10 +353,10 @@ def run_ours(args):
     lo, blow, up = first_bounds(chefsi, op, N)
     # the large workload (4096 vectors) is filtered in blocks of 256, the others in one block
     blk = 256 if args.workload == "large" else N
-    fused = not args.no_fused
+    fused = args.filter == "fused"
     params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=blk, wfcBlockSize=blk,
                                  mixed_precision="mixed", rr_precision=args.rr_precision,
-                                 fused_recurrence=fused)
+                                 filter_variant=args.filter)
     solver = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(params)
     solver.reinitSpectrumBounds(lo, blow, up)
     solver.set_profiling(True, mixed=True)
@@ -416,7 +416,7 @@ def run_ours(args):
                    "fe_degree": pr.mesh.p, "n_wfc": N, "cheb_degree": m, "wells": 64,
                    "projectors_per_well": 8, "precision": "mixed",
                    "rr_hx_precision": args.rr_precision, "l2": "inputs > L2 (X is 14 GB)",
-                   "filter": "fused recurrence" if fused else "separate recurrence pass",
+                   "filter": args.filter,
                    "parallelism": f"replicas{world}"},
         "hx_gflops": hx_flops / (avg_hx_ms * 1e-3) / 1e9,
         "hx_ms": avg_hx_ms, "hx_launches_timed": hx_n,
@@ -428,10 +428,13 @@ def run_ours(args):
                      "traffic": TC_TRAFFIC_BYTES.get((args.workload, fused)), "peak_source": src,
                      "traffic_scope": "the filter step's tensor-core kernel launch alone, dram "
                                       "read + write, ncu (profiles/)",
-                     "kernel": ("cell_hx_tc_kernel<FUSED> + nonlocal projection: one filter step "
-                                "(HX, nonlocal, recurrence)") if fused else
-                               "cell_hx_tc_kernel + nonlocal kernels (filter HX; recurrence pass "
-                               "not included)",
+                     "kernel": {"fused": "cell_hx_tc_kernel<FUSED> + nonlocal projection: one "
+                                         "filter step (HX, nonlocal, recurrence)",
+                                "folded": "cell_hx_tc_kernel with the nonlocal apply as extra K "
+                                          "columns + nonlocal projection (filter HX; recurrence "
+                                          "pass not included)",
+                                "separate": "cell_hx_tc_kernel + nonlocal kernels (filter HX; "
+                                            "recurrence pass not included)"}[args.filter],
                      "algorithmic_bytes_per_launch": hx_bytes},
         "e2e": e2e,
         "clocks": clk.summary(),
@@ -872,8 +875,10 @@ def main():
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
-    ap.add_argument("--no-fused", action="store_true",
-                    help="filter with the separate recurrence pass and nonlocal kernels")
+    ap.add_argument("--filter", default="folded", choices=["folded", "fused", "separate"],
+                    help="mixed filter variant: recurrence pass + HX with the nonlocal apply as "
+                         "tensor-core K columns (folded), recurrence in the HX launch (fused), "
+                         "or separate nonlocal kernels (separate)")
     ap.add_argument("--no-fp64-leg", action="store_true",
                     help="skip the FP64 iteration and the Ritz-error comparison after the timed steps")
     ap.add_argument("--density-check", action="store_true",

@@ -75,7 +75,7 @@ class Params(ctypes.Structure):
         ("first_scf_degree_scale", ctypes.c_double), ("keep_hx", ctypes.c_int32),
         ("rr_precision", ctypes.c_int32), ("ss_frac_reduced", ctypes.c_int32),
         ("rr_block", ctypes.c_int32), ("rr_slab_rows", ctypes.c_int32),
-        ("fused_recurrence", ctypes.c_int32),
+        ("filter_variant", ctypes.c_int32),
     ]
 
 

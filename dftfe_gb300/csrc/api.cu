@@ -147,21 +147,33 @@ void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double
 // split once.
 void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
                     int B, int m, double a, double b, double a0, cudaStream_t st) {
-  if (s->p.fused_recurrence >= 0 && fused_plan_usable(op)) {
+  if (s->p.filter_variant == 1 && fused_plan_usable(op)) {
     // one launch per degree finishes the recurrence and applies the nonlocal term
     cheb_filter_fused(op, s->fzw, X, M, B, m, a, b, a0, [&] { s->hx_mark(st); }, st);
     return;
   }
-  __half* hi = s->xs_hi.ensure((size_t)M * B);
-  __half* lo = s->xs_lo.ensure((size_t)M * B);
+  // the nonlocal apply folded into the tensor-core launch (extra K columns of the cell
+  // matrices fed by split rows of 2^t C^T x after the dof rows), unless the separate nonlocal
+  // kernels are asked for
+  const bool fold = s->p.filter_variant == 0 && op->n_atoms > 0 && fused_plan_usable(op) &&
+                    ((B * 2) % 16) == 0;
+  if (fold) prepare_fused_plan(op, st);
+  const size_t rows = fold ? (size_t)op->fz.rows : (size_t)M;
+  __half* hi = s->xs_hi.ensure(rows * B);
+  __half* lo = s->xs_lo.ensure(rows * B);
+  float* W = fold ? s->fzw.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
   const double e = (b - a) / 2.0, c = (b + a) / 2.0;
   double sigma = e / (a0 - c);
   const double sigma1 = sigma, gamma = 2.0 / sigma1;
   double alpha1 = sigma1 / e, alpha2 = -c;
   auto hx = [&](const float* src, float* dst, double sc) {
     s->hx_mark(st);
-    if (!hx_tc_split(op, hi, lo, src, B, dst, B, B, sc, true, st))
+    if (fold) {
+      nl_project_to_split(op, src, B, W, hi, lo, st);
+      hx_tc_folded_launch(op, hi, lo, dst, B, B, sc, st);
+    } else if (!hx_tc_split(op, hi, lo, src, B, dst, B, B, sc, true, st)) {
       throw Error(CHEFSI_ERR_INVALID, "tensor-core filter HX not applicable to this block");
+    }
     s->hx_mark(st);
   };
   axpby_split_f32(X, Y, M, B, alpha1 * alpha2, 0.0, hi, lo, st);   // Y = a X, split(X)
@@ -1213,7 +1225,7 @@ chefsi_params default_params() {
   p.ss_frac_reduced = 0;
   p.rr_block = 0;
   p.rr_slab_rows = 0;
-  p.fused_recurrence = 0;
+  p.filter_variant = 0;
   return p;
 }
 

@@ -366,6 +366,17 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   fp.ready = true;
 }
 
+void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W, __half* hi,
+                         __half* lo, cudaStream_t st) {
+  if (op->n_atoms == 0) return;
+  const FusedPlan& fp = op->fz;
+  nl_project_f32(op, x, B, W, B, st);   // zeroes W first
+  const int64_t nw = (int64_t)op->n_atoms * op->n_proj * B;
+  const int64_t off = op->n_dofs * (int64_t)B;
+  k_fz_w_split<<<grid_for(nw / 4, 256), 256, 0, st>>>(W, nw, fp.wscale, hi + off, lo + off);
+  CHEFSI_CHECK_LAUNCH();
+}
+
 // The filter of one block: X [M][B] FP32 in (scaled so that max |x| ~ 2^8), p_m(A) X out.
 // Coefficients of the sigma-scaled recurrence (linearAlgebraOperationsDevice.cc:531-727):
 //   x_1 = alpha1 (A - c) x_0, alpha1 = sigma1 / e;

@@ -189,6 +189,14 @@ struct TcFusedLaunch {
   int has_next;
 };
 void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st);
+// dst += scalar (A + C V C^T) x on the tensor cores with the nonlocal apply as the plan's extra
+// K columns: x given by split rows [plan rows][B], the projector rows holding 2^t C^T x
+void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
+                         int64_t ldd, int B, double scalar, cudaStream_t st);
+// the projector rows of a split buffer: (hi, lo)[n_dofs + a P + j] = split(2^t (C^T x)[a][j])
+// from FP32 vectors x [n_dofs][B] (W: n_atoms n_proj B floats of workspace)
+void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W, __half* hi,
+                         __half* lo, cudaStream_t st);
 // row halves of the tensor-core tiles for n_e nodes (n_half rows each)
 void tc_row_split(int n_e, int* n_half, int* n_halves);
 // (cell, half, K-block) tiles of 2^s A_e over nkb K-blocks (columns past n_e zero)

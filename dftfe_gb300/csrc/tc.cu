@@ -199,6 +199,10 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned* p, unsigned v
                : "memory");
   return old;
 }
+// fire-and-forget FP32 reduction at L2 (no returned value)
+__device__ __forceinline__ void red_add_f32(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
 // 16-byte load at L2 (the reductions of other SMs live there; never an L1 copy)
 __device__ __forceinline__ float4 ld_cg_f4(const float* p) {
   float4 v;
@@ -493,8 +497,11 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     auto load_next = [&]() {
       nxt.valid = c_it < my_units;
       if (nxt.valid) {
-        const int kst = FUSED ? args.fz.kstride : args.n_e;
-        const int* mrow = (FUSED ? args.fz.mapk : args.prob[c_w.p].map) + (int64_t)c_w.cell * kst;
+        // the extended K side (the cell's nodes, then its projector columns) for the fused step
+        // and for a single apply with the nonlocal term folded in
+        const bool kext = FUSED || args.fz.mapk != nullptr;
+        const int kst = kext ? args.fz.kstride : args.n_e;
+        const int* mrow = (kext ? args.fz.mapk : args.prob[c_w.p].map) + (int64_t)c_w.cell * kst;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int J = c_kb * kKB + j * 8 + rsub;
@@ -736,7 +743,7 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
               const int d = rinfo[c0 + i].x;
-              if (d >= 0) atomicAdd(accb + (int64_t)d * pr.ldx, osc * vals[i]);
+              if (d >= 0) red_add_f32(accb + (int64_t)d * pr.ldx, osc * vals[i]);
             }
           }
         }
@@ -1198,6 +1205,61 @@ void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __
   const int64_t n = (int64_t)op->n_cells * p.n_halves * nkb * p.n_half * 32;
   k_split_mats_ext<<<grid_for(n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, op->n_e, p.n_half,
                                                      p.n_halves, nkb, scale, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// dst += scalar (A + C V C^T) x for one operator: the split rows xhi / xlo [plan rows][B] hold x
+// in rows [0, n_dofs) and 2^t C^T x in the projector rows after them; the nonlocal apply runs
+// on the tensor cores as the plan's extra K columns of the cell matrices
+void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
+                         int64_t ldd, int B, double scalar, cudaStream_t st) {
+  const FusedPlan& fp = op->fz;
+  CHEFSI_REQUIRE(fp.ready, "folded nonlocal HX: tables not prepared");
+  const int n_e = op->n_e;
+  const TcPlan p = plan_for(n_e, 2);
+  CHEFSI_REQUIRE(B % 8 == 0 && ldd % 4 == 0 && (reinterpret_cast<uintptr_t>(xhi) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(xlo) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(dst) & 15) == 0,
+                 "folded nonlocal HX: 16-byte aligned rows, B a multiple of 8");
+  TcArgs a{};
+  a.n_probs = 1;
+  a.n_e = n_e;
+  a.n_rows = n_e;
+  a.nkb = fp.nkb;
+  a.n_half = p.n_half;
+  a.n_halves = p.n_halves;
+  a.buf_stride = p.buf_stride;
+  a.tmem_cols = p.tmem_cols;
+  a.stages = p.stages;
+  a.xstages = p.xstages;
+  a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
+  if (!op->tc_err.ptr) {
+    op->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  }
+  a.err = op->tc_err.ptr;
+  TcProblem& pr = a.prob[0];
+  pr.xhi = xhi;
+  pr.xlo = xlo;
+  pr.xlo3 = xlo;
+  pr.dst = dst;
+  pr.map = op->map.ptr;
+  pr.ahi = fp.hi.ptr;
+  pr.alo = fp.lo.ptr;
+  pr.alo3 = fp.lo.ptr;
+  pr.ldx = B;
+  pr.ldd = ldd;
+  pr.B = B;
+  pr.n_chunks = (B + kVec - 1) / kVec;
+  pr.out_scale = (float)(scalar / fp.scale);
+  pr.pair_begin = 0;
+  a.n_pairs = (int64_t)op->n_cells * pr.n_chunks;
+  a.fz.mapk = fp.mapk.ptr;
+  a.fz.kstride = fp.kstride;
+  auto kernel = cell_hx_tc_kernel<2, false>;
+  CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
+  kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
   CHEFSI_CHECK_LAUNCH();
 }
 

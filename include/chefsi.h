@@ -155,11 +155,12 @@ typedef struct {
                                    would not fit the free device memory, > 0 always with
                                    blocks of that many vectors, < 0 never */
   int32_t rr_slab_rows;         /* dofs per row slab of the blocked step (0: about 2^30 / N) */
-  int32_t fused_recurrence;     /* mixed tensor-core filter: 0 (default) finishes the
-                                   recurrence and applies the nonlocal term inside the HX
-                                   launch (one launch per degree, vectors kept as FP16 hi + lo
-                                   rows); -1 runs the separate recurrence pass and nonlocal
-                                   kernels */
+  int32_t filter_variant;       /* mixed tensor-core filter: 0 (default) one recurrence pass
+                                   per degree and the HX launch, with the nonlocal apply folded
+                                   into that launch as extra tensor-core K columns; 1 the fused
+                                   step (the recurrence finished in the HX launch, vectors kept
+                                   as FP16 hi + lo rows); -1 the recurrence pass, the HX launch
+                                   and separate nonlocal kernels */
 } chefsi_params;
 
 const char* chefsi_last_error(void);

@@ -259,14 +259,16 @@ def test_hx_golden_fixture(chefsi):
 
 @pytest.mark.parametrize("p,n,B,proj", [(2, 3, 8, True), (4, 2, 136, True), (6, 2, 136, True),
                                         (5, 2, 256, True), (4, 3, 64, False)])
-def test_fused_filter_matches_oracle_and_separate_pass(chefsi, p, n, B, proj):
-    """The fused tensor-core filter (the recurrence finished in the HX launch's epilogue, the
-    vectors kept as FP16 hi + lo rows, the nonlocal term as extra K columns of the cell
-    matrices) against the oracle's FP64 filter and against the separate-pass tensor-core
-    filter: 5e-6 relative to max |p(A) X| for both, and between them. Cell sizes with one
-    K-block of nodes (p = 2, several atoms per cell), one row half (p = 4, 5) and two (p = 6);
-    partial and several 128-vector chunks; a second filter call on the same solver (arrival
-    counters restart)."""
+def test_filter_variants_match_oracle(chefsi, p, n, B, proj):
+    """The three mixed tensor-core filters against the oracle's FP64 filter (5e-6 relative to
+    max |p(A) X|) and against each other (5e-6):
+    * folded: recurrence pass + HX launch with the nonlocal apply as extra tensor-core K columns
+      of the cell matrices (the projector coefficients 2^t C^T x as extra split rows);
+    * fused: the recurrence finished in the HX launch's epilogue (vectors kept as FP16 hi + lo);
+    * separate: recurrence pass, HX launch and the SIMT nonlocal kernels.
+    Cell sizes with one K-block of nodes (p = 2, several atoms per cell), one row half (p = 4,
+    5) and two (p = 6); partial and several 128-vector chunks; a second filter call on the same
+    solver."""
     pr = small_problem(n=n, L=2.0 * n, p=p, wells=3, projectors=proj)
     op, ora = gpu_op(chefsi, pr), oracle_op(pr)
     X = np.random.default_rng(p + B).uniform(-1, 1, (pr.n_dofs, B))
@@ -274,14 +276,14 @@ def test_fused_filter_matches_oracle_and_separate_pass(chefsi, p, n, B, proj):
     a, b, a0, m = lo + 0.3 * (up - lo), up, lo, 10
     ref = ora.chebyshev_filter(X, m, a, b, a0)
     out = {}
-    for fused in (True, False):
+    for variant in ("folded", "fused", "separate"):
         s = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
-            chebyshevOrder=m, chebyWfcBlockSize=B, wfcBlockSize=B, fused_recurrence=fused))
+            chebyshevOrder=m, chebyWfcBlockSize=B, wfcBlockSize=B, filter_variant=variant))
         s.reinitSpectrumBounds(a0, a, b)
         for _ in range(2):
             Xt = torch.from_numpy(X.copy()).cuda()
             s.solveNoRR(op, Xt, 1, useMixedPrec=True)
-        out[fused] = Xt.cpu().numpy()
-    assert rel(out[True], ref) < 5e-6
-    assert rel(out[False], ref) < 5e-6
-    assert rel(out[True], out[False]) < 5e-6
+        out[variant] = Xt.cpu().numpy()
+        assert rel(out[variant], ref) < 5e-6, variant
+    assert rel(out["folded"], out["separate"]) < 5e-6
+    assert rel(out["fused"], out["separate"]) < 5e-6
