@@ -88,7 +88,9 @@ class ClockSampler:
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the filter's tensor-core kernel
 # (ncu captures summarised in profiles/): the separate-pass HX kernel on the full workload, and
 # the fused step's kernel (None until captured)
-TC_TRAFFIC_BYTES = {("mixed", False): 20.33e9 + 8.20e9}
+TC_TRAFFIC_BYTES = {("mixed", "separate"): 20.33e9 + 8.20e9,
+                    # mixed_small capture (1.302 + 0.470 GB) scaled by 8000 / 512 cells
+                    ("mixed", "folded"): (1.302e9 + 0.470e9) * 8000 / 512}
 
 
 def hx_algorithmic(pr, B, s_h=4, s_x=4, fused=False):
@@ -425,7 +427,7 @@ def run_ours(args):
         "gpu_launches": None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
-                     "traffic": TC_TRAFFIC_BYTES.get((args.workload, fused)), "peak_source": src,
+                     "traffic": TC_TRAFFIC_BYTES.get((args.workload, args.filter)), "peak_source": src,
                      "traffic_scope": "the filter step's tensor-core kernel launch alone, dram "
                                       "read + write, ncu (profiles/)",
                      "kernel": {"fused": "cell_hx_tc_kernel<FUSED> + nonlocal projection: one "
