@@ -42,8 +42,10 @@ EXPORTS = [
     "chefsi_assemble_cell_hamiltonians_bloch", "chefsi_assemble_cell_hamiltonians_gga",
     "chefsi_assemble_cell_hamiltonians_bloch_gga",
     "chefsi_operator_update_cell_matrices",
-    "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract",
+    "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract", "chefsi_set_wait_limits",
 ]
+DEFAULT_WAIT_TRIES = 65536
+DEFAULT_BARRIER_SPINS = 1 << 26
 
 
 class ChefsiError(RuntimeError):
@@ -144,6 +146,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_solve_batched": ([i32, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32], ctypes.c_int),
         "chefsi_solve_no_rr": ([vp, vp, vp, i32, i32, i32, vp], ctypes.c_int),
         "chefsi_chebyshev_order": ([f64], i32),
+        "chefsi_set_wait_limits": ([ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -1766,6 +1766,14 @@ int chefsi_residual_norms(chefsi_operator op, const void* X, int64_t ld, int32_t
   CHEFSI_API_END
 }
 
+int chefsi_set_wait_limits(uint32_t mbarrier_tries, uint32_t barrier_spins) {
+  CHEFSI_API_BEGIN
+  tcx::tc_set_wait_tries(mbarrier_tries);
+  tcx::dense_tc_set_wait_tries(mbarrier_tries);
+  dense_set_barrier_spins(barrier_spins);
+  CHEFSI_API_END
+}
+
 int chefsi_solver_create(const chefsi_params* params, chefsi_solver* out) {
   CHEFSI_API_BEGIN
   CHEFSI_REQUIRE(out != nullptr, "null output handle");

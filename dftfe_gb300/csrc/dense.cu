@@ -1012,6 +1012,8 @@ struct GridSync {
   unsigned int* gen;
   int* err;
 };
+// polls of a grid-barrier wait before it expires (lowered by chefsi_set_wait_limits in tests)
+static __device__ uint32_t g_barrier_spins = 1u << 26;
 
 __device__ __forceinline__ bool grid_barrier(const GridSync& gs, unsigned int nblocks) {
   __shared__ int fail;
@@ -1025,13 +1027,14 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& gs, unsigned int nb
       __threadfence();
       atomicAdd(gs.gen, 1u);
     } else {
+      const uint32_t spins = *reinterpret_cast<volatile uint32_t*>(&g_barrier_spins);
       uint32_t i = 0;
-      for (; i < (1u << 26); ++i) {
+      for (; i < spins; ++i) {
         if (*reinterpret_cast<volatile unsigned int*>(gs.gen) != g) break;
         if (*reinterpret_cast<volatile int*>(gs.err) != 0) break;
         if (i > 32) __nanosleep(32);
       }
-      if (i == (1u << 26)) atomicExch(gs.err, CHEFSI_ERR_TIMEOUT);
+      if (i == spins) atomicExch(gs.err, CHEFSI_ERR_TIMEOUT);
     }
     __threadfence();
     fail = *reinterpret_cast<volatile int*>(gs.err) != 0;
@@ -1121,6 +1124,10 @@ __global__ void __launch_bounds__(256)
     }
     if (!grid_barrier(gs, active)) return;
   }
+}
+
+void dense_set_barrier_spins(uint32_t spins) {
+  CHEFSI_CUDA(cudaMemcpyToSymbol(g_barrier_spins, &spins, sizeof(spins)));
 }
 
 // Householder tridiagonalisation of the N x N row-major symmetric A: one cooperative launch

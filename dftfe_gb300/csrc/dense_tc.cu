@@ -783,6 +783,12 @@ void tc_rotate(const TcOperand& Xr, const double* W, int64_t ldw, int n_out, dou
   CHEFSI_CHECK_LAUNCH();
 }
 
+namespace tcx {
+void dense_tc_set_wait_tries(uint32_t tries) {
+  CHEFSI_CUDA(cudaMemcpyToSymbol(g_wait_tries, &tries, sizeof(tries)));
+}
+}  // namespace tcx
+
 int tc_dense_check_error(TcDenseWork& w, cudaStream_t st) {
   if (!w.err.ptr) return CHEFSI_OK;
   int h = 0;

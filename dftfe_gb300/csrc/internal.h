@@ -306,6 +306,13 @@ void trtri_lower(double* L, int N, cudaStream_t st);
 // symmetric eigensolve (Householder tridiagonalisation, bisection, inverse iteration,
 // back-transformation); A overwritten; eigenvalues ascending in w; vectors in columns of Z.
 int syevd(double* A, int N, double* w, double* Z, cudaStream_t st);
+// polls of a grid-barrier wait in the cooperative tridiagonalisation before it expires
+void dense_set_barrier_spins(uint32_t spins);
+namespace tcx {
+// tries of the bounded mbarrier waits of the tensor-core kernels (tc.cu, dense_tc.cu)
+void tc_set_wait_tries(uint32_t tries);
+void dense_tc_set_wait_tries(uint32_t tries);
+}  // namespace tcx
 int syevd_range(double* A, int N, int il, int count, double* w, double* Z, cudaStream_t st);
 // complex Hermitian counterparts (dense_c.cu)
 int cholesky_lower_c(cplx* A, int N, cudaStream_t st);

@@ -1065,6 +1065,9 @@ TcPlan plan_for(int n_e, int ns, bool fused = false) {
 }  // namespace
 
 namespace tcx {
+void tc_set_wait_tries(uint32_t tries) {
+  CHEFSI_CUDA(cudaMemcpyToSymbol(g_wait_tries, &tries, sizeof(tries)));
+}
 bool tcgen05_device() {
   int dev = 0, major = 0;
   CHEFSI_CUDA(cudaGetDevice(&dev));

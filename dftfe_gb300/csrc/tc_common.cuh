@@ -50,10 +50,14 @@ static __device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_
 }
 static constexpr uint32_t kWaitHintNs = 20000;  // 20 us per try
 static constexpr uint32_t kWaitTries = 1u << 16; // bound: ~1.3 s
+// the number of tries of every bounded wait of this translation unit's kernels (kWaitTries;
+// lowered by chefsi_set_wait_limits to make waits expire in tests)
+static __device__ uint32_t g_wait_tries = kWaitTries;
 // bounded wait; returns false on expiry (and records the timeout)
 static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
                                                  volatile int* abort_flag) {
-  for (uint32_t i = 0; i < kWaitTries; ++i) {
+  const uint32_t tries = *reinterpret_cast<volatile uint32_t*>(&g_wait_tries);
+  for (uint32_t i = 0; i < tries; ++i) {
     if (mbar_try_wait_hint(bar, parity, kWaitHintNs)) return true;
     if (*abort_flag) return false;
   }
@@ -217,6 +221,10 @@ static __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t col
 // ---- host side
 // true on an sm_100-family device (tcgen05, tensor memory, bulk async copies)
 bool tcgen05_device();
+// the tries of the bounded waits in the tensor-core HX kernels (tc.cu) and in the tensor-core
+// Gram and rotation kernels (dense_tc.cu)
+void tc_set_wait_tries(uint32_t tries);
+void dense_tc_set_wait_tries(uint32_t tries);
 
 }  // namespace tcx
 }  // namespace chefsi

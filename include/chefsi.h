@@ -163,6 +163,18 @@ typedef struct {
                                    and separate nonlocal kernels */
 } chefsi_params;
 
+/* Bounds of the device-side waits (no counterpart in the reference: a test hook for failure
+   detection). mbarrier_tries: tries of every mbarrier wait in the tensor-core kernels (each a
+   hardware suspend of up to 20 us; default CHEFSI_DEFAULT_WAIT_TRIES, about 1.3 s);
+   barrier_spins: polls of a grid-barrier wait in the cooperative tridiagonalisation (default
+   CHEFSI_DEFAULT_BARRIER_SPINS). A wait that runs out records CHEFSI_ERR_TIMEOUT, the kernel
+   returns after its own copies and tensor-core operations have finished, and the call that
+   launched it returns CHEFSI_ERR_TIMEOUT with the context still usable; 0 makes every such
+   wait expire at once. Applies to kernels launched after the call, on the current device. */
+#define CHEFSI_DEFAULT_WAIT_TRIES 65536u
+#define CHEFSI_DEFAULT_BARRIER_SPINS 67108864u
+int chefsi_set_wait_limits(uint32_t mbarrier_tries, uint32_t barrier_spins);
+
 const char* chefsi_last_error(void);
 const char* chefsi_version(void);
 /* number of kernels this library has launched in the process (all streams) */

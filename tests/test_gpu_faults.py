@@ -69,3 +69,44 @@ def test_bad_map_is_rejected(C):
     with pytest.raises(_lib.ChefsiError) as ei:
         C.KohnShamOperator.from_problem(pr)
     assert ei.value.code == _lib.CHEFSI_ERR_INVALID
+
+
+def test_bounded_device_waits_expire_and_context_stays_usable(C):
+    """Every device-side wait is bounded. With the bounds lowered to zero (a wait expires at
+    its first poll) the tensor-core filter HX, the tensor-core Gram of the mixed overlap and
+    the cooperative tridiagonalisation of the eigensolver each return CHEFSI_ERR_TIMEOUT; with
+    the bounds restored the same calls on the same context succeed and agree with the oracle."""
+    from dftfe_gb300 import _lib
+    from oracle import oracle as orc
+    from tests.helpers import oracle_op
+    lib = _lib.load()
+    pr = small_problem(n=2, L=4.0, p=4, wells=2, projectors=True)
+    op, ora = C.KohnShamOperator.from_problem(pr), oracle_op(pr)
+    X = np.random.default_rng(3).uniform(-1, 1, (pr.n_dofs, 32))
+    lo, up = orc.lanczos_bounds(ora, np.ones(pr.n_dofs), 20)
+    a, b, a0 = lo + 0.3 * (up - lo), up, lo
+    rng = np.random.default_rng(4)
+    Q, _ = np.linalg.qr(rng.standard_normal((300, 300)))
+    A = (Q * np.sort(rng.standard_normal(300))) @ Q.T
+    A = 0.5 * (A + A.T)
+    try:
+        _lib.check(lib.chefsi_set_wait_limits(0, _lib.DEFAULT_BARRIER_SPINS))
+        with pytest.raises(_lib.ChefsiError) as ei:
+            C.chebyshevFilter(op, torch.from_numpy(X.copy()).cuda(), 10, a, b, a0, precision="mixed")
+        assert ei.value.code == _lib.CHEFSI_ERR_TIMEOUT
+        with pytest.raises(_lib.ChefsiError) as ei:
+            C.pseudoGramSchmidtOrthogonalization(op, torch.from_numpy(X.copy()).cuda(),
+                                                 precision="mixed")
+        assert ei.value.code == _lib.CHEFSI_ERR_TIMEOUT
+        _lib.check(lib.chefsi_set_wait_limits(_lib.DEFAULT_WAIT_TRIES, 0))
+        with pytest.raises(_lib.ChefsiError) as ei:
+            C.syevd(torch.from_numpy(A.copy()).cuda())
+        assert ei.value.code == _lib.CHEFSI_ERR_TIMEOUT
+    finally:
+        _lib.check(lib.chefsi_set_wait_limits(_lib.DEFAULT_WAIT_TRIES, _lib.DEFAULT_BARRIER_SPINS))
+    Xt = torch.from_numpy(X.copy()).cuda()
+    C.chebyshevFilter(op, Xt, 10, a, b, a0, precision="mixed")
+    ref = ora.chebyshev_filter(X, 10, a, b, a0)
+    assert np.abs(Xt.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
+    w, _ = C.syevd(torch.from_numpy(A.copy()).cuda())
+    assert np.abs(w.cpu().numpy() - np.linalg.eigvalsh(A)).max() < 1e-11
