@@ -155,20 +155,26 @@ void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* 
   // the nonlocal apply folded into the tensor-core launch (extra K columns of the cell
   // matrices fed by split rows of 2^t C^T x after the dof rows), unless the separate nonlocal
   // kernels are asked for
-  const bool fold = s->p.filter_variant == 0 && op->n_atoms > 0 && fused_plan_usable(op) &&
-                    ((B * 2) % 16) == 0;
+  // operators with constraint rows: distribute on the split rows, the plan's tiles (M^{-1/2}
+  // folded in by the plan), the adjoint after the launch
+  const bool constrained = !op->folded;
+  const bool fold = constrained || (s->p.filter_variant == 0 && op->n_atoms > 0 &&
+                                    fused_plan_usable(op));
   if (fold) prepare_fused_plan(op, st);
   const size_t rows = fold ? (size_t)op->fz.rows : (size_t)M;
   __half* hi = s->xs_hi.ensure(rows * B);
   __half* lo = s->xs_lo.ensure(rows * B);
-  float* W = fold ? s->fzw.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
+  float* W = fold && op->n_atoms ? s->fzw.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
+  float* save = constrained ? s->fzw.acc.ensure((size_t)op->n_con * B) : nullptr;
   const double e = (b - a) / 2.0, c = (b + a) / 2.0;
   double sigma = e / (a0 - c);
   const double sigma1 = sigma, gamma = 2.0 / sigma1;
   double alpha1 = sigma1 / e, alpha2 = -c;
   auto hx = [&](const float* src, float* dst, double sc) {
     s->hx_mark(st);
-    if (fold) {
+    if (constrained) {
+      hx_tc_constrained_split(op, hi, lo, dst, B, B, sc, W, save, st);
+    } else if (fold) {
       nl_project_to_split(op, src, B, W, hi, lo, st);
       hx_tc_folded_launch(op, hi, lo, dst, B, B, sc, st);
     } else if (!hx_tc_split(op, hi, lo, src, B, dst, B, B, sc, true, st)) {
@@ -222,7 +228,7 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
   float* Xb = s->Xb32.ensure((size_t)M * B);
   float* Yb = s->Yb32.ensure((size_t)M * B);
   copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
-  if (prec == CHEFSI_PREC_MIXED && tc_split_usable(op, B)) {
+  if (prec == CHEFSI_PREC_MIXED && (tc_split_usable(op, B) || constrained_tc_usable(op, B))) {
     cheb_filter_tc(s, op, Xb, Yb, M, B, m, a, b, a0, st);
   } else {
     cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
@@ -1284,8 +1290,14 @@ int chefsi_hx(chefsi_operator op, const void* src, int64_t ld_src, void* dst, in
   } else if (precision == CHEFSI_PREC_MIXED) {
     // tensor cores need a real, unconstrained operator and 16-byte aligned rows; otherwise the
     // SIMT FP32 apply serves the call
-    if (!hx_tc(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st))
-      hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+    if (!hx_tc(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st)) {
+      if (constrained_tc_usable(op, n_vec) && ld_src % 2 == 0 && ld_dst % 4 == 0 &&
+          (reinterpret_cast<uintptr_t>(dst) & 15) == 0)
+        hx_tc_constrained(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar,
+                          accumulate != 0, st);
+      else
+        hx_f32(op, (const float*)src, ld_src, (float*)dst, ld_dst, n_vec, scalar, accumulate != 0, st);
+    }
     const int tc = tc_check_error(op, st);
     if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   } else if (precision == CHEFSI_PREC_FP32) {

@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256, PP <= 8 ? 4 : 2)
 
 template <int PP, int U>
 void launch_project_split(chefsi_operator_s* op, const __half* xh, const __half* xl, int B,
-                          float* W, cudaStream_t st) {
+                          float* W, cudaStream_t st, const float* C32 = nullptr) {
   dim3 grid(op->nl_n_chunks, (B + 127) / 128);
   const size_t red = sizeof(float4) * 8 * op->n_proj * 32;
   CHEFSI_CUDA(cudaFuncSetAttribute(k_nl_project_split<PP, U>,
@@ -180,8 +180,61 @@ void launch_project_split(chefsi_operator_s* op, const __half* xh, const __half*
                                    (int)(sizeof(float4) * 8 * PP * 32)));
   k_nl_project_split<PP, U><<<grid, 256, red, st>>>(op->nl_chunk_atom.ptr, op->nl_chunk_row0.ptr,
                                                     op->nl_ptr.ptr, op->nl_dofs.ptr,
-                                                    op->nl_vals32.ptr, op->n_proj, xh, xl, B, W, B);
+                                                    C32 ? C32 : op->nl_vals32.ptr, op->n_proj, xh,
+                                                    xl, B, W, B);
   CHEFSI_CHECK_LAUNCH();
+}
+
+// distribute on the split rows: x_s = sum_e w'_e x_m(e) for every slave row s
+// (constraintMatrixInfoDevice.cc:546-594 in the folded basis), written as its FP16 split
+__global__ void k_con_split_distribute(const int* __restrict__ ids, const int* __restrict__ ptr,
+                                       const int* __restrict__ mas, const double* __restrict__ w,
+                                       int n_con, int B, __half* hi, __half* lo) {
+  const int64_t n = (int64_t)n_con * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / B), b = (int)(t - (int64_t)k * B);
+    float acc = 0.f;
+    for (int e = ptr[k]; e < ptr[k + 1]; ++e) {
+      const int64_t o = (int64_t)mas[e] * B + b;
+      acc = fmaf((float)w[e], __half2float(hi[o]) + __half2float(lo[o]), acc);
+    }
+    const __half h = __float2half_rn(acc);
+    const int64_t o = (int64_t)ids[k] * B + b;
+    hi[o] = h;
+    lo[o] = __float2half_rn(acc - __half2float(h));
+  }
+}
+
+// save[k] = y[slave k]; y[slave k] = 0 (the launch then reduces only its own contributions
+// into the slave rows)
+__global__ void k_con_stash(const int* __restrict__ ids, int n_con, float* y, int64_t ldy, int B,
+                            float* __restrict__ save) {
+  const int64_t n = (int64_t)n_con * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / B), b = (int)(t - (int64_t)k * B);
+    float* p = y + (int64_t)ids[k] * ldy + b;
+    save[t] = *p;
+    *p = 0.f;
+  }
+}
+
+// distribute_slave_to_master (constraintMatrixInfoDevice.cc:597-816 in the folded basis):
+// y_m += w'_e y_s, then the slave row gets its saved value back
+__global__ void k_con_adjoint(const int* __restrict__ ids, const int* __restrict__ ptr,
+                              const int* __restrict__ mas, const double* __restrict__ w, int n_con,
+                              float* y, int64_t ldy, int B, const float* __restrict__ save) {
+  const int64_t n = (int64_t)n_con * B;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / B), b = (int)(t - (int64_t)k * B);
+    float* p = y + (int64_t)ids[k] * ldy + b;
+    const float v = *p;
+    for (int e = ptr[k]; e < ptr[k + 1]; ++e)
+      atomicAdd(y + (int64_t)mas[e] * ldy + b, (float)w[e] * v);
+    *p = save[t];
+  }
 }
 
 template <typename T>
@@ -199,14 +252,21 @@ void to_device(DeviceBuffer<T>& b, const std::vector<T>& h) {
 
 }  // namespace
 
-bool fused_plan_usable(chefsi_operator_s* op) {
-  return tc_usable(op) && !op->is_complex && op->folded && op->n_proj <= 16;
+// the plan's tables serve real operators of at most 512 nodes per cell on an sm_100-family
+// device, with M^{-1/2} folded in by the operator or (constraint rows) by the plan itself
+bool plan_usable(chefsi_operator_s* op) {
+  return !op->is_complex && op->n_e <= 512 && op->n_proj <= 16 &&
+         (op->folded || op->n_con > 0) && tcx::tcgen05_device();
+}
+bool fused_plan_usable(chefsi_operator_s* op) { return plan_usable(op) && op->folded; }
+bool constrained_tc_usable(chefsi_operator_s* op, int B) {
+  return plan_usable(op) && !op->folded && B % 8 == 0;
 }
 
 void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   FusedPlan& fp = op->fz;
   if (fp.ready) return;
-  CHEFSI_REQUIRE(fused_plan_usable(op), "fused filter step: operator not supported");
+  CHEFSI_REQUIRE(plan_usable(op), "tensor-core plan: operator not supported");
   const int nc = op->n_cells, ne = op->n_e;
   const int64_t M = op->n_dofs;
   CHEFSI_CUDA(cudaStreamSynchronize(st));
@@ -251,6 +311,18 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
     nptr = to_host(op->nl_ptr, (size_t)op->n_atoms + 1);
     ndofs = to_host(op->nl_dofs, (size_t)op->nl_nnz);
     C = to_host(op->nl_vals64, (size_t)op->nl_nnz * P);
+    if (!op->folded) {
+      // constraint rows: the operator keeps C unscaled; the plan folds M^{-1/2} in (and keeps
+      // an FP32 copy for the projection from the split rows)
+      const std::vector<double> d = to_host(op->inv_sqrt_mass, (size_t)M);
+      std::vector<float> c32((size_t)op->nl_nnz * P);
+      for (int64_t r = 0; r < op->nl_nnz; ++r)
+        for (int j = 0; j < P; ++j) {
+          C[(size_t)r * P + j] *= d[ndofs[r]];
+          c32[(size_t)r * P + j] = (float)C[(size_t)r * P + j];
+        }
+      to_device(fp.nl_c32, c32);
+    }
     V = to_host(op->couplings, (size_t)op->n_atoms * P);
     // rows owned by one cell entry fix their cell; the others join a cell of theirs that has
     // the atom already, else the one with the fewest atoms
@@ -311,6 +383,24 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   double am = 0.0;
   CHEFSI_CUDA(cudaMemcpyAsync(&am, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
   CHEFSI_CUDA(cudaStreamSynchronize(st));
+  if (!op->folded) {
+    // the plan's tiles hold d_I A_IJ d_J: bound their largest entry by max|A| max(d)^2, and
+    // rescale the constraint weights for the folded basis: x_s = sum (w d_m / d_s) x_m
+    DeviceBuffer<double> dm(1);
+    absmax_block_f64(op->inv_sqrt_mass.ptr, 1, M, 1, dm.ptr, st);
+    double dmax = 0.0;
+    CHEFSI_CUDA(cudaMemcpyAsync(&dmax, dm.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+    am *= dmax * dmax;
+    const std::vector<double> d = to_host(op->inv_sqrt_mass, (size_t)M);
+    const std::vector<int> ids = to_host(op->con_ids, (size_t)op->n_con);
+    const std::vector<int> ptr = to_host(op->con_ptr, (size_t)op->n_con + 1);
+    const std::vector<int> mas = to_host(op->con_master, (size_t)ptr[op->n_con]);
+    std::vector<double> w = to_host(op->con_w, (size_t)ptr[op->n_con]);
+    for (int k = 0; k < op->n_con; ++k)
+      for (int e = ptr[k]; e < ptr[k + 1]; ++e) w[e] *= d[mas[e]] / d[ids[k]];
+    to_device(fp.con_wp, w);
+  }
   am = std::max(am, ext_max);
   const int e = (am > 0 && std::isfinite(am)) ? 14 - (int)std::floor(std::log2(am)) : 0;
   const double scale = std::ldexp(1.0, e);
@@ -375,6 +465,53 @@ void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W,
   const int64_t off = op->n_dofs * (int64_t)B;
   k_fz_w_split<<<grid_for(nw / 4, 256), 256, 0, st>>>(W, nw, fp.wscale, hi + off, lo + off);
   CHEFSI_CHECK_LAUNCH();
+}
+
+void hx_tc_constrained_split(chefsi_operator_s* op, __half* hi, __half* lo, float* dst,
+                             int64_t ldd, int B, double scalar, float* W, float* save,
+                             cudaStream_t st) {
+  prepare_fused_plan(op, st);
+  const FusedPlan& fp = op->fz;
+  const int64_t nc = (int64_t)op->n_con * B;
+  k_con_split_distribute<<<grid_for(nc, 256), 256, 0, st>>>(
+      op->con_ids.ptr, op->con_ptr.ptr, op->con_master.ptr, fp.con_wp.ptr, op->n_con, B, hi, lo);
+  CHEFSI_CHECK_LAUNCH();
+  if (op->n_atoms) {
+    const int64_t nw = (int64_t)op->n_atoms * op->n_proj * B;
+    CHEFSI_CUDA(cudaMemsetAsync(W, 0, sizeof(float) * nw, st));
+    if (op->n_proj <= 4)
+      launch_project_split<4, 8>(op, hi, lo, B, W, st, fp.nl_c32.ptr);
+    else if (op->n_proj <= 8)
+      launch_project_split<8, 4>(op, hi, lo, B, W, st, fp.nl_c32.ptr);
+    else
+      launch_project_split<16, 4>(op, hi, lo, B, W, st, fp.nl_c32.ptr);
+    const int64_t off = op->n_dofs * (int64_t)B;
+    k_fz_w_split<<<grid_for(nw / 4, 256), 256, 0, st>>>(W, nw, fp.wscale, hi + off, lo + off);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  k_con_stash<<<grid_for(nc, 256), 256, 0, st>>>(op->con_ids.ptr, op->n_con, dst, ldd, B, save);
+  CHEFSI_CHECK_LAUNCH();
+  hx_tc_folded_launch(op, hi, lo, dst, ldd, B, scalar, st);
+  k_con_adjoint<<<grid_for(nc, 256), 256, 0, st>>>(op->con_ids.ptr, op->con_ptr.ptr,
+                                                   op->con_master.ptr, fp.con_wp.ptr, op->n_con,
+                                                   dst, ldd, B, save);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void hx_tc_constrained(chefsi_operator_s* op, const float* src, int64_t lds, float* dst,
+                       int64_t ldd, int B, double scalar, bool accumulate, cudaStream_t st) {
+  CHEFSI_REQUIRE(constrained_tc_usable(op, B) && lds % 2 == 0 && ldd % 4 == 0 &&
+                     (reinterpret_cast<uintptr_t>(dst) & 15) == 0,
+                 "constrained tensor-core HX: real operator, B a multiple of 8, aligned rows");
+  prepare_fused_plan(op, st);
+  const size_t rows = (size_t)op->fz.rows;
+  __half* hi = op->xs_hi.ensure(rows * B);
+  __half* lo = op->xs_lo.ensure(rows * B);
+  float* W = op->n_atoms ? op->nlW32.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
+  float* save = op->ws32x.ensure((size_t)op->n_con * B);
+  split_rows_f32(src, lds, op->n_dofs, B, hi, lo, st);
+  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  hx_tc_constrained_split(op, hi, lo, dst, ldd, B, scalar, W, save, st);
 }
 
 // The filter of one block: X [M][B] FP32 in (scaled so that max |x| ~ 2^8), p_m(A) X out.

@@ -57,6 +57,9 @@ struct FusedPlan {
   DeviceBuffer<int> rowinfo;      // [n_cells][n_e] x {dof, shared index or -1}
   DeviceBuffer<unsigned char> ncontrib;  // [n_shared]
   DeviceBuffer<__half> hi, lo;    // extended cell-matrix tiles [n_cells][halves][nkb][n_half x 32]
+  // operators with constraint rows (M^{-1/2} folded in by the plan, not the operator):
+  DeviceBuffer<float> nl_c32;     // M^{-1/2} C in FP32 for the projection
+  DeviceBuffer<double> con_wp;    // constraint weights in the folded basis, w d_m / d_s
 };
 
 }  // namespace chefsi
@@ -216,6 +219,20 @@ void cheb_filter_fused(chefsi_operator_s* op, FusedWork& w, float* X, int64_t M,
                        cudaStream_t st);
 // the tables of the fused step (fused.cu); false if the operator does not take the fused path
 bool fused_plan_usable(chefsi_operator_s* op);
+// an operator with constraint rows on the tensor cores (the plan's tiles fold M^{-1/2} in)
+bool constrained_tc_usable(chefsi_operator_s* op, int B);
+// dst (+)= scalar A x for an operator with constraint rows, x given by its FP16 split rows
+// (hi, lo) [plan rows][B]: the slave rows of the split are overwritten by the distributed
+// values (sum w' x_m), the projector rows by 2^t C^T x; dst's slave rows keep their values
+// (the launch's contributions to them are moved to their masters). W: n_atoms n_proj B floats,
+// save: n_constrained B floats of workspace.
+void hx_tc_constrained_split(chefsi_operator_s* op, __half* hi, __half* lo, float* dst,
+                             int64_t ldd, int B, double scalar, float* W, float* save,
+                             cudaStream_t st);
+// the same from FP32 vectors src [n_dofs][lds] (split into the operator's workspace); dst is
+// zeroed first unless accumulate
+void hx_tc_constrained(chefsi_operator_s* op, const float* src, int64_t lds, float* dst,
+                       int64_t ldd, int B, double scalar, bool accumulate, cudaStream_t st);
 void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st);
 // device error flag of the tensor-core kernel (CHEFSI_OK or CHEFSI_ERR_TIMEOUT); clears it
 int tc_check_error(chefsi_operator_s* op, cudaStream_t st);

@@ -881,8 +881,11 @@ __global__ void k_split_mats(const double* __restrict__ mats, int n_cells, int n
 
 // the fused step's tiles: (cell, half, K-block) tiles over nkb K-blocks; nodes J < n_e from the
 // cell matrices, the projector columns (J >= n_e) left zero here and scattered afterwards
+// (d, map non-null: the cell matrices are unscaled and D = diag(d) is folded in here,
+// d[map I] A_IJ d[map J], as for the operators with constraint rows)
 __global__ void k_split_mats_ext(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
-                                 int n_halves, int nkb, double scale, __half* __restrict__ hi,
+                                 int n_halves, int nkb, double scale, const double* __restrict__ d,
+                                 const int* __restrict__ map, __half* __restrict__ hi,
                                  __half* __restrict__ lo) {
   const int64_t n = (int64_t)n_cells * n_halves * nkb * n_half * 32;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
@@ -890,7 +893,10 @@ __global__ void k_split_mats_ext(const double* __restrict__ mats, int n_cells, i
     int c, I, J;
     tile_entry(t, n_half, n_halves, nkb, c, I, J);
     double v = 0.0;
-    if (I < n_e && J < n_e) v = scale * mats[((int64_t)c * n_e + I) * n_e + J];
+    if (I < n_e && J < n_e) {
+      v = scale * mats[((int64_t)c * n_e + I) * n_e + J];
+      if (d) v *= d[map[(int64_t)c * n_e + I]] * d[map[(int64_t)c * n_e + J]];
+    }
     const __half h = __double2half(v);
     hi[t] = h;
     lo[t] = __double2half(v - (double)__half2float(h));
@@ -1206,8 +1212,10 @@ void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __
                     cudaStream_t st) {
   const TcPlan p = plan_for(op->n_e, 2, true);
   const int64_t n = (int64_t)op->n_cells * p.n_halves * nkb * p.n_half * 32;
-  k_split_mats_ext<<<grid_for(n, 256), 256, 0, st>>>(op->mats64.ptr, op->n_cells, op->n_e, p.n_half,
-                                                     p.n_halves, nkb, scale, hi, lo);
+  const bool fold = !op->folded;   // constraint rows: fold M^{-1/2} into this copy
+  k_split_mats_ext<<<grid_for(n, 256), 256, 0, st>>>(
+      op->mats64.ptr, op->n_cells, op->n_e, p.n_half, p.n_halves, nkb, scale,
+      fold ? op->inv_sqrt_mass.ptr : nullptr, fold ? op->map.ptr : nullptr, hi, lo);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -287,3 +287,62 @@ def test_filter_variants_match_oracle(chefsi, p, n, B, proj):
         assert rel(out[variant], ref) < 5e-6, variant
     assert rel(out["folded"], out["separate"]) < 5e-6
     assert rel(out["fused"], out["separate"]) < 5e-6
+
+
+def _unfolded_operators(chefsi, pr, projectors):
+    """The problem's operator on the unfolded lattice with periodicity as constraint rows
+    (slave = master, weight 1), on the GPU and in the oracle; projectors (optional) moved to
+    the masters' extended numbering."""
+    from dftfe_gb300 import fe
+    emap, n_ext, cons, mass_ext = unfolded_setup(pr)
+    nl = None
+    if projectors and pr.nonlocal_ is not None:
+        npt, m = pr.mesh.npts, pr.mesh.npts + 1
+        f = pr.nonlocal_.dofs.astype(np.int64)
+        ext = (f % npt) + m * ((f // npt) % npt + m * (f // (npt * npt)))
+        nl = fe.NonlocalProjectors(pr.nonlocal_.n_atoms, pr.nonlocal_.n_proj, pr.nonlocal_.ptr,
+                                   ext.astype(np.int32), pr.nonlocal_.values,
+                                   pr.nonlocal_.couplings)
+    op = chefsi.KohnShamOperator(emap, pr.cell_mats, np.sqrt(mass_ext), 1 / np.sqrt(mass_ext),
+                                 n_ext, projectors=nl, constraints=cons)
+    ora = orc.OracleOperator(emap, pr.cell_mats, 1 / np.sqrt(mass_ext), n_ext, projectors=nl,
+                             constraints=cons)
+    return op, ora, n_ext, cons[0]
+
+
+@pytest.mark.parametrize("p,n,B,proj", [(4, 2, 96, False), (2, 3, 8, True), (6, 2, 136, False),
+                                        (4, 2, 64, True)])
+def test_hx_tensor_cores_with_constraint_rows(chefsi, p, n, B, proj):
+    """The mixed (tensor-core) HX of an operator with constraint rows (the periodic cube
+    unfolded, periodicity as slave rows): distribute on the FP16 split rows, the plan's tiles
+    with M^{-1/2} folded in, the adjoint after the launch; against the oracle's constrained HX,
+    2e-6 relative (the tolerance of the unconstrained tensor-core HX)."""
+    pr = small_problem(n=n, L=2.0 * n, p=p, wells=3, projectors=proj)
+    op, ora, n_ext, _ = _unfolded_operators(chefsi, pr, proj)
+    X = np.random.default_rng(p + B).uniform(-1, 1, (n_ext, B))
+    Xt = torch.from_numpy(X).float().cuda()
+    Y = torch.zeros_like(Xt)
+    op.HX(Xt, Y, precision="mixed")
+    ref = ora.HX(Xt.double().cpu().numpy())
+    assert rel(Y.double().cpu().numpy(), ref) < 2e-6
+
+
+def test_mixed_solve_with_constraint_rows_matches_oracle(chefsi):
+    """Ten mixed CheFSI iterations (tensor-core filter with the constraint rows, mixed
+    Rayleigh-Ritz) on the unfolded periodic operator with projectors, from X0 with zero slave
+    rows (as DFT-FE keeps them), with the oracle's bounds before every iteration: the occupied
+    Ritz values within 1e-6 Ha of the oracle's FP64 CheFSI."""
+    pr = small_problem(n=3, L=6.0, p=4, wells=3, nwfc=16, seed=5, projectors=True)
+    op, ora, n_ext, slaves = _unfolded_operators(chefsi, pr, True)
+    X0 = np.random.default_rng(9).uniform(-1, 1, (n_ext, 16))
+    X0[slaves] = 0.0
+    lo, up = orc.lanczos_bounds(ora, np.ones(n_ext), 20)
+    st = orc.SolverState(lo, lo + 0.3 * (up - lo), up)
+    s = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
+        chebyshevOrder=16, chebyWfcBlockSize=16, wfcBlockSize=16, rr_precision="fp32tc"))
+    Xo, Xg = X0.copy(), torch.from_numpy(X0.copy()).cuda()
+    for _ in range(10):
+        s.reinitSpectrumBounds(st.a0, st.b_low, st.b_up)
+        ev, _ = s.solve(op, Xg, useMixedPrec=True)
+        ev_o, res_o, Xo = orc.solve(ora, Xo, st, m=16)
+    assert np.abs(ev[:8] - ev_o[:8]).max() < 1e-6, ev[:8] - ev_o[:8]
