@@ -325,6 +325,56 @@ def fp64_leg(pr, op, X, solver, params, up):
                         "bounds (CUDA events); Ritz errors against the FP64 iteration"}
 
 
+def fp64_leg_reduced(pr, op, args, up, n_r=512):
+    """The FP64 leg where the full block does not fit twice (the large workload): on the
+    workload's operator with n_r vectors (blocks of 256, the workload's degree), two mixed
+    iterations from a seeded block, then one FP64 and one mixed iteration from the same block
+    and bounds; Ritz errors of the mixed iteration against the FP64 one."""
+    import torch
+    from dftfe_gb300 import chefsi
+    N, m, M = pr.n_wfc, pr.cheb_degree, pr.n_dofs
+    nocc = n_r // 2
+    prm = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=256, wfcBlockSize=256,
+                              mixed_precision="mixed", rr_precision=args.rr_precision,
+                              filter_variant=args.filter)
+    lo, blow, up0 = first_bounds(chefsi, op, N)
+    sv = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(prm)
+    sv.reinitSpectrumBounds(lo, blow, up)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed + 2)
+    X = torch.rand((M, n_r), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    for _ in range(2):
+        ev, _ = sv.solve(op, X, useMixedPrec=True)
+        sv.reinitSpectrumBounds(ev[0], ev[-1], up)
+    out, occ = {}, {}
+    for mode in ("fp64", "mixed"):
+        s2 = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(prm)
+        s2.reinitSpectrumBounds(ev[0], ev[-1], up)
+        Xc = X.clone()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        e, r = s2.solve(op, Xc, useMixedPrec=(mode == "mixed"))
+        e1.record()
+        torch.cuda.synchronize()
+        out[mode] = (e.copy(), r.copy(), e0.elapsed_time(e1) / 1e3)
+        occ[mode] = Xc[:, :nocc].contiguous()
+        del Xc, s2
+        torch.cuda.empty_cache()
+    Qf, Qm = occ["fp64"], occ["mixed"]
+    angle = float(np.arcsin(min(1.0, float(torch.linalg.matrix_norm(Qm - Qf @ (Qf.T @ Qm), ord=2)))))
+    d = np.abs(out["mixed"][0] - out["fp64"][0])
+    return {"fp64_leg_reduced": {
+        "n_wfc": n_r, "fp64_s_per_iter": out["fp64"][2], "mixed_s_per_iter": out["mixed"][2],
+        "ritz_err_vs_fp64_Ha": {"occupied": float(d[:nocc].max()), "all": float(d.max()),
+                                "occupied_states": nocc},
+        "subspace_angle_rad": angle,
+        "res_occ_max": {"mixed": float(out["mixed"][1][:nocc].max()),
+                        "fp64": float(out["fp64"][1][:nocc].max())},
+        "note": "the workload's operator with 512 of its 4096 vectors: X (134 GB) cannot be held "
+                "twice for an FP64 iteration of the full block"}}
+
+
 def solver_bounds(solver):
     import ctypes
     from dftfe_gb300 import _lib
@@ -400,8 +450,11 @@ def run_ours(args):
         t_ms = pools.max_over_ranks(t_ms)
     phases = solver.timings(True)
 
-    e2e = e2e_pipeline(step, X, max(2, min(args.steps, 4)))
+    large = args.workload == "large"
+    # the large workload's X (134 GB) leaves no room for the pipelined copies' device buffers
+    e2e = None if large else e2e_pipeline(step, X, max(2, min(args.steps, 4)))
     torch.cuda.empty_cache()
+    free_b, total_b = torch.cuda.mem_get_info()
 
     hx_flops, hx_bytes = hx_algorithmic(pr, blk, fused=fused)
     hx_flops *= N / blk
@@ -415,9 +468,12 @@ def run_ours(args):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f16split/f64",
         "data": "synthetic (seeded wells/projectors, X0 ~ U(-1,1)); inputs larger than L2",
         "config": {"workload": args.workload, "n_dofs": M, "n_cells": pr.mesh.n_cells,
-                   "fe_degree": pr.mesh.p, "n_wfc": N, "cheb_degree": m, "wells": 64,
-                   "projectors_per_well": 8, "precision": "mixed",
-                   "rr_hx_precision": args.rr_precision, "l2": "inputs > L2 (X is 14 GB)",
+                   "fe_degree": pr.mesh.p, "n_wfc": N, "cheb_degree": m,
+                   "wells": int(pr.info["n_wells"]),
+                   "projectors_per_well": 0 if pr.nonlocal_ is None else pr.nonlocal_.n_proj,
+                   "precision": "mixed", "filter_block": blk,
+                   "rr_hx_precision": args.rr_precision,
+                   "l2": f"inputs > L2 (X is {M * N * 8 / 1e9:.1f} GB)",
                    "filter": args.filter,
                    "parallelism": f"replicas{world}"},
         "hx_gflops": hx_flops / (avg_hx_ms * 1e-3) / 1e9,
@@ -439,12 +495,16 @@ def run_ours(args):
                                             "recurrence pass not included)"}[args.filter],
                      "algorithmic_bytes_per_launch": hx_bytes},
         "e2e": e2e,
+        "device_memory_used_gb": (total_b - free_b) / 1e9,
         "clocks": clk.summary(),
     }
     line["gpu_launches"] = int(launches)
     if not args.no_fp64_leg and world == 1:
-        line.update(fp64_leg(pr, op, X, solver, params, up))
-    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        if large:
+            line.update(fp64_leg_reduced(pr, op, args, up))
+        else:
+            line.update(fp64_leg(pr, op, X, solver, params, up))
+    if rank == 0 and not args.no_cpu_baseline and world == 1 and not large:
         line["cpu_baseline"] = cpu_baseline_line(pr, m)
     if rank == 0:
         print(json.dumps(line))
