@@ -414,7 +414,10 @@ def run_ours(args):
     solver.set_profiling(True, mixed=True)
     g = torch.Generator(device=dev)
     g.manual_seed(args.seed + 1)
-    X = (torch.rand((M, N), generator=g, device=dev, dtype=torch.float64) * 2 - 1)
+    # filled in place: X of the large workload is 134 GB, and temporaries of its size would stay
+    # in torch's cache, out of the library's reach
+    X = torch.empty((M, N), device=dev, dtype=torch.float64).uniform_(-1.0, 1.0, generator=g)
+    torch.cuda.empty_cache()
 
     def step(Xd):
         ev, res = solver.solve(op, Xd, useMixedPrec=True)
