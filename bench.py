@@ -345,11 +345,11 @@ def fp64_leg_reduced(pr, op, args, up, n_r=512):
     X = torch.rand((M, n_r), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
     for _ in range(2):
         ev, _ = sv.solve(op, X, useMixedPrec=True)
-        sv.reinitSpectrumBounds(ev[0], ev[-1], up)
+        sv.reinitSpectrumBounds(ev[0], blow, up)
     out, occ = {}, {}
     for mode in ("fp64", "mixed"):
         s2 = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(prm)
-        s2.reinitSpectrumBounds(ev[0], ev[-1], up)
+        s2.reinitSpectrumBounds(ev[0], blow, up)
         Xc = X.clone()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -372,7 +372,8 @@ def fp64_leg_reduced(pr, op, args, up, n_r=512):
         "res_occ_max": {"mixed": float(out["mixed"][1][:nocc].max()),
                         "fp64": float(out["fp64"][1][:nocc].max())},
         "note": "the workload's operator with 512 of its 4096 vectors: X (134 GB) cannot be held "
-                "twice for an FP64 iteration of the full block"}}
+                "twice for an FP64 iteration of the full block; bLow kept at its first-call "
+                "value"}}
 
 
 def solver_bounds(solver):
@@ -419,9 +420,16 @@ def run_ours(args):
     X = torch.empty((M, N), device=dev, dtype=torch.float64).uniform_(-1.0, 1.0, generator=g)
     torch.cuda.empty_cache()
 
+    large = args.workload == "large"
+
     def step(Xd):
         ev, res = solver.solve(op, Xd, useMixedPrec=True)
-        solver.reinitSpectrumBounds(ev[0], ev[-1], up)
+        # the large workload keeps its first-call bounds: 4096 vectors filtered from random ones
+        # with bLow at their largest Ritz value (some 28,000 states below it) leave an overlap
+        # with condition ~1e10, beyond the 22 bits of the mixed Gram; the cost of an iteration
+        # does not depend on the bounds
+        if not large:
+            solver.reinitSpectrumBounds(ev[0], ev[-1], up)
         return ev, res
 
     for _ in range(args.warmup):
@@ -453,7 +461,6 @@ def run_ours(args):
         t_ms = pools.max_over_ranks(t_ms)
     phases = solver.timings(True)
 
-    large = args.workload == "large"
     # the large workload's X (134 GB) leaves no room for the pipelined copies' device buffers
     e2e = None if large else e2e_pipeline(step, X, max(2, min(args.steps, 4)))
     torch.cuda.empty_cache()
