@@ -511,6 +511,11 @@ def run_ours(args):
     line["gpu_launches"] = int(launches)
     if not args.no_fp64_leg and world == 1:
         if large:
+            # the timed block and its solver's workspaces make room for the reduced leg
+            del X, solver
+            import gc
+            gc.collect()
+            torch.cuda.empty_cache()
             line.update(fp64_leg_reduced(pr, op, args, up))
         else:
             line.update(fp64_leg(pr, op, X, solver, params, up))
