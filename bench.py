@@ -466,9 +466,8 @@ def run_ours(args):
     torch.cuda.empty_cache()
     free_b, total_b = torch.cuda.mem_get_info()
 
+    # one filter HX launch covers one column block of blk vectors
     hx_flops, hx_bytes = hx_algorithmic(pr, blk, fused=fused)
-    hx_flops *= N / blk
-    hx_bytes *= N / blk
     hbm, bf16, src = peaks()
     avg_hx_ms = hx_ms / max(hx_n, 1)
     achieved = hx_bytes / (avg_hx_ms * 1e-3) / 1e9
