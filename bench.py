@@ -96,7 +96,8 @@ TC_TRAFFIC_BYTES = {("mixed", "separate"): 20.33e9 + 8.20e9,
 def hx_algorithmic(pr, B, s_h=4, s_x=4, fused=False):
     """Bytes and flops of one filter HX over B vectors (reference formulation):
     flops = 2 n_c n_e^2 B + 4 n_nlc-rows P B; bytes = s_H n_c n_e^2 + 2 s_X M B + 4 n_c n_e.
-    A fused filter step (the recurrence finished in the same launch) also reads x_{k-2}:
+    A filter step that finishes the recurrence in the same launch (the fused step; the shifted
+    default, which reduces a (A - c) x_{k-1} into the buffer of x_{k-2}) also reads x_{k-2}:
     + s_X M B."""
     nc, ne = pr.mesh.n_cells, pr.mesh.nodes_per_cell
     nl_rows = 0 if pr.nonlocal_ is None else int(pr.nonlocal_.ptr[-1])
@@ -406,7 +407,9 @@ def run_ours(args):
     lo, blow, up = first_bounds(chefsi, op, N)
     # the large workload (4096 vectors) is filtered in blocks of 256, the others in one block
     blk = 256 if args.workload == "large" else N
-    fused = args.filter == "fused"
+    # the fused step and the shifted default each finish the recurrence in the HX launch (it
+    # reads x_{j-2} as well)
+    fused = args.filter in ("fused", "folded")
     params = chefsi.SolverParams(chebyshevOrder=m, chebyWfcBlockSize=blk, wfcBlockSize=blk,
                                  mixed_precision="mixed", rr_precision=args.rr_precision,
                                  filter_variant=args.filter)
@@ -497,9 +500,14 @@ def run_ours(args):
                                       "read + write, ncu (profiles/)",
                      "kernel": {"fused": "cell_hx_tc_kernel<FUSED> + nonlocal projection: one "
                                          "filter step (HX, nonlocal, recurrence)",
-                                "folded": "cell_hx_tc_kernel with the nonlocal apply as extra K "
-                                          "columns + nonlocal projection (filter HX; recurrence "
-                                          "pass not included)",
+                                "folded": "cell_hx_tc_kernel with the shift on the tiles' "
+                                          "diagonals and the nonlocal apply as extra K columns "
+                                          "+ nonlocal projection: one filter step x_j = a (A - c) "
+                                          "x_{j-1} + b x_{j-2} reduced into x_{j-2}'s buffer "
+                                          "(the split pass of the next input not included)",
+                                "axpby": "cell_hx_tc_kernel with the nonlocal apply as extra K "
+                                         "columns + nonlocal projection (filter HX; recurrence "
+                                         "pass not included)",
                                 "separate": "cell_hx_tc_kernel + nonlocal kernels (filter HX; "
                                             "recurrence pass not included)"}[args.filter],
                      "algorithmic_bytes_per_launch": hx_bytes},
@@ -951,7 +959,7 @@ def main():
                     help="time only the tensor-core filter HX (K launches after W warm-up)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
-    ap.add_argument("--filter", default="folded", choices=["folded", "fused", "separate"],
+    ap.add_argument("--filter", default="folded", choices=["folded", "fused", "separate", "axpby"],
                     help="mixed filter variant: recurrence pass + HX with the nonlocal apply as "
                          "tensor-core K columns (folded), recurrence in the HX launch (fused), "
                          "or separate nonlocal kernels (separate)")

@@ -397,9 +397,11 @@ class SolverParams:
     # dofs per row slab (0 automatic)
     rr_block: int = 0
     rr_slab_rows: int = 0
-    # mixed tensor-core filter: "folded" (recurrence pass + HX launch with the nonlocal apply as
-    # extra tensor-core K columns), "fused" (the recurrence finished inside the HX launch) or
-    # "separate" (recurrence pass, HX launch, separate nonlocal kernels)
+    # mixed tensor-core filter: "folded" (one HX launch per degree with the Chebyshev shift on
+    # the tiles' diagonals and the nonlocal apply as extra tensor-core K columns, no recurrence
+    # pass), "axpby" (recurrence pass + that HX launch without the shift), "fused" (the
+    # recurrence finished inside the HX launch) or "separate" (recurrence pass, HX launch,
+    # separate nonlocal kernels)
     filter_variant: str = "folded"
 
 
@@ -427,7 +429,7 @@ class ChebyshevOrthogonalizedSubspaceIterationSolver:
             p.ss_frac_reduced = int(self.params.spectrum_split_frac_reduced)
             p.rr_block = int(self.params.rr_block)
             p.rr_slab_rows = int(self.params.rr_slab_rows)
-            p.filter_variant = {"folded": 0, "fused": 1, "separate": -1}[self.params.filter_variant]
+            p.filter_variant = {"folded": 0, "fused": 1, "separate": -1, "axpby": 2}[self.params.filter_variant]
             h = ctypes.c_void_p()
             check(self._lib.chefsi_solver_create(ctypes.byref(p), ctypes.byref(h)))
             self._h[key] = h

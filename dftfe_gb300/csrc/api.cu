@@ -141,6 +141,64 @@ void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double
   if (y != X) copy_block<T, T>(y, B, X, B, M, B, 1.0, st);
 }
 
+// Mixed Chebyshev filter with the shift on the tensor-core tiles. In the sigma form every degree
+// is x_j = alpha1_j (A - c) x_{j-1} + alpha2_j x_{j-2} with the same c, so the plan's tiles carry
+// 2^s (A_II - c / n_I) on their diagonals for the whole call and each degree is one HX launch
+// reducing into the buffer of x_{j-2}. Each buffer holds its vector up to a factor kept here
+// (vector = factor * buffer): the update alpha2 x_{j-2} only changes the factor, so no
+// recurrence pass runs (the reference's combinedDeviceKernel,
+// linearAlgebraOperationsDevice.cc:37-104, reads and writes both vectors every degree). Per
+// degree the buffer of x_{j-1} is read once more to write the FP16 split of f x_{j-1} (f the
+// power of two nearest its factor, which keeps the split at the vector's own magnitude) and the
+// projector rows. Returns false (nothing done) when the shifted diagonals would leave FP16's
+// range.
+bool cheb_filter_shifted(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
+                         int B, int m, double a, double b, double a0, cudaStream_t st) {
+  prepare_fused_plan(op, st);
+  const double e = (b - a) / 2.0, c = (b + a) / 2.0;
+  if (!set_tile_shift(op, c, st)) return false;
+  const FusedPlan& fp = op->fz;
+  __half* hi = s->xs_hi.ensure((size_t)fp.rows * B);
+  __half* lo = s->xs_lo.ensure((size_t)fp.rows * B);
+  float* W = op->n_atoms ? s->fzw.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
+  const int64_t n = M * (int64_t)B;
+  // out += scalar (A - c) v for the vector v = s_in in: the launch multiplies the split of f in,
+  // so its scalar is scalar s_in / f; with a factor beyond 2^+-64 the input buffer is rewritten
+  // as f in (its factor then divides by f)
+  auto apply = [&](float* in, double& s_in, float* out, double scalar) {
+    const double f = std::ldexp(1.0, (int)std::lround(std::log2(std::fabs(s_in))));
+    const bool rewrite = std::fabs(std::log2(f)) > 64.0;
+    split_scaled_f32(in, n, f, rewrite, hi, lo, st);
+    s->hx_mark(st);
+    nl_project_to_split(op, in, B, W, hi, lo, st, rewrite ? 1.0 : f);
+    hx_tc_folded_launch(op, hi, lo, out, B, B, scalar * s_in / f, st, c);
+    s->hx_mark(st);
+    if (rewrite) s_in /= f;
+  };
+  double sigma = e / (a0 - c);
+  const double sigma1 = sigma, gamma = 2.0 / sigma1;
+  double sx = 1.0, sy = 1.0;   // x_0 = X, x_1 = sy Y
+  CHEFSI_CUDA(cudaMemsetAsync(Y, 0, sizeof(float) * (size_t)n, st));
+  apply(X, sx, Y, sigma1 / e);
+  float* x = X;   // x_{j-2}
+  float* y = Y;   // x_{j-1}
+  for (int degree = 2; degree < m + 1; ++degree) {
+    const double sigma2 = 1.0 / (gamma - sigma);
+    const double alpha1 = 2.0 * sigma2 / e, alpha2 = -(sigma * sigma2);
+    // x_j = alpha2 sx [x + alpha1 / (alpha2 sx) (A - c) x_{j-1}] in the buffer of x_{j-2}
+    apply(y, sy, x, alpha1 / (alpha2 * sx));
+    sx *= alpha2;
+    std::swap(x, y);
+    std::swap(sx, sy);
+    sigma = sigma2;
+  }
+  if (y != X)
+    copy_block<float, float>(y, B, X, B, M, B, sy, st);
+  else
+    scale_block<float>(X, B, M, B, sy, st);
+  return true;
+}
+
 // Mixed Chebyshev filter on the tensor cores (same recurrence as cheb_filter). The HX input
 // is also kept as FP16 hi + lo rows: the step y_{k-1} <- -c alpha1 y_k + alpha2 y_{k-1}
 // reads y_k, the next HX's input, and writes its split in the same pass; the first input is
@@ -158,8 +216,13 @@ void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* 
   // operators with constraint rows: distribute on the split rows, the plan's tiles (M^{-1/2}
   // folded in by the plan), the adjoint after the launch
   const bool constrained = !op->folded;
-  const bool fold = constrained || (s->p.filter_variant == 0 && op->n_atoms > 0 &&
-                                    fused_plan_usable(op));
+  if (s->p.filter_variant == 0 && !constrained && fused_plan_usable(op) &&
+      cheb_filter_shifted(s, op, X, Y, M, B, m, a, b, a0, st))
+    return;
+  // variant 2 (and variant 0 when the shift does not fit the tiles): a recurrence pass per
+  // degree and the HX launch with the nonlocal apply folded in
+  const bool fold = constrained || ((s->p.filter_variant == 0 || s->p.filter_variant == 2) &&
+                                    op->n_atoms > 0 && fused_plan_usable(op));
   if (fold) prepare_fused_plan(op, st);
   const size_t rows = fold ? (size_t)op->fz.rows : (size_t)M;
   __half* hi = s->xs_hi.ensure(rows * B);

@@ -1020,6 +1020,8 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& gs, unsigned int nb
   __syncthreads();
   if (threadIdx.x == 0) {
     fail = 0;
+    // the limit is loaded ahead of the atomics (its latency overlaps theirs)
+    const uint32_t spins = g_barrier_spins;
     const unsigned int g = atomicAdd(gs.gen, 0u);
     __threadfence();
     if (atomicAdd(gs.count, 1u) == nblocks - 1) {
@@ -1027,7 +1029,6 @@ __device__ __forceinline__ bool grid_barrier(const GridSync& gs, unsigned int nb
       __threadfence();
       atomicAdd(gs.gen, 1u);
     } else {
-      const uint32_t spins = *reinterpret_cast<volatile uint32_t*>(&g_barrier_spins);
       uint32_t i = 0;
       for (; i < spins; ++i) {
         if (*reinterpret_cast<volatile unsigned int*>(gs.gen) != g) break;

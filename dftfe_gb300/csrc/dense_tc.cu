@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       mbar_init(&acc_empty[b], kGramEpiWarps);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
-    *abort_flag = 0;
+    *abort_flag = wait_limit_init(a.err);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) tmem_alloc(tmem_slot, 512);
@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(kRotThreads, 1)
       mbar_init(&acc_empty[b], 4);   // one arrival per epilogue warp
     }
     mbar_init(mma_done, 1);
-    *abort_flag = 0;
+    *abort_flag = wait_limit_init(a.err);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) tmem_alloc(tmem_slot, 512);

@@ -62,6 +62,72 @@ __global__ void k_fz_w_split(const float* __restrict__ W, int64_t n, float scale
   }
 }
 
+// the tiles' diagonal entries (cell c, node I) = split of 2^s (A_II - shift / n_I), n_I the cell
+// entries of the node's dof (1 for a row of one entry); shift 0 restores the split of 2^s A_II
+// exactly as the plan wrote it
+__global__ void k_fz_shift(const double* __restrict__ mats, int n_cells, int n_e, int n_half,
+                           int n_halves, int nkb, const int2* __restrict__ rowinfo,
+                           const unsigned char* __restrict__ ncontrib, double scale, double shift,
+                           __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int64_t n = (int64_t)n_cells * n_e;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / n_e;
+    const int I = (int)(t - c * n_e);
+    const int sh = rowinfo[t].y;
+    const double ne = sh < 0 ? 1.0 : (double)ncontrib[sh];
+    const double v = scale * (mats[(c * n_e + I) * n_e + I] - shift / ne);
+    const int half = I / n_half, ri = I % n_half;
+    const int64_t tix = (c * n_halves + half) * nkb + I / 32;
+    const int64_t o =
+        tix * n_half * 32 + tcx::sw64_offset((uint32_t)ri, 2u * (uint32_t)(I % 32)) / 2;
+    const __half h = __double2half(v);
+    hi[o] = h;
+    lo[o] = __double2half(v - (double)__half2float(h));
+  }
+}
+
+// the largest |A_II| over the cells (one block)
+__global__ void k_fz_diag_max(const double* __restrict__ mats, int64_t n, int n_e,
+                              double* __restrict__ out) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
+    const int64_t c = t / n_e;
+    const int I = (int)(t - c * n_e);
+    m = fmax(m, fabs(mats[(c * n_e + I) * n_e + I]));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// (hi, lo) = split(f x) over n entries (float4 units); rewrite: x = f x as well
+__global__ void k_split_scaled(float* __restrict__ x, int64_t n, float f, int rewrite,
+                               __half* __restrict__ hi, __half* __restrict__ lo) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n / 4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float4 v = reinterpret_cast<const float4*>(x)[t];
+    v.x *= f, v.y *= f, v.z *= f, v.w *= f;
+    if (rewrite) reinterpret_cast<float4*>(x)[t] = v;
+    const float a[4] = {v.x, v.y, v.z, v.w};
+    __half h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      h[i] = __float2half_rn(a[i]);
+      l[i] = __float2half_rn(a[i] - __half2float(h[i]));
+    }
+    reinterpret_cast<__half2*>(hi)[2 * t] = __halves2half2(h[0], h[1]);
+    reinterpret_cast<__half2*>(hi)[2 * t + 1] = __halves2half2(h[2], h[3]);
+    reinterpret_cast<__half2*>(lo)[2 * t] = __halves2half2(l[0], l[1]);
+    reinterpret_cast<__half2*>(lo)[2 * t + 1] = __halves2half2(l[2], l[3]);
+  }
+}
+
 // x = hi + lo over n entries (float4 units)
 __global__ void k_fz_join(const __half* __restrict__ hi, const __half* __restrict__ lo, int64_t n,
                           float* __restrict__ x) {
@@ -402,8 +468,19 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
     to_device(fp.con_wp, w);
   }
   am = std::max(am, ext_max);
-  const int e = (am > 0 && std::isfinite(am)) ? 14 - (int)std::floor(std::log2(am)) : 0;
+  // largest entry in [2^11, 2^12): room on the diagonals for the filter's shift (FP16 keeps
+  // its 11-bit significand at every magnitude, so the headroom costs no precision)
+  const int e = (am > 0 && std::isfinite(am)) ? 11 - (int)std::floor(std::log2(am)) : 0;
   const double scale = std::ldexp(1.0, e);
+  fp.diag_max = 0.0;
+  if (op->folded) {
+    DeviceBuffer<double> dmx(1);
+    k_fz_diag_max<<<1, 256, 0, st>>>(op->mats64.ptr, (int64_t)nc * ne, ne, dmx.ptr);
+    CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CUDA(cudaMemcpyAsync(&fp.diag_max, dmx.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+  }
+  fp.shift = 0.0;
   int n_half = 0, n_halves = 0;
   tc_row_split(ne, &n_half, &n_halves);
   const size_t ntile = (size_t)nc * n_halves * nkb * n_half * 32;
@@ -457,13 +534,43 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
 }
 
 void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W, __half* hi,
-                         __half* lo, cudaStream_t st) {
+                         __half* lo, cudaStream_t st, double f) {
   if (op->n_atoms == 0) return;
   const FusedPlan& fp = op->fz;
   nl_project_f32(op, x, B, W, B, st);   // zeroes W first
   const int64_t nw = (int64_t)op->n_atoms * op->n_proj * B;
   const int64_t off = op->n_dofs * (int64_t)B;
-  k_fz_w_split<<<grid_for(nw / 4, 256), 256, 0, st>>>(W, nw, fp.wscale, hi + off, lo + off);
+  k_fz_w_split<<<grid_for(nw / 4, 256), 256, 0, st>>>(W, nw, (float)(fp.wscale * f), hi + off,
+                                                      lo + off);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+bool set_tile_shift(chefsi_operator_s* op, double shift, cudaStream_t st) {
+  FusedPlan& fp = op->fz;
+  CHEFSI_REQUIRE(fp.ready, "tile shift: plan not prepared");
+  if (shift == fp.shift) return true;
+  if (!op->folded) return false;
+  // |A_II - shift / n_I| <= max |A_II| + |shift| must stay inside FP16's range once scaled
+  if (!(((double)fp.scale) * (fp.diag_max + std::fabs(shift)) < 60000.0)) return false;
+  int n_half = 0, n_halves = 0;
+  tc_row_split(op->n_e, &n_half, &n_halves);
+  const int64_t n = (int64_t)op->n_cells * op->n_e;
+  k_fz_shift<<<grid_for(n, 256), 256, 0, st>>>(
+      op->mats64.ptr, op->n_cells, op->n_e, n_half, n_halves, fp.nkb,
+      reinterpret_cast<const int2*>(fp.rowinfo.ptr), fp.ncontrib.ptr, (double)fp.scale, shift,
+      fp.hi.ptr, fp.lo.ptr);
+  CHEFSI_CHECK_LAUNCH();
+  fp.shift = shift;
+  return true;
+}
+
+void split_scaled_f32(float* x, int64_t n, double f, bool rewrite, __half* hi, __half* lo,
+                      cudaStream_t st) {
+  CHEFSI_REQUIRE(n % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(hi) & 7) == 0 &&
+                     (reinterpret_cast<uintptr_t>(lo) & 7) == 0,
+                 "scaled split: 16-byte aligned block, a multiple of 4 entries");
+  k_split_scaled<<<grid_for(n / 4, 256), 256, 0, st>>>(x, n, (float)f, rewrite ? 1 : 0, hi, lo);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -57,6 +57,11 @@ struct FusedPlan {
   DeviceBuffer<int> rowinfo;      // [n_cells][n_e] x {dof, shared index or -1}
   DeviceBuffer<unsigned char> ncontrib;  // [n_shared]
   DeviceBuffer<__half> hi, lo;    // extended cell-matrix tiles [n_cells][halves][nkb][n_half x 32]
+  // the tiles' diagonal entries (operators with M^{-1/2} folded in): the shifted filter keeps
+  // 2^s (A_II - c / n_I) there (n_I = cell entries of the row's dof, so the shift adds up to
+  // c once per dof); shift = the c the tiles hold now
+  double diag_max = 0.0;          // max |A_II| over the cells
+  double shift = 0.0;
   // operators with constraint rows (M^{-1/2} folded in by the plan, not the operator):
   DeviceBuffer<float> nl_c32;     // M^{-1/2} C in FP32 for the projection
   DeviceBuffer<double> con_wp;    // constraint weights in the folded basis, w d_m / d_s
@@ -194,12 +199,21 @@ struct TcFusedLaunch {
 void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st);
 // dst += scalar (A + C V C^T) x on the tensor cores with the nonlocal apply as the plan's extra
 // K columns: x given by split rows [plan rows][B], the projector rows holding 2^t C^T x
+// (shift != 0: dst += scalar (A - shift I + C V C^T) x, the shift held on the tiles' diagonals;
+// set_tile_shift must have accepted it)
 void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
-                         int64_t ldd, int B, double scalar, cudaStream_t st);
-// the projector rows of a split buffer: (hi, lo)[n_dofs + a P + j] = split(2^t (C^T x)[a][j])
+                         int64_t ldd, int B, double scalar, cudaStream_t st, double shift = 0.0);
+// the projector rows of a split buffer: (hi, lo)[n_dofs + a P + j] = split(2^t (C^T f x)[a][j])
 // from FP32 vectors x [n_dofs][B] (W: n_atoms n_proj B floats of workspace)
 void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W, __half* hi,
-                         __half* lo, cudaStream_t st);
+                         __half* lo, cudaStream_t st, double f = 1.0);
+// the plan's tiles with 2^s (A_II - shift / n_I) on their diagonals; false (tiles unchanged) if
+// the shifted entries would leave FP16's range or the operator has constraint rows
+bool set_tile_shift(chefsi_operator_s* op, double shift, cudaStream_t st);
+// (hi, lo) = split(f x) over a contiguous block of n FP32 entries (n a multiple of 4); with
+// rewrite also x = f x
+void split_scaled_f32(float* x, int64_t n, double f, bool rewrite, __half* hi, __half* lo,
+                      cudaStream_t st);
 // row halves of the tensor-core tiles for n_e nodes (n_half rows each)
 void tc_row_split(int n_e, int* n_half, int* n_halves);
 // (cell, half, K-block) tiles of 2^s A_e over nkb K-blocks (columns past n_e zero)

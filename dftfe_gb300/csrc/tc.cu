@@ -20,7 +20,10 @@
 //     quarter and drain half of the columns each (8 epilogue warps: 1.10x faster than 4).
 //     Measured and rejected: float4 reductions after a lane-quad transpose (1.6x slower),
 //     plain load + store for the rows only one cell touches (more latency on the same
-//     critical path, 1.08x slower), L2 prefetch of the output rows (1.07x slower).
+//     critical path, 1.08x slower), L2 prefetch of the output rows (1.07x slower), rows
+//     staged in shared memory 16 at a time and added by the bulk-copy unit
+//     (cp.reduce.async.bulk .add.f32, one 512-byte row segment per instruction: 1.15x
+//     slower).
 // An mbarrier pipeline of up to 8 stages overlaps the copies, the MMAs and the scatter of the
 // previous unit. Every mbarrier wait is bounded: on expiry the CTA records
 // CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own bulk copies, frees its
@@ -340,7 +343,7 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
         mbar_init(&rows_empty[b], kFinWarps);
       }
     }
-    *abort_flag = 0;
+    *abort_flag = wait_limit_init(args.err);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) tmem_alloc(tmem_slot, args.tmem_cols);
@@ -1223,9 +1226,10 @@ void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __
 // in rows [0, n_dofs) and 2^t C^T x in the projector rows after them; the nonlocal apply runs
 // on the tensor cores as the plan's extra K columns of the cell matrices
 void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
-                         int64_t ldd, int B, double scalar, cudaStream_t st) {
+                         int64_t ldd, int B, double scalar, cudaStream_t st, double shift) {
   const FusedPlan& fp = op->fz;
   CHEFSI_REQUIRE(fp.ready, "folded nonlocal HX: tables not prepared");
+  CHEFSI_REQUIRE(set_tile_shift(op, shift, st), "folded nonlocal HX: shift out of the tiles' range");
   const int n_e = op->n_e;
   const TcPlan p = plan_for(n_e, 2);
   CHEFSI_REQUIRE(B % 8 == 0 && ldd % 4 == 0 && (reinterpret_cast<uintptr_t>(xhi) & 15) == 0 &&
@@ -1278,6 +1282,7 @@ void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
   chefsi_operator_s* op = f.op;
   const FusedPlan& fp = op->fz;
   CHEFSI_REQUIRE(fp.ready, "fused filter step: tables not prepared");
+  CHEFSI_REQUIRE(set_tile_shift(op, 0.0, st), "fused filter step: tiles not restored");
   const int n_e = op->n_e;
   const TcPlan p = plan_for(n_e, 2, true);
   CHEFSI_REQUIRE(f.B % 8 == 0 && (reinterpret_cast<uintptr_t>(f.xhi) & 15) == 0 &&

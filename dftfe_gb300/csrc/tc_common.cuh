@@ -53,14 +53,25 @@ static constexpr uint32_t kWaitTries = 1u << 16; // bound: ~1.3 s
 // the number of tries of every bounded wait of this translation unit's kernels (kWaitTries;
 // lowered by chefsi_set_wait_limits to make waits expire in tests)
 static __device__ uint32_t g_wait_tries = kWaitTries;
-// bounded wait; returns false on expiry (and records the timeout)
+// the abort flag's value at launch (thread 0): 0, or 1 with CHEFSI_ERR_TIMEOUT recorded when the
+// wait limit is zero (every wait of the launch then expires at its first failed try)
+static __device__ __forceinline__ int wait_limit_init(int* err) {
+  if (g_wait_tries != 0) return 0;
+  atomicExch(err, CHEFSI_ERR_TIMEOUT);
+  return 1;
+}
+// bounded wait; returns false on expiry (and records the timeout). The limit is read only
+// after a first try failed: a global load ahead of every wait would sit on the pipeline's
+// critical path (it slowed the filter HX by a fifth).
 static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
                                                  volatile int* abort_flag) {
-  const uint32_t tries = *reinterpret_cast<volatile uint32_t*>(&g_wait_tries);
-  for (uint32_t i = 0; i < tries; ++i) {
-    if (mbar_try_wait_hint(bar, parity, kWaitHintNs)) return true;
+  if (mbar_try_wait_hint(bar, parity, kWaitHintNs)) return true;
+  const uint32_t tries = g_wait_tries;
+  for (uint32_t i = 1; i < tries; ++i) {
     if (*abort_flag) return false;
+    if (mbar_try_wait_hint(bar, parity, kWaitHintNs)) return true;
   }
+  if (*abort_flag) return false;
   atomicExch(err, CHEFSI_ERR_TIMEOUT);
   *abort_flag = 1;
   return false;

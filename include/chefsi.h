@@ -155,12 +155,15 @@ typedef struct {
                                    would not fit the free device memory, > 0 always with
                                    blocks of that many vectors, < 0 never */
   int32_t rr_slab_rows;         /* dofs per row slab of the blocked step (0: about 2^30 / N) */
-  int32_t filter_variant;       /* mixed tensor-core filter: 0 (default) one recurrence pass
-                                   per degree and the HX launch, with the nonlocal apply folded
-                                   into that launch as extra tensor-core K columns; 1 the fused
-                                   step (the recurrence finished in the HX launch, vectors kept
-                                   as FP16 hi + lo rows); -1 the recurrence pass, the HX launch
-                                   and separate nonlocal kernels */
+  int32_t filter_variant;       /* mixed tensor-core filter: 0 (default) one HX launch per
+                                   degree with the Chebyshev shift on the tiles' diagonals and
+                                   the nonlocal apply as extra tensor-core K columns, reducing
+                                   into the older vector's buffer (kept up to a scalar factor:
+                                   no recurrence pass, one split pass of the HX input); 2 a
+                                   recurrence pass per degree and that HX launch without the
+                                   shift; 1 the fused step (the recurrence finished in the HX
+                                   launch, vectors kept as FP16 hi + lo rows); -1 the recurrence
+                                   pass, the HX launch and separate nonlocal kernels */
 } chefsi_params;
 
 /* Bounds of the device-side waits (no counterpart in the reference: a test hook for failure

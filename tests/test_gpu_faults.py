@@ -107,6 +107,7 @@ def test_bounded_device_waits_expire_and_context_stays_usable(C):
     Xt = torch.from_numpy(X.copy()).cuda()
     C.chebyshevFilter(op, Xt, 10, a, b, a0, precision="mixed")
     ref = ora.chebyshev_filter(X, 10, a, b, a0)
-    assert np.abs(Xt.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
+    # the default (shifted) mixed filter's bound (tests/test_gpu_parity.py)
+    assert np.abs(Xt.cpu().numpy() - ref).max() < 4e-5 * np.abs(ref).max()
     w, _ = C.syevd(torch.from_numpy(A.copy()).cuda())
     assert np.abs(w.cpu().numpy() - np.linalg.eigvalsh(A)).max() < 1e-11

@@ -147,6 +147,17 @@ def test_filter_fp64_matches_oracle_and_polynomial(chefsi):
     assert rel(ref, poly) < 1e-10
 
 
+# The default mixed filter carries the Chebyshev shift c on the tensor-core tiles' diagonals.
+# Its per-cell partial sums are then ~ c |x| in size instead of ~ |A x| (small for the smooth,
+# wanted components), and the tensor core's FP32 accumulation, which behaves like
+# round-toward-zero after each K = 16 step (a CPU model with that rounding reproduces the
+# measured errors of both the shifted and the unshifted filter), leaves a bias of ~2^-23 per
+# step relative to those sums: about 1e-5 of max |p(A) X| after 10 to 30 degrees, against 5e-7
+# with the shift applied in FP32 by a recurrence pass. The Ritz values do not see it (they are
+# set by the Rayleigh-Ritz step: the 20-iteration 64,000-dof test holds 1e-6 Ha either way).
+MIXED_SHIFTED_TOL = 4e-5
+
+
 def test_filter_mixed_close_to_fp64(chefsi):
     pr = small_problem(n=2, L=4.0, p=4, wells=2, projectors=True)
     op, ora = gpu_op(chefsi, pr), oracle_op(pr)
@@ -155,7 +166,7 @@ def test_filter_mixed_close_to_fp64(chefsi):
     Xt = torch.from_numpy(X).cuda()
     chefsi.chebyshevFilter(op, Xt, 10, lo + 0.3 * (up - lo), up, lo, precision="mixed")
     ref = ora.chebyshev_filter(X, 10, lo + 0.3 * (up - lo), up, lo)
-    assert rel(Xt.cpu().numpy(), ref) < 5e-6
+    assert rel(Xt.cpu().numpy(), ref) < MIXED_SHIFTED_TOL
 
 
 @pytest.mark.parametrize("N,degenerate", [(1, False), (7, False), (50, False), (130, True),
@@ -260,10 +271,12 @@ def test_hx_golden_fixture(chefsi):
 @pytest.mark.parametrize("p,n,B,proj", [(2, 3, 8, True), (4, 2, 136, True), (6, 2, 136, True),
                                         (5, 2, 256, True), (4, 3, 64, False)])
 def test_filter_variants_match_oracle(chefsi, p, n, B, proj):
-    """The three mixed tensor-core filters against the oracle's FP64 filter (5e-6 relative to
-    max |p(A) X|) and against each other (5e-6):
-    * folded: recurrence pass + HX launch with the nonlocal apply as extra tensor-core K columns
-      of the cell matrices (the projector coefficients 2^t C^T x as extra split rows);
+    """The four mixed tensor-core filters against the oracle's FP64 filter (relative to
+    max |p(A) X|: 5e-6, the shifted default MIXED_SHIFTED_TOL) and against each other:
+    * folded: one HX launch per degree with the shift c on the tiles' diagonals and the
+      nonlocal apply as extra tensor-core K columns of the cell matrices (the projector
+      coefficients 2^t C^T x as extra split rows), reducing into the older vector's buffer;
+    * axpby: recurrence pass + the same HX launch without the shift;
     * fused: the recurrence finished in the HX launch's epilogue (vectors kept as FP16 hi + lo);
     * separate: recurrence pass, HX launch and the SIMT nonlocal kernels.
     Cell sizes with one K-block of nodes (p = 2, several atoms per cell), one row half (p = 4,
@@ -276,7 +289,7 @@ def test_filter_variants_match_oracle(chefsi, p, n, B, proj):
     a, b, a0, m = lo + 0.3 * (up - lo), up, lo, 10
     ref = ora.chebyshev_filter(X, m, a, b, a0)
     out = {}
-    for variant in ("folded", "fused", "separate"):
+    for variant in ("separate", "folded", "axpby", "fused"):
         s = chefsi.ChebyshevOrthogonalizedSubspaceIterationSolver(chefsi.SolverParams(
             chebyshevOrder=m, chebyWfcBlockSize=B, wfcBlockSize=B, filter_variant=variant))
         s.reinitSpectrumBounds(a0, a, b)
@@ -284,9 +297,9 @@ def test_filter_variants_match_oracle(chefsi, p, n, B, proj):
             Xt = torch.from_numpy(X.copy()).cuda()
             s.solveNoRR(op, Xt, 1, useMixedPrec=True)
         out[variant] = Xt.cpu().numpy()
-        assert rel(out[variant], ref) < 5e-6, variant
-    assert rel(out["folded"], out["separate"]) < 5e-6
-    assert rel(out["fused"], out["separate"]) < 5e-6
+        tol = MIXED_SHIFTED_TOL if variant == "folded" else 5e-6
+        assert rel(out[variant], ref) < tol, variant
+        assert rel(out[variant], out.get("separate", ref)) < tol + 5e-6, variant
 
 
 def _unfolded_operators(chefsi, pr, projectors):
