@@ -141,39 +141,44 @@ void cheb_filter(T* X, T* Y, int64_t M, int B, int m, double a, double b, double
   if (y != X) copy_block<T, T>(y, B, X, B, M, B, 1.0, st);
 }
 
+// rows of the filter's FP32 work blocks: the vectors, then (shifted filter) the projector rows
+int64_t filter_rows(chefsi_operator_s* op) {
+  return op->n_dofs + (op->is_complex ? 0 : (int64_t)op->n_atoms * op->n_proj);
+}
+
 // Mixed Chebyshev filter with the shift on the tensor-core tiles. In the sigma form every degree
 // is x_j = alpha1_j (A - c) x_{j-1} + alpha2_j x_{j-2} with the same c, so the plan's tiles carry
 // 2^s (A_II - c / n_I) on their diagonals for the whole call and each degree is one HX launch
 // reducing into the buffer of x_{j-2}. Each buffer holds its vector up to a factor kept here
 // (vector = factor * buffer): the update alpha2 x_{j-2} only changes the factor, so no
 // recurrence pass runs (the reference's combinedDeviceKernel,
-// linearAlgebraOperationsDevice.cc:37-104, reads and writes both vectors every degree). Per
-// degree the buffer of x_{j-1} is read once more to write the FP16 split of f x_{j-1} (f the
-// power of two nearest its factor, which keeps the split at the vector's own magnitude) and the
-// projector rows. Returns false (nothing done) when the shifted diagonals would leave FP16's
-// range.
+// linearAlgebraOperationsDevice.cc:37-104, reads and writes both vectors every degree), and
+// no split pass either: the launch gathers x_{j-1} as FP32 rows and its producer warps write
+// the FP16 split of f x_{j-1} (f the power of two nearest its factor, which keeps the split at
+// the vector's own magnitude). Besides the launch, a degree only runs the projection C^T x_{j-1}
+// into the buffer's rows past n_dofs. X and Y hold filter_rows(op) rows. Returns false
+// (nothing done) when the shifted diagonals would leave FP16's range.
 bool cheb_filter_shifted(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
                          int B, int m, double a, double b, double a0, cudaStream_t st) {
   prepare_fused_plan(op, st);
   const double e = (b - a) / 2.0, c = (b + a) / 2.0;
   if (!set_tile_shift(op, c, st)) return false;
-  const FusedPlan& fp = op->fz;
-  __half* hi = s->xs_hi.ensure((size_t)fp.rows * B);
-  __half* lo = s->xs_lo.ensure((size_t)fp.rows * B);
-  float* W = op->n_atoms ? s->fzw.W.ensure((size_t)op->n_atoms * op->n_proj * B) : nullptr;
   const int64_t n = M * (int64_t)B;
-  // out += scalar (A - c) v for the vector v = s_in in: the launch multiplies the split of f in,
-  // so its scalar is scalar s_in / f; with a factor beyond 2^+-64 the input buffer is rewritten
-  // as f in (its factor then divides by f)
+  // out += scalar (A - c) v for the vector v = s_in in: the launch's producer warps split f in
+  // (f the power of two nearest s_in: the split sees the vector's own magnitude), so its scalar
+  // is scalar s_in / f; the projection writes C^T in into the buffer's rows past n_dofs. A
+  // factor beyond 2^+-64 is first moved into the buffer (one scaling pass; rare).
   auto apply = [&](float* in, double& s_in, float* out, double scalar) {
-    const double f = std::ldexp(1.0, (int)std::lround(std::log2(std::fabs(s_in))));
-    const bool rewrite = std::fabs(std::log2(f)) > 64.0;
-    split_scaled_f32(in, n, f, rewrite, hi, lo, st);
+    double f = std::ldexp(1.0, (int)std::lround(std::log2(std::fabs(s_in))));
+    if (std::fabs(std::log2(f)) > 64.0) {
+      scale_block<float>(in, B, M, B, f, st);
+      s_in /= f;
+      f = 1.0;
+    }
     s->hx_mark(st);
-    nl_project_to_split(op, in, B, W, hi, lo, st, rewrite ? 1.0 : f);
-    hx_tc_folded_launch(op, hi, lo, out, B, B, scalar * s_in / f, st, c);
+    nl_project_f32(op, in, B, in + n, B, st);
+    hx_tc_folded_f32_launch(op, in, out, B, B, scalar * s_in / f, f, st, c);
     s->hx_mark(st);
-    if (rewrite) s_in /= f;
   };
   double sigma = e / (a0 - c);
   const double sigma1 = sigma, gamma = 2.0 / sigma1;
@@ -288,8 +293,9 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
   CHEFSI_CUDA(cudaStreamSynchronize(st));
   double scale = 1.0;
   if (amax > 0.0 && std::isfinite(amax)) scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
-  float* Xb = s->Xb32.ensure((size_t)M * B);
-  float* Yb = s->Yb32.ensure((size_t)M * B);
+  // (rows past n_dofs: the shifted filter's projector rows)
+  float* Xb = s->Xb32.ensure((size_t)filter_rows(op) * B);
+  float* Yb = s->Yb32.ensure((size_t)filter_rows(op) * B);
   copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
   if (prec == CHEFSI_PREC_MIXED && (tc_split_usable(op, B) || constrained_tc_usable(op, B))) {
     cheb_filter_tc(s, op, Xb, Yb, M, B, m, a, b, a0, st);
@@ -328,8 +334,8 @@ void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m
       double scale = 1.0;
       if (amax > 0.0 && std::isfinite(amax))
         scale = std::ldexp(1.0, 8 - (int)std::ceil(std::log2(amax)));
-      float* xr = s->Xb32.ensure((size_t)2 * M * B);
-      float* yr = s->Yb32.ensure((size_t)2 * M * B);
+      float* xr = s->Xb32.ensure((size_t)filter_rows(rv) * B);
+      float* yr = s->Yb32.ensure((size_t)filter_rows(rv) * B);
       complex_to_real_rows(Xc + j0, N, M, B, scale, xr, st);
       if (prec == CHEFSI_PREC_MIXED && tc_split_usable(rv, B)) {
         cheb_filter_tc(s, rv, xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0, st);

@@ -203,6 +203,10 @@ void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st);
 // set_tile_shift must have accepted it)
 void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
                          int64_t ldd, int B, double scalar, cudaStream_t st, double shift = 0.0);
+// the same launch with x given as FP32 rows x32 [plan rows][B] (the projector rows holding
+// C^T x unscaled), split by the kernel's producer warps after scaling by xf
+void hx_tc_folded_f32_launch(chefsi_operator_s* op, const float* x32, float* dst, int64_t ldd,
+                             int B, double scalar, double xf, cudaStream_t st, double shift);
 // the projector rows of a split buffer: (hi, lo)[n_dofs + a P + j] = split(2^t (C^T f x)[a][j])
 // from FP32 vectors x [n_dofs][B] (W: n_atoms n_proj B floats of workspace)
 void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W, __half* hi,

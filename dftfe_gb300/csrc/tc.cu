@@ -23,7 +23,8 @@
 //     critical path, 1.08x slower), L2 prefetch of the output rows (1.07x slower), rows
 //     staged in shared memory 16 at a time and added by the bulk-copy unit
 //     (cp.reduce.async.bulk .add.f32, one 512-byte row segment per instruction: 1.15x
-//     slower).
+//     slower), and loading the rows of one cell entry a 16-row group ahead and storing them
+//     instead of reducing (1.6x slower).
 // An mbarrier pipeline of up to 8 stages overlaps the copies, the MMAs and the scatter of the
 // previous unit. Every mbarrier wait is bounded: on expiry the CTA records
 // CHEFSI_ERR_TIMEOUT in a device flag, waits (bounded) for its own bulk copies, frees its
@@ -122,6 +123,13 @@ struct TcArgs {
   int stages;      // cell-matrix ring depth
   int xstages;     // X ring depth
   int lookahead;   // K-blocks of X copies in flight per producer thread
+  // F32X launches: X given as FP32 rows x32 [rows][ldx] (rows >= w_row: the projector
+  // coefficients), split into FP16 hi + lo by the producer warps after scaling by xf (dof rows)
+  // or wf (projector rows); sstages FP32 staging slots per producer thread ring
+  const float* x32;
+  float xf, wf;
+  int64_t w_row;
+  int sstages;
   int* err;
   TcFused fz;      // FUSED launches only
 };
@@ -136,20 +144,23 @@ struct Layout {
   int xstage;   // ns X tiles
   int astage;   // ns matrix tiles
   int aoff;     // start of the matrix ring
+  int soff;     // start of the FP32 staging ring (F32X: 32 nodes x 128 vectors a slot)
   int bars;     // barrier block
   int offs;     // epilogue row offsets: 2 x 256 int64 (one table per accumulator)
   int queue;    // fused step: two queues of finished shared rows (count + 256 entries each)
   int total;
 };
 constexpr int kQueueStride = 264;  // ints per queue (count, 256 entries, padding)
+constexpr int kStageF32 = 32 * 128 * 4;  // bytes of one FP32 staging slot
 __host__ __device__ inline Layout make_layout(int n_half, int stages, int xstages, int ns,
-                                              bool fused = false) {
+                                              bool fused = false, int sstages = 0) {
   Layout L;
   L.a_tile = ((n_half * kRowBytes + 1023) / 1024) * 1024;
   L.xstage = ns * kXTile;
   L.astage = ns * L.a_tile;
   L.aoff = xstages * L.xstage;
-  L.bars = L.aoff + stages * L.astage;
+  L.soff = L.aoff + stages * L.astage;
+  L.bars = L.soff + sstages * kStageF32;
   L.offs = L.bars + 8 * (2 * stages + 2 * xstages + 12);
   L.queue = L.offs + 2 * 256 * 8;
   L.total = L.queue + (fused ? 2 * kQueueStride * 4 : 0);
@@ -293,14 +304,16 @@ constexpr int kChunkCols = 96;
 // FUSED: the fused filter step (see TcFused): the K side gathers through the extended map
 //        (the cell's nodes, then its projector coefficients W), the epilogue finishes the
 //        recurrence.
-template <int NS, bool KCHUNK, bool DENS = false, bool FUSED = false>
+// F32X: the X rows come as FP32 (args.x32), copied into a per-thread staging ring and split by
+//       the producer warps themselves (no separate split pass over the vectors).
+template <int NS, bool KCHUNK, bool DENS = false, bool FUSED = false, bool F32X = false>
 __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     cell_hx_tc_kernel(TcArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int S = args.stages, SX = args.xstages;
-  const Layout L = make_layout(args.n_half, S, SX, NS, FUSED);
+  const Layout L = make_layout(args.n_half, S, SX, NS, FUSED, F32X ? args.sstages : 0);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* tma_full = bars;            // [S] cell-matrix tile bytes landed
   uint64_t* a_empty = bars + S;         // [S] MMA finished reading the matrix stage
@@ -481,11 +494,18 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     // the hi and lo rows of the K-block's nodes 8 j + t / 16 (j = 0..3). Element (vector m,
     // node k) of the tile sits in atom (m / 64, k / 8), row k % 8, 16-byte chunk
     // (m % 64) / 8 XOR k % 8.
+    // F32X: the thread's FP32 pieces of a K-block (4 rows x 8 vectors, 32 B each) go to
+    // its staging slot, row r at r x 512 B, vectors 8 cc..8 cc + 7 as 16-byte chunks
+    // 2 cc + (h XOR (cc / 4) % 2) (the XOR spreads a warp's read-back over all banks); the
+    // thread splits its own pieces into the tile once they landed, so staging needs no barrier.
     const int t = threadIdx.x - 64;
     const int cc = t & 15, rsub = t >> 4;
     const int mi = cc >> 3, c = cc & 7;
     const uint32_t dst_base = mi * kXAtomM + rsub * 128 + ((uint32_t)(c ^ rsub) << 4);
-    const int D = args.lookahead;
+    const int D = F32X ? args.sstages - 1 : args.lookahead;
+    const uint32_t sw = (uint32_t)(cc >> 2) & 1u;
+    const uint32_t s_base = smem_u32(smem + L.soff) + (uint32_t)rsub * 512u + (uint32_t)cc * 32u;
+    uint32_t wmask = 0;   // F32X: bit 4 slot + j = row j of the slot is a projector row
     // cursor over this CTA's K-blocks (no per-block divisions): unit it, K-block kb
     int64_t c_it = 0;
     int c_kb = 0;
@@ -524,6 +544,27 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     auto issue = [&]() -> bool {
       const Pending cur = nxt;
       load_next();
+      if (F32X) {
+        // into staging slot s_iss (free: its previous block was split by this thread)
+        if (cur.valid) {
+          const TcProblem& pr = args.prob[cur.p];
+          const bool vok = cur.vb < pr.B;
+          const uint32_t st = s_base + (uint32_t)s_iss * kStageF32;
+          wmask &= ~(15u << (4 * s_iss));
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const bool ok = vok && cur.rows[j] >= 0;
+            const int64_t off = ok ? (int64_t)cur.rows[j] * pr.ldx + cur.vb : 0;
+            const uint32_t d = st + (uint32_t)j * 8u * 512u;
+            cp_async16(d + (sw << 4), args.x32 + off, ok);
+            cp_async16(d + ((sw ^ 1u) << 4), args.x32 + off + 4, ok);
+            if (ok && cur.rows[j] >= args.w_row) wmask |= 1u << (4 * s_iss + j);
+          }
+        }
+        cp_async_commit();
+        if (++s_iss == D + 1) s_iss = 0;
+        return true;
+      }
       if (cur.valid) {
         // warp-uniform decision: the warp arrives on x_full as one
         if (!__all_sync(0xffffffffu, mbar_wait(&x_empty[s_iss], (r_iss & 1) ^ 1, args.err, abort_flag)))
@@ -549,13 +590,54 @@ __global__ void __launch_bounds__(FUSED ? kThreadsFused : kThreads3, 1)
     bool ok = true;
     for (int i = 0; i < D && ok; ++i) ok = issue();
     int s_arr = 0;
+    uint32_t r_arr = 0;
+    int s_cv = 0;   // F32X: staging slot of block g
     for (int64_t g = 0; g < my_blocks && ok; ++g) {
       ok = issue();
       cp_async_wait_n(D);                      // this thread's copies of block g landed
+      if (F32X) {
+        // split the staged block into X stage s_arr once the MMA has released it
+        if (!__all_sync(0xffffffffu, mbar_wait(&x_empty[s_arr], (r_arr & 1) ^ 1, args.err, abort_flag))) {
+          ok = false;
+          break;
+        }
+        const uint32_t sb = s_base + (uint32_t)s_cv * kStageF32;
+        const uint32_t tb = smem_u32(smem + s_arr * L.xstage) + dst_base;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float f = (wmask >> (4 * s_cv + j)) & 1u ? args.wf : args.xf;
+          float v[8];
+          asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                       : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+                       : "r"(sb + (uint32_t)j * 8u * 512u + (sw << 4)));
+          asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                       : "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                       : "r"(sb + (uint32_t)j * 8u * 512u + ((sw ^ 1u) << 4)));
+          // the split of split_f32, two values per conversion
+          uint32_t h[4], l[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float a0 = f * v[2 * i], a1 = f * v[2 * i + 1];
+            const __half2 h2 = __floats2half2_rn(a0, a1);
+            const float2 hf = __half22float2(h2);
+            const __half2 l2 = __floats2half2_rn(a0 - hf.x, a1 - hf.y);
+            h[i] = *reinterpret_cast<const uint32_t*>(&h2);
+            l[i] = *reinterpret_cast<const uint32_t*>(&l2);
+          }
+          const uint32_t d = tb + (uint32_t)j * kXGroupK;
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d), "r"(h[0]), "r"(h[1]),
+                       "r"(h[2]), "r"(h[3])
+                       : "memory");
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(d + kXTile), "r"(l[0]),
+                       "r"(l[1]), "r"(l[2]), "r"(l[3])
+                       : "memory");
+        }
+        if (++s_cv == D + 1) s_cv = 0;
+      }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&x_full[s_arr]);
-      if (++s_arr == SX) s_arr = 0;
+      if (++s_arr == SX) s_arr = 0, ++r_arr;
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
   } else if (FUSED && warp >= 6 + kEpiWarps) {
@@ -1275,6 +1357,71 @@ void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half*
   CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
   kernel<<<(unsigned)grid, kThreads3, p.smem, st>>>(a);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+// dst += scalar (A - shift I + C V C^T) (xf x) with x given as FP32 rows x32 [plan rows][B]
+// (rows [0, n_dofs) the vectors, the projector rows after them C^T x unscaled): the producer
+// warps split xf x (and 2^t xf C^T x) into FP16 hi + lo themselves
+void hx_tc_folded_f32_launch(chefsi_operator_s* op, const float* x32, float* dst, int64_t ldd,
+                             int B, double scalar, double xf, cudaStream_t st, double shift) {
+  const FusedPlan& fp = op->fz;
+  CHEFSI_REQUIRE(fp.ready, "folded nonlocal HX: tables not prepared");
+  CHEFSI_REQUIRE(set_tile_shift(op, shift, st), "folded nonlocal HX: shift out of the tiles' range");
+  const int n_e = op->n_e;
+  TcPlan p = plan_for(n_e, 2);
+  CHEFSI_REQUIRE(B % 8 == 0 && ldd % 4 == 0 && (reinterpret_cast<uintptr_t>(x32) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(dst) & 15) == 0,
+                 "folded nonlocal HX: 16-byte aligned rows, B a multiple of 8");
+  // X ring of split tiles (at least 3 stages) and the FP32 staging ring (at most 8 slots: its
+  // depth - 1 K-blocks of copies in flight per producer thread)
+  int xs = 4, ss = 7;
+  auto total = [&] { return make_layout(p.n_half, p.stages, xs, 2, false, ss).total + 1024; };
+  while (ss > 4 && total() > 220 * 1024) --ss;
+  while (xs > 3 && total() > 220 * 1024) --xs;
+  while (ss > 3 && total() > 220 * 1024) --ss;
+  CHEFSI_REQUIRE(total() <= 227 * 1024, "folded nonlocal HX: shared memory");
+  TcArgs a{};
+  a.n_probs = 1;
+  a.n_e = n_e;
+  a.n_rows = n_e;
+  a.nkb = fp.nkb;
+  a.n_half = p.n_half;
+  a.n_halves = p.n_halves;
+  a.buf_stride = p.buf_stride;
+  a.tmem_cols = p.tmem_cols;
+  a.stages = p.stages;
+  a.xstages = xs;
+  a.sstages = ss;
+  a.lookahead = ss - 1;
+  a.x32 = x32;
+  a.xf = (float)xf;
+  a.wf = (float)(xf * fp.wscale);
+  a.w_row = op->n_dofs;
+  if (!op->tc_err.ptr) {
+    op->tc_err.reset(1);
+    CHEFSI_CUDA(cudaMemsetAsync(op->tc_err.ptr, 0, sizeof(int), st));
+  }
+  a.err = op->tc_err.ptr;
+  TcProblem& pr = a.prob[0];
+  pr.dst = dst;
+  pr.map = op->map.ptr;
+  pr.ahi = fp.hi.ptr;
+  pr.alo = fp.lo.ptr;
+  pr.alo3 = fp.lo.ptr;
+  pr.ldx = B;
+  pr.ldd = ldd;
+  pr.B = B;
+  pr.n_chunks = (B + kVec - 1) / kVec;
+  pr.out_scale = (float)(scalar / fp.scale);
+  pr.pair_begin = 0;
+  a.n_pairs = (int64_t)op->n_cells * pr.n_chunks;
+  a.fz.mapk = fp.mapk.ptr;
+  a.fz.kstride = fp.kstride;
+  auto kernel = cell_hx_tc_kernel<2, false, false, false, true>;
+  CHEFSI_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  const int64_t grid = std::min<int64_t>(device_sms(), a.n_pairs);
+  kernel<<<(unsigned)grid, kThreads3, total(), st>>>(a);
   CHEFSI_CHECK_LAUNCH();
 }
 
