@@ -89,8 +89,10 @@ class ClockSampler:
 # (ncu captures summarised in profiles/): the separate-pass HX kernel on the full workload, and
 # the fused step's kernel (None until captured)
 TC_TRAFFIC_BYTES = {("mixed", "separate"): 20.33e9 + 8.20e9,
-                    # mixed_small capture (1.302 + 0.470 GB) scaled by 8000 / 512 cells
-                    ("mixed", "folded"): (1.302e9 + 0.470e9) * 8000 / 512}
+                    # mixed_small captures scaled by 8000 / 512 cells: the shifted step with
+                    # FP32 input (1.310 + 0.479 GB), the unshifted kernel (1.302 + 0.470 GB)
+                    ("mixed", "folded"): (1.310375e9 + 0.478750e9) * 8000 / 512,
+                    ("mixed", "axpby"): (1.302e9 + 0.470e9) * 8000 / 512}
 
 
 def hx_algorithmic(pr, B, s_h=4, s_x=4, fused=False):
@@ -503,8 +505,8 @@ def run_ours(args):
                                 "folded": "cell_hx_tc_kernel with the shift on the tiles' "
                                           "diagonals and the nonlocal apply as extra K columns "
                                           "+ nonlocal projection: one filter step x_j = a (A - c) "
-                                          "x_{j-1} + b x_{j-2} reduced into x_{j-2}'s buffer "
-                                          "(the split pass of the next input not included)",
+                                          "x_{j-1} + b x_{j-2} reduced into x_{j-2}'s buffer, "
+                                          "the FP32 input split by the launch's producer warps",
                                 "axpby": "cell_hx_tc_kernel with the nonlocal apply as extra K "
                                          "columns + nonlocal projection (filter HX; recurrence "
                                          "pass not included)",
