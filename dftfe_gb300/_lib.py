@@ -40,7 +40,7 @@ EXPORTS = [
     "chefsi_solve", "chefsi_solve_spectrum_split", "chefsi_solve_batched", "chefsi_solve_no_rr", "chefsi_chebyshev_order", "chefsi_gemm",
     "chefsi_axpby", "chefsi_convert_block", "chefsi_density", "chefsi_assemble_cell_hamiltonians",
     "chefsi_assemble_cell_hamiltonians_bloch", "chefsi_assemble_cell_hamiltonians_gga",
-    "chefsi_assemble_cell_hamiltonians_bloch_gga",
+    "chefsi_assemble_cell_hamiltonians_bloch_gga", "chefsi_assemble_cell_hamiltonians_geometry",
     "chefsi_operator_update_cell_matrices",
     "chefsi_cell_outer_accumulate", "chefsi_cell_quadrature_contract", "chefsi_set_wait_limits",
 ]
@@ -123,6 +123,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "chefsi_assemble_cell_hamiltonians": ([i32, i32, i32, vp, vp, vp, vp, vp], ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians_gga": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp],
                                                   ctypes.c_int),
+        "chefsi_assemble_cell_hamiltonians_geometry": ([i32, i32, i32, vp, vp, vp, vp, vp, vp],
+                                                       ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians_bloch_gga": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, i32,
                                                          vp, vp, vp], ctypes.c_int),
         "chefsi_assemble_cell_hamiltonians_bloch": ([i32, i32, i32, vp, vp, vp, vp, vp, i32, vp, vp,

@@ -311,6 +311,25 @@ def assemble_cell_hamiltonians(shape: torch.Tensor, stiffness: torch.Tensor,
     return out
 
 
+def assemble_cell_hamiltonians_geometry(shape: torch.Tensor, shape_grad_ref: torch.Tensor,
+                                        jacobian_factor: torch.Tensor,
+                                        v_jxw: torch.Tensor) -> torch.Tensor:
+    """Cell Hamiltonians [n_cells, n_e, n_e] of cells of any shape on the GPU: the per-cell
+    stiffness of FEBasisOperations::computeCellStiffnessMatrix from the reference-cell gradients
+    shape_grad_ref [3, n_q, n_e] and the Jacobian factors jacobian_factor [n_cells, n_q, 3, 3]
+    (J^-1 J^-T JxW), plus the LDA potential term v_jxw [n_cells, n_q]."""
+    nc, nq = v_jxw.shape
+    ne = shape.shape[1]
+    if tuple(jacobian_factor.shape) != (nc, nq, 3, 3) or tuple(shape_grad_ref.shape) != (3, nq, ne):
+        raise ValueError("jacobian_factor must be [n_cells, n_q, 3, 3], shape_grad_ref [3, n_q, n_e]")
+    F = jacobian_factor.contiguous()
+    out = torch.empty((nc, ne, ne), dtype=torch.float64, device=v_jxw.device)
+    check(_lib.load().chefsi_assemble_cell_hamiltonians_geometry(
+        nc, ne, nq, _ptr(shape), _ptr(shape_grad_ref), _ptr(F), _ptr(v_jxw), _ptr(out),
+        _stream()))
+    return out
+
+
 def assemble_cell_hamiltonians_gga(shape: torch.Tensor, shape_grad: torch.Tensor,
                                    stiffness: torch.Tensor, v_jxw: torch.Tensor,
                                    gga_jxw: torch.Tensor) -> torch.Tensor:

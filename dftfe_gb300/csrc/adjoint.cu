@@ -3,6 +3,9 @@
 //   * k_assemble_cells: H_c = 1/2 K + N^T diag(v_c) N, the formula of hamMatrixKernelLDA
 //     (src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:61-115), written as a
 //     per-cell product over quadrature points;
+//   * k_assemble_geom: the same for cells of any shape, the stiffness formed per cell from the
+//     reference-cell gradients and the per-point Jacobian factors J^-1 J^-T JxW
+//     (FEBasisOperations::computeCellStiffnessMatrix, utils/FEBasisOperations.cc:1133-1300);
 //   * k_cell_outer: G_c[I][J] += alpha sum_b (D u)[map I][b] (D v)[map J][b] -- the
 //     contraction of an adjoint pair (u = adjoint block, v = state block) with dA/dH_c, where
 //     A = D H D and D = M^{-1/2};
@@ -220,6 +223,74 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Cells of any shape: out[c][I][J] = sum_q ( 0.5 sum_ij dN[i][q][I] F[c][q][i][j] dN[j][q][J]
+// + v[c][q] N[q][I] N[q][J] ), dN the reference-cell gradients and F the per-point Jacobian
+// factor J^-1 J^-T JxW (symmetric). Per 16 quadrature points the cell's A side
+// (v N_I, 0.5 sum_i dN_i F_ij) and the shared B side (N_J, dN_j) go through shared memory.
+__global__ void __launch_bounds__(256)
+    k_assemble_geom(int n_cells, int n_e, int n_q, const double* __restrict__ N,
+                    const double* __restrict__ dN, const double* __restrict__ F,
+                    const double* __restrict__ v, double* __restrict__ out, int nt) {
+  __shared__ double A[4][16][T + 1];
+  __shared__ double Bt[4][16][T + 1];
+  const int64_t blk = blockIdx.x;
+  const int tj = (int)(blk % nt), ti = (int)((blk / nt) % nt);
+  const int c = (int)(blk / ((int64_t)nt * nt));
+  const int i0 = ti * T, j0 = tj * T;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 2x2 per thread
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  const double* vc = v + (int64_t)c * n_q;
+  const double* Fc = F + (int64_t)c * n_q * 9;
+  const int64_t qn = (int64_t)n_q * n_e;
+  for (int q0 = 0; q0 < n_q; q0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * T; idx += 256) {
+      const int qq = idx / T, k = idx % T;
+      const int q = q0 + qq;
+      const bool okq = q < n_q;
+      const bool oki = okq && i0 + k < n_e, okj = okq && j0 + k < n_e;
+      if (oki) {
+        const int64_t iI = (int64_t)q * n_e + i0 + k;
+        const double d0 = dN[iI], d1 = dN[qn + iI], d2 = dN[2 * qn + iI];
+        const double* f = Fc + 9 * q;
+        A[0][qq][k] = N[iI] * vc[q];
+        A[1][qq][k] = 0.5 * (d0 * f[0] + d1 * f[3] + d2 * f[6]);
+        A[2][qq][k] = 0.5 * (d0 * f[1] + d1 * f[4] + d2 * f[7]);
+        A[3][qq][k] = 0.5 * (d0 * f[2] + d1 * f[5] + d2 * f[8]);
+      } else {
+        A[0][qq][k] = A[1][qq][k] = A[2][qq][k] = A[3][qq][k] = 0.0;
+      }
+      if (okj) {
+        const int64_t iJ = (int64_t)q * n_e + j0 + k;
+        Bt[0][qq][k] = N[iJ];
+        Bt[1][qq][k] = dN[iJ];
+        Bt[2][qq][k] = dN[qn + iJ];
+        Bt[3][qq][k] = dN[2 * qn + iJ];
+      } else {
+        Bt[0][qq][k] = Bt[1][qq][k] = Bt[2][qq][k] = Bt[3][qq][k] = 0.0;
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int qq = 0; qq < 16; ++qq)
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int ii = ty + 16 * r, jj = tx + 16 * s;
+          double t = acc[r][s];
+#pragma unroll
+          for (int f = 0; f < 4; ++f) t = fma(A[f][qq][ii], Bt[f][qq][jj], t);
+          acc[r][s] = t;
+        }
+    __syncthreads();
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int s = 0; s < 2; ++s) {
+      const int I = i0 + ty + 16 * r, J = j0 + tx + 16 * s;
+      if (I < n_e && J < n_e) out[((int64_t)c * n_e + I) * n_e + J] = acc[r][s];
+    }
+}
+
 // G[c][I][J] += alpha * sum_b d[gI] u[gI][b] d[gJ] w[gJ][b], g = map[c][.]
 __global__ void __launch_bounds__(256)
     k_cell_outer(const int* __restrict__ map, int n_e, const double* __restrict__ d,
@@ -308,6 +379,15 @@ void assemble_cells_bloch(int n_cells, int n_e, int n_q, const double* N, const 
     k_assemble_bloch<false><<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, K, v, w,
                                                             nullptr, n_k, kpts,
                                                             reinterpret_cast<double2*>(out), nt);
+  CHEFSI_CHECK_LAUNCH();
+}
+
+void assemble_cells_geometry(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                             const double* F, const double* v, double* out, cudaStream_t st) {
+  const int nt = (n_e + T - 1) / T;
+  const int64_t blocks = (int64_t)n_cells * nt * nt;
+  CHEFSI_REQUIRE(blocks < (1ll << 31), "assembly grid too large");
+  k_assemble_geom<<<(unsigned)blocks, 256, 0, st>>>(n_cells, n_e, n_q, N, dN, F, v, out, nt);
   CHEFSI_CHECK_LAUNCH();
 }
 

@@ -1740,6 +1740,20 @@ int chefsi_assemble_cell_hamiltonians_gga(int32_t n_cells, int32_t nodes_per_cel
   CHEFSI_API_END
 }
 
+int chefsi_assemble_cell_hamiltonians_geometry(int32_t n_cells, int32_t nodes_per_cell,
+                                               int32_t n_q, const double* shape,
+                                               const double* shape_grad_ref,
+                                               const double* jacobian_factor,
+                                               const double* v_jxw, double* out, void* stream) {
+  CHEFSI_API_BEGIN
+  CHEFSI_REQUIRE(shape && shape_grad_ref && jacobian_factor && v_jxw && out && n_cells > 0 &&
+                     nodes_per_cell > 0 && n_q > 0,
+                 "bad argument");
+  assemble_cells_geometry(n_cells, nodes_per_cell, n_q, shape, shape_grad_ref, jacobian_factor,
+                          v_jxw, out, as_stream(stream));
+  CHEFSI_API_END
+}
+
 int chefsi_assemble_cell_hamiltonians_bloch(int32_t n_cells, int32_t nodes_per_cell, int32_t n_q,
                                             const double* shape, const double* shape_grad,
                                             const double* stiffness, const double* v_jxw,

@@ -365,6 +365,9 @@ void dot_f64(const double* x, const double* y, int64_t n, double* out_dev, cudaS
 // adjoint / assembly building blocks (adjoint.cu)
 void assemble_cells(int n_cells, int n_e, int n_q, const double* N, const double* K,
                     const double* v, double* out, cudaStream_t st);
+// cells of any shape: 0.5 sum_q dN^T F_cq dN (F = J^-1 J^-T JxW per point) + N^T diag(v_c) N
+void assemble_cells_geometry(int n_cells, int n_e, int n_q, const double* N, const double* dN,
+                             const double* F, const double* v, double* out, cudaStream_t st);
 void assemble_cells_gga(int n_cells, int n_e, int n_q, const double* N, const double* dN,
                         const double* K, const double* v, const double* g, double* out,
                         cudaStream_t st);

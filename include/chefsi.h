@@ -312,6 +312,21 @@ int chefsi_assemble_cell_hamiltonians(int32_t n_cells, int32_t nodes_per_cell, i
                                       const double* shape, const double* stiffness,
                                       const double* v_jxw, double* out, void* stream);
 
+/* Cell Hamiltonians of cells of any shape (the per-cell stiffness of
+   FEBasisOperations::computeCellStiffnessMatrix, utils/FEBasisOperations.cc:1133-1300, with the
+   potential term of hamMatrixKernelLDA):
+   out[c][I][J] = sum_q ( 0.5 sum_ij shape_grad_ref[i][q][I] jacobian_factor[c][q][i][j]
+                          shape_grad_ref[j][q][J] + v_jxw[c][q] shape[q][I] shape[q][J] )
+   shape [n_q][n_e], shape_grad_ref [3][n_q][n_e] the gradients on the reference cell,
+   jacobian_factor [n_cells][n_q][3][3] = sum_k invJ[i][k] invJ[j][k] JxW (invJ[i][k] =
+   d xi_i / d x_k, the reference's jacobianFactor), v_jxw [n_cells][n_q], out
+   [n_cells][n_e][n_e]; device pointers. */
+int chefsi_assemble_cell_hamiltonians_geometry(int32_t n_cells, int32_t nodes_per_cell,
+                                               int32_t n_q, const double* shape,
+                                               const double* shape_grad_ref,
+                                               const double* jacobian_factor,
+                                               const double* v_jxw, double* out, void* stream);
+
 /* GGA cell Hamiltonians, real (hamMatrixKernelGGAMemOpt,
    src/dftOperator/hamiltonianMatrixCalculatorFlattenedDevice.cc:283-456):
    out[c][I][J] = 0.5 stiffness[I][J] + sum_q ( v_jxw[c][q] N_qI N_qJ

@@ -173,6 +173,26 @@ def cell_hamiltonians_direct(K: np.ndarray, N: np.ndarray, vjxw: np.ndarray) -> 
     return H
 
 
+def cell_hamiltonians_geometry_direct(N: np.ndarray, dNref: np.ndarray, F: np.ndarray,
+                                      vjxw: np.ndarray) -> np.ndarray:
+    """Cell matrices of cells of any shape by the q-loop: the per-cell stiffness of
+    FEBasisOperations::computeCellStiffnessMatrix (utils/FEBasisOperations.cc:1133-1300:
+    jacobianFactor = J^-1 J^-T JxW per point, then gradients^T jacobianFactor gradients) halved,
+    plus the LDA potential term of hamMatrixKernelLDA
+    (hamiltonianMatrixCalculatorFlattenedDevice.cc:61-115). dNref [3][n_q][n_e] reference-cell
+    gradients, F [n_cells][n_q][3][3]; returns [n_cells, n_e, n_e]."""
+    nc, nq = vjxw.shape
+    ne = N.shape[1]
+    out = np.empty((nc, ne, ne))
+    for c in range(nc):
+        val = np.zeros((ne, ne))
+        for q in range(nq):
+            g = dNref[:, q, :]                       # [3][n_e]
+            val += 0.5 * g.T @ F[c, q] @ g + vjxw[c, q] * np.outer(N[q], N[q])
+        out[c] = val
+    return out
+
+
 def cell_hamiltonians_gga_direct(K: np.ndarray, N: np.ndarray, dN: np.ndarray, vjxw: np.ndarray,
                                  gjxw: np.ndarray) -> np.ndarray:
     """Real GGA cell matrices by the q-loop of hamMatrixKernelGGAMemOpt

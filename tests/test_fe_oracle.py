@@ -284,3 +284,47 @@ def test_oracle_bloch_gga_is_bloch_lda_plus_the_real_gga_terms():
     real_term = orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, g) - \
         orc.cell_hamiltonians_gga_direct(K, N, dN, vjxw, np.zeros_like(g))
     assert np.abs(gga - lda - real_term).max() < 1e-12 * np.abs(gga).max()
+
+
+def _box_geometry(mesh, scales):
+    """Reference-cell gradients and Jacobian factors of the periodic mesh stretched by
+    diag(scales): every cell is h diag(scales) times the reference cube."""
+    from tests.helpers import shape_tables
+    N, dN, w3 = shape_tables(mesh)
+    h = mesh.h
+    dNref = dN * h                                   # d/dxi on [0, 1]^3
+    inv = np.diag(1.0 / (h * np.asarray(scales, float)))
+    det = h ** 3 * np.prod(scales)
+    F = np.einsum('ik,jk->ij', inv, inv)[None, None] * (w3 / h ** 3 * det)[None, :, None, None]
+    F = np.broadcast_to(F, (mesh.n_cells,) + F.shape[1:]).copy()
+    return N, dNref, F, det / h ** 3
+
+
+def test_oracle_geometry_cell_matrices_uniform_and_stretched():
+    """The per-cell stiffness from reference gradients and Jacobian factors: on the uniform mesh
+    it equals 0.5 K + N^T diag(v) N. The free-particle operator (lumped mass scaled by the
+    volume factor) is separable: stretched by 2 in every direction its spectrum is the uniform
+    one over 4; stretched by diag(1, 1, 2) its two lowest nonzero eigenvalues are the two
+    distinct wave-1 eigenvalues of the uniform mesh over 4 (the z modes), exact to rounding."""
+    from tests.helpers import shape_tables
+    pr = small_problem(n=2, L=4.0, p=3, wells=2)
+    mesh = pr.mesh
+    N, dNref, F, _ = _box_geometry(mesh, (1.0, 1.0, 1.0))
+    vjxw = pr.info["vjxw"]
+    H = orc.cell_hamiltonians_geometry_direct(N, dNref, F, vjxw)
+    ref = fe.cell_hamiltonians(mesh, vjxw)
+    assert np.abs(H - ref).max() < 1e-12 * np.abs(ref).max()
+    mass = mesh.lumped_mass()
+    zero = np.zeros_like(vjxw)
+    ev = {}
+    for sc in ((1.0, 1.0, 1.0), (2.0, 2.0, 2.0), (1.0, 1.0, 2.0)):
+        N, dNref, F, vol = _box_geometry(mesh, sc)
+        mats = orc.cell_hamiltonians_geometry_direct(N, dNref, F, zero)
+        op = orc.OracleOperator(mesh.cell_dof_map(), mats, 1 / np.sqrt(mass * vol), mesh.n_dofs)
+        ev[sc] = np.linalg.eigvalsh(op.dense())
+    u, iso, z2 = ev[(1.0, 1.0, 1.0)], ev[(2.0, 2.0, 2.0)], ev[(1.0, 1.0, 2.0)]
+    assert np.abs(iso - u / 4.0).max() < 1e-10 * u.max()
+    waves = np.unique(np.round(u[1:7], 9))       # the two distinct wave-1 eigenvalues
+    assert len(waves) == 2
+    assert abs(z2[0]) < 1e-10
+    assert np.allclose(z2[1:3], waves / 4.0, rtol=1e-9)

@@ -108,3 +108,57 @@ def test_partitions_cover_every_index_once():
 
     kpoints()
     bands()
+
+
+N_STATES, N_ELECTRONS, T_FERMI = 8, 8.0, 500.0
+
+
+def _bloch_eigenvalues(k):
+    """Lowest N_STATES eigenvalues of Hamiltonian k of the 32-entry Bloch set (degree-2 cells
+    so that the CPU test stays fast; the oracle's dense Hermitian operator)."""
+    from dftfe_gb300 import problems
+    from tests.helpers import dense_operator
+    pr = problems.bloch_set(32, p=2, small=True)[k]
+    return np.linalg.eigvalsh(dense_operator(pr))[:N_STATES]
+
+
+def _pool_worker(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        solved = pools.solve_kpoint_pool(32, _bloch_eigenvalues)
+        ev = pools.gather_over_pools(solved, 32, N_STATES)
+        mine = [solved[k] for k in sorted(solved)]
+        fe = pools.fermi_energy(mine, [1.0 / 32] * len(mine), N_ELECTRONS, T_FERMI)
+        out.put((rank, sorted(solved), ev, fe))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_bloch_set_over_two_kpoint_pools():
+    """The 32 Bloch Hamiltonians split over two k-point pools (ranks of a gloo group): each
+    rank solves only its pool's range (kpoint_pool_ranges: 0..16 and 17..31), every rank then
+    holds all 32 eigenvalue rows (summed over the pools) and the same Fermi energy, and both
+    equal the single-process results."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_pool_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    ranges = pools.kpoint_pool_ranges(32, 2)
+    assert [r[1] for r in res] == [list(range(*ranges[0])), list(range(*ranges[1]))]
+    ref = np.array([_bloch_eigenvalues(k) for k in range(32)])
+    fe_ref = pools.fermi_energy(list(ref), [1.0 / 32] * 32, N_ELECTRONS, T_FERMI)
+    for _, _, ev, fe in res:
+        assert np.abs(ev - ref).max() < 1e-12
+        assert abs(fe - fe_ref) < 1e-12
+    # the electron count at the Fermi energy
+    f, _ = pools._fermi_dirac_sums(fe_ref, list(ref), [1.0 / 32] * 32, T_FERMI, 2.0)
+    assert abs(f - N_ELECTRONS) < 1e-9

@@ -1,6 +1,7 @@
-"""Real GGA cell Hamiltonians on the device (chefsi_assemble_cell_hamiltonians_gga) against the
-oracle's q-loop of the GGA cell-matrix formula. Tolerance 1e-12 relative (FP64 sums in another
-order). Collected after the other GPU files and before the allocation-free entry point's file.
+"""Real GGA cell Hamiltonians on the device (chefsi_assemble_cell_hamiltonians_gga), their Bloch
+form, and the cell Hamiltonians of cells of any shape (chefsi_assemble_cell_hamiltonians_geometry)
+against the oracle's q-loops. Tolerance 1e-12 relative (FP64 sums in another order). Collected
+after the other GPU files and before the allocation-free entry point's file.
 """
 import numpy as np
 import pytest
@@ -59,3 +60,30 @@ def test_bloch_gga_cell_assembly_matches_oracle(C, p):
     assert rel(out, ref) < 1e-12
     lda = C.assemble_cell_hamiltonians_bloch(t(N), t(dN), t(K_), t(vjxw), t(jxw), kp[:1])
     assert rel(lda.cpu().numpy()[0], pr.cell_mats) < 1e-12
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_geometry_cell_assembly_matches_oracle(C, p):
+    """Cells of any shape: a different Jacobian factor at every quadrature point of every cell
+    (random symmetric positive definite, scaled like J^-1 J^-T JxW of the mesh) against the
+    oracle's q-loop; with the uniform mesh's factors the result is the workload's own cell
+    matrices (0.5 K + N^T diag(v) N)."""
+    from tests.helpers import shape_tables
+    pr = small_problem(n=2, L=4.0, p=p, wells=2)
+    mesh = pr.mesh
+    N, dN, w3 = shape_tables(mesh)
+    h = mesh.h
+    dNref = dN * h
+    vjxw = pr.info["vjxw"]
+    nq = len(w3)
+    rng = np.random.default_rng(20 + p)
+    R = rng.standard_normal((mesh.n_cells, nq, 3, 3)) * 0.3 + np.eye(3)
+    F = np.einsum('cqik,cqjk->cqij', R, R) * (w3 / h ** 2)[None, :, None, None]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda()
+    out = C.assemble_cell_hamiltonians_geometry(t(N), t(dNref), t(F), t(vjxw)).cpu().numpy()
+    ref = orc.cell_hamiltonians_geometry_direct(N, dNref, F, vjxw)
+    assert rel(out, ref) < 1e-12
+    Fu = np.broadcast_to(np.eye(3)[None, None] * (w3 / h ** 2)[None, :, None, None],
+                         (mesh.n_cells, nq, 3, 3))
+    out = C.assemble_cell_hamiltonians_geometry(t(N), t(dNref), t(Fu), t(vjxw)).cpu().numpy()
+    assert rel(out, pr.cell_mats) < 1e-12
