@@ -2070,7 +2070,11 @@ TcPipeline autotune_pipeline(const std::vector<TcGroupItem>& items, cudaStream_t
     auto f = g_tune_cache.find(key);
     if (f != g_tune_cache.end()) return f->second;
   }
-  const TcPipeline cand[] = {{8, 6}, {8, 4}, {6, 4}, {6, 2}, {4, 2}};
+  // X-ring depth x copies in flight, then the order the (cell, 128-vector chunk) pairs are
+  // dealt in: a cell's chunks back to back (its tiles shared in L2 by the chunks), or tiles of
+  // 8 or 64 cells with all their chunks (neighbouring cells' shared rows meet in L2)
+  const TcPipeline cand[] = {{8, 6, 1}, {8, 4, 1}, {6, 4, 1}, {6, 2, 1}, {4, 2, 1},
+                             {8, 6, 8}, {8, 6, 64}};
   cudaEvent_t e0, e1;
   CHEFSI_CUDA(cudaEventCreate(&e0));
   CHEFSI_CUDA(cudaEventCreate(&e1));

@@ -139,6 +139,7 @@ struct TcGroupItem {
 struct TcPipeline {
   int xstages;
   int lookahead;
+  int cell_tile;   // > 1: (cell, chunk) pairs dealt as tiles of that many cells, chunk-major
 };
 // one block of a grouped recurrence step: y = a x + b y (b == 0: y not read), (hi, lo) = split(x)
 struct AxpbyGroupItem {

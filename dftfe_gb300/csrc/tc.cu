@@ -123,6 +123,8 @@ struct TcArgs {
   int stages;      // cell-matrix ring depth
   int xstages;     // X ring depth
   int lookahead;   // K-blocks of X copies in flight per producer thread
+  int cell_tile;   // > 1: (cell, chunk) pairs dealt as tiles of cell_tile cells, every chunk of
+                   // a tile's cells before the next tile; <= 1: a cell's chunks back to back
   // F32X launches: X given as FP32 rows x32 [rows][ldx] (rows >= w_row: the projector
   // coefficients), split into FP16 hi + lo by the producer warps after scaling by xf (dof rows)
   // or wf (projector rows); sstages FP32 staging slots per producer thread ring
@@ -249,8 +251,21 @@ __device__ __forceinline__ Unit unit_at(int64_t it, int64_t first, int64_t step,
     if (cc >= a.prob[q].pair_begin) p = q;   // problems in ascending pair order
   const int64_t lc = cc - a.prob[p].pair_begin;
   const int nch = a.prob[p].n_chunks;
-  w.chunk = (int)(lc % nch);
-  w.cell = (int)(lc / nch);
+  const int G = a.cell_tile;
+  if (G <= 1 || nch == 1) {
+    w.chunk = (int)(lc % nch);
+    w.cell = (int)(lc / nch);
+  } else {
+    // tile t holds cells [t G, t G + g) (g = G but for the last tile), chunk-major inside
+    const int64_t span = (int64_t)G * nch;
+    const int64_t t = lc / span;
+    const int64_t r = lc - t * span;
+    const int64_t pairs = (p + 1 < a.n_probs ? a.prob[p + 1].pair_begin : a.n_pairs) -
+                          a.prob[p].pair_begin;
+    const int g = (int)min((int64_t)G, pairs / nch - t * G);
+    w.chunk = (int)(r / g);
+    w.cell = (int)(t * G + r % g);
+  }
   w.p = p;
   return w;
 }
@@ -1236,6 +1251,7 @@ void hx_tc_group_launch(const TcGroupItem* items, int n, int ns, const TcPipelin
   a.stages = p.stages;
   a.xstages = p.xstages;
   a.lookahead = std::max(1, std::min(p.xstages - 2, 6));
+  if (pipe) a.cell_tile = pipe->cell_tile;
   if (pipe && pipe->xstages >= 3 && pipe->xstages <= p.xstages) {
     a.xstages = pipe->xstages;
     p.smem = make_layout(p.n_half, p.stages, a.xstages, ns).total + 1024;
