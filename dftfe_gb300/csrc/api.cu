@@ -156,10 +156,18 @@ int64_t filter_rows(chefsi_operator_s* op) {
 // no split pass either: the launch gathers x_{j-1} as FP32 rows and its producer warps write
 // the FP16 split of f x_{j-1} (f the power of two nearest its factor, which keeps the split at
 // the vector's own magnitude). Besides the launch, a degree only runs the projection C^T x_{j-1}
-// into the buffer's rows past n_dofs. X and Y hold filter_rows(op) rows. Returns false
-// (nothing done) when the shifted diagonals would leave FP16's range.
+// into the buffer's rows past n_dofs. X and Y hold filter_rows(op) rows; the result is left in
+// one of them up to a factor (*res). Returns false (nothing done) when the shifted diagonals
+// would leave FP16's range.
+// where a mixed filter left its result: the block out (X or Y) times factor
+struct FilterOut {
+  const float* out;
+  double factor;
+};
+
 bool cheb_filter_shifted(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
-                         int B, int m, double a, double b, double a0, cudaStream_t st) {
+                         int B, int m, double a, double b, double a0, cudaStream_t st,
+                         FilterOut* res) {
   prepare_fused_plan(op, st);
   const double e = (b - a) / 2.0, c = (b + a) / 2.0;
   if (!set_tile_shift(op, c, st)) return false;
@@ -197,23 +205,21 @@ bool cheb_filter_shifted(chefsi_solver_s* s, chefsi_operator_s* op, float* X, fl
     std::swap(sx, sy);
     sigma = sigma2;
   }
-  if (y != X)
-    copy_block<float, float>(y, B, X, B, M, B, sy, st);
-  else
-    scale_block<float>(X, B, M, B, sy, st);
+  *res = FilterOut{y, sy};   // applied by the caller's conversion back to FP64
   return true;
 }
 
-// Mixed Chebyshev filter on the tensor cores (same recurrence as cheb_filter). The HX input
-// is also kept as FP16 hi + lo rows: the step y_{k-1} <- -c alpha1 y_k + alpha2 y_{k-1}
-// reads y_k, the next HX's input, and writes its split in the same pass; the first input is
-// split once.
-void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
-                    int B, int m, double a, double b, double a0, cudaStream_t st) {
+// Mixed Chebyshev filter on the tensor cores (same recurrence as cheb_filter): the shifted
+// filter by default; otherwise (variant 2, operators with constraint rows, shifts beyond the
+// tiles' range) a recurrence step per degree y_{k-1} <- -c alpha1 y_k + alpha2 y_{k-1} that also
+// writes the FP16 hi + lo split of y_k, the next HX's input. Returns the block holding the
+// result and its factor.
+FilterOut cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y,
+                         int64_t M, int B, int m, double a, double b, double a0, cudaStream_t st) {
   if (s->p.filter_variant == 1 && fused_plan_usable(op)) {
     // one launch per degree finishes the recurrence and applies the nonlocal term
     cheb_filter_fused(op, s->fzw, X, M, B, m, a, b, a0, [&] { s->hx_mark(st); }, st);
-    return;
+    return FilterOut{X, 1.0};
   }
   // the nonlocal apply folded into the tensor-core launch (extra K columns of the cell
   // matrices fed by split rows of 2^t C^T x after the dof rows), unless the separate nonlocal
@@ -221,9 +227,10 @@ void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* 
   // operators with constraint rows: distribute on the split rows, the plan's tiles (M^{-1/2}
   // folded in by the plan), the adjoint after the launch
   const bool constrained = !op->folded;
+  FilterOut res{X, 1.0};
   if (s->p.filter_variant == 0 && !constrained && fused_plan_usable(op) &&
-      cheb_filter_shifted(s, op, X, Y, M, B, m, a, b, a0, st))
-    return;
+      cheb_filter_shifted(s, op, X, Y, M, B, m, a, b, a0, st, &res))
+    return res;
   // variant 2 (and variant 0 when the shift does not fit the tiles): a recurrence pass per
   // degree and the HX launch with the nonlocal apply folded in
   const bool fold = constrained || ((s->p.filter_variant == 0 || s->p.filter_variant == 2) &&
@@ -263,7 +270,7 @@ void cheb_filter_tc(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* 
     std::swap(x, y);
     sigma = sigma2;
   }
-  if (y != X) copy_block<float, float>(y, B, X, B, M, B, 1.0, st);
+  return FilterOut{y, 1.0};
 }
 
 // filter columns [j0, j0+B) of X (ld) in place
@@ -297,8 +304,9 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
   float* Xb = s->Xb32.ensure((size_t)filter_rows(op) * B);
   float* Yb = s->Yb32.ensure((size_t)filter_rows(op) * B);
   copy_block<double, float>(X + j0, ld, Xb, B, M, B, scale, st);
+  FilterOut fo{Xb, 1.0};
   if (prec == CHEFSI_PREC_MIXED && (tc_split_usable(op, B) || constrained_tc_usable(op, B))) {
-    cheb_filter_tc(s, op, Xb, Yb, M, B, m, a, b, a0, st);
+    fo = cheb_filter_tc(s, op, Xb, Yb, M, B, m, a, b, a0, st);
   } else {
     cheb_filter<float>(Xb, Yb, M, B, m, a, b, a0,
                        [&](const float* src, float* dst, double scv, bool acc) {
@@ -312,7 +320,8 @@ void filter_columns(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_
     const int tc = tc_check_error(op, st);
     if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
   }
-  copy_block<float, double>(Xb, B, X + j0, ld, M, B, 1.0 / scale, st);
+  // the filter's own factor rides in the conversion back to FP64
+  copy_block<float, double>(fo.out, B, X + j0, ld, M, B, fo.factor / scale, st);
 }
 
 void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m, int prec,
@@ -337,8 +346,9 @@ void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m
       float* xr = s->Xb32.ensure((size_t)filter_rows(rv) * B);
       float* yr = s->Yb32.ensure((size_t)filter_rows(rv) * B);
       complex_to_real_rows(Xc + j0, N, M, B, scale, xr, st);
+      FilterOut fo{xr, 1.0};
       if (prec == CHEFSI_PREC_MIXED && tc_split_usable(rv, B)) {
-        cheb_filter_tc(s, rv, xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0, st);
+        fo = cheb_filter_tc(s, rv, xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0, st);
       } else {
         cheb_filter<float>(xr, yr, 2 * M, B, m, s->b_low, s->b_up, s->a0,
                            [&](const float* src, float* dst, double scv, bool acc) {
@@ -352,7 +362,7 @@ void filter_all(chefsi_solver_s* s, chefsi_operator_s* op, void* X, int N, int m
         const int tc = tc_check_error(rv, st);
         if (tc != CHEFSI_OK) throw Error(tc, "tensor-core HX: a bounded device wait expired");
       }
-      real_rows_to_complex(xr, M, B, 1.0 / scale, Xc + j0, N, st);
+      real_rows_to_complex(fo.out, M, B, fo.factor / scale, Xc + j0, N, st);
     } else if (op->is_complex) {
       cplx* Xc = reinterpret_cast<cplx*>(X);
       cplx* Xb = reinterpret_cast<cplx*>(s->Xb64.ensure((size_t)op->n_dofs * B * 2));
