@@ -480,11 +480,21 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
     y32 = s->Yb32.ensure((size_t)M * N);
     double scale = 1.0;
     if (tc2 || tc3) {
-      double* sc = s->scal.ensure(1);
-      absmax_block_f64(X, ld, M, N, sc, st);
       double amax = 0.0;
-      CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
-      CHEFSI_CUDA(cudaStreamSynchronize(st));
+      if (tcd) {
+        // the largest of the column maxima the tensor-core Gram just took (no pass over X)
+        std::vector<unsigned long long> bits(N);
+        CHEFSI_CUDA(cudaMemcpyAsync(bits.data(), s->tx.bits.ptr, sizeof(unsigned long long) * N,
+                                    cudaMemcpyDeviceToHost, st));
+        CHEFSI_CUDA(cudaStreamSynchronize(st));
+        const unsigned long long mb = *std::max_element(bits.begin(), bits.end());
+        std::memcpy(&amax, &mb, sizeof(double));
+      } else {
+        double* sc = s->scal.ensure(1);
+        absmax_block_f64(X, ld, M, N, sc, st);
+        CHEFSI_CUDA(cudaMemcpyAsync(&amax, sc, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CHEFSI_CUDA(cudaStreamSynchronize(st));
+      }
       if (amax > 0.0 && std::isfinite(amax))
         scale = std::ldexp(1.0, (tc3 ? 14 : 8) - (int)std::ceil(std::log2(amax)));
     }

@@ -1594,7 +1594,12 @@ bool hx_tc3(chefsi_operator_s* op, const float* src, int64_t lds, float* dst, in
   k_split_rows3<<<grid_for(op->n_dofs * (B / 2), 256), 256, 0, st>>>(src, lds, op->n_dofs, B, hi,
                                                                       lo, lo3);
   CHEFSI_CHECK_LAUNCH();
-  if (!accumulate) scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  if (!accumulate) {
+    if (ldd == B)
+      CHEFSI_CUDA(cudaMemsetAsync(dst, 0, sizeof(float) * n, st));
+    else
+      scale_block<float>(dst, ldd, op->n_dofs, B, 0.0, st);
+  }
   launch_tc(op, hi, lo, lo3, dst, ldd, B, scalar, 3, st);
   apply_nonlocal_f32(op, src, lds, dst, ldd, B, scalar, st);
   return true;
