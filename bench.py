@@ -470,7 +470,9 @@ def run_ours(args):
     phases = solver.timings(True)
 
     # the large workload's X (134 GB) leaves no room for the pipelined copies' device buffers
-    e2e = None if large else e2e_pipeline(step, X, max(2, min(args.steps, 4)))
+    # the pipeline's fill (first upload) and drain (last download) are in the timed region; at
+    # least 4 steps so that they weigh as in a longer run of iterations
+    e2e = None if large else e2e_pipeline(step, X, max(4, min(args.steps, 8)))
     torch.cuda.empty_cache()
     free_b, total_b = torch.cuda.mem_get_info()
 
