@@ -3,13 +3,14 @@
 //
 // DFT-FE's local HX (src/dftOperator/matrixVectorProductImplementationsDevice.cc:27-117)
 // gathers X into n_cells x n_e x B cell blocks, calls gemmStridedBatched and scatter-adds.
-// Here no cell block is materialised. The filter keeps its FP32 vectors also as FP16 hi + lo
-// rows (written by the recurrence step that reads them anyway), and one CTA owns one
-// (cell, 128-vector chunk, half of the cell's rows) at a time:
+// Here no cell block is materialised, and one CTA owns one (cell, 128-vector chunk, half of
+// the cell's rows) at a time:
 //   * producer warps copy the chunk's X rows through the cell's dof map (cp.async, 16-byte
-//     pieces) into a 128B-swizzled, MN-major tile, and one bulk copy per split term loads
-//     the cell-matrix K-block (FP16 hi and lo of 2^s A_e, stored tile by tile as the K-major,
-//     64B-swizzled shared-memory image);
+//     pieces) into a 128B-swizzled, MN-major tile: either FP16 hi + lo rows the caller split
+//     (the Rayleigh-Ritz apply, the unshifted filter variants) or, for the default filter step
+//     (F32X), FP32 rows staged per thread and split by the producers themselves; one bulk copy
+//     per split term loads the cell-matrix K-block (FP16 hi and lo of 2^s A_e, stored tile by
+//     tile as the K-major, 64B-swizzled shared-memory image);
 //   * one lane issues tcgen05.mma kind::f16 with M = 128 vectors, N = the half's rows
 //     (<= 256), K = 16:  D += Xhi Ahi^T + Xhi Alo^T + Xlo Ahi^T  (lo*lo is below 2^-22);
 //   * the epilogue warps read D with tcgen05.ld (lane = vector) and scatter-add

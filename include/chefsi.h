@@ -159,7 +159,7 @@ typedef struct {
                                    degree with the Chebyshev shift on the tiles' diagonals and
                                    the nonlocal apply as extra tensor-core K columns, reducing
                                    into the older vector's buffer (kept up to a scalar factor:
-                                   no recurrence pass, one split pass of the HX input); 2 a
+                                   no recurrence pass; the launch splits its FP32 input); 2 a
                                    recurrence pass per degree and that HX launch without the
                                    shift; 1 the fused step (the recurrence finished in the HX
                                    launch, vectors kept as FP16 hi + lo rows); -1 the recurrence
