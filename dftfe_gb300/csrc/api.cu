@@ -2254,9 +2254,12 @@ int chefsi_solve_batched(int32_t count, chefsi_solver* solvers, chefsi_operator*
   for (int i = 0; i < count; ++i)
     CHEFSI_REQUIRE(solvers[i] && ops[i] && X[i] && eig_host[i] && N[i] >= 1,
                    "bad argument in batch entry " + std::to_string(i));
+  // distinct operators too: the entries run concurrently on several streams, and a mixed
+  // filter writes its Chebyshev shift into its operator's tensor-core tiles
   for (int i = 0; i < count; ++i)
     for (int j = 0; j < i; ++j)
-      CHEFSI_REQUIRE(solvers[i] != solvers[j], "batch entries must use distinct solvers");
+      CHEFSI_REQUIRE(solvers[i] != solvers[j] && ops[i] != ops[j],
+                     "batch entries must use distinct solvers and operators");
   // largest first: work ~ n_dofs * N * (degree + 2) (filter) + n_dofs * N^2 (dense steps)
   std::vector<double> cost(count);
   for (int i = 0; i < count; ++i) {

@@ -434,7 +434,10 @@ int chefsi_solve_spectrum_split(chefsi_solver s, chefsi_operator op, void* X, in
    dftClass::kohnShamEigenSpaceCompute, src/dft/kohnShamEigenSolve.cc:507-655, which calls
    solve() once per (k, spin)): problem i is (solvers[i], ops[i], X[i], N[i]) with its
    eigenvalues (and residual norms) written to eig_host[i] (res_host[i]); res_host may be
-   null. Every entry needs its own solver (bounds and workspaces).
+   null. Every entry needs its own solver (bounds and workspaces) and its own operator (the
+   entries run concurrently, and a mixed filter writes its shift into the operator's
+   tensor-core tiles; as in DFT-FE, every (k, spin) has its own Hamiltonian). The same holds
+   for operators used by several host threads or streams at once.
    With group_filter != 0, the entries whose mixed filter runs on the tensor cores in one
    block (chebyWfcBlockSize >= N) are filtered together: per Chebyshev degree one grouped
    recurrence launch and one persistent tensor-core HX launch cover all problems of a cell
