@@ -56,6 +56,11 @@
  *     chefsi_last_error() returns the message of the last failure on the calling thread.
  *   - Compute calls take a cudaStream_t (passed as void*) and enqueue work on it. Calls that
  *     return host results (eigenvalues, residuals, bounds) synchronise that stream.
+ *   - Stream capture: the FP64 and FP32 SIMT chefsi_hx only enqueue work once their
+ *     workspaces exist (capture them after a first call). The tensor-core paths read their
+ *     bounded-wait status back and the mixed filter reads its block's largest entry back (to
+ *     scale the block by a power of two), so those calls synchronise their stream and cannot
+ *     be captured; chefsi_solve_batched captures its own grouped filter.
  *   - Handles are not thread-safe: one host thread per handle.
  *   - Precision: CHEFSI_PREC_FP64 computes everything in FP64. CHEFSI_PREC_MIXED runs the
  *     filter HX on the tensor cores with FP16-split operands (hi+lo, three products,
