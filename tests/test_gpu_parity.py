@@ -169,6 +169,24 @@ def test_filter_mixed_close_to_fp64(chefsi):
     assert rel(Xt.cpu().numpy(), ref) < MIXED_SHIFTED_TOL
 
 
+def test_filter_mixed_shift_beyond_tiles_falls_back(chefsi):
+    """A damped interval reaching far past the spectrum puts the Chebyshev shift c beyond what
+    the FP16 tiles' diagonals can hold (here c / max|A| ~ 19): the default filter then runs
+    the recurrence pass with the shift in FP32 and meets that variant's 5e-6 bound; a normal
+    filter afterwards on the same operator takes the shifted path again."""
+    pr = small_problem(n=2, L=4.0, p=4, wells=2, projectors=True)
+    op, ora = gpu_op(chefsi, pr), oracle_op(pr)
+    X = np.random.default_rng(8).uniform(-1, 1, (pr.n_dofs, 32))
+    lo, up = orc.lanczos_bounds(ora, np.ones(pr.n_dofs), 20)
+    a, b = lo + 0.3 * (up - lo), 8.0 * up
+    Xt = torch.from_numpy(X.copy()).cuda()
+    chefsi.chebyshevFilter(op, Xt, 10, a, b, lo, precision="mixed")
+    assert rel(Xt.cpu().numpy(), ora.chebyshev_filter(X, 10, a, b, lo)) < 5e-6
+    Xt = torch.from_numpy(X.copy()).cuda()
+    chefsi.chebyshevFilter(op, Xt, 10, a, up, lo, precision="mixed")
+    assert rel(Xt.cpu().numpy(), ora.chebyshev_filter(X, 10, a, up, lo)) < MIXED_SHIFTED_TOL
+
+
 @pytest.mark.parametrize("N,degenerate", [(1, False), (7, False), (50, False), (130, True),
                                           (257, True)])
 def test_syevd_matches_numpy(chefsi, N, degenerate):
