@@ -146,6 +146,12 @@ int64_t filter_rows(chefsi_operator_s* op) {
   return op->n_dofs + (op->is_complex ? 0 : (int64_t)op->n_atoms * op->n_proj);
 }
 
+// where a mixed filter left its result: the block out (X or Y) times factor
+struct FilterOut {
+  const float* out;
+  double factor;
+};
+
 // Mixed Chebyshev filter with the shift on the tensor-core tiles. In the sigma form every degree
 // is x_j = alpha1_j (A - c) x_{j-1} + alpha2_j x_{j-2} with the same c, so the plan's tiles carry
 // 2^s (A_II - c / n_I) on their diagonals for the whole call and each degree is one HX launch
@@ -159,12 +165,6 @@ int64_t filter_rows(chefsi_operator_s* op) {
 // into the buffer's rows past n_dofs. X and Y hold filter_rows(op) rows; the result is left in
 // one of them up to a factor (*res). Returns false (nothing done) when the shifted diagonals
 // would leave FP16's range.
-// where a mixed filter left its result: the block out (X or Y) times factor
-struct FilterOut {
-  const float* out;
-  double factor;
-};
-
 bool cheb_filter_shifted(chefsi_solver_s* s, chefsi_operator_s* op, float* X, float* Y, int64_t M,
                          int B, int m, double a, double b, double a0, cudaStream_t st,
                          FilterOut* res) {
