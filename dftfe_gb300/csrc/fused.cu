@@ -142,12 +142,13 @@ __global__ void k_fz_join(const __half* __restrict__ hi, const __half* __restric
 }
 
 // the projector columns of the extended tiles: entry idx[k] of the tile array receives the split
-// of val[k] (already scaled)
+// of scale * val[k]
 __global__ void k_fz_scatter(const int64_t* __restrict__ idx, const double* __restrict__ val,
-                             int64_t n, __half* __restrict__ hi, __half* __restrict__ lo) {
+                             int64_t n, double scale, __half* __restrict__ hi,
+                             __half* __restrict__ lo) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const double v = val[t];
+    const double v = scale * val[t];
     const __half h = __double2half(v);
     hi[idx[t]] = h;
     lo[idx[t]] = __double2half(v - (double)__half2float(h));
@@ -329,9 +330,57 @@ bool constrained_tc_usable(chefsi_operator_s* op, int B) {
   return plan_usable(op) && !op->folded && B % 8 == 0;
 }
 
+// The plan's tiles from the current cell matrices (on the device; the map-dependent tables
+// and the projector columns' values stay): the power-of-two scale, the split of the cell
+// matrices, the projector columns scattered at that scale, the diagonal bound of the shift.
+static void build_plan_tiles(chefsi_operator_s* op, cudaStream_t st) {
+  FusedPlan& fp = op->fz;
+  const int nc = op->n_cells, ne = op->n_e;
+  DeviceBuffer<double> amax(1);
+  absmax_block_f64(op->mats64.ptr, ne, (int64_t)nc * ne, ne, amax.ptr, st);
+  double am = 0.0;
+  CHEFSI_CUDA(cudaMemcpyAsync(&am, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  // constraint rows: the plan's tiles hold d_I A_IJ d_J, bounded by max|A| max(d)^2
+  if (!op->folded) am *= fp.dmax2;
+  am = std::max(am, fp.ext_max);
+  // largest entry in [2^11, 2^12): room on the diagonals for the filter's shift (FP16 keeps
+  // its 11-bit significand at every magnitude, so the headroom costs no precision)
+  const int e = (am > 0 && std::isfinite(am)) ? 11 - (int)std::floor(std::log2(am)) : 0;
+  const double scale = std::ldexp(1.0, e);
+  fp.diag_max = 0.0;
+  if (op->folded) {
+    DeviceBuffer<double> dmx(1);
+    k_fz_diag_max<<<1, 256, 0, st>>>(op->mats64.ptr, (int64_t)nc * ne, ne, dmx.ptr);
+    CHEFSI_CHECK_LAUNCH();
+    CHEFSI_CUDA(cudaMemcpyAsync(&fp.diag_max, dmx.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CHEFSI_CUDA(cudaStreamSynchronize(st));
+  }
+  fp.shift = 0.0;
+  int n_half = 0, n_halves = 0;
+  tc_row_split(ne, &n_half, &n_halves);
+  const size_t ntile = (size_t)nc * n_halves * fp.nkb * n_half * 32;
+  if (fp.hi.n != ntile) {
+    fp.hi.reset(ntile);
+    fp.lo.reset(ntile);
+  }
+  split_mats_ext(op, fp.nkb, scale, fp.hi.ptr, fp.lo.ptr, st);
+  const int64_t n_ext = (int64_t)fp.ext_idx.n;
+  if (n_ext) {
+    k_fz_scatter<<<grid_for(n_ext, 256), 256, 0, st>>>(fp.ext_idx.ptr, fp.ext_val.ptr, n_ext,
+                                                       scale, fp.hi.ptr, fp.lo.ptr);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  fp.scale = (float)scale;
+  fp.tiles_ready = true;
+}
+
 void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   FusedPlan& fp = op->fz;
-  if (fp.ready) return;
+  if (fp.ready) {
+    if (!fp.tiles_ready) build_plan_tiles(op, st);
+    return;
+  }
   CHEFSI_REQUIRE(plan_usable(op), "tensor-core plan: operator not supported");
   const int nc = op->n_cells, ne = op->n_e;
   const int64_t M = op->n_dofs;
@@ -444,11 +493,7 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
         for (int j = 0; j < P; ++j)
           ext_max = std::max(ext_max, std::fabs(C[(size_t)r * P + j] * V[(size_t)a * P + j]) / wscale);
   }
-  DeviceBuffer<double> amax(1);
-  absmax_block_f64(op->mats64.ptr, ne, (int64_t)nc * ne, ne, amax.ptr, st);
-  double am = 0.0;
-  CHEFSI_CUDA(cudaMemcpyAsync(&am, amax.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
-  CHEFSI_CUDA(cudaStreamSynchronize(st));
+  fp.dmax2 = 1.0;
   if (!op->folded) {
     // the plan's tiles hold d_I A_IJ d_J: bound their largest entry by max|A| max(d)^2, and
     // rescale the constraint weights for the folded basis: x_s = sum (w d_m / d_s) x_m
@@ -457,7 +502,7 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
     double dmax = 0.0;
     CHEFSI_CUDA(cudaMemcpyAsync(&dmax, dm.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
     CHEFSI_CUDA(cudaStreamSynchronize(st));
-    am *= dmax * dmax;
+    fp.dmax2 = dmax * dmax;
     const std::vector<double> d = to_host(op->inv_sqrt_mass, (size_t)M);
     const std::vector<int> ids = to_host(op->con_ids, (size_t)op->n_con);
     const std::vector<int> ptr = to_host(op->con_ptr, (size_t)op->n_con + 1);
@@ -467,26 +512,9 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
       for (int e = ptr[k]; e < ptr[k + 1]; ++e) w[e] *= d[mas[e]] / d[ids[k]];
     to_device(fp.con_wp, w);
   }
-  am = std::max(am, ext_max);
-  // largest entry in [2^11, 2^12): room on the diagonals for the filter's shift (FP16 keeps
-  // its 11-bit significand at every magnitude, so the headroom costs no precision)
-  const int e = (am > 0 && std::isfinite(am)) ? 11 - (int)std::floor(std::log2(am)) : 0;
-  const double scale = std::ldexp(1.0, e);
-  fp.diag_max = 0.0;
-  if (op->folded) {
-    DeviceBuffer<double> dmx(1);
-    k_fz_diag_max<<<1, 256, 0, st>>>(op->mats64.ptr, (int64_t)nc * ne, ne, dmx.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    CHEFSI_CUDA(cudaMemcpyAsync(&fp.diag_max, dmx.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
-    CHEFSI_CUDA(cudaStreamSynchronize(st));
-  }
-  fp.shift = 0.0;
+  fp.ext_max = ext_max;
   int n_half = 0, n_halves = 0;
   tc_row_split(ne, &n_half, &n_halves);
-  const size_t ntile = (size_t)nc * n_halves * nkb * n_half * 32;
-  fp.hi.reset(ntile);
-  fp.lo.reset(ntile);
-  split_mats_ext(op, nkb, scale, fp.hi.ptr, fp.lo.ptr, st);
   if (P) {
     std::vector<int64_t> idx;
     std::vector<double> val;
@@ -507,18 +535,11 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
           const int J = ne + sl * P + j;
           const int64_t tix = ((int64_t)c * n_halves + half) * nkb + J / 32;
           idx.push_back(tix * n_half * 32 + tcx::sw64_offset((uint32_t)ri, 2u * (uint32_t)(J % 32)) / 2);
-          val.push_back(scale / wscale * C[(size_t)r * P + j] * V[(size_t)a * P + j]);
+          val.push_back(C[(size_t)r * P + j] * V[(size_t)a * P + j] / wscale);
         }
       }
-    DeviceBuffer<int64_t> didx;
-    DeviceBuffer<double> dval;
-    to_device(didx, idx);
-    to_device(dval, val);
-    k_fz_scatter<<<grid_for((int64_t)idx.size(), 256), 256, 0, st>>>(didx.ptr, dval.ptr,
-                                                                     (int64_t)idx.size(), fp.hi.ptr,
-                                                                     fp.lo.ptr);
-    CHEFSI_CHECK_LAUNCH();
-    CHEFSI_CUDA(cudaStreamSynchronize(st));
+    to_device(fp.ext_idx, idx);
+    to_device(fp.ext_val, val);
   }
   to_device(fp.mapk, mapk);
   to_device(fp.rowinfo, rowinfo);
@@ -528,8 +549,8 @@ void prepare_fused_plan(chefsi_operator_s* op, cudaStream_t st) {
   fp.max_slots = max_slots;
   fp.n_shared = n_shared;
   fp.rows = M + (int64_t)op->n_atoms * P;
-  fp.scale = (float)scale;
   fp.wscale = (float)wscale;
+  build_plan_tiles(op, st);
   fp.ready = true;
 }
 
@@ -547,7 +568,7 @@ void nl_project_to_split(chefsi_operator_s* op, const float* x, int B, float* W,
 
 bool set_tile_shift(chefsi_operator_s* op, double shift, cudaStream_t st) {
   FusedPlan& fp = op->fz;
-  CHEFSI_REQUIRE(fp.ready, "tile shift: plan not prepared");
+  CHEFSI_REQUIRE(fp.ready && fp.tiles_ready, "tile shift: plan not prepared");
   if (shift == fp.shift) return true;
   if (!op->folded) return false;
   // |A_II - shift / n_I| <= max |A_II| + |shift| must stay inside FP16's range once scaled

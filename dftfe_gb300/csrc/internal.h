@@ -62,6 +62,13 @@ struct FusedPlan {
   // c once per dof); shift = the c the tiles hold now
   double diag_max = 0.0;          // max |A_II| over the cells
   double shift = 0.0;
+  // the tiles depend on the cell matrices, the tables above on the map and the projectors:
+  // a cell-matrix update rebuilds the tiles only (on the device)
+  bool tiles_ready = false;
+  DeviceBuffer<int64_t> ext_idx;  // tile elements of the projector columns
+  DeviceBuffer<double> ext_val;   // their values C V / 2^t (the tile scale applied on scatter)
+  double ext_max = 0.0;           // max |ext_val|
+  double dmax2 = 1.0;             // constraint rows: max(M^{-1/2})^2 (the tiles fold it in)
   // operators with constraint rows (M^{-1/2} folded in by the plan, not the operator):
   DeviceBuffer<float> nl_c32;     // M^{-1/2} C in FP32 for the projection
   DeviceBuffer<double> con_wp;    // constraint weights in the folded basis, w d_m / d_s

@@ -892,7 +892,7 @@ void update_cell_matrices(chefsi_operator_s* op, const double* mats_dev, cudaStr
   k_to_f32<<<grid_for((int64_t)nm, 256), 256, 0, st>>>(op->mats64.ptr, op->mats32.ptr, nm);
   CHEFSI_CHECK_LAUNCH();
   op->tc.ready = false;  // the FP16 split is rebuilt on the next tensor-core apply
-  op->fz.ready = false;  // and so are the fused filter step's tiles
+  op->fz.tiles_ready = false;  // and so are the filter plan's tiles (its tables stay)
 }
 
 // real form of the complex cell matrices: row (I, p), column (J, q), p/q = 0 real part,

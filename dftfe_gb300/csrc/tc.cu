@@ -1327,7 +1327,7 @@ void split_mats_ext(chefsi_operator_s* op, int nkb, double scale, __half* hi, __
 void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half* xlo, float* dst,
                          int64_t ldd, int B, double scalar, cudaStream_t st, double shift) {
   const FusedPlan& fp = op->fz;
-  CHEFSI_REQUIRE(fp.ready, "folded nonlocal HX: tables not prepared");
+  CHEFSI_REQUIRE(fp.ready && fp.tiles_ready, "folded nonlocal HX: tables not prepared");
   CHEFSI_REQUIRE(set_tile_shift(op, shift, st), "folded nonlocal HX: shift out of the tiles' range");
   const int n_e = op->n_e;
   const TcPlan p = plan_for(n_e, 2);
@@ -1383,7 +1383,7 @@ void hx_tc_folded_launch(chefsi_operator_s* op, const __half* xhi, const __half*
 void hx_tc_folded_f32_launch(chefsi_operator_s* op, const float* x32, float* dst, int64_t ldd,
                              int B, double scalar, double xf, cudaStream_t st, double shift) {
   const FusedPlan& fp = op->fz;
-  CHEFSI_REQUIRE(fp.ready, "folded nonlocal HX: tables not prepared");
+  CHEFSI_REQUIRE(fp.ready && fp.tiles_ready, "folded nonlocal HX: tables not prepared");
   CHEFSI_REQUIRE(set_tile_shift(op, shift, st), "folded nonlocal HX: shift out of the tiles' range");
   const int n_e = op->n_e;
   TcPlan p = plan_for(n_e, 2);
@@ -1445,7 +1445,7 @@ void hx_tc_folded_f32_launch(chefsi_operator_s* op, const float* x32, float* dst
 void hx_tc_fused_launch(const TcFusedLaunch& f, cudaStream_t st) {
   chefsi_operator_s* op = f.op;
   const FusedPlan& fp = op->fz;
-  CHEFSI_REQUIRE(fp.ready, "fused filter step: tables not prepared");
+  CHEFSI_REQUIRE(fp.ready && fp.tiles_ready, "fused filter step: tables not prepared");
   CHEFSI_REQUIRE(set_tile_shift(op, 0.0, st), "fused filter step: tiles not restored");
   const int n_e = op->n_e;
   const TcPlan p = plan_for(n_e, 2, true);

@@ -169,6 +169,33 @@ def test_filter_mixed_close_to_fp64(chefsi):
     assert rel(Xt.cpu().numpy(), ref) < MIXED_SHIFTED_TOL
 
 
+def test_filter_mixed_after_cell_matrix_update(chefsi):
+    """An SCF step replaces the cell matrices: the filter plan keeps its map and projector
+    tables and rebuilds its tiles on the device (new scale, new diagonals, the projector
+    columns re-scattered). The mixed filter and the mixed HX after the update match the oracle
+    of the new matrices, and a second update back to the first matrices reproduces the first
+    filter."""
+    pr = small_problem(n=2, L=4.0, p=4, wells=2, projectors=True)
+    op = gpu_op(chefsi, pr)
+    X = np.random.default_rng(9).uniform(-1, 1, (pr.n_dofs, 32))
+    mats2 = 1.7 * pr.cell_mats + 0.3 * np.swapaxes(pr.cell_mats, 1, 2)
+    out = []
+    for mats in (pr.cell_mats, mats2, pr.cell_mats):
+        op.update_cell_matrices(torch.from_numpy(np.ascontiguousarray(mats)).cuda())
+        ora = orc.OracleOperator(pr.cell_map, mats, pr.inv_sqrt_mass, pr.n_dofs,
+                                 projectors=pr.nonlocal_)
+        lo, up = orc.lanczos_bounds(ora, np.ones(pr.n_dofs), 20)
+        a = lo + 0.3 * (up - lo)
+        Xt = torch.from_numpy(X.copy()).cuda()
+        chefsi.chebyshevFilter(op, Xt, 10, a, up, lo, precision="mixed")
+        out.append(Xt.cpu().numpy())
+        assert rel(out[-1], ora.chebyshev_filter(X, 10, a, up, lo)) < MIXED_SHIFTED_TOL
+        Y = torch.zeros((pr.n_dofs, 32), dtype=torch.float32, device="cuda")
+        op.HX(torch.from_numpy(X.astype(np.float32)).cuda(), Y, precision="mixed")
+        assert rel(Y.cpu().numpy(), ora.HX(X.astype(np.float32).astype(np.float64))) < 2e-6
+    assert rel(out[2], out[0]) < 1e-5   # reduction order differs between runs
+
+
 def test_filter_mixed_shift_beyond_tiles_falls_back(chefsi):
     """A damped interval reaching far past the spectrum puts the Chebyshev shift c beyond what
     the FP16 tiles' diagonals can hold (here c / max|A| ~ 19): the default filter then runs
