@@ -427,6 +427,32 @@ __global__ void k_transpose(const double* __restrict__ A, double* __restrict__ B
     B[t] = A[(t % N) * N + t / N];
 }
 
+// The overlap's Cholesky factor (lower, in place of S). A tensor-core S resolves 22 bits: for a
+// block whose overlap is conditioned beyond that (a filtered block far from convergence), its
+// Cholesky fails although the FP64 one would not, so S is taken again with the FP64 Gram
+// before CHEFSI_ERR_NOT_SPD is reported. CHEFSI_FAULT_INJECT=not_spd spoils every S,
+// =not_spd_mixed only the tensor-core one (to exercise the second attempt).
+int cholesky_overlap(double* S, const double* X, int64_t ld, int64_t M, int N, bool tc_gram_used,
+                     cudaStream_t st) {
+  if (fault_injected("not_spd") || (tc_gram_used && fault_injected("not_spd_mixed"))) {
+    k_negate_diag0<<<1, 1, 0, st>>>(S);
+    CHEFSI_CHECK_LAUNCH();
+  }
+  int rc = cholesky_lower(S, N, st);
+  if (rc != CHEFSI_OK && tc_gram_used) {
+    CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
+    gram_f64(X, ld, X, ld, M, N, N, S, N, CHEFSI_PREC_FP64, true, st);
+    symmetrize_lower(S, N, st);
+    if (fault_injected("not_spd")) {
+      k_negate_diag0<<<1, 1, 0, st>>>(S);
+      CHEFSI_CHECK_LAUNCH();
+    }
+    rc = cholesky_lower(S, N, st);
+  }
+  if (rc != CHEFSI_OK) set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
+  return rc;
+}
+
 // Rayleigh-Ritz, generalised form (rayleighRitzGEP): returns eigenvalues (device) and
 // rotates X (and HX if requested) to the Ritz basis.
 int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int64_t ld, int N,
@@ -451,15 +477,8 @@ int rayleigh_ritz_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, int
     gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
   }
   symmetrize_lower(S, N, st);
-  if (fault_injected("not_spd")) {
-    k_negate_diag0<<<1, 1, 0, st>>>(S);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  int rc = cholesky_lower(S, N, st);
-  if (rc != CHEFSI_OK) {
-    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
-    return rc;
-  }
+  int rc = cholesky_overlap(S, X, ld, M, N, tcd, st);
+  if (rc != CHEFSI_OK) return rc;
   trtri_lower(S, N, st);  // S now holds L^{-1}
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
   // Hp = X^T (A X). The HX is FP64 unless the mixed mode asks for the FP32 SIMT apply; then
@@ -594,15 +613,8 @@ int rayleigh_ritz_real_blocked(chefsi_solver_s* s, chefsi_operator_s* op, double
     gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
   }
   symmetrize_lower(S, N, st);
-  if (fault_injected("not_spd")) {
-    k_negate_diag0<<<1, 1, 0, st>>>(S);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  int rc = cholesky_lower(S, N, st);
-  if (rc != CHEFSI_OK) {
-    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
-    return rc;
-  }
+  int rc = cholesky_overlap(S, X, ld, M, N, tcd, st);
+  if (rc != CHEFSI_OK) return rc;
   trtri_lower(S, N, st);
   CHEFSI_CUDA(cudaEventRecord(s->ev[2], st));
   const int rrp = s->p.rr_precision;
@@ -757,15 +769,8 @@ int rayleigh_ritz_ss_real(chefsi_solver_s* s, chefsi_operator_s* op, double* X, 
     gram_f64(X, ld, X, ld, M, N, N, S, N, prec, true, st);
   }
   symmetrize_lower(S, N, st);
-  if (fault_injected("not_spd")) {
-    k_negate_diag0<<<1, 1, 0, st>>>(S);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  int rc = cholesky_lower(S, N, st);
-  if (rc != CHEFSI_OK) {
-    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
-    return rc;
-  }
+  int rc = cholesky_overlap(S, X, ld, M, N, tcd, st);
+  if (rc != CHEFSI_OK) return rc;
   trtri_lower(S, N, st);
   k_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);
   CHEFSI_CHECK_LAUNCH();
@@ -1601,15 +1606,8 @@ int chefsi_cholesky_gs(chefsi_operator op, void* X, int64_t ld, int32_t N, int32
   CHEFSI_CUDA(cudaMemsetAsync(S, 0, sizeof(double) * N * N, st));
   gram_f64((double*)X, ld, (double*)X, ld, op->n_dofs, N, N, S, N, precision, true, st);
   symmetrize_lower(S, N, st);
-  if (fault_injected("not_spd")) {
-    k_negate_diag0<<<1, 1, 0, st>>>(S);
-    CHEFSI_CHECK_LAUNCH();
-  }
-  int rc = cholesky_lower(S, N, st);
-  if (rc != CHEFSI_OK) {
-    set_last_error("overlap matrix is not positive definite (Cholesky pivot <= 0)");
-    return rc;
-  }
+  int rc = cholesky_overlap(S, (const double*)X, ld, op->n_dofs, N, is_mixed(precision), st);
+  if (rc != CHEFSI_OK) return rc;
   trtri_lower(S, N, st);
   // X <- X L^{-T}
   k_transpose<<<grid_for((int64_t)N * N, 256), 256, 0, st>>>(S, W, N);

@@ -31,6 +31,40 @@ def test_not_spd_overlap_is_reported(C, monkeypatch):
     assert np.abs(Y.T @ Y - np.eye(Y.shape[1])).max() < 1e-12
 
 
+def test_mixed_overlap_beyond_its_precision_is_taken_again_in_fp64(C, monkeypatch):
+    """A tensor-core overlap whose Cholesky fails (made on the host: CHEFSI_FAULT_INJECT=
+    not_spd_mixed spoils the tensor-core S only) is recomputed with the FP64 Gram: the mixed
+    iteration then succeeds and its lowest Ritz values meet the mixed bar against the oracle
+    (the setup of smoke(): 1e-5 Ha after one degree-12 iteration). With every S spoiled
+    (not_spd) the mixed iteration still reports CHEFSI_ERR_NOT_SPD."""
+    from dftfe_gb300 import _lib, problems
+    from oracle import oracle as orc
+    pr = problems.make_problem(n=2, L=4.0, p=4, n_wells=2, n_wfc=16, seed=3, projectors=True)
+    op = C.KohnShamOperator.from_problem(pr)
+    ora = orc.OracleOperator(pr.cell_map, pr.cell_mats, pr.inv_sqrt_mass, pr.n_dofs,
+                             projectors=pr.nonlocal_)
+    X0 = pr.initial_vectors()
+    lo, up = orc.lanczos_bounds(ora, np.ones(pr.n_dofs), 20)
+    bl = lo + 0.2 * (up - lo)
+    ev_o, _, _ = orc.solve(ora, X0.copy(), orc.SolverState(lo, bl, up), m=12)
+
+    def mixed_solve():
+        s = C.ChebyshevOrthogonalizedSubspaceIterationSolver(C.SolverParams(chebyshevOrder=12))
+        s.reinitSpectrumBounds(lo, bl, up)
+        return s.solve(op, torch.from_numpy(X0.copy()).cuda(), useMixedPrec=True)[0]
+
+    monkeypatch.setenv("CHEFSI_FAULT_INJECT", "not_spd_mixed")
+    ev = mixed_solve()
+    assert np.abs(ev[:8] - ev_o[:8]).max() < 1e-5
+    monkeypatch.setenv("CHEFSI_FAULT_INJECT", "not_spd")
+    with pytest.raises(_lib.ChefsiError) as ei:
+        mixed_solve()
+    assert ei.value.code == _lib.CHEFSI_ERR_NOT_SPD
+    monkeypatch.delenv("CHEFSI_FAULT_INJECT")
+    ev = mixed_solve()
+    assert np.abs(ev[:8] - ev_o[:8]).max() < 1e-5
+
+
 def test_rank_deficient_overlap_is_not_spd(C):
     from dftfe_gb300 import _lib
     pr = small_problem(projectors=True)
