@@ -12,10 +12,11 @@ runs with exactly those, so the runs differ only in arithmetic.
 Tolerance, written in the test: FP64, every Ritz value within 1e-8 Ha and every residual norm
 within 1e-8 (measured: 4e-15 Ha, 7e-15). The mixed path is not compared here: from random
 vectors, the first-call bounds for 16 vectors (a short Lanczos run puts a0 above the spectrum's
-bottom and bLow just above it) make the filtered block's overlap matrix more ill-conditioned
-than the mixed Gram's 22 bits resolve, and its Cholesky reports CHEFSI_ERR_NOT_SPD; the mixed
-path is compared with the oracle over 20 iterations at the 64,000-dof workload and with the
-FP64 path at this operator with 1024 vectors (the benchmark's FP64 leg).
+bottom and bLow just above it) make the filtered block more ill-conditioned than its FP32
+storage resolves, so its overlap is not positive definite even when taken again in FP64 and
+the mixed iteration reports CHEFSI_ERR_NOT_SPD (the reference's FP32 filter vectors have the
+same limit); the mixed path is compared with the oracle over 20 iterations at the 64,000-dof
+workload and with the FP64 path at this operator with 1024 vectors (the benchmark's FP64 leg).
 
 Collected after the other GPU files (building the workload and the oracle's iterations take
 about a minute on the host).
