@@ -39,6 +39,25 @@ def test_single_process_reductions_are_identity():
     assert pools.max_highest_occupied_residual([np.array([0.1, 0.3]), np.array([0.2, 0.05])], 1) == 0.3
 
 
+def test_single_process_pool_helpers():
+    """Without a process group: one pool holds every k-point, the gathered array is the local
+    one, and the Fermi level puts the requested electron count into the states (spin-degenerate
+    and spin-polarised counting, src/dft/fermiEnergy.cc:26-60), between the highest fully and
+    the lowest empty level at low temperature."""
+    assert list(pools.my_kpoints(5)) == [0, 1, 2, 3, 4]
+    solved = pools.solve_kpoint_pool(3, lambda k: np.arange(4.0) + k)
+    assert sorted(solved) == [0, 1, 2]
+    ev = pools.gather_over_pools(solved, 3, 4)
+    assert np.array_equal(ev, np.arange(4.0)[None, :] + np.arange(3.0)[:, None])
+    eig = [np.array([-1.0, -0.5, 0.3, 0.8])] * 2
+    w = [0.5, 0.5]
+    for spin_polarized, ne in ((False, 4.0), (True, 2.0)):
+        fe = pools.fermi_energy(eig, w, ne, 300.0, spin_polarized=spin_polarized)
+        f, _ = pools._fermi_dirac_sums(fe, eig, w, 300.0, 1.0 if spin_polarized else 2.0)
+        assert abs(f - ne) < 1e-9
+        assert -0.5 < fe < 0.3
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
