@@ -967,9 +967,11 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rr-precision", default="fp32tc", choices=["fp64", "fp32", "fp32tc", "mixed"])
     ap.add_argument("--filter", default="folded", choices=["folded", "fused", "separate", "axpby"],
-                    help="mixed filter variant: recurrence pass + HX with the nonlocal apply as "
-                         "tensor-core K columns (folded), recurrence in the HX launch (fused), "
-                         "or separate nonlocal kernels (separate)")
+                    help="mixed filter variant: one tensor-core launch per degree with the "
+                         "Chebyshev shift on the tiles' diagonals and the nonlocal apply as extra "
+                         "K columns (folded, default), a recurrence pass + that launch without "
+                         "the shift (axpby), the recurrence in the HX launch (fused), or "
+                         "separate nonlocal kernels (separate)")
     ap.add_argument("--no-fp64-leg", action="store_true",
                     help="skip the FP64 iteration and the Ritz-error comparison after the timed steps")
     ap.add_argument("--density-check", action="store_true",
